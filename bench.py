@@ -1,0 +1,347 @@
+"""Benchmark of the field_fmm hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--arm fp64|mixed|learned]
+    python bench.py --impl reference ...
+
+One "step" is one field_fmm call on the benchmark system: N = 999,999
+water-like particles (333,333 triplets) in a 270 bohr cube, AMOEBA damping,
+multipoles of order 2, field_order 1, ncrit 64 (synthetic, seeded).  `value`
+is particles/s with all inputs resident in device memory; `e2e` is the same
+call through the host C ABI with the host<->device copies inside the timed
+region.  Accuracy (RMS / max per-particle relative field error, order >= 1
+columns) is measured against the FP64 GPU direct sum on 8192 random
+particles.  Prints one JSON line.
+
+With --gpus N (launched by torch.distributed.run) every rank runs its own
+replica of the system (the path does not shard: replicas only); timing is the
+maximum over ranks and `value` the particles of all ranks divided by it.
+
+--impl reference times the CPU restatement of the reference algorithm
+(oracle/, the reference itself is Fortran and has no build here) on a bounded
+sample of the same workload, on the host cores.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "field_fmm particles/s at N=1M: learned+mixed vs plain FP64 GPU @1e-6 rel err"
+N_MOL = 333_333
+BOX = 270.0
+THETA, NCRIT, P_ORDER, F_ORDER = 0.5, 64, 8, 1
+DAMP = "AMOEBA"
+
+
+def n_t(k):
+    return (k + 1) * (k + 2) * (k + 3) // 6
+
+
+def comb(n, k):
+    return math.comb(n, k)
+
+
+def pair_flops(m, f):
+    return 2 * n_t(f) * n_t(m) + 2 * comb(m + f + 4, 4) + 12
+
+
+def m2l_flops(p):
+    return 2 * n_t(p) ** 2 + 2 * comb(2 * p + 4, 4) + 12
+
+
+def workload_config(arm):
+    return {
+        "workload": "water-like triplets N=999,999 in a 270 bohr cube, AMOEBA damping, multipoles order 2, "
+                    "field_order 1, theta 0.5, ncrit 64, expansion_order 8",
+        "arm": arm,
+        "n_particles": 3 * N_MOL,
+        "l2": "inputs plus working set > 129 MB L2; a 256 MB buffer is also written between timed steps",
+        "accuracy_oracle": "FP64 GPU direct sum on 8192 random particles, field columns of order >= 1",
+    }
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], None, set()
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.remove(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_system(seed=0, n_mol=N_MOL, box=BOX):
+    from fmm_gb300 import systems
+    return systems.water(n_mol, box, order=2, seed=seed)
+
+
+def arm_options(arm):
+    from fmm_gb300 import Options
+    if arm == "fp64":
+        return Options.exact(precision="fp64")
+    if arm == "mixed":
+        return Options.exact(precision="mixed", mac_mode="damping")
+    if arm == "learned":
+        return Options.exact(precision="mixed", mac_mode="damping", selector="learned")
+    raise ValueError(arm)
+
+
+def cpu_sample(n_mol=10_000, threads=None):
+    """Times the oracle (reference semantics) on a sample of the same workload
+    at the same density; returns particles/s and the description."""
+    import oracle
+    box = BOX * (n_mol / N_MOL) ** (1.0 / 3.0)
+    s = make_system(seed=11, n_mol=n_mol, box=box)
+    args = (0, s["coordinates"], s["multipoles"], s["exclusions"])
+    nth = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.field_fmm(*args, THETA, NCRIT, P_ORDER, F_ORDER, DAMP, s["damping_factors"], nthreads=nth)
+    dt = time.perf_counter() - t0
+    return 3 * n_mol / dt, nth, ("oracle field_fmm (reference semantics: int32 Cnij, 1e10 exclusions) on N=%d "
+                                 "water-like particles at the benchmark density (%.1f bohr cube), AMOEBA, p=8, f=1, "
+                                 "%.2f s" % (3 * n_mol, box, dt))
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    vals = []
+    for k in range(args.warmup + args.steps):
+        v, nth, desc = cpu_sample(n_mol=args.ref_sample)
+        if k >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    line = {
+        "metric": METRIC, "value": value, "unit": "particles/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * 3 * args.ref_sample / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config("reference-cpu"),
+        "cpu_baseline": {"value": value, "unit": "particles/s", "cores": nth, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--arm", default="fp64", choices=["fp64", "mixed", "learned"])
+    ap.add_argument("--ref-sample", type=int, default=10_000, help="molecules in the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-mol", type=int, default=N_MOL)
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import fmm_gb300
+    from fmm_gb300 import _lib
+    L = _lib.lib()
+    opts = arm_options(args.arm)
+    stream = torch.cuda.current_stream()
+    opts.stream = stream.cuda_stream
+
+    n_mol = args.n_mol
+    box = BOX * (n_mol / N_MOL) ** (1.0 / 3.0)
+    s = make_system(seed=rank, n_mol=n_mol, box=box)
+    n = s["coordinates"].shape[0]
+    dev = torch.device("cuda", local)
+    tX = torch.from_numpy(np.ascontiguousarray(s["coordinates"].T).reshape(-1)).to(dev)  # column-major (n,3)
+    tM = torch.from_numpy(np.ascontiguousarray(s["multipoles"].T).reshape(-1)).to(dev)
+    tE = torch.from_numpy(np.ascontiguousarray(s["exclusions"].T).reshape(-1)).to(dev)
+    tD = torch.from_numpy(s["damping_factors"].copy()).to(dev)
+    nf = n_t(F_ORDER)
+    tF = torch.empty(n * nf, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    class Shape:  # minimal view with .shape for the device API
+        def __init__(self, t, rows, cols):
+            self.t, self.shape = t, (rows, cols)
+
+        def data_ptr(self):
+            return self.t.data_ptr()
+
+    X, M, E = Shape(tX, n, 3), Shape(tM, n, 10), Shape(tE, n, 3)
+
+    def step():
+        fmm_gb300.field_fmm_device(X, M, E, THETA, NCRIT, P_ORDER, F_ORDER, tF, DAMP, tD, options=opts)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    l0 = L.fmm_launch_count()
+    times = []
+    phase = {k: 0.0 for k in ("t_tree", "t_lists", "t_p2m_m2m", "t_p2p", "t_m2l", "t_l2l_l2p")}
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+            st = fmm_gb300.last_stats()
+            for k in phase:
+                phase[k] += st[k] / args.steps
+    launches = (L.fmm_launch_count() - l0) // args.steps
+    if dist:
+        dist.barrier()
+    ms = float(np.mean(times))
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    stats = fmm_gb300.last_stats()
+    value = world * n / (ms * 1e-3)
+
+    if rank != 0:
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    # accuracy against the FP64 direct sum on 8192 random particles
+    rng = np.random.default_rng(123)
+    tgt = np.sort(rng.choice(n, size=min(8192, n), replace=False)).astype(np.int64)
+    tT = torch.from_numpy(tgt).to(dev)
+    tRef = torch.empty(len(tgt) * nf, dtype=torch.float64, device=dev)
+    from fmm_gb300 import Options
+    o = Options(excl_mode="mask").to_c()
+    import ctypes
+    st_ = L.fmm_field_direct_targets_device(n, ctypes.c_void_p(tX.data_ptr()), 10, ctypes.c_void_p(tM.data_ptr()), 3,
+                                            ctypes.c_void_p(tE.data_ptr()), len(tgt), ctypes.c_void_p(tT.data_ptr()),
+                                            F_ORDER, ctypes.c_void_p(tRef.data_ptr()), DAMP.encode(), len(DAMP),
+                                            ctypes.c_void_p(tD.data_ptr()), ctypes.byref(o))
+    _lib.check(st_, "direct on sampled targets")
+    torch.cuda.synchronize()
+    Fref = tRef.cpu().numpy().reshape(nf, -1).T
+    Fgot = tF.cpu().numpy().reshape(nf, n).T[tgt]
+    d = np.linalg.norm(Fgot[:, 1:] - Fref[:, 1:], axis=1)
+    g = np.linalg.norm(Fref[:, 1:], axis=1)
+    per = d / g
+    accuracy = {"rms_rel_err": float(np.sqrt(np.mean(per ** 2))), "max_rel_err": float(per.max()),
+                "global_rel_err": float(np.linalg.norm(d) / np.linalg.norm(g)), "targets": int(len(tgt))}
+
+    # end to end through the host C ABI (pageable host buffers, copies timed)
+    e2e_times = []
+    Fh = None
+    for k in range(2 + args.steps):
+        t0 = time.perf_counter()
+        Fh = fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"], THETA, NCRIT, P_ORDER,
+                                 F_ORDER, DAMP, s["damping_factors"], options=arm_options(args.arm))
+        if k >= 2:
+            e2e_times.append(time.perf_counter() - t0)
+    h2d = 8 * (3 * n + 10 * n + n) + 4 * 3 * n
+    d2h = 8 * nf * n
+    e2e = {"value": world * n / float(np.mean(e2e_times)), "unit": "particles/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+
+    # roofline of the dominant phase (CUDA-core FP64 / FP32 compute)
+    prec = 1 if args.arm != "fp64" else 0
+    peak = ctypes.c_double(0)
+    _lib.check(L.fmm_measure_fma_peak(prec, ctypes.byref(peak)), "fma peak")
+    p2p_pairs = stats["p2p_particle_pairs"] - n
+    flops = {"t_p2p": p2p_pairs * pair_flops(2, F_ORDER), "t_m2l": stats["m2l_pairs"] * m2l_flops(P_ORDER)}
+    dom = max(flops, key=lambda k: phase[k])
+    achieved = flops[dom] / (phase[dom] * 1e-3) / 1e12
+    roofline = {"bound": "fp64" if prec == 0 else "fp32", "kernel": {"t_p2p": "k_p2p", "t_m2l": "k_m2l"}[dom],
+                "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
+                "peak_source": "measured live by fmm_measure_fma_peak (FMA loop over all SMs); MEASURED_PEAKS.json "
+                               "has no CUDA-core figure",
+                "algorithmic_flops_per_launch": flops[dom], "traffic": None,
+                "phase_ms": {k: round(v, 3) for k, v in phase.items()}}
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, nth, desc = cpu_sample()
+        cpu = {"value": v, "unit": "particles/s", "cores": nth, "kind": "port", "sample": desc}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.arm == "fp64" else "f32+f64", "data": "synthetic", "config": workload_config(args.arm),
+        "accuracy": accuracy, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+        "tree": {k: stats[k] for k in ("num_nodes", "num_leaves", "max_depth", "m2l_pairs", "p2p_leaf_pairs",
+                                       "p2p_particle_pairs")},
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

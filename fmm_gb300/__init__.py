@@ -1,0 +1,178 @@
+"""GB300-native (sm_103a) field evaluation for Cartesian-multipole FMM.
+
+Drop-in for the field-evaluation path of peter-reinholdt/fmm
+(``field_direct`` / ``field_fmm``, src/fmm.F90:1338-1400).  The functions
+here take the reference's arguments in the reference's order and layouts;
+extra behaviour is selected through keyword-only ``Options``.
+
+All arithmetic runs in the CUDA library ``libfmm_gb300.so`` (built in-tree by
+``fmm_gb300.build``); there is no CPU code path.
+"""
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import FmmError
+
+__all__ = ["field_direct", "field_fmm", "field_direct_device", "field_fmm_device", "Options", "last_stats",
+           "n_components", "FmmError", "version"]
+
+
+def n_components(order):
+    """Packed components of all orders <= order: (k+1)(k+2)(k+3)/6."""
+    return (order + 1) * (order + 2) * (order + 3) // 6
+
+
+@dataclass
+class Options:
+    """Behaviour switches that the reference API does not have.
+
+    The defaults reproduce the reference (int32 Cnij closed form in M2L,
+    excluded sources at R = 1e10, reference MAC, FP64, fixed order)."""
+
+    coef_mode: str = "ref"        # "ref" | "exact"
+    excl_mode: str = "ref"        # "ref" (1e10 displacement) | "mask"
+    precision: str = "fp64"       # "fp64" | "mixed"
+    centroid_mode: str = "sequential"  # "sequential" | "blocked"
+    mac_mode: str = "ref"         # "ref" | "damping"
+    selector: str = "fixed"       # "fixed" | "learned"
+    target_rel_err: float = 1e-6
+    stream: int = 0               # cudaStream_t for the *_device calls
+
+    @classmethod
+    def exact(cls, **kw):
+        d = dict(coef_mode="exact", excl_mode="mask", centroid_mode="blocked")
+        d.update(kw)
+        return cls(**d)
+
+    def to_c(self):
+        o = _lib.FmmOpts()
+        o.version = 1
+        o.coef_mode = {"ref": 0, "exact": 1}[self.coef_mode]
+        o.excl_mode = {"ref": 0, "mask": 1}[self.excl_mode]
+        o.precision = {"fp64": 0, "mixed": 1}[self.precision]
+        o.centroid_mode = {"sequential": 0, "blocked": 1}[self.centroid_mode]
+        o.mac_mode = {"ref": 0, "damping": 1}[self.mac_mode]
+        o.selector = {"fixed": 0, "learned": 1}[self.selector]
+        o.target_rel_err = float(self.target_rel_err)
+        o.stream = int(self.stream) or None
+        return o
+
+
+def _damp_bytes(damp_type):
+    s = (damp_type or "").encode()
+    return s, len(s)
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _prep(coordinates, multipoles, exclusions, damping_factors):
+    X = np.asfortranarray(coordinates, dtype=np.float64)
+    if X.ndim != 2 or X.shape[1] != 3:
+        raise ValueError("coordinates must be (N, 3)")
+    n = X.shape[0]
+    M = np.asfortranarray(multipoles, dtype=np.float64)
+    if M.ndim == 1:
+        M = M.reshape(n, 1, order="F")
+    if M.shape[0] != n:
+        raise ValueError("multipoles must be (N, dim)")
+    E = np.asfortranarray(exclusions, dtype=np.int32)
+    if E.ndim == 1:
+        E = E.reshape(n, -1, order="F")
+    if E.shape[0] != n:
+        raise ValueError("exclusions must be (N, width)")
+    d = None
+    if damping_factors is not None and np.size(damping_factors) > 0:
+        d = np.ascontiguousarray(damping_factors, dtype=np.float64)
+        if d.size < n:
+            raise ValueError("damping_factors must have N entries")
+    return X, M, E, d
+
+
+def field_direct(comm, coordinates, multipoles, exclusions, field_order, damp_type="", damping_factors=None, *,
+                 options=None):
+    """Direct-sum field, ``fmm::field_direct`` (src/fmm.F90:1338-1352).
+
+    Returns the (N, nT(field_order)) Fortran-ordered field array."""
+    X, M, E, d = _prep(coordinates, multipoles, exclusions, damping_factors)
+    n = X.shape[0]
+    F = np.zeros((n, n_components(field_order)), order="F")
+    ds, dl = _damp_bytes(damp_type)
+    o = (options or Options()).to_c()
+    st = _lib.lib().fmm_field_direct(int(comm or 0), n, _dptr(X), M.shape[1], _dptr(M), E.shape[1],
+                                     E.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), int(field_order), _dptr(F),
+                                     ds, dl, _dptr(d) if d is not None else None, ctypes.byref(o))
+    _lib.check(st, "field_direct")
+    return F
+
+
+def field_fmm(comm, coordinates, multipoles, exclusions, theta, ncrit, expansion_order, field_order, damp_type="",
+              damping_factors=None, is_periodic=False, box_matrix=None, *, options=None):
+    """FMM field, ``fmm::field_fmm`` (src/fmm.F90:1354-1400).
+
+    Returns the (N, nT(field_order)) Fortran-ordered field array."""
+    X, M, E, d = _prep(coordinates, multipoles, exclusions, damping_factors)
+    n = X.shape[0]
+    F = np.zeros((n, n_components(field_order)), order="F")
+    ds, dl = _damp_bytes(damp_type)
+    o = (options or Options()).to_c()
+    box = None
+    if box_matrix is not None:
+        box = np.asfortranarray(box_matrix, dtype=np.float64)
+    st = _lib.lib().fmm_field_fmm(int(comm or 0), n, _dptr(X), M.shape[1], _dptr(M), E.shape[1],
+                                  E.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), float(theta), int(ncrit),
+                                  int(expansion_order), int(field_order), _dptr(F), ds, dl,
+                                  _dptr(d) if d is not None else None, int(bool(is_periodic)),
+                                  _dptr(box) if box is not None else None, ctypes.byref(o))
+    _lib.check(st, "field_fmm")
+    return F
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(int(t.data_ptr()))
+
+
+def field_direct_device(coordinates, multipoles, exclusions, field_order, field, damp_type="", damping_factors=None,
+                        *, options=None):
+    """Device-resident direct sum.  Arguments are CUDA tensors (anything with
+    ``data_ptr()``) in the reference's column-major layouts; ``field`` is
+    written.  Work is enqueued on ``options.stream``."""
+    n = coordinates.shape[0]
+    ds, dl = _damp_bytes(damp_type)
+    o = (options or Options()).to_c()
+    st = _lib.lib().fmm_field_direct_device(n, _ptr(coordinates), multipoles.shape[1], _ptr(multipoles),
+                                            exclusions.shape[1], _ptr(exclusions), int(field_order), _ptr(field), ds,
+                                            dl, _ptr(damping_factors), ctypes.byref(o))
+    _lib.check(st, "field_direct_device")
+
+
+def field_fmm_device(coordinates, multipoles, exclusions, theta, ncrit, expansion_order, field_order, field,
+                     damp_type="", damping_factors=None, *, options=None):
+    """Device-resident FMM (see ``field_direct_device``)."""
+    n = coordinates.shape[0]
+    ds, dl = _damp_bytes(damp_type)
+    o = (options or Options()).to_c()
+    st = _lib.lib().fmm_field_fmm_device(n, _ptr(coordinates), multipoles.shape[1], _ptr(multipoles),
+                                         exclusions.shape[1], _ptr(exclusions), float(theta), int(ncrit),
+                                         int(expansion_order), int(field_order), _ptr(field), ds, dl,
+                                         _ptr(damping_factors), ctypes.byref(o))
+    _lib.check(st, "field_fmm_device")
+
+
+STAT_NAMES = ["num_nodes", "num_leaves", "max_depth", "m2l_pairs", "p2p_leaf_pairs", "p2p_particle_pairs", "t_tree",
+              "t_lists", "t_p2m_m2m", "t_p2p", "t_m2l", "t_l2l_l2p", "t_total"]
+
+
+def last_stats():
+    """Sizes and per-phase device times (ms) of the last FMM call on this thread."""
+    buf = (ctypes.c_double * len(STAT_NAMES))()
+    k = _lib.lib().fmm_last_stats(buf, len(STAT_NAMES))
+    return {STAT_NAMES[i]: buf[i] for i in range(k)}
+
+
+def version():
+    return _lib.lib().fmm_version().decode()

@@ -1,0 +1,137 @@
+// Internal declarations shared by the translation units of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace fmm {
+
+// A growable device allocation (grows, never shrinks; freed with the context).
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes);
+    void release();
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+// Octree in device memory.  Particles are kept in key-sorted order; nodes in
+// depth-first preorder over octants 0..7 (the reference's numbering,
+// src/fmm.F90:275-299), with the root at index 0.
+struct TreeDev {
+    int64_t n = 0;
+    int ncrit = 0;
+    int num_nodes = 0;
+    int num_leaves = 0;
+    int max_depth = 0;  // root has depth 1
+    int nlevels = 0;
+    int level_start[kMaxDepth + 3] = {0};  // ranges of level_nodes per depth (index = depth)
+    double root_c[3] = {0, 0, 0};
+    double root_r = 0;
+    // per sorted particle
+    uint32_t* perm = nullptr;    // sorted position -> original index
+    int32_t* pos_of = nullptr;   // original index -> sorted position
+    int32_t* leaf_of = nullptr;  // sorted position -> leaf node id
+    // per node
+    double *cx = nullptr, *cy = nullptr, *cz = nullptr, *r = nullptr, *rmax = nullptr;
+    int32_t *depth = nullptr, *parent = nullptr, *start = nullptr, *count = nullptr, *is_leaf = nullptr;
+    int32_t* child = nullptr;        // 8 per node, -1 where empty
+    int32_t* level_nodes = nullptr;  // node ids grouped by depth
+    int32_t* leaves = nullptr;       // ids of the leaves
+    // interaction lists, CSR by target node, sources ascending
+    int64_t nfar = 0, nnear = 0;
+    int64_t near_particle_pairs = 0;
+    int32_t *far_off = nullptr, *far_src = nullptr;
+    int32_t *near_off = nullptr, *near_src = nullptr;
+};
+
+struct Workspace;
+
+// Tree and list construction (tree.cu).
+struct TreeParams {
+    int ncrit;
+    double theta;
+    int centroid_mode;     // 0 sequential, 1 blocked
+    int have_host_centroid;
+    double host_centroid[3];
+    int mac_mode;          // 0 reference MAC
+};
+int build_tree(Workspace& ws, const double* d_coords, int64_t n, const TreeParams& tp, TreeDev& t, cudaStream_t st);
+int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st);
+
+// Host-side sequential centroid (the reference's SUM order).
+void host_centroid_sequential(const double* coords, int64_t n, double c[3]);
+
+struct Workspace {
+    // inputs on device (host entry points copy here)
+    DevBuf in_coords, in_mp, in_excl, in_damp, out_field;
+    // tree
+    DevBuf keys_a, keys_b, vals_a, vals_b, cub_tmp;
+    DevBuf perm, pos_of, leaf_of;
+    DevBuf node_d, node_i, child, level_nodes, leaves, node_key, node_val, node_key2, node_val2;
+    DevBuf counters, scalars;
+    DevBuf front_a, front_b, far_pairs, near_pairs, far_sorted, near_sorted;
+    DevBuf node_dfs, far_src, near_src;
+    // sorted particle data
+    DevBuf sx, sy, sz, smc, sd;
+    DevBuf fsorted;
+    // expansions
+    DevBuf mom, loc;
+    // direct-sum partial sums
+    DevBuf partial;
+    // ref-mode closed-form tensor tables
+    DevBuf term_off, term_abc, term_c;
+    int term_order = -1;
+    // timing
+    cudaEvent_t ev[16] = {};
+    bool events_ready = false;
+    int device = -1;
+    int64_t node_cap = 0;
+    ~Workspace();
+};
+
+Workspace& thread_workspace();
+
+// Adds k to the calling thread's count of this library's kernel launches.
+void count_launches(int k);
+
+// Kernels launchers (direct.cu, near.cu, expansions.cu).
+struct Particles {
+    int64_t n;
+    const double* x;  // coordinates, column-major (n,3) in the caller's order
+    int dim;
+    const double* mp;  // (n, dim)
+    int exw;
+    const int32_t* excl;  // (n, exw)
+    const double* damp;   // (n) or null
+    int damp_type;
+};
+
+struct Modes {
+    int coef_mode;
+    int excl_mode;
+    int precision;
+};
+
+int launch_direct_f64(Workspace& ws, const Particles& P, int field_order, const Modes& md, double* d_field,
+                      cudaStream_t st, int64_t ntgt = 0, const int64_t* d_targets = nullptr);
+
+// FMM phases (near.cu / expansions.cu)
+int gather_sorted(Workspace& ws, const Particles& P, const TreeDev& t, cudaStream_t st);
+int launch_p2p_f64(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, const Modes& md,
+                   cudaStream_t st);
+int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, cudaStream_t st);
+int launch_m2l(Workspace& ws, const TreeDev& t, int p, const Modes& md, cudaStream_t st);
+int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, int field_order, cudaStream_t st);
+int launch_excl_correction(Workspace& ws, const Particles& P, const TreeDev* t, int field_order, const Modes& md,
+                           double* d_field_sorted_or_orig, cudaStream_t st);
+int scatter_field(Workspace& ws, const TreeDev& t, int64_t n, int nf, double* d_field, cudaStream_t st);
+
+}  // namespace fmm

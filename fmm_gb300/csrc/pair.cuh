@@ -1,0 +1,338 @@
+// Pair interaction math shared by the direct-sum and near-field kernels.
+//
+// The reference evaluates interaction tensors with a closed form for the
+// undamped kernel (src/tensors_recursive.F90:95-135) and with generated
+// straight-line code for the damped ones (src/tensors_damped_*.F90).  Here
+// every kernel goes through one path:
+//   1. radial functions g_j(r) = (r^-1 d/dr)^j phi(r), j = 0..N, for the
+//      kernel phi (1/r, Thole, AMOEBA, erf);
+//   2. the Cartesian derivative tensor T_{tuv} = d^t/dx^t d^u/dy^u d^v/dz^v phi
+//      of every order <= N from the g_j by the Hermite-type recursion
+//        R^(j)_{t+1,u,v} = t R^(j+1)_{t-1,u,v} + X R^(j+1)_{t,u,v},
+//      R^(j)_{000} = g_j, T = R^(0) (done in place, highest level first);
+//   3. the contraction of the reference's multipole_field
+//      (src/fmm.F90:596-620): F_f += sum_s c_s M_s T_{s+f}, where the
+//      source coefficients c_s = (-1)^(|s|+1) / (sx! sy! sz!) are folded into
+//      the multipoles once per particle.
+// Everything is templated on the multipole order M and field order F, so the
+// compiler unrolls it into straight-line register code.
+#pragma once
+
+#include <math.h>
+
+#include "common.cuh"
+#include "series_tables.h"
+
+namespace fmm {
+
+#define FMM_INV_ODD_N 64
+#ifdef __CUDACC__
+__constant__ double cInvOdd[FMM_INV_ODD_N] = {
+#define X(i) 1.0 / (2.0 * (i) + 1.0),
+    X(0) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15)
+    X(16) X(17) X(18) X(19) X(20) X(21) X(22) X(23) X(24) X(25) X(26) X(27) X(28) X(29) X(30) X(31)
+    X(32) X(33) X(34) X(35) X(36) X(37) X(38) X(39) X(40) X(41) X(42) X(43) X(44) X(45) X(46) X(47)
+    X(48) X(49) X(50) X(51) X(52) X(53) X(54) X(55) X(56) X(57) X(58) X(59) X(60) X(61) X(62) X(63)
+#undef X
+};
+__constant__ double cTholeSeries[FMM_SER_JMAX + 1][FMM_SER_KT + 1] = FMM_THOLE_SERIES_INIT;
+__constant__ double cAmoebaSeries[FMM_SER_JMAX + 1][FMM_SER_KA + 1] = FMM_AMOEBA_SERIES_INIT;
+__constant__ double cAmoebaQ[FMM_SER_JMAX + 1][FMM_SER_JMAX] = FMM_AMOEBA_Q_INIT;
+__constant__ float cTholeSeriesF[FMM_SER_JMAX + 1][FMM_SER_KT + 1] = FMM_THOLE_SERIES_INIT;
+__constant__ float cAmoebaSeriesF[FMM_SER_JMAX + 1][FMM_SER_KA + 1] = FMM_AMOEBA_SERIES_INIT;
+__constant__ float cAmoebaQF[FMM_SER_JMAX + 1][FMM_SER_JMAX] = FMM_AMOEBA_Q_INIT;
+#endif
+static const double hTholeSeries[FMM_SER_JMAX + 1][FMM_SER_KT + 1] = FMM_THOLE_SERIES_INIT;
+static const double hAmoebaSeries[FMM_SER_JMAX + 1][FMM_SER_KA + 1] = FMM_AMOEBA_SERIES_INIT;
+static const double hAmoebaQ[FMM_SER_JMAX + 1][FMM_SER_JMAX] = FMM_AMOEBA_Q_INIT;
+
+// Per-precision math and the switch-over points between the series and the
+// closed forms (chosen so the closed form's cancellation stays below the
+// precision's rounding; checked against high-precision values in the tests).
+template <typename R>
+struct Real;
+
+template <>
+struct Real<double> {
+    static constexpr double kTholeX = 0.5;   // series for a*r below this
+    static constexpr int kTholeK = 18;       // series terms used
+    static constexpr double kAmoebaU = 0.5;  // series for (a r)^3 below this
+    static constexpr int kAmoebaK = 16;
+    static constexpr double kErfS = 3.0;     // Boys series for a r^2 below this
+    static constexpr int kErfK = 40;
+    __host__ __device__ static __forceinline__ double rsqrt_(double x) {
+#ifdef __CUDA_ARCH__
+        return ::rsqrt(x);
+#else
+        return 1.0 / ::sqrt(x);
+#endif
+    }
+    __host__ __device__ static __forceinline__ double exp_(double x) { return ::exp(x); }
+    __host__ __device__ static __forceinline__ double erf_(double x) { return ::erf(x); }
+    __host__ __device__ static __forceinline__ double sqrt_(double x) { return ::sqrt(x); }
+    __host__ __device__ static __forceinline__ double inv_odd(int i) {
+#ifdef __CUDA_ARCH__
+        return cInvOdd[i];
+#else
+        return 1.0 / (2.0 * i + 1.0);
+#endif
+    }
+    __host__ __device__ static __forceinline__ double thole(int j, int k) {
+#ifdef __CUDA_ARCH__
+        return cTholeSeries[j][k];
+#else
+        return hTholeSeries[j][k];
+#endif
+    }
+    __host__ __device__ static __forceinline__ double amoeba(int j, int k) {
+#ifdef __CUDA_ARCH__
+        return cAmoebaSeries[j][k];
+#else
+        return hAmoebaSeries[j][k];
+#endif
+    }
+    __host__ __device__ static __forceinline__ double amoebaQ(int j, int d) {
+#ifdef __CUDA_ARCH__
+        return cAmoebaQ[j][d];
+#else
+        return hAmoebaQ[j][d];
+#endif
+    }
+};
+
+template <>
+struct Real<float> {
+    static constexpr float kTholeX = 2.0f;
+    static constexpr int kTholeK = 20;
+    static constexpr float kAmoebaU = 2.0f;
+    static constexpr int kAmoebaK = 24;
+    static constexpr float kErfS = 6.0f;
+    static constexpr int kErfK = 36;
+    __host__ __device__ static __forceinline__ float rsqrt_(float x) {
+#ifdef __CUDA_ARCH__
+        return ::rsqrtf(x);
+#else
+        return 1.0f / ::sqrtf(x);
+#endif
+    }
+    __host__ __device__ static __forceinline__ float exp_(float x) { return ::expf(x); }
+    __host__ __device__ static __forceinline__ float erf_(float x) { return ::erff(x); }
+    __host__ __device__ static __forceinline__ float sqrt_(float x) { return ::sqrtf(x); }
+    __host__ __device__ static __forceinline__ float inv_odd(int i) {
+#ifdef __CUDA_ARCH__
+        return (float)cInvOdd[i];
+#else
+        return 1.0f / (2.0f * i + 1.0f);
+#endif
+    }
+    __host__ __device__ static __forceinline__ float thole(int j, int k) {
+#ifdef __CUDA_ARCH__
+        return cTholeSeriesF[j][k];
+#else
+        return (float)hTholeSeries[j][k];
+#endif
+    }
+    __host__ __device__ static __forceinline__ float amoeba(int j, int k) {
+#ifdef __CUDA_ARCH__
+        return cAmoebaSeriesF[j][k];
+#else
+        return (float)hAmoebaSeries[j][k];
+#endif
+    }
+    __host__ __device__ static __forceinline__ float amoebaQ(int j, int d) {
+#ifdef __CUDA_ARCH__
+        return cAmoebaQF[j][d];
+#else
+        return (float)hAmoebaQ[j][d];
+#endif
+    }
+};
+
+__host__ __device__ constexpr double dfact_odd(int j) {  // (2j-1)!!, (-1)!! = 1
+    double p = 1.0;
+    for (int i = 1; i <= j; ++i) p *= (double)(2 * i - 1);
+    return p;
+}
+
+// g_j(r), j = 0..N, of the kernel `damp` at squared distance r2 and pair
+// damping factor a (the product of the two particles' factors).
+template <int N, typename R>
+__host__ __device__ __forceinline__ void radial_g(int damp, R r2, R a, R* g) {
+    using RT = Real<R>;
+    const R ir = RT::rsqrt_(r2);
+    const R ir2 = ir * ir;
+    if (damp == DAMP_NONE) {
+        g[0] = ir;
+#pragma unroll
+        for (int j = 1; j <= N; ++j) g[j] = -(R)(2 * j - 1) * g[j - 1] * ir2;
+        return;
+    }
+    if (damp == DAMP_ERF) {
+        // g_j = (-1)^j sqrt(a) (2a)^j (2/sqrt(pi)) F_j(a r^2), F_j the Boys function
+        const R s = a * r2;
+        const R es = RT::exp_(-s);
+        R Fb[N + 1];
+        if (s < RT::kErfS) {
+            R term = (R)(1.0 / (2 * N + 1)), sum = term;
+            const R two_s = s + s;
+#pragma unroll 1
+            for (int k = 1; k <= RT::kErfK; ++k) {
+                term = term * two_s * RT::inv_odd(N + k);
+                sum += term;
+            }
+            Fb[N] = es * sum;
+#pragma unroll
+            for (int j = N - 1; j >= 0; --j) Fb[j] = (two_s * Fb[j + 1] + es) * (R)(1.0 / (2 * j + 1));
+        } else {
+            const R rs = RT::sqrt_(s);
+            Fb[0] = (R)0.88622692545275801365 * RT::erf_(rs) / rs;  // sqrt(pi)/2
+            const R i2s = (R)0.5 / s;
+#pragma unroll
+            for (int j = 0; j < N; ++j) Fb[j + 1] = ((R)(2 * j + 1) * Fb[j] - es) * i2s;
+        }
+        R pre = RT::sqrt_(a) * (R)1.12837916709551257390;  // 2/sqrt(pi)
+        const R twoa = a + a;
+#pragma unroll
+        for (int j = 0; j <= N; ++j) {
+            g[j] = (j % 2 ? -pre : pre) * Fb[j];
+            pre *= twoa;
+        }
+        return;
+    }
+    R num[N + 1];
+    if (damp == DAMP_THOLE) {
+        const R x = a * (r2 * ir);
+        if (x < RT::kTholeX) {
+#pragma unroll
+            for (int j = 0; j <= N; ++j) {
+                R acc = RT::thole(j, RT::kTholeK);
+#pragma unroll 1
+                for (int k = RT::kTholeK - 1; k >= 0; --k) acc = acc * x + RT::thole(j, k);
+                num[j] = acc;
+            }
+        } else {
+            const R e = RT::exp_(-x);
+            const R x2 = x * x;
+            R ym1 = (R)1, y0 = -((R)1 + x);  // y_0, y_1 (Yukawa numerators)
+            num[0] = (R)1 - e * ((R)1 + (R)0.5 * x);
+#pragma unroll
+            for (int j = 1; j <= N; ++j) {
+                const R P = y0 - (R)0.5 * x2 * ym1;
+                num[j] = (R)((j % 2 ? -1.0 : 1.0) * dfact_odd(j)) - e * P;
+                const R yn = x2 * ym1 - (R)(2 * j + 1) * y0;
+                ym1 = y0;
+                y0 = yn;
+            }
+        }
+    } else {  // AMOEBA: T0 = 0, g_1 = -(1 - e^{-u}) / r^3, u = (a r)^3
+        const R x = a * (r2 * ir);
+        const R u = x * x * x;
+        num[0] = (R)0;
+        if (u < RT::kAmoebaU) {
+#pragma unroll
+            for (int j = 1; j <= N; ++j) {
+                R acc = RT::amoeba(j, RT::kAmoebaK);
+#pragma unroll 1
+                for (int k = RT::kAmoebaK - 1; k >= 0; --k) acc = acc * u + RT::amoeba(j, k);
+                num[j] = acc;
+            }
+        } else {
+            const R e = RT::exp_(-u);
+#pragma unroll
+            for (int j = 1; j <= N; ++j) {
+                R q = RT::amoebaQ(j, j - 1);
+#pragma unroll
+                for (int d = j - 2; d >= 0; --d) q = q * u + RT::amoebaQ(j, d);
+                num[j] = (R)((j % 2 ? -1.0 : 1.0) * dfact_odd(j)) + e * q;
+            }
+        }
+    }
+    R irp = ir;
+#pragma unroll
+    for (int j = 0; j <= N; ++j) {
+        g[j] = num[j] * irp;
+        irp *= ir2;
+    }
+}
+
+// Cartesian derivative tensor of all orders <= N from g_0..g_N (in place).
+template <int N, typename R>
+__host__ __device__ __forceinline__ void md_tensor(R X, R Y, R Z, const R* g, R* T) {
+    T[0] = g[N];
+#pragma unroll
+    for (int j = N - 1; j >= 0; --j) {
+#pragma unroll
+        for (int k = N - j; k >= 1; --k) {
+#pragma unroll
+            for (int tx = k; tx >= 0; --tx) {
+#pragma unroll
+                for (int ty = k - tx; ty >= 0; --ty) {
+                    const int tz = k - tx - ty;
+                    R v;
+                    if (tx > 0) {
+                        v = X * T[pidx(tx - 1, ty, tz)];
+                        if (tx > 1) v += (R)(tx - 1) * T[pidx(tx - 2, ty, tz)];
+                    } else if (ty > 0) {
+                        v = Y * T[pidx(tx, ty - 1, tz)];
+                        if (ty > 1) v += (R)(ty - 1) * T[pidx(tx, ty - 2, tz)];
+                    } else {
+                        v = Z * T[pidx(tx, ty, tz - 1)];
+                        if (tz > 1) v += (R)(tz - 1) * T[pidx(tx, ty, tz - 2)];
+                    }
+                    T[pidx(tx, ty, tz)] = v;
+                }
+            }
+        }
+        T[0] = g[j];
+    }
+}
+
+// Source coefficient c_s = (-1)^(|s|+1) / (sx! sy! sz!) of the reference's
+// contraction (taylor * symfac in src/fmm.F90:598-615).
+__host__ __device__ constexpr double src_coef(int s) {
+    return ((order_of(s) + 1) % 2 ? -1.0 : 1.0) / (cfact(comp_x(s)) * cfact(comp_y(s)) * cfact(comp_z(s)));
+}
+
+// acc_f += sum_s Mc_s T_{s+f}; Mc already carries src_coef.
+template <int M, int F, typename R>
+__host__ __device__ __forceinline__ void contract(const R* T, const R* Mc, R* acc) {
+#pragma unroll
+    for (int fo = 0; fo <= F; ++fo)
+#pragma unroll
+        for (int fx = fo; fx >= 0; --fx)
+#pragma unroll
+            for (int fy = fo - fx; fy >= 0; --fy) {
+                const int fz = fo - fx - fy;
+                R a = acc[pidx(fx, fy, fz)];
+#pragma unroll
+                for (int so = 0; so <= M; ++so)
+#pragma unroll
+                    for (int sx = so; sx >= 0; --sx)
+#pragma unroll
+                        for (int sy = so - sx; sy >= 0; --sy) {
+                            const int sz = so - sx - sy;
+                            a += Mc[pidx(sx, sy, sz)] * T[pidx(sx + fx, sy + fy, sz + fz)];
+                        }
+                acc[pidx(fx, fy, fz)] = a;
+            }
+}
+
+// Field of one source at displacement (dx, dy, dz) = target - source.
+template <int M, int F, typename R>
+__host__ __device__ __forceinline__ void pair_field(R dx, R dy, R dz, R a, int damp, const R* Mc, R* acc) {
+    constexpr int N = M + F;
+    const R r2 = dx * dx + dy * dy + dz * dz;
+    R g[N + 1];
+    radial_g<N, R>(damp, r2, a, g);
+    R T[nT(N)];
+    md_tensor<N, R>(dx, dy, dz, g, T);
+    contract<M, F, R>(T, Mc, acc);
+}
+
+// Out-of-line variant for cold paths (exclusion fix-ups) to keep code size down.
+template <int M, int F, typename R>
+__device__ __noinline__ void pair_field_cold(R dx, R dy, R dz, R a, int damp, const R* Mc, R* acc) {
+    pair_field<M, F, R>(dx, dy, dz, a, damp, Mc, acc);
+}
+
+}  // namespace fmm

@@ -1,0 +1,147 @@
+/*
+ * fmm_gpu.h - C ABI of the GB300 (sm_103a) implementation of the fmm
+ * field-evaluation path (peter-reinholdt/fmm).
+ *
+ * The two entry points replace the reference's Fortran module procedures
+ *   field_direct  (src/fmm.F90:1338-1352)
+ *   field_fmm     (src/fmm.F90:1354-1400)
+ * with the same argument meaning.  Arrays are Fortran column-major and
+ * owned by the caller:
+ *   coordinates  n x 3            double  (x column, y column, z column)
+ *   multipoles   n x mdim         double  packed alphabetical order
+ *                                         (q; x,y,z; xx,xy,xz,yy,yz,zz; ...),
+ *                                         mdim = (m+1)(m+2)(m+3)/6
+ *   exclusions   n x exw          int32   1-based particle indices, 0-padded
+ *   field        n x nT(f)        double  written (zeroed by the callee first:
+ *                                         the reference only accumulates into
+ *                                         it, src/fmm.F90:731,813,1113)
+ *   damping      n                double  per-particle damping factors, or
+ *                                         NULL when damp_type is empty
+ * field(:,1) is minus the potential, field(:,2:4) the electric field, and
+ * the order-k block minus the k-th derivative of the potential.
+ *
+ * `damp` is the reference's damp_type: "AMOEBA", "THOLE", "ERF" or "" (any
+ * trailing blanks are ignored, as Fortran's trim() does), with length
+ * `damp_len` (no NUL terminator needed).  `comm` is accepted and ignored:
+ * this build runs on one GPU and performs no MPI or collective calls.
+ *
+ * Every call returns FMM_OK (0) or a negative status; nothing aborts the
+ * process (the reference uses `error stop`, src/fmm.F90:594,1376,1382).
+ */
+#ifndef FMM_GPU_H
+#define FMM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FMM_OK 0
+#define FMM_EINVAL (-1)    /* bad argument (unknown damp type, bad sizes, exclusion index out of range) */
+#define FMM_ENOTSUP (-2)   /* unsupported mode (periodic boxes, orders outside the built kernels)      */
+#define FMM_ENOMEM (-3)    /* device or host allocation failed                                         */
+#define FMM_ECUDA (-4)     /* a CUDA runtime call failed                                               */
+#define FMM_EDEPTH (-5)    /* the octree would need more than 21 levels (near-coincident particles)   */
+#define FMM_EORDER (-6)    /* damped interaction above the supported tensor order                     */
+#define FMM_ETIMEOUT (-7)  /* a bounded device wait gave up                                           */
+
+/* Options that do not exist in the reference API.  A NULL pointer means the
+ * defaults, which reproduce the reference's behaviour (all fields 0). */
+typedef struct fmm_opts {
+    int version;        /* must be 1 (or 0 for "defaults")                                      */
+    int coef_mode;      /* 0 ref: M2L tensors from the reference's int32 Cnij closed form
+                               (src/tensors_recursive.F90; wraps at tensor order >= 11)
+                           1 exact: exact Cartesian tensors (Hermite recursion)               */
+    int excl_mode;      /* 0 ref: excluded sources moved to R=(1e10,1e10,1e10), self pair only
+                               skipped if listed (src/fmm.F90:714-720, 802-806)
+                           1 mask: excluded pairs and the self pair skipped; excluded pairs
+                               that the far field counted are subtracted again           */
+    int precision;      /* 0 fp64; 1 mixed: FP32 near field and M2L with blocked FP64
+                           accumulation, FP64 tree, M2M/L2L and final sums               */
+    int centroid_mode;  /* 0 sequential sum (as the reference), 1 blocked (1024 lanes)       */
+    int mac_mode;       /* 0 reference MAC (r*theta > rmax_i + rmax_j)
+                           1 damping-aware: additionally demote cell pairs whose closest
+                               particles are within the damping range to the near field  */
+    int selector;       /* 0 fixed expansion order; 1 learned per-pair order (MLP)           */
+    double target_rel_err; /* error target for mac_mode 1 / selector 1 (default 1e-6)       */
+    void *stream;       /* cudaStream_t for the *_device entry points (NULL = legacy stream) */
+    int reserved[8];
+} fmm_opts;
+
+/* Replaces fmm::field_direct (src/fmm.F90:1338-1352); O(N^2) direct sum.
+ * Host pointers; blocks until `field` holds the result. */
+int fmm_field_direct(int comm, int64_t n, const double *coordinates, int mdim, const double *multipoles, int exw,
+                     const int32_t *exclusions, int field_order, double *field, const char *damp, int damp_len,
+                     const double *damping_factors, const fmm_opts *opts);
+
+/* Replaces fmm::field_fmm (src/fmm.F90:1354-1400).  Falls back to the direct
+ * sum when n <= ncrit, as the reference does (src/fmm.F90:1381-1383).
+ * is_periodic != 0 returns FMM_ENOTSUP; box_matrix (3x3, may be NULL) is
+ * otherwise ignored.  Host pointers; blocks until `field` holds the result. */
+int fmm_field_fmm(int comm, int64_t n, const double *coordinates, int mdim, const double *multipoles, int exw,
+                  const int32_t *exclusions, double theta, int ncrit, int expansion_order, int field_order,
+                  double *field, const char *damp, int damp_len, const double *damping_factors, int is_periodic,
+                  const double *box_matrix, const fmm_opts *opts);
+
+/* Same computations on arrays already resident in device memory (same
+ * layouts), enqueued on opts->stream.  No host<->device copies of particle
+ * data; the call returns after enqueueing all work except where it must read
+ * a size back (tree build), which it does with a stream synchronisation. */
+int fmm_field_direct_device(int64_t n, const double *d_coordinates, int mdim, const double *d_multipoles, int exw,
+                            const int32_t *d_exclusions, int field_order, double *d_field, const char *damp,
+                            int damp_len, const double *d_damping_factors, const fmm_opts *opts);
+
+int fmm_field_fmm_device(int64_t n, const double *d_coordinates, int mdim, const double *d_multipoles, int exw,
+                         const int32_t *d_exclusions, double theta, int ncrit, int expansion_order, int field_order,
+                         double *d_field, const char *damp, int damp_len, const double *d_damping_factors,
+                         const fmm_opts *opts);
+
+/* Direct sum evaluated at a subset of the particles only (every particle is
+ * still a source): d_targets holds ntgt 0-based particle indices, d_field is
+ * (ntgt x nT(field_order)) column-major.  No counterpart in the reference;
+ * this is the FP64 error oracle used to measure the accuracy of the fast
+ * paths on sampled targets. */
+int fmm_field_direct_targets_device(int64_t n, const double *d_coordinates, int mdim, const double *d_multipoles,
+                                    int exw, const int32_t *d_exclusions, int64_t ntgt, const int64_t *d_targets,
+                                    int field_order, double *d_field, const char *damp, int damp_len,
+                                    const double *d_damping_factors, const fmm_opts *opts);
+
+/* Statistics of the last fmm_field_fmm* call on this thread: tree and list
+ * sizes and per-phase device times in milliseconds.  `out` receives up to
+ * `len` doubles in this order: num_nodes, num_leaves, max_depth, m2l_pairs,
+ * p2p_leaf_pairs, p2p_particle_pairs, t_tree, t_lists, t_p2m_m2m, t_p2p,
+ * t_m2l, t_l2l_l2p, t_total.  Returns the number written. */
+int fmm_last_stats(double *out, int len);
+
+/* Diagnostics (no counterpart in the reference): builds the octree and
+ * interaction lists of `coordinates` exactly as fmm_field_fmm does and copies
+ * them out.  sizes[0..3] receive num_nodes, far pairs, near pairs, max_depth;
+ * call first with all array pointers NULL to get the sizes.  Per node (DFS
+ * preorder ids): centre (3 per node), half-width r, rmax, depth, parent id
+ * (-1 for the root), leaf flag, particle count; per particle (input order):
+ * leaf id; far/near lists as (target, source) id pairs sorted ascending. */
+int fmm_debug_tree(int64_t n, const double *coordinates, int ncrit, double theta, int centroid_mode, int64_t *sizes,
+                   double *center, double *r, double *rmax, int32_t *depth, int32_t *parent, int32_t *is_leaf,
+                   int32_t *count, int32_t *leaf_of, int32_t *far_pairs, int32_t *near_pairs);
+
+/* Diagnostics: sustained CUDA-core FMA rate of this GPU, measured by a short
+ * register-resident FMA loop over all SMs.  precision 0 = FP64, 1 = FP32.
+ * Writes TFLOP/s (2 flops per FMA) to *tflops. */
+int fmm_measure_fma_peak(int precision, double *tflops);
+
+/* Number of kernels this library launched on the calling thread so far. */
+int64_t fmm_launch_count(void);
+
+/* Human-readable text for a status code. */
+const char *fmm_strerror(int status);
+
+/* Library version string. */
+const char *fmm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FMM_GPU_H */

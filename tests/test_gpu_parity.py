@@ -1,0 +1,170 @@
+"""GPU parity: the CUDA library against the CPU oracle on the same inputs.
+
+Bars: bit-exact for the tree and lists (integer work); relative field error
+<= 1e-12 for the FP64 paths (spec precision bar for the plain FP64
+path).  Every call goes through the C ABI (include/fmm_gpu.h) via ctypes.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import fmm_gb300
+import oracle
+from fmm_gb300 import Options, _lib
+from helpers import rel_err, small_system
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _fmm_args(s):
+    return (0, s["coordinates"], s["multipoles"], s["exclusions"])
+
+
+@pytest.mark.parametrize("damp", ["", "THOLE", "AMOEBA", "ERF"])
+@pytest.mark.parametrize("mf", [(0, 0), (0, 1), (1, 1), (2, 1), (2, 2), (1, 2)])
+@pytest.mark.parametrize("excl", ["ref", "mask"])
+def test_direct_matches_oracle(damp, mf, excl):
+    m, f = mf
+    s = small_system(500, 18.0, order=m, seed=1, damp=damp)
+    d = s["damping_factors"] if damp else None
+    G = fmm_gb300.field_direct(*_fmm_args(s), f, damp, d, options=Options(excl_mode=excl))
+    O = oracle.field_direct(*_fmm_args(s), f, damp, d, excl_mode=excl)
+    cols = slice(1, None) if (damp == "AMOEBA" and f > 0) else slice(0, None)
+    assert np.all(np.isfinite(G))
+    assert rel_err(G, O, cols) <= TOL
+
+
+def _gpu_tree(X, ncrit, theta, centroid):
+    L = _lib.lib()
+    X = np.asfortranarray(X)
+    n = X.shape[0]
+    sizes = np.zeros(4, dtype=np.int64)
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    L.fmm_debug_tree.restype = ctypes.c_int
+    L.fmm_debug_tree.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_double,
+                                 ctypes.c_int, ctypes.POINTER(ctypes.c_int64)] + [ctypes.c_void_p] * 10
+    st = L.fmm_debug_tree(n, dp(X), ncrit, theta, centroid, sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                          *([None] * 10))
+    assert st == 0
+    M, nf, nn, md = (int(v) for v in sizes)
+    out = dict(center=np.zeros((M, 3)), r=np.zeros(M), rmax=np.zeros(M), depth=np.zeros(M, np.int32),
+               parent=np.zeros(M, np.int32), is_leaf=np.zeros(M, np.int32), count=np.zeros(M, np.int32),
+               leaf_of=np.zeros(n, np.int32), far=np.zeros((max(nf, 1), 2), np.int32),
+               near=np.zeros((max(nn, 1), 2), np.int32))
+    st = L.fmm_debug_tree(n, dp(X), ncrit, theta, centroid, sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                          dp(out["center"]), dp(out["r"]), dp(out["rmax"]), ip(out["depth"]), ip(out["parent"]),
+                          ip(out["is_leaf"]), ip(out["count"]), ip(out["leaf_of"]), ip(out["far"]),
+                          ip(out["near"]))
+    assert st == 0
+    out["far"] = out["far"][:nf]
+    out["near"] = out["near"][:nn]
+    out["max_depth"] = md
+    return out
+
+
+@pytest.mark.parametrize("centroid", ["sequential", "blocked"])
+@pytest.mark.parametrize("case", ["uniform", "water", "blobs"])
+def test_tree_and_lists_bit_exact(centroid, case):
+    from fmm_gb300 import systems
+    if case == "uniform":
+        X = systems.uniform_triplets(4096, 40.0, seed=0)["coordinates"]
+        ncrit, theta = 64, 0.5
+    elif case == "water":
+        X = systems.water(3000, 60.0, seed=2)["coordinates"]
+        ncrit, theta = 64, 0.5
+    else:
+        X = systems.blobs(20000, n_blobs=8, box=200.0, seed=3)["coordinates"]
+        ncrit, theta = 32, 0.4
+    g = _gpu_tree(X, ncrit, theta, {"sequential": 0, "blocked": 1}[centroid])
+    o = oracle.tree(X, ncrit, theta, centroid=centroid)
+    assert g["center"].shape == o["center"].shape
+    assert np.array_equal(g["center"], o["center"])
+    assert np.array_equal(g["r"], o["r"])
+    assert np.array_equal(g["rmax"], o["rmax"])
+    for k in ("depth", "parent", "is_leaf", "count", "leaf_of"):
+        assert np.array_equal(g[k], o[k]), k
+    assert np.array_equal(g["far"], o["far"])
+    assert np.array_equal(g["near"], o["near"])
+
+
+def test_fmm_ref_mode_matches_oracle_config1():
+    """Config-1 shape: N=4096 uniform triplets, p=5, f=1, theta=0.5, ncrit=64."""
+    from fmm_gb300 import systems
+    s = systems.uniform_triplets(4096, 40.0, seed=0)
+    G = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 64, 5, 1)
+    O = oracle.field_fmm(*_fmm_args(s), 0.5, 64, 5, 1)
+    assert np.all(np.isfinite(G))
+    assert rel_err(G, O) <= TOL
+
+
+@pytest.mark.parametrize("damp,p,f", [("THOLE", 6, 2), ("AMOEBA", 8, 1), ("ERF", 4, 1), ("", 8, 2)])
+def test_fmm_ref_mode_matches_oracle_damped(damp, p, f):
+    """Reference semantics including the int32-wrapped Cnij table at p >= 6."""
+    from fmm_gb300 import systems
+    s = systems.water(800, 40.0, seed=4)
+    if damp == "ERF":
+        s["damping_factors"] = np.random.default_rng(5).uniform(0.3, 0.8, 2400)
+    d = s["damping_factors"] if damp else None
+    G = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, p, f, damp, d)
+    O = oracle.field_fmm(*_fmm_args(s), 0.5, 32, p, f, damp, d)
+    cols = slice(1, None) if damp == "AMOEBA" else slice(0, None)
+    assert rel_err(G, O, cols) <= TOL
+
+
+@pytest.mark.parametrize("damp", ["", "THOLE"])
+def test_fmm_exact_mode_matches_oracle(damp):
+    from fmm_gb300 import systems
+    s = systems.water(1200, 45.0, seed=6)
+    d = s["damping_factors"] if damp else None
+    opt = Options.exact()
+    G = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, 6, 1, damp, d, options=opt)
+    O = oracle.field_fmm(*_fmm_args(s), 0.5, 32, 6, 1, damp, d, coef_mode="exact", excl_mode="mask",
+                         centroid_mode="blocked")
+    assert rel_err(G, O) <= TOL
+
+
+def test_theta_to_zero_is_direct():
+    s = small_system(700, 20.0, seed=7)
+    G = fmm_gb300.field_fmm(*_fmm_args(s), 1e-3, 16, 4, 1)
+    D = fmm_gb300.field_direct(*_fmm_args(s), 1)
+    assert rel_err(G, D) <= 1e-13
+
+
+def test_small_n_falls_back_to_direct():
+    s = small_system(50, 8.0, seed=8)
+    G = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 64, 5, 1)
+    D = fmm_gb300.field_direct(*_fmm_args(s), 1)
+    assert np.array_equal(G, D)
+
+
+def test_exclusion_edge_cases():
+    s = small_system(300, 12.0, seed=9)
+    X, M = s["coordinates"], s["multipoles"]
+    # no exclusion column at all: reference semantics give a non-finite self term
+    E0 = np.zeros((300, 0), dtype=np.int32)
+    F = fmm_gb300.field_direct(0, X, M, E0, 1)
+    assert not np.all(np.isfinite(F))
+    Fm = fmm_gb300.field_direct(0, X, M, E0, 1, options=Options(excl_mode="mask"))
+    Om = oracle.field_direct(0, X, M, E0, 1, excl_mode="mask")
+    assert rel_err(Fm, Om) <= TOL
+    # duplicated and zero-padded entries behave like the set of listed partners
+    E = np.asfortranarray(np.concatenate([s["exclusions"], s["exclusions"][:, :1], np.zeros((300, 1), np.int32)], 1))
+    G = fmm_gb300.field_direct(0, X, M, E, 1)
+    O = oracle.field_direct(0, X, M, E, 1)
+    assert rel_err(G, O) <= TOL
+
+
+def test_invalid_arguments_raise():
+    s = small_system(100, 10.0, seed=10)
+    with pytest.raises(fmm_gb300.FmmError):
+        fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 16, 4, 1, "BOGUS", None)
+    bad = s["exclusions"].copy()
+    bad[0, 0] = 101
+    with pytest.raises(fmm_gb300.FmmError):
+        fmm_gb300.field_direct(0, s["coordinates"], s["multipoles"], bad, 1)
+    with pytest.raises(fmm_gb300.FmmError):
+        fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 16, 4, 1, "", None, True, np.eye(3))
