@@ -37,7 +37,7 @@ Workspace::~Workspace() {
                      &node_val2, &counters,  &scalars,     &front_a,    &front_b,    &far_pairs,  &near_pairs,
                      &far_sorted, &near_sorted, &node_dfs, &far_src,    &near_src,   &sx,         &sy,
                      &sz,        &smc,       &sd,          &fsorted,    &mom,        &loc,        &partial,
-                     &term_off,  &term_abc,  &term_c};
+                     &term_off,  &term_abc,  &term_c, &f32buf};
     for (DevBuf* b : all) b->release();
     if (events_ready)
         for (auto& e : ev) cudaEventDestroy(e);
@@ -180,7 +180,10 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     FMM_TRY(gather_sorted(ws, P, t, st));
     FMM_TRY(launch_p2m_m2m(ws, P, t, p, st));
     cudaEventRecord(ws.ev[3], st);
-    FMM_TRY(launch_p2p_f64(ws, P, t, f, md, st));
+    if (md.precision == 1)
+        FMM_TRY(launch_p2p_f32(ws, P, t, f, st));
+    else
+        FMM_TRY(launch_p2p_f64(ws, P, t, f, md, st));
     FMM_TRY(launch_excl_correction(ws, P, &t, f, md, ws.fsorted.as<double>(), st));
     cudaEventRecord(ws.ev[4], st);
     FMM_TRY(launch_m2l(ws, t, p, md, st));

@@ -81,6 +81,7 @@ struct Workspace {
     DevBuf node_dfs, far_src, near_src;
     // sorted particle data
     DevBuf sx, sy, sz, smc, sd;
+    DevBuf f32buf;  // FP32 particle data of the mixed-precision near field
     DevBuf fsorted;
     // expansions
     DevBuf mom, loc;
@@ -130,6 +131,7 @@ int launch_p2p_f64(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
 int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, cudaStream_t st);
 int launch_m2l(Workspace& ws, const TreeDev& t, int p, const Modes& md, cudaStream_t st);
 int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, int field_order, cudaStream_t st);
+int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, cudaStream_t st);
 int launch_excl_correction(Workspace& ws, const Particles& P, const TreeDev* t, int field_order, const Modes& md,
                            double* d_field_sorted_or_orig, cudaStream_t st);
 int scatter_field(Workspace& ws, const TreeDev& t, int64_t n, int nf, double* d_field, cudaStream_t st);

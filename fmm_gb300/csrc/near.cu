@@ -12,6 +12,7 @@
 
 #include "internal.h"
 #include "pair.cuh"
+#include "dispatch.cuh"
 
 namespace fmm {
 
@@ -184,7 +185,7 @@ __global__ void k_excl_fix(int64_t n, int64_t ntgt, const int64_t* __restrict__ 
                            const double* __restrict__ damp, int damp_type, int excl_mode,
                            const int32_t* __restrict__ pos_of, const int32_t* __restrict__ leaf_of,
                            const int32_t* __restrict__ near_off, const int32_t* __restrict__ near_src,
-                           double* __restrict__ field, int64_t ld) {
+                           double* __restrict__ field, int64_t ld, int near_masked) {
     constexpr int NF = nT(F), NM = nT(M);
     const int64_t ti = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (ti >= ntgt) return;
@@ -215,6 +216,7 @@ __global__ void k_excl_fix(int64_t n, int64_t ntgt, const int64_t* __restrict__ 
         const double a = di * (damp ? damp[j] : 0.0);
         const bool near = fmm ? is_near_leaf(near_off, near_src, leaf_of[ki], leaf_of[pos_of[j]]) : true;
         if (near) {
+            if (near_masked) continue;  // the near-field kernel already skipped this pair
             pair_field_cold<M, F, double>(xi - X[j], yi - X[n + j], zi - X[2 * n + j], a, damp_type, m, sub);
             if (excl_mode == 0) pair_field_cold<M, F, double>(1e10, 1e10, 1e10, a, damp_type, m, add);
         } else if (excl_mode == 1) {
@@ -241,21 +243,6 @@ __global__ void k_scatter(int64_t n, int nf, const uint32_t* __restrict__ perm, 
     const uint32_t o = perm[k];
     for (int f = 0; f < nf; ++f) field[(size_t)f * n + o] = fs[(size_t)f * n + k];
 }
-
-#define FMM_MF_SWITCH(M_, F_, BODY)      \
-    switch ((M_) * 3 + (F_)) {           \
-        case 0: { constexpr int MM = 0, FF = 0; BODY; } break; \
-        case 1: { constexpr int MM = 0, FF = 1; BODY; } break; \
-        case 2: { constexpr int MM = 0, FF = 2; BODY; } break; \
-        case 3: { constexpr int MM = 1, FF = 0; BODY; } break; \
-        case 4: { constexpr int MM = 1, FF = 1; BODY; } break; \
-        case 5: { constexpr int MM = 1, FF = 2; BODY; } break; \
-        case 6: { constexpr int MM = 2, FF = 0; BODY; } break; \
-        case 7: { constexpr int MM = 2, FF = 1; BODY; } break; \
-        case 8: { constexpr int MM = 2, FF = 2; BODY; } break; \
-        default: return FMM_ENOTSUP;     \
-    }                                    \
-    count_launches(1);
 
 }  // namespace
 
@@ -289,7 +276,7 @@ int launch_direct_f64(Workspace& ws, const Particles& P, int field_order, const 
         FMM_MF_SWITCH(m, field_order,
                       (k_excl_fix<MM, FF><<<grid_for(ntgt, 128), 128, 0, st>>>(
                           n, ntgt, d_targets, P.x, mc, P.exw, P.excl, P.damp, P.damp_type, md.excl_mode, nullptr,
-                          nullptr, nullptr, nullptr, d_field, ntgt)));
+                          nullptr, nullptr, nullptr, d_field, ntgt, 0)));
     }
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
@@ -339,7 +326,7 @@ int launch_excl_correction(Workspace& ws, const Particles& P, const TreeDev* t, 
     FMM_MF_SWITCH(m, field_order,
                   (k_excl_fix<MM, FF><<<grid_for(n, 128), 128, 0, st>>>(
                       n, n, nullptr, P.x, mc_orig, P.exw, P.excl, P.damp, P.damp_type, md.excl_mode, t->pos_of,
-                      t->leaf_of, t->near_off, t->near_src, d_field, n)));
+                      t->leaf_of, t->near_off, t->near_src, d_field, n, md.precision == 1 ? 1 : 0)));
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
