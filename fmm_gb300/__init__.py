@@ -34,7 +34,7 @@ class Options:
 
     coef_mode: str = "ref"        # "ref" | "exact"
     excl_mode: str = "ref"        # "ref" (1e10 displacement) | "mask"
-    precision: str = "fp64"       # "fp64" | "mixed"
+    precision: str = "fp64"       # "fp64" | "mixed" | "mixed_near" | "mixed_far"
     centroid_mode: str = "sequential"  # "sequential" | "blocked"
     mac_mode: str = "ref"         # "ref" | "damping"
     selector: str = "fixed"       # "fixed" | "learned"
@@ -52,7 +52,7 @@ class Options:
         o.version = 1
         o.coef_mode = {"ref": 0, "exact": 1}[self.coef_mode]
         o.excl_mode = {"ref": 0, "mask": 1}[self.excl_mode]
-        o.precision = {"fp64": 0, "mixed": 1}[self.precision]
+        o.precision = {"fp64": 0, "mixed": 1, "mixed_near": 2, "mixed_far": 3}[self.precision]
         o.centroid_mode = {"sequential": 0, "blocked": 1}[self.centroid_mode]
         o.mac_mode = {"ref": 0, "damping": 1}[self.mac_mode]
         o.selector = {"fixed": 0, "learned": 1}[self.selector]

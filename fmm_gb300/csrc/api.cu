@@ -37,7 +37,7 @@ Workspace::~Workspace() {
                      &node_val2, &counters,  &scalars,     &front_a,    &front_b,    &far_pairs,  &near_pairs,
                      &far_sorted, &near_sorted, &node_dfs, &far_src,    &near_src,   &sx,         &sy,
                      &sz,        &smc,       &sd,          &fsorted,    &mom,        &loc,        &partial,
-                     &term_off,  &term_abc,  &term_c, &f32buf};
+                     &term_off,  &term_abc,  &term_c, &f32buf, &wred};
     for (DevBuf* b : all) b->release();
     if (events_ready)
         for (auto& e : ev) cudaEventDestroy(e);
@@ -85,7 +85,7 @@ int parse_opts(const fmm_opts* o, Opts* out) {
     if (!o) return FMM_OK;
     if (o->version != 0 && o->version != 1) return FMM_EINVAL;
     if (o->coef_mode < 0 || o->coef_mode > 1 || o->excl_mode < 0 || o->excl_mode > 1 || o->precision < 0 ||
-        o->precision > 1 || o->centroid_mode < 0 || o->centroid_mode > 1 || o->mac_mode < 0 || o->mac_mode > 1 ||
+        o->precision > 3 || o->centroid_mode < 0 || o->centroid_mode > 1 || o->mac_mode < 0 || o->mac_mode > 1 ||
         o->selector < 0 || o->selector > 1)
         return FMM_EINVAL;
     out->coef_mode = o->coef_mode;
@@ -170,17 +170,27 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
             const TreeParams& tp, double* d_field, cudaStream_t st) {
     ensure_events(ws);
     Modes md{o.coef_mode, o.excl_mode, o.precision};
+    if (md.precision != 0) {
+        // the mixed paths mask exclusions in the FP32 loop and use exact tensors
+        md.excl_mode = 1;
+        md.coef_mode = 1;
+    }
+    TreeParams tpl = tp;
+    if (o.mac_mode == 1 && P.damp_type != DAMP_NONE && P.damp) {
+        const double dmin = min_damping_factor(ws, P.damp, P.n, st);
+        tpl.rdamp = damping_range(P.damp_type, dmin * dmin, dim_to_order(P.dim) + f, 0.1 * o.target);
+    }
     TreeDev t;
     const int nf = nT(f);
     cudaEventRecord(ws.ev[0], st);
     FMM_TRY(build_tree(ws, P.x, P.n, tp, t, st));
     cudaEventRecord(ws.ev[1], st);
-    FMM_TRY(build_lists(ws, t, tp, st));
+    FMM_TRY(build_lists(ws, t, tpl, st));
     cudaEventRecord(ws.ev[2], st);
     FMM_TRY(gather_sorted(ws, P, t, st));
     FMM_TRY(launch_p2m_m2m(ws, P, t, p, st));
     cudaEventRecord(ws.ev[3], st);
-    if (md.precision == 1)
+    if (md.precision == 1 || md.precision == 2)
         FMM_TRY(launch_p2p_f32(ws, P, t, f, st));
     else
         FMM_TRY(launch_p2p_f64(ws, P, t, f, md, st));
@@ -312,7 +322,7 @@ int fmm_field_fmm_device(int64_t n, const double* d_X, int mdim, const double* d
         Modes md{o.coef_mode, o.excl_mode, o.precision};
         return launch_direct_f64(ws, P, field_order, md, d_field, o.stream);
     }
-    TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode};
+    TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode, 0.0};
     return run_fmm(ws, P, theta, ncrit, p, field_order, o, tp, d_field, o.stream);
 }
 
@@ -337,7 +347,7 @@ int fmm_field_fmm(int comm, int64_t n, const double* X, int mdim, const double* 
     Particles P;
     FMM_TRY(upload(ws, n, X, mdim, mp, exw, ex, dt != DAMP_NONE ? dampf : nullptr, nf, &P, st));
     P.damp_type = dt;
-    TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode};
+    TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode, 0.0};
     if (o.centroid_mode == 0) {
         host_centroid_sequential(X, n, tp.host_centroid);
         tp.have_host_centroid = 1;

@@ -302,130 +302,6 @@ __global__ void k_m2l_f64(const TreeDev t, const double* __restrict__ mom, doubl
 }
 
 
-// FP32 M2L (mixed precision).  Lengths are scaled by the target's half-width
-// h: with R' = R/h, M~_s = M'_s / h^|s| and L~_f = h^(|f|+1) L_f the
-// contraction keeps its form, L~_f = sum_s (-1)^(|s|+1) M~_s T_{s+f}(R'), and
-// every quantity stays O(1) in FP32 up to tensor order 2p.  Per-pair
-// contributions are summed in FP32 over blocks of 8 sources and the block
-// sums are added in FP64.
-__global__ void k_m2l_f32(const TreeDev t, const double* __restrict__ mom, double* __restrict__ loc, int p) {
-    extern __shared__ double smem[];
-    const int nq = nT(p), N = 2 * p, nqT = nT(N);
-    int* comp = reinterpret_cast<int*>(smem);
-    float* base = reinterpret_cast<float*>(smem + (nqT + 1) / 2 + 1);
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int per_warp = 2 * nqT + nq + (N + 1) + 1;
-    float* TA = base + wib * per_warp;
-    float* TB = TA + nqT;
-    float* ms = TB + nqT;
-    float* gsh = ms + nq;
-    fill_comp(comp, nqT);
-    __syncthreads();
-    const int i = blockIdx.x * (blockDim.x >> 5) + wib;
-    if (i >= t.num_nodes) return;
-    const double cxi = t.cx[i], cyi = t.cy[i], czi = t.cz[i];
-    const double h = t.r[i], ih = 1.0 / h;
-    const int q0 = t.far_off[i], q1 = t.far_off[i + 1];
-    int fcomp[kMaxNPL];
-#pragma unroll
-    for (int r = 0; r < kMaxNPL; ++r) fcomp[r] = (lane + 32 * r < nq) ? comp[lane + 32 * r] : 0;
-    double acc[kMaxNPL];
-    float a32[kMaxNPL];
-#pragma unroll
-    for (int r = 0; r < kMaxNPL; ++r) {
-        acc[r] = 0.0;
-        a32[r] = 0.0f;
-    }
-    // (1/h)^k for the source moments, per lane's entries
-    for (int q = q0; q < q1; ++q) {
-        const int j = t.far_src[q];
-        const float X = (float)((cxi - t.cx[j]) * ih);
-        const float Y = (float)((cyi - t.cy[j]) * ih);
-        const float Z = (float)((czi - t.cz[j]) * ih);
-        for (int s = lane; s < nq; s += 32) {
-            const int k = order_of(s);
-            double v = mom[(size_t)j * nq + s];
-            double sc = 1.0;
-            for (int e = 0; e < k; ++e) sc *= ih;
-            v *= sc;
-            ms[s] = (float)(((k + 1) % 2) ? -v : v);
-        }
-        const float r2 = X * X + Y * Y + Z * Z;
-        const float rinv = rsqrtf(r2);
-        const float rinv2 = rinv * rinv;
-        if (lane <= N) {
-            float v = rinv, c = 1.0f;
-            for (int jj = 1; jj <= lane; ++jj) {
-                v *= rinv2;
-                c *= -(float)(2 * jj - 1);
-            }
-            gsh[lane] = c * v;
-        }
-        __syncwarp();
-        float* A = TA;
-        float* B = TB;
-        if (lane == 0) A[0] = gsh[N];
-        __syncwarp();
-        for (int lev = N - 1; lev >= 0; --lev) {
-            const int lim = nT(N - lev);
-            for (int c = lane; c < lim; c += 32) {
-                float v;
-                if (c == 0) {
-                    v = gsh[lev];
-                } else {
-                    const int cc = comp[c];
-                    const int tx = cx_(cc), ty = cy_(cc), tz = cz_(cc);
-                    if (tx > 0) {
-                        v = X * A[pidx(tx - 1, ty, tz)];
-                        if (tx > 1) v += (float)(tx - 1) * A[pidx(tx - 2, ty, tz)];
-                    } else if (ty > 0) {
-                        v = Y * A[pidx(tx, ty - 1, tz)];
-                        if (ty > 1) v += (float)(ty - 1) * A[pidx(tx, ty - 2, tz)];
-                    } else {
-                        v = Z * A[pidx(tx, ty, tz - 1)];
-                        if (tz > 1) v += (float)(tz - 1) * A[pidx(tx, ty, tz - 2)];
-                    }
-                }
-                B[c] = v;
-            }
-            __syncwarp();
-            float* tmp = A;
-            A = B;
-            B = tmp;
-        }
-#pragma unroll
-        for (int r = 0; r < kMaxNPL; ++r) {
-            if (lane + 32 * r < nq) {
-                const int fx = cx_(fcomp[r]), fy = cy_(fcomp[r]), fz = cz_(fcomp[r]);
-                float a = 0.0f;
-                for (int s = 0; s < nq; ++s) {
-                    const int cs = comp[s];
-                    a += ms[s] * A[pidx(cx_(cs) + fx, cy_(cs) + fy, cz_(cs) + fz)];
-                }
-                a32[r] += a;
-            }
-        }
-        if (((q - q0) & 7) == 7) {
-#pragma unroll
-            for (int r = 0; r < kMaxNPL; ++r) {
-                acc[r] += (double)a32[r];
-                a32[r] = 0.0f;
-            }
-        }
-        __syncwarp();
-    }
-#pragma unroll
-    for (int r = 0; r < kMaxNPL; ++r) {
-        const int fq = lane + 32 * r;
-        if (fq < nq) {
-            const int k = order_of(fq);
-            double sc = ih;
-            for (int e = 0; e < k; ++e) sc *= ih;
-            loc[(size_t)i * nq + fq] = (acc[r] + (double)a32[r]) * sc;
-        }
-    }
-}
-
 // ---------------------------------------------------------------- L2L
 __global__ void k_l2l(const TreeDev t, const int32_t* __restrict__ nodes, int cnt, int p, double* __restrict__ loc) {
     extern __shared__ double smem[];
@@ -609,16 +485,7 @@ int launch_m2l(Workspace& ws, const TreeDev& t, int p, const Modes& md, cudaStre
         FMM_CUDA_TRY(cudaStreamSynchronize(st));
         ws.term_order = N;
     }
-    if (md.precision == 1) {
-        const int per_warp = 2 * nqT + nq + (N + 1) + 1;
-        const int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (100 * 1024) / (sizeof(float) * per_warp)));
-        const size_t sm = comp_bytes(nqT) + sizeof(float) * wpb * per_warp + 16;
-        FMM_TRY(set_smem((const void*)k_m2l_f32, sm));
-        count_launches(1);
-        k_m2l_f32<<<grid_for(t.num_nodes, wpb), 32 * wpb, sm, st>>>(t, ws.mom.as<double>(), ws.loc.as<double>(), p);
-        FMM_CUDA_TRY(cudaGetLastError());
-        return FMM_OK;
-    }
+    if (!ref) return launch_m2l_reduced(ws, t, p, md.precision == 1 || md.precision == 3, st);
     const int per_warp = 2 * nqT + nq + 5 * (N + 1);
     int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (100 * 1024) / (sizeof(double) * per_warp)));
     const size_t sm = comp_bytes(nqT) + sizeof(double) * wpb * per_warp;

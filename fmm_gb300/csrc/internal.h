@@ -61,10 +61,18 @@ struct TreeParams {
     int centroid_mode;     // 0 sequential, 1 blocked
     int have_host_centroid;
     double host_centroid[3];
-    int mac_mode;          // 0 reference MAC
+    int mac_mode;          // 0 reference MAC, 1 also demote pairs within the damping range
+    double rdamp;          // damping range for mac_mode 1 (bohr)
 };
+
+// Distance beyond which the damped kernel's radial derivatives g_j (j <= nmax)
+// differ from the undamped ones by at most eps (relative), for pair damping
+// factor a (smallest a gives the longest range).
+double damping_range(int damp, double a, int nmax, double eps);
 int build_tree(Workspace& ws, const double* d_coords, int64_t n, const TreeParams& tp, TreeDev& t, cudaStream_t st);
 int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st);
+// Smallest damping factor of n particles (device array), 0 if none is positive.
+double min_damping_factor(Workspace& ws, const double* d_damp, int64_t n, cudaStream_t st);
 
 // Host-side sequential centroid (the reference's SUM order).
 void host_centroid_sequential(const double* coords, int64_t n, double c[3]);
@@ -84,7 +92,7 @@ struct Workspace {
     DevBuf f32buf;  // FP32 particle data of the mixed-precision near field
     DevBuf fsorted;
     // expansions
-    DevBuf mom, loc;
+    DevBuf mom, loc, wred;
     // direct-sum partial sums
     DevBuf partial;
     // ref-mode closed-form tensor tables
@@ -130,6 +138,7 @@ int launch_p2p_f64(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
                    cudaStream_t st);
 int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, cudaStream_t st);
 int launch_m2l(Workspace& ws, const TreeDev& t, int p, const Modes& md, cudaStream_t st);
+int launch_m2l_reduced(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaStream_t st);
 int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, int field_order, cudaStream_t st);
 int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, cudaStream_t st);
 int launch_excl_correction(Workspace& ws, const Particles& P, const TreeDev* t, int field_order, const Modes& md,

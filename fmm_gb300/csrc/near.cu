@@ -326,7 +326,8 @@ int launch_excl_correction(Workspace& ws, const Particles& P, const TreeDev* t, 
     FMM_MF_SWITCH(m, field_order,
                   (k_excl_fix<MM, FF><<<grid_for(n, 128), 128, 0, st>>>(
                       n, n, nullptr, P.x, mc_orig, P.exw, P.excl, P.damp, P.damp_type, md.excl_mode, t->pos_of,
-                      t->leaf_of, t->near_off, t->near_src, d_field, n, md.precision == 1 ? 1 : 0)));
+                      t->leaf_of, t->near_off, t->near_src, d_field, n,
+                      (md.precision == 1 || md.precision == 2) ? 1 : 0)));
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }

@@ -157,9 +157,17 @@ __host__ __device__ constexpr double dfact_odd(int j) {  // (2j-1)!!, (-1)!! = 1
 // g_j(r), j = 0..N, of the kernel `damp` at squared distance r2 and pair
 // damping factor a (the product of the two particles' factors).
 template <int N, typename R>
+__host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, R* g);
+
+template <int N, typename R>
 __host__ __device__ __forceinline__ void radial_g(int damp, R r2, R a, R* g) {
+    radial_g_ir<N, R>(damp, r2, Real<R>::rsqrt_(r2), a, g);
+}
+
+// Same, with 1/r supplied by the caller (e.g. a refined FP32 value).
+template <int N, typename R>
+__host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, R* g) {
     using RT = Real<R>;
-    const R ir = RT::rsqrt_(r2);
     const R ir2 = ir * ir;
     if (damp == DAMP_NONE) {
         g[0] = ir;
@@ -327,6 +335,32 @@ __host__ __device__ __forceinline__ void pair_field(R dx, R dy, R dz, R a, int d
     R T[nT(N)];
     md_tensor<N, R>(dx, dy, dz, g, T);
     contract<M, F, R>(T, Mc, acc);
+}
+
+// FP32 pair with an accurate displacement: r^2 is formed with FMA-captured
+// rounding errors and 1/r refined by one Newton step on the compensated r^2,
+// so 1/r carries about one rounding instead of rsqrtf's few.
+template <int M, int F>
+__device__ __forceinline__ void pair_field_f32acc(float dx, float dy, float dz, float a, int damp, const float* Mc,
+                                                  float* acc) {
+    constexpr int N = M + F;
+    const float px = dx * dx, py = dy * dy, pz = dz * dz;
+    const float ex = fmaf(dx, dx, -px), ey = fmaf(dy, dy, -py), ez = fmaf(dz, dz, -pz);
+    const float s1 = px + py;
+    const float e1 = (px - (s1 - (s1 - px))) + (py - (s1 - px));  // two-sum error of px + py
+    const float r2 = s1 + pz;
+    const float e2 = (s1 - (r2 - (r2 - s1))) + (pz - (r2 - s1));
+    const float r2lo = (ex + ey + ez) + (e1 + e2);
+    const float y0 = rsqrtf(r2);
+    const float h = r2 * y0;
+    const float hl = fmaf(r2, y0, -h);
+    const float res = fmaf(-h, y0, 1.0f) - (hl + r2lo * y0) * y0;
+    const float ir = fmaf(0.5f * y0, res, y0);
+    float g[N + 1];
+    radial_g_ir<N, float>(damp, r2, ir, a, g);
+    float T[nT(N)];
+    md_tensor<N, float>(dx, dy, dz, g, T);
+    contract<M, F, float>(T, Mc, acc);
 }
 
 // Out-of-line variant for cold paths (exclusion fix-ups) to keep code size down.

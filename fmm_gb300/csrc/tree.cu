@@ -28,9 +28,11 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "internal.h"
+#include "pair.cuh"
 
 namespace fmm {
 
@@ -98,6 +100,16 @@ __global__ void k_centroid_seq(const double* __restrict__ X, int64_t n, double* 
         cur ^= 1;
     }
     if (threadIdx.x == 0) scalars[blockIdx.x] = __ddiv_rn(s, (double)n);
+}
+
+__global__ void k_min_damp(const double* __restrict__ d, int64_t n, double* out) {
+    double m = 1e300;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = fmin(m, d[i]);
+    typedef cub::BlockReduce<double, 256> BR;
+    __shared__ typename BR::TempStorage tmp;
+    double bm = BR(tmp).Reduce(m, [](double a, double b) { return fmin(a, b); });
+    if (threadIdx.x == 0 && bm >= 0.0) atomicMin(reinterpret_cast<unsigned long long*>(out), __double_as_longlong(bm));
 }
 
 __global__ void k_set_centroid(double* scalars, double c0, double c1, double c2) {
@@ -276,7 +288,8 @@ __global__ void k_pos_of(int64_t n, const uint32_t* __restrict__ perm, int32_t* 
 // counters: [0] next frontier size, [1] far count, [2] near count, [3] overflow flag
 __global__ void k_list_iter(const int2* __restrict__ in, int nin, int2* __restrict__ out, int64_t cap_out,
                             uint64_t* __restrict__ far, int64_t cap_far, uint64_t* __restrict__ nearp,
-                            int64_t cap_near, const TreeDev t, double theta, unsigned long long* counters) {
+                            int64_t cap_near, const TreeDev t, double theta, double rdamp,
+                            unsigned long long* counters) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nin) return;
     const int i = in[q].x, j = in[q].y;
@@ -286,7 +299,13 @@ __global__ void k_list_iter(const int2* __restrict__ in, int nin, int2* __restri
     const double r = norm2_3(dx, dy, dz);
     const double ri = t.rmax[i], rj = t.rmax[j];
     const bool li = t.is_leaf[i] != 0, lj = t.is_leaf[j] != 0;
-    if (__dmul_rn(r, theta) > __dadd_rn(ri, rj)) {
+    bool accept = __dmul_rn(r, theta) > __dadd_rn(ri, rj);
+    if (accept && rdamp > 0.0) {
+        // closest possible particle distance: centre distance minus the cube circumradii
+        const double gap = __dsub_rn(r, __dmul_rn(1.7320508075688772, __dadd_rn(t.r[i], t.r[j])));
+        accept = gap >= rdamp;
+    }
+    if (accept) {
         const unsigned long long k = atomicAdd(&counters[1], 1ull);
         if (k < (unsigned long long)cap_far)
             far[k] = ((uint64_t)(uint32_t)i << 32) | (uint32_t)j;
@@ -378,6 +397,25 @@ int grow_nodes(Workspace& ws, int64_t new_cap, int keep, cudaStream_t st) {
 }
 
 }  // namespace
+
+double damping_range(int damp, double a, int nmax, double eps) {
+    if (damp == DAMP_NONE || !(a > 0.0)) return 0.0;
+    constexpr int NM = 6;
+    nmax = std::min(nmax, NM);
+    const int j0 = damp == DAMP_AMOEBA ? 1 : 0;
+    double last_bad = 0.0;
+    // log-spaced scan of r in [1e-3, 1e5]; the deviation decays monotonically at large r
+    for (int k = 0; k <= 4000; ++k) {
+        const double r = 1e-3 * std::pow(1e8, k / 4000.0);
+        double g[NM + 1], g0[NM + 1];
+        radial_g<NM, double>(damp, r * r, a, g);
+        radial_g<NM, double>(DAMP_NONE, r * r, a, g0);
+        double dev = 0.0;
+        for (int j = j0; j <= nmax; ++j) dev = std::max(dev, std::fabs(g[j] - g0[j]) / std::fabs(g0[j]));
+        if (dev > eps) last_bad = r;
+    }
+    return last_bad * std::pow(1e8, 1.0 / 4000.0);
+}
 
 void host_centroid_sequential(const double* X, int64_t n, double c[3]) {
     for (int d = 0; d < 3; ++d) {
@@ -546,6 +584,19 @@ int build_tree(Workspace& ws, const double* d_X, int64_t n, const TreeParams& tp
     return FMM_OK;
 }
 
+double min_damping_factor(Workspace& ws, const double* d, int64_t n, cudaStream_t st) {
+    if (ws.scalars.ensure(sizeof(double) * (8 + 3 * kLanes)) != FMM_OK) return 0.0;
+    double* out = ws.scalars.as<double>() + 7;
+    const double big = 1e300;
+    if (cudaMemcpyAsync(out, &big, sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess) return 0.0;
+    count_launches(1);
+    k_min_damp<<<(unsigned)std::min<int64_t>(1024, grid_for(n, 256)), 256, 0, st>>>(d, n, out);
+    double h = 0.0;
+    if (cudaMemcpyAsync(&h, out, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess) return 0.0;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return 0.0;
+    return h >= 1e299 ? 0.0 : h;
+}
+
 int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st) {
     const int M = t.num_nodes;
     int64_t cap_front = std::max<int64_t>(4096, 64LL * M);
@@ -570,7 +621,8 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
             count_launches(1);
             k_list_iter<<<grid_for(nin, 256), 256, 0, st>>>(fin, (int)nin, fout, cap_front,
                                                              ws.far_pairs.as<uint64_t>(), cap_far,
-                                                             ws.near_pairs.as<uint64_t>(), cap_near, t, tp.theta, ctr);
+                                                             ws.near_pairs.as<uint64_t>(), cap_near, t, tp.theta,
+                                                             tp.mac_mode == 1 ? tp.rdamp : 0.0, ctr);
             FMM_CUDA_TRY(cudaMemcpyAsync(h, ctr, sizeof(h), cudaMemcpyDeviceToHost, st));
             FMM_CUDA_TRY(cudaStreamSynchronize(st));
             if (h[3]) {

@@ -59,7 +59,8 @@ typedef struct fmm_opts {
                            1 mask: excluded pairs and the self pair skipped; excluded pairs
                                that the far field counted are subtracted again           */
     int precision;      /* 0 fp64; 1 mixed: FP32 near field and M2L with blocked FP64
-                           accumulation, FP64 tree, M2M/L2L and final sums               */
+                           accumulation, FP64 tree, M2M/L2L and final sums;
+                           2 FP32 near field only; 3 FP32 M2L only                       */
     int centroid_mode;  /* 0 sequential sum (as the reference), 1 blocked (1024 lanes)       */
     int mac_mode;       /* 0 reference MAC (r*theta > rmax_i + rmax_j)
                            1 damping-aware: additionally demote cell pairs whose closest

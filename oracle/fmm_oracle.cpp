@@ -56,6 +56,8 @@ struct OracleOpts {
     int excl_mode;      // 0 ref1e10, 1 mask
     int centroid_mode;  // 0 sequential, 1 blocked(1024 lanes)
     int nthreads;       // <=0: library default
+    int mac_mode;       // 0 reference MAC, 1 also demote pairs within the damping range
+    double target_rel_err;
 };
 }
 
@@ -371,6 +373,8 @@ struct Ctx {
     int coef_mode = 0;
     int excl_mode = 0;
     int centroid_mode = 0;
+    int mac_mode = 0;
+    double target = 1e-6;
     Cnij cn;  // table for the closed-form tensors
     void ensure_cnij(int maxo) {
         if (cn.maxo < maxo) cn = make_cnij(maxo, coef_mode == 0);
@@ -577,7 +581,29 @@ int build_tree(const double* X, int64_t n, int ncrit, int centroid_mode, Tree& t
     return OK;
 }
 
-// interact_fmm (fmm.F90:352-385), non-periodic.
+// Distance beyond which the damped g_j (j <= nmax) deviate from the undamped
+// ones by at most eps (relative): scan of r on a fixed log grid.
+double damping_range(int damp, double a, int nmax, double eps) {
+    if (damp == DAMP_NONE || !(a > 0.0)) return 0.0;
+    nmax = std::min(nmax, 6);
+    const int j0 = damp == DAMP_AMOEBA ? 1 : 0;
+    double last_bad = 0.0;
+    double g[7], g0[7];
+    for (int k = 0; k <= 4000; ++k) {
+        const double r = 1e-3 * std::pow(1e8, k / 4000.0);
+        radial_g(damp, r, a, 6, g);
+        radial_g(DAMP_NONE, r, a, 6, g0);
+        double dev = 0.0;
+        for (int j = j0; j <= nmax; ++j) dev = std::max(dev, std::fabs(g[j] - g0[j]) / std::fabs(g0[j]));
+        if (dev > eps) last_bad = r;
+    }
+    return last_bad * std::pow(1e8, 1.0 / 4000.0);
+}
+
+// interact_fmm (fmm.F90:352-385), non-periodic.  With rdamp > 0 a pair that
+// passes the reference test is still refused when its closest possible
+// particle distance is inside the damping range.
+double g_rdamp = 0.0;
 void interact(Tree& t, int i, int j, double theta) {
     const Node& a = t.nd[i];
     const Node& b = t.nd[j];
@@ -585,7 +611,9 @@ void interact(Tree& t, int i, int j, double theta) {
     double dy = a.c[1] - (b.c[1] + 0.0);
     double dz = a.c[2] - (b.c[2] + 0.0);
     double r = norm2_3(dx, dy, dz);
-    if (r * theta > a.rmax + b.rmax) {
+    bool accept = r * theta > a.rmax + b.rmax;
+    if (accept && g_rdamp > 0.0) accept = (r - 1.7320508075688772 * (a.r + b.r)) >= g_rdamp;
+    if (accept) {
         t.far[a.idx].push_back(b.idx);
     } else if (a.terminal && b.terminal) {
         t.nearl[a.idx].push_back(b.idx);
@@ -598,7 +626,8 @@ void interact(Tree& t, int i, int j, double theta) {
     }
 }
 
-void build_lists(Tree& t, double theta) {
+void build_lists(Tree& t, double theta, double rdamp = 0.0) {
+    g_rdamp = rdamp;
     size_t M = t.nd.size();
     t.far.assign(M, {});
     t.nearl.assign(M, {});
@@ -690,7 +719,13 @@ int run_fmm(const Problem& P, double theta, int ncrit, int p, const Ctx& ctx0, d
     Tree t;
     int st = build_tree(P.X, n, ncrit, ctx.centroid_mode, t);
     if (st) return st;
-    build_lists(t, theta);
+    double rdamp = 0.0;
+    if (ctx.mac_mode == 1 && P.damp != DAMP_NONE) {
+        double dmin = 1e300;
+        for (int64_t q = 0; q < n; ++q) dmin = std::min(dmin, P.dampf[q]);
+        rdamp = damping_range(P.damp, dmin * dmin, pm + P.pf, 0.1 * ctx.target);
+    }
+    build_lists(t, theta, rdamp);
     int M = (int)t.nd.size();
     int ms = nT(p);
     // leaf id of every particle
@@ -935,6 +970,8 @@ Ctx make_ctx(const OracleOpts* o) {
         c.coef_mode = o->coef_mode;
         c.excl_mode = o->excl_mode;
         c.centroid_mode = o->centroid_mode;
+        c.mac_mode = o->mac_mode;
+        c.target = o->target_rel_err > 0 ? o->target_rel_err : 1e-6;
     }
     return c;
 }

@@ -19,7 +19,8 @@ DAMP = {"": 0, "AMOEBA": 1, "THOLE": 2, "ERF": 3}
 
 class _Opts(ctypes.Structure):
     _fields_ = [("coef_mode", ctypes.c_int), ("excl_mode", ctypes.c_int),
-                ("centroid_mode", ctypes.c_int), ("nthreads", ctypes.c_int)]
+                ("centroid_mode", ctypes.c_int), ("nthreads", ctypes.c_int), ("mac_mode", ctypes.c_int),
+                ("target_rel_err", ctypes.c_double)]
 
 
 _lib = None
@@ -62,9 +63,11 @@ def _ip(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
 
 
-def _opts(coef_mode="ref", excl_mode="ref", centroid_mode="sequential", nthreads=0):
+def _opts(coef_mode="ref", excl_mode="ref", centroid_mode="sequential", nthreads=0, mac_mode="ref",
+          target_rel_err=1e-6):
     return _Opts({"ref": 0, "exact": 1}[coef_mode], {"ref": 0, "mask": 1}[excl_mode],
-                 {"sequential": 0, "blocked": 1}[centroid_mode], int(nthreads))
+                 {"sequential": 0, "blocked": 1}[centroid_mode], int(nthreads), {"ref": 0, "damping": 1}[mac_mode],
+                 float(target_rel_err))
 
 
 def _prep(coordinates, multipoles, exclusions, damp_type, damping_factors):

@@ -168,3 +168,45 @@ def test_invalid_arguments_raise():
         fmm_gb300.field_direct(0, s["coordinates"], s["multipoles"], bad, 1)
     with pytest.raises(fmm_gb300.FmmError):
         fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 16, 4, 1, "", None, True, np.eye(3))
+
+
+@pytest.mark.parametrize("damp", ["AMOEBA", "THOLE", "ERF"])
+def test_damping_aware_acceptance_matches_oracle(damp):
+    """mac_mode 'damping': far-field pairs closer than the damping range are
+    demoted to the near field; same lists and fields as the oracle."""
+    from fmm_gb300 import systems
+    s = systems.water(1500, 50.0, seed=12)
+    if damp == "ERF":
+        s["damping_factors"] = np.random.default_rng(13).uniform(0.3, 0.8, 4500)
+    d = s["damping_factors"]
+    opt = Options.exact(mac_mode="damping")
+    G = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, 6, 1, damp, d, options=opt)
+    O = oracle.field_fmm(*_fmm_args(s), 0.5, 32, 6, 1, damp, d, coef_mode="exact", excl_mode="mask",
+                         centroid_mode="blocked", mac_mode="damping")
+    assert rel_err(G, O) <= TOL
+    st = fmm_gb300.last_stats()
+    G0 = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, 6, 1, damp, d, options=Options.exact())
+    st0 = fmm_gb300.last_stats()
+    assert st["p2p_particle_pairs"] > st0["p2p_particle_pairs"]
+    D = fmm_gb300.field_direct(*_fmm_args(s), 1, damp, d, options=Options(excl_mode="mask"))
+    assert rel_err(G, D, slice(1, 4)) < rel_err(G0, D, slice(1, 4))
+
+
+@pytest.mark.parametrize("damp,mf", [("AMOEBA", (2, 1)), ("", (2, 2)), ("ERF", (1, 1)), ("THOLE", (0, 1))])
+def test_mixed_precision_close_to_fp64(damp, mf):
+    """FP32 near field and M2L with FP64 sums: within FP32 accuracy of the FP64
+    path on the same tree and lists."""
+    from fmm_gb300 import systems
+    m, f = mf
+    s = systems.water(4000, 70.0, order=m, seed=14)
+    if damp == "ERF":
+        s["damping_factors"] = np.random.default_rng(15).uniform(0.3, 0.8, 12000)
+    d = s["damping_factors"] if damp else None
+    F64 = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 64, 8, f, damp, d, options=Options.exact())
+    F32 = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 64, 8, f, damp, d, options=Options.exact(precision="mixed"))
+    assert np.all(np.isfinite(F32))
+    # field columns (order >= 1); the potential column of a neutral system is a
+    # sum with heavy cancellation and is not part of the accuracy target.  The
+    # bound is the FP32 floor of a system of neutral groups of large charges
+    # (per-pair rounding ~1e-7, amplified by the cancellation inside groups).
+    assert rel_err(F32, F64, slice(1, None)) < 5e-6
