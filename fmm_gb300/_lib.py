@@ -45,6 +45,7 @@ EXPORTED = [
     "fmm_field_direct_device",
     "fmm_field_fmm_device",
     "fmm_field_direct_targets_device",
+    "fmm_field_direct_targets_noalloc",
     "fmm_last_stats",
     "fmm_debug_tree",
     "fmm_measure_fma_peak",
@@ -86,6 +87,7 @@ def lib():
     L.fmm_field_direct_targets_device.argtypes = [i64, ctypes.c_void_p, c, ctypes.c_void_p, c, ctypes.c_void_p,
                                                   i64, ctypes.c_void_p, c, ctypes.c_void_p, cs, c,
                                                   ctypes.c_void_p, op]
+    L.fmm_field_direct_targets_noalloc.argtypes = L.fmm_field_direct_targets_device.argtypes
     L.fmm_last_stats.argtypes = [d, c]
     L.fmm_measure_fma_peak.argtypes = [c, d]
     L.fmm_launch_count.restype = ctypes.c_int64
@@ -94,7 +96,8 @@ def lib():
     L.fmm_strerror.argtypes = [c]
     L.fmm_version.restype = ctypes.c_char_p
     for name in ("fmm_field_direct", "fmm_field_fmm", "fmm_field_direct_device", "fmm_field_fmm_device",
-                 "fmm_field_direct_targets_device", "fmm_last_stats", "fmm_measure_fma_peak"):
+                 "fmm_field_direct_targets_device", "fmm_field_direct_targets_noalloc", "fmm_last_stats",
+                 "fmm_measure_fma_peak"):
         getattr(L, name).restype = c
     _lib = L
     return L

@@ -109,6 +109,28 @@ int fmm_field_direct_targets_device(int64_t n, const double *d_coordinates, int 
                                     int field_order, double *d_field, const char *damp, int damp_len,
                                     const double *d_damping_factors, const fmm_opts *opts);
 
+/* Allocation-free variant of fmm_field_direct_targets_device (no counterpart
+ * in the reference).  For callers that cannot let a library allocate device
+ * memory: host programs whose memory manager already owns the device (a
+ * framework's caching allocator, a simulation code that reserved its pools up
+ * front) and code that must avoid the implicit synchronisation cudaMalloc and
+ * cudaFree can cause.  The caller passes the same device inputs and the output
+ * array; the only scratch is a fixed 4 MiB static device array inside this
+ * library (present on every GPU that loads it, until the process exits), so
+ * ntgt * nT(field_order) may be at most FMM_NOALLOC_MAX_VALUES, otherwise the
+ * call returns FMM_EINVAL without doing any work.  The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  All calls share the array, so calls
+ * whose work overlaps on the GPU (different streams, threads or captured
+ * graphs in flight) race and must be serialised by the caller.  The call
+ * blocks until its stream has finished (it reads a status word back).
+ * Supports opts->excl_mode and opts->stream; other options are ignored. */
+#define FMM_NOALLOC_MAX_VALUES 524256
+int fmm_field_direct_targets_noalloc(int64_t n, const double *d_coordinates, int mdim, const double *d_multipoles,
+                                     int exw, const int32_t *d_exclusions, int64_t ntgt, const int64_t *d_targets,
+                                     int field_order, double *d_field, const char *damp, int damp_len,
+                                     const double *d_damping_factors, const fmm_opts *opts);
+
 /* Statistics of the last fmm_field_fmm* call on this thread: tree and list
  * sizes and per-phase device times in milliseconds.  `out` receives up to
  * `len` doubles in this order: num_nodes, num_leaves, max_depth, m2l_pairs,
