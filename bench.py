@@ -38,8 +38,18 @@ sys.path.insert(0, ROOT)
 METRIC = "field_fmm particles/s at N=1M: learned+mixed vs plain FP64 GPU @1e-6 rel err"
 N_MOL = 333_333
 BOX = 270.0
-THETA, NCRIT, P_ORDER, F_ORDER = 0.5, 64, 8, 1
+NCRIT, F_ORDER = 64, 1
 DAMP = "AMOEBA"
+# The reference's own settings (theta 0.5, p 8) give RMS ~2e-4 on this system
+# (the undamped far field and the loose acceptance test); the fixed rule below
+# is the cheapest one measured to reach <= 1e-6 RMS in FP64 and in mixed
+# precision: damping-aware acceptance, theta 0.3, expansion order 10.
+ARMS = {
+    "fp64": dict(theta=0.3, p=10, precision="fp64", mac_mode="damping", selector="fixed"),
+    "mixed": dict(theta=0.3, p=10, precision="mixed", mac_mode="damping", selector="fixed"),
+    "learned": dict(theta=0.3, p=10, precision="mixed", mac_mode="damping", selector="learned"),
+}
+REF_SETTINGS = dict(theta=0.5, p=8)  # the reference's rule, used for the CPU baseline
 
 
 def n_t(k):
@@ -59,10 +69,14 @@ def m2l_flops(p):
 
 
 def workload_config(arm):
+    a = ARMS.get(arm, dict(theta=REF_SETTINGS["theta"], p=REF_SETTINGS["p"]))
     return {
         "workload": "water-like triplets N=999,999 in a 270 bohr cube, AMOEBA damping, multipoles order 2, "
-                    "field_order 1, theta 0.5, ncrit 64, expansion_order 8",
+                    "field_order 1, ncrit 64",
         "arm": arm,
+        "theta": a["theta"],
+        "expansion_order": a["p"],
+        "settings": {k: v for k, v in a.items() if k not in ("theta", "p")},
         "n_particles": 3 * N_MOL,
         "l2": "inputs plus working set > 129 MB L2; a 256 MB buffer is also written between timed steps",
         "accuracy_oracle": "FP64 GPU direct sum on 8192 random particles, field columns of order >= 1",
@@ -130,13 +144,18 @@ def make_system(seed=0, n_mol=N_MOL, box=BOX):
 
 def arm_options(arm):
     from fmm_gb300 import Options
-    if arm == "fp64":
-        return Options.exact(precision="fp64")
-    if arm == "mixed":
-        return Options.exact(precision="mixed", mac_mode="damping")
-    if arm == "learned":
-        return Options.exact(precision="mixed", mac_mode="damping", selector="learned")
-    raise ValueError(arm)
+    a = ARMS[arm]
+    return Options.exact(precision=a["precision"], mac_mode=a["mac_mode"], selector=a["selector"])
+
+
+def m2l_reduced_flops(p):
+    """FLOPs one reduced-basis M2L pair executes: contraction over (p+1)^2
+    sources and outputs, the restricted tensor recursion (z-index <= 2, orders
+    <= 2p) and the scaling of the source weights."""
+    N = 2 * p
+    rb = lambda n: 0 if n == 0 else 1 + 3 * (n - 1) * n // 2
+    recursion = sum(rb(N - lev + 1) for lev in range(N))
+    return 2 * (p + 1) ** 4 + 2 * recursion + (p + 1) ** 2
 
 
 def cpu_sample(n_mol=10_000, threads=None):
@@ -148,11 +167,13 @@ def cpu_sample(n_mol=10_000, threads=None):
     args = (0, s["coordinates"], s["multipoles"], s["exclusions"])
     nth = threads or os.cpu_count() or 1
     t0 = time.perf_counter()
-    oracle.field_fmm(*args, THETA, NCRIT, P_ORDER, F_ORDER, DAMP, s["damping_factors"], nthreads=nth)
+    oracle.field_fmm(*args, REF_SETTINGS["theta"], NCRIT, REF_SETTINGS["p"], F_ORDER, DAMP, s["damping_factors"],
+                     nthreads=nth)
     dt = time.perf_counter() - t0
-    return 3 * n_mol / dt, nth, ("oracle field_fmm (reference semantics: int32 Cnij, 1e10 exclusions) on N=%d "
-                                 "water-like particles at the benchmark density (%.1f bohr cube), AMOEBA, p=8, f=1, "
-                                 "%.2f s" % (3 * n_mol, box, dt))
+    return 3 * n_mol / dt, nth, ("oracle field_fmm with the reference's semantics and settings (int32 Cnij, 1e10 "
+                                 "exclusions, theta 0.5, p 8) on N=%d water-like particles at the benchmark density "
+                                 "(%.1f bohr cube), AMOEBA, f=1, %d OpenMP threads, %.2f s"
+                                 % (3 * n_mol, box, nth, dt))
 
 
 def run_reference(args, rank, world):
@@ -181,7 +202,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--arm", default="fp64", choices=["fp64", "mixed", "learned"])
+    ap.add_argument("--arm", default="mixed", choices=list(ARMS))
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP64 comparison arm")
+    ap.add_argument("--profile", action="store_true", help="only the untimed/timed device steps (for ncu)")
     ap.add_argument("--ref-sample", type=int, default=10_000, help="molecules in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-mol", type=int, default=N_MOL)
@@ -230,12 +253,20 @@ def main():
 
     X, M, E = Shape(tX, n, 3), Shape(tM, n, 10), Shape(tE, n, 3)
 
-    def step():
-        fmm_gb300.field_fmm_device(X, M, E, THETA, NCRIT, P_ORDER, F_ORDER, tF, DAMP, tD, options=opts)
+    arm = ARMS[args.arm]
+
+    def step(a=arm, o=opts):
+        fmm_gb300.field_fmm_device(X, M, E, a["theta"], NCRIT, a["p"], F_ORDER, tF, DAMP, tD, options=o)
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    if args.profile:
+        for _ in range(args.steps):
+            step()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_run": args.arm, "n": n, "stats": fmm_gb300.last_stats()}), flush=True)
+        return
     if dist:
         dist.barrier()
     l0 = L.fmm_launch_count()
@@ -273,6 +304,7 @@ def main():
         return
 
     # accuracy against the FP64 direct sum on 8192 random particles
+    Fgot_all = tF.cpu().numpy().reshape(nf, n).T
     rng = np.random.default_rng(123)
     tgt = np.sort(rng.choice(n, size=min(8192, n), replace=False)).astype(np.int64)
     tT = torch.from_numpy(tgt).to(dev)
@@ -287,20 +319,24 @@ def main():
     _lib.check(st_, "direct on sampled targets")
     torch.cuda.synchronize()
     Fref = tRef.cpu().numpy().reshape(nf, -1).T
-    Fgot = tF.cpu().numpy().reshape(nf, n).T[tgt]
-    d = np.linalg.norm(Fgot[:, 1:] - Fref[:, 1:], axis=1)
-    g = np.linalg.norm(Fref[:, 1:], axis=1)
-    per = d / g
-    accuracy = {"rms_rel_err": float(np.sqrt(np.mean(per ** 2))), "max_rel_err": float(per.max()),
+
+    def accuracy_of(Fall):
+        Fgot = Fall[tgt]
+        d = np.linalg.norm(Fgot[:, 1:] - Fref[:, 1:], axis=1)
+        g = np.linalg.norm(Fref[:, 1:], axis=1)
+        per = d / g
+        return {"rms_rel_err": float(np.sqrt(np.mean(per ** 2))), "max_rel_err": float(per.max()),
                 "global_rel_err": float(np.linalg.norm(d) / np.linalg.norm(g)), "targets": int(len(tgt))}
+
+    accuracy = accuracy_of(Fgot_all)
 
     # end to end through the host C ABI (pageable host buffers, copies timed)
     e2e_times = []
     Fh = None
     for k in range(2 + args.steps):
         t0 = time.perf_counter()
-        Fh = fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"], THETA, NCRIT, P_ORDER,
-                                 F_ORDER, DAMP, s["damping_factors"], options=arm_options(args.arm))
+        Fh = fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"], arm["theta"], NCRIT,
+                                 arm["p"], F_ORDER, DAMP, s["damping_factors"], options=arm_options(args.arm))
         if k >= 2:
             e2e_times.append(time.perf_counter() - t0)
     h2d = 8 * (3 * n + 10 * n + n) + 4 * 3 * n
@@ -313,15 +349,40 @@ def main():
     peak = ctypes.c_double(0)
     _lib.check(L.fmm_measure_fma_peak(prec, ctypes.byref(peak)), "fma peak")
     p2p_pairs = stats["p2p_particle_pairs"] - n
-    flops = {"t_p2p": p2p_pairs * pair_flops(2, F_ORDER), "t_m2l": stats["m2l_pairs"] * m2l_flops(P_ORDER)}
+    flops = {"t_p2p": p2p_pairs * pair_flops(2, F_ORDER), "t_m2l": stats["m2l_pairs"] * m2l_reduced_flops(arm["p"])}
     dom = max(flops, key=lambda k: phase[k])
     achieved = flops[dom] / (phase[dom] * 1e-3) / 1e12
-    roofline = {"bound": "fp64" if prec == 0 else "fp32", "kernel": {"t_p2p": "k_p2p", "t_m2l": "k_m2l"}[dom],
+    kname = {"t_p2p": "k_p2p_f32" if prec else "k_p2p_f64", "t_m2l": "k_m2l_red<float>" if prec else "k_m2l_red<double>"}
+    roofline = {"bound": "fp64" if prec == 0 else "fp32", "kernel": kname[dom],
                 "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
-                "peak_source": "measured live by fmm_measure_fma_peak (FMA loop over all SMs); MEASURED_PEAKS.json "
-                               "has no CUDA-core figure",
-                "algorithmic_flops_per_launch": flops[dom], "traffic": None,
-                "phase_ms": {k: round(v, 3) for k, v in phase.items()}}
+                "peak_source": "measured live by fmm_measure_fma_peak (register FMA loop on all SMs); "
+                               "MEASURED_PEAKS.json has only HBM and bf16 tensor figures",
+                "algorithmic_flops_per_launch": flops[dom],
+                "flop_convention": "P2P pair 2*nT(f)*nT(m)+2*C(m+f+4,4)+12; M2L pair as executed by the reduced basis "
+                                   "2*(p+1)^4 + recursion; full-Cartesian convention would be %.3g per pair"
+                                   % m2l_flops(arm["p"]),
+                "traffic": None, "phase_ms": {k: round(v, 3) for k, v in phase.items()}}
+
+    compare = None
+    if args.arm != "fp64" and not args.no_compare:
+        # plain FP64 GPU arm: same workload, fixed rule, FP64 everywhere
+        o64 = arm_options("fp64")
+        o64.stream = stream.cuda_stream
+        step(ARMS["fp64"], o64)
+        torch.cuda.synchronize()
+        t64 = []
+        for _ in range(2):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step(ARMS["fp64"], o64)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t64.append(e0.elapsed_time(e1))
+        acc64 = accuracy_of(tF.cpu().numpy().reshape(nf, n).T)
+        v64 = n / (float(np.mean(t64)) * 1e-3)
+        compare = {"arm": "fp64", "value": v64, "unit": "particles/s", "ms_per_step": float(np.mean(t64)),
+                   "accuracy": acc64, "speedup_of_this_arm": value / v64, "settings": ARMS["fp64"]}
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -332,7 +393,8 @@ def main():
         "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.arm == "fp64" else "f32+f64", "data": "synthetic", "config": workload_config(args.arm),
-        "accuracy": accuracy, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+        "accuracy": accuracy, "e2e": e2e, "roofline": roofline, "plain_fp64": compare, "cpu_baseline": cpu,
+        "clocks": clk.summary(),
         "gpu_launches": int(launches),
         "tree": {k: stats[k] for k in ("num_nodes", "num_leaves", "max_depth", "m2l_pairs", "p2p_leaf_pairs",
                                        "p2p_particle_pairs")},

@@ -120,6 +120,24 @@ __global__ void k_check_excl(int64_t total, int64_t n, const int32_t* __restrict
         if (ex[q] < 0 || ex[q] > n) atomicExch(bad, 1);
 }
 
+__global__ void k_check_targets(int64_t ntgt, int64_t n, const int64_t* __restrict__ tg, int* bad) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ntgt; q += (int64_t)gridDim.x * blockDim.x)
+        if (tg[q] < 0 || tg[q] >= n) atomicExch(bad, 1);
+}
+
+// Validates device-resident target indices (0..n-1).
+int check_targets_device(Workspace& ws, int64_t n, int64_t ntgt, const int64_t* d_t, cudaStream_t st) {
+    FMM_TRY(ws.counters.ensure(sizeof(unsigned long long) * 16));
+    int* flag = reinterpret_cast<int*>(ws.counters.as<unsigned long long>() + 13);
+    FMM_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    count_launches(1);
+    k_check_targets<<<(unsigned)std::min<int64_t>(4096, (ntgt + 255) / 256), 256, 0, st>>>(ntgt, n, d_t, flag);
+    int h = 0;
+    FMM_CUDA_TRY(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FMM_CUDA_TRY(cudaStreamSynchronize(st));
+    return h ? FMM_EINVAL : FMM_OK;
+}
+
 // Validates device-resident exclusion indices (0 or 1..n) before any kernel uses them.
 int check_exclusions_device(Workspace& ws, int64_t n, int exw, const int32_t* d_ex, cudaStream_t st) {
     if (exw == 0) return FMM_OK;
@@ -169,6 +187,7 @@ int upload(Workspace& ws, int64_t n, const double* X, int mdim, const double* mp
 int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, int f, const Opts& o,
             const TreeParams& tp, double* d_field, cudaStream_t st) {
     ensure_events(ws);
+    if (o.selector == 1) return FMM_ENOTSUP;  // learned selector: not built yet
     Modes md{o.coef_mode, o.excl_mode, o.precision};
     if (md.precision != 0) {
         // the mixed paths mask exclusions in the FP32 loop and use exact tensors
@@ -300,6 +319,7 @@ int fmm_field_direct_targets_device(int64_t n, const double* d_X, int mdim, cons
     FMM_TRY(parse_opts(opts, &o));
     Workspace& ws = thread_workspace();
     FMM_TRY(check_exclusions_device(ws, n, exw, d_ex, o.stream));
+    FMM_TRY(check_targets_device(ws, n, ntgt, d_targets, o.stream));
     Particles P{n, d_X, mdim, d_mp, exw, d_ex, dt != DAMP_NONE ? d_damp : nullptr, dt};
     Modes md{o.coef_mode, o.excl_mode, o.precision};
     return launch_direct_f64(ws, P, field_order, md, d_field, o.stream, ntgt, d_targets);
