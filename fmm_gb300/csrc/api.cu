@@ -37,7 +37,7 @@ Workspace::~Workspace() {
                      &node_val2, &counters,  &scalars,     &front_a,    &front_b,    &far_pairs,  &near_pairs,
                      &far_sorted, &near_sorted, &node_dfs, &far_src,    &near_src,   &sx,         &sy,
                      &sz,        &smc,       &sd,          &fsorted,    &mom,        &loc,        &partial,
-                     &term_off,  &term_abc,  &term_c, &f32buf, &wred};
+                     &term_off,  &term_abc,  &term_c, &f32buf, &wred, &far_ord, &sel_norms, &sel_params, &sel_scratch};
     for (DevBuf* b : all) b->release();
     if (events_ready)
         for (auto& e : ev) cudaEventDestroy(e);
@@ -342,7 +342,7 @@ int fmm_field_fmm_device(int64_t n, const double* d_X, int mdim, const double* d
         Modes md{o.coef_mode, o.excl_mode, o.precision};
         return launch_direct_f64(ws, P, field_order, md, d_field, o.stream);
     }
-    TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode, 0.0};
+    TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode, 0.0, p};
     return run_fmm(ws, P, theta, ncrit, p, field_order, o, tp, d_field, o.stream);
 }
 
@@ -367,7 +367,7 @@ int fmm_field_fmm(int comm, int64_t n, const double* X, int mdim, const double* 
     Particles P;
     FMM_TRY(upload(ws, n, X, mdim, mp, exw, ex, dt != DAMP_NONE ? dampf : nullptr, nf, &P, st));
     P.damp_type = dt;
-    TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode, 0.0};
+    TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode, 0.0, p};
     if (o.centroid_mode == 0) {
         host_centroid_sequential(X, n, tp.host_centroid);
         tp.have_host_centroid = 1;

@@ -68,7 +68,7 @@ int fmm_debug_tree(int64_t n, const double* X, int ncrit, double theta, int cent
     cudaStream_t st = nullptr;
     FMM_TRY(ws.in_coords.ensure(sizeof(double) * 3 * n));
     FMM_CUDA_TRY(cudaMemcpy(ws.in_coords.p, X, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
-    TreeParams tp{ncrit, theta, centroid_mode, 0, {0, 0, 0}, 0, 0.0};
+    TreeParams tp{ncrit, theta, centroid_mode, 0, {0, 0, 0}, 0, 0.0, 0};
     if (centroid_mode == 0) {
         host_centroid_sequential(X, n, tp.host_centroid);
         tp.have_host_centroid = 1;

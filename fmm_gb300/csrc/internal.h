@@ -49,6 +49,7 @@ struct TreeDev {
     int64_t nfar = 0, nnear = 0;
     int64_t near_particle_pairs = 0;
     int32_t *far_off = nullptr, *far_src = nullptr;
+    uint8_t* far_ord = nullptr;  // expansion order of each far pair
     int32_t *near_off = nullptr, *near_src = nullptr;
 };
 
@@ -63,6 +64,14 @@ struct TreeParams {
     double host_centroid[3];
     int mac_mode;          // 0 reference MAC, 1 also demote pairs within the damping range
     double rdamp;          // damping range for mac_mode 1 (bohr)
+    int order;             // expansion order stored with every far pair (fixed rule)
+    // learned acceptance (selector); null params = fixed rule
+    const float* sel_params = nullptr;  // MLP parameter blob (device)
+    const float* sel_lnorm = nullptr;   // per node log10 norms of reduced weights by order
+    const float* sel_dmin = nullptr;    // per node smallest damping factor
+    int sel_P = 0;                      // order of the stored norms
+    float sel_log_budget = 0.0f;        // log10 of the per-pair error budget
+    double sel_theta = 0.0;             // loose acceptance test applied before the network
 };
 
 // Distance beyond which the damped kernel's radial derivatives g_j (j <= nmax)
@@ -86,7 +95,8 @@ struct Workspace {
     DevBuf node_d, node_i, child, level_nodes, leaves, node_key, node_val, node_key2, node_val2;
     DevBuf counters, scalars;
     DevBuf front_a, front_b, far_pairs, near_pairs, far_sorted, near_sorted;
-    DevBuf node_dfs, far_src, near_src;
+    DevBuf node_dfs, far_src, near_src, far_ord;
+    DevBuf sel_norms, sel_params, sel_scratch;
     // sorted particle data
     DevBuf sx, sy, sz, smc, sd;
     DevBuf f32buf;  // FP32 particle data of the mixed-precision near field
@@ -139,6 +149,12 @@ int launch_p2p_f64(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
 int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, cudaStream_t st);
 int launch_m2l(Workspace& ws, const TreeDev& t, int p, const Modes& md, cudaStream_t st);
 int launch_m2l_reduced(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaStream_t st);
+int launch_reduce_moments(Workspace& ws, const TreeDev& t, int p, cudaStream_t st);
+// selector.cu
+int selector_node_norms(Workspace& ws, const TreeDev& t, int P, const double* d_sorted_damp, cudaStream_t st);
+int selector_pair_data(Workspace& ws, const Particles& Pt, const TreeDev& t, int P, const int2* d_pairs, int npairs,
+                       float* d_feats, float* d_labels, cudaStream_t st);
+int selector_unpack_far(Workspace& ws, const TreeDev& t, int2* d_out, cudaStream_t st);
 int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, int field_order, cudaStream_t st);
 int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, cudaStream_t st);
 int launch_excl_correction(Workspace& ws, const Particles& P, const TreeDev* t, int field_order, const Modes& md,

@@ -134,8 +134,7 @@ __global__ void __launch_bounds__(256) k_m2l_red(const TreeDev t, const double* 
     const int N = 2 * p, nTr = rbase(N + 1), nr = (p + 1) * (p + 1), nq = nT(p);
     // block-shared tables
     int2* rule = reinterpret_cast<int2*>(sm_raw);
-    uint16_t* idx2 = reinterpret_cast<uint16_t*>(rule + nTr);
-    size_t off = sizeof(int2) * nTr + sizeof(uint16_t) * nr * nr;
+    size_t off = sizeof(int2) * nTr;
     off = (off + 15) & ~(size_t)15;
     R* wbase = reinterpret_cast<R*>(reinterpret_cast<char*>(sm_raw) + off);
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -161,12 +160,6 @@ __global__ void __launch_bounds__(256) k_m2l_red(const TreeDev t, const double* 
             dir = 2; par = ridx(0, 0, v - 1); cnt = v - 1; gp = v > 1 ? ridx(0, 0, v - 2) : 0;
         }
         rule[e] = make_int2(par | (dir << 16), gp | (cnt << 16));
-    }
-    for (int e = threadIdx.x; e < nr * nr; e += blockDim.x) {
-        const int s = e / nr, f = e % nr;
-        const int cs = qcomp(s), cf = qcomp(f);
-        idx2[e] = (uint16_t)ridx((cs & 0xff) + (cf & 0xff), ((cs >> 8) & 0xff) + ((cf >> 8) & 0xff),
-                                 ((cs >> 16) & 0xff) + ((cf >> 16) & 0xff));
     }
     __syncthreads();
     const int i = blockIdx.x * (blockDim.x >> 5) + wib;
@@ -195,16 +188,19 @@ __global__ void __launch_bounds__(256) k_m2l_red(const TreeDev t, const double* 
     }
     for (int q = q0; q < q1; ++q) {
         const int j = t.far_src[q];
+        // per-pair expansion order (the far list stores it; at most p)
+        const int pq = t.far_ord ? min((int)t.far_ord[q], p) : p;
+        const int Nq = 2 * pq, nrq = (pq + 1) * (pq + 1);
         const R X = (R)((cxi - t.cx[j]) * ih), Y = (R)((cyi - t.cy[j]) * ih), Z = (R)((czi - t.cz[j]) * ih);
 #pragma unroll
         for (int r = 0; r < (kMaxR + 31) / 32; ++r) {
             const int s = lane + 32 * r;
-            if (s < nr) ws[s] = (R)wred[(size_t)j * nr + s] * sc[r];
+            if (s < nrq) ws[s] = (R)wred[(size_t)j * nr + s] * sc[r];
         }
         const R r2 = X * X + Y * Y + Z * Z;
         const R rinv = Real<R>::rsqrt_(r2);
         const R rinv2 = rinv * rinv;
-        if (lane <= N) {
+        if (lane <= Nq) {
             R v = rinv, c = (R)1;
             for (int jj = 1; jj <= lane; ++jj) {
                 v *= rinv2;
@@ -215,10 +211,10 @@ __global__ void __launch_bounds__(256) k_m2l_red(const TreeDev t, const double* 
         __syncwarp();
         R* A = TA;
         R* B = TB;
-        if (lane == 0) A[0] = gsh[N];
+        if (lane == 0) A[0] = gsh[Nq];
         __syncwarp();
-        for (int lev = N - 1; lev >= 0; --lev) {
-            const int lim = rbase(N - lev + 1);
+        for (int lev = Nq - 1; lev >= 0; --lev) {
+            const int lim = rbase(Nq - lev + 1);
             for (int e = lane; e < lim; e += 32) {
                 R v;
                 if (e == 0) {
@@ -237,16 +233,45 @@ __global__ void __launch_bounds__(256) k_m2l_red(const TreeDev t, const double* 
             A = B;
             B = tmp;
         }
-        // contraction over the reduced bases
+        // contraction over the reduced bases: sources by (order k, z-block sz,
+        // y index); for a fixed output the tensor index then runs
+        // contiguously along y, and each source weight is loaded once for all
+        // of the lane's outputs
+        {
+            int fx_[kMaxRPL], fy_[kMaxRPL], fz_[kMaxRPL], fk_[kMaxRPL];
 #pragma unroll
-        for (int r = 0; r < kMaxRPL; ++r) {
-            const int f = lane + 32 * r;
-            if (f < nr) {
-                R a = (R)0;
-                const uint16_t* col = idx2 + f;
-                for (int s = 0; s < nr; ++s) a += ws[s] * A[col[s * nr]];
-                part[r] += a;
+            for (int r = 0; r < kMaxRPL; ++r) {
+                const int c = (lane + 32 * r < nr) ? qcomp(lane + 32 * r) : 0;
+                fx_[r] = c & 0xff;
+                fy_[r] = (c >> 8) & 0xff;
+                fz_[r] = (c >> 16) & 0xff;
+                fk_[r] = c >> 24;
             }
+            R a[kMaxRPL];
+#pragma unroll
+            for (int r = 0; r < kMaxRPL; ++r) a[r] = (R)0;
+            for (int k = 0; k <= pq; ++k) {
+#pragma unroll
+                for (int sz = 0; sz <= 1; ++sz) {
+                    const int len = k + 1 - sz;
+                    if (len <= 0) continue;
+                    const int soff = k * k + (sz == 0 ? 0 : k + 1);
+                    int base[kMaxRPL];
+#pragma unroll
+                    for (int r = 0; r < kMaxRPL; ++r) {
+                        const int n = k + fk_[r], v = sz + fz_[r];
+                        base[r] = rbase(n) + (v == 0 ? 0 : (v == 1 ? n + 1 : 2 * n + 1)) + fy_[r];
+                    }
+                    for (int sy = 0; sy < len; ++sy) {
+                        const R w = ws[soff + sy];
+#pragma unroll
+                        for (int r = 0; r < kMaxRPL; ++r)
+                            if (lane + 32 * r < nrq) a[r] += w * A[base[r] + sy];
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < kMaxRPL; ++r) part[r] += a[r];
         }
         if (Acc<R>::kBlock == 1 || ((q - q0) % Acc<R>::kBlock) == Acc<R>::kBlock - 1) {
 #pragma unroll
@@ -279,7 +304,7 @@ int set_smem(const void* fn, size_t bytes) {
 template <typename R>
 int launch_red(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
     const int N = 2 * p, nTr = rbase(N + 1), nr = (p + 1) * (p + 1);
-    size_t tab = sizeof(int2) * nTr + sizeof(uint16_t) * nr * nr;
+    size_t tab = sizeof(int2) * nTr;
     tab = (tab + 15) & ~(size_t)15;
     const size_t per_warp = sizeof(R) * (2 * nTr + nr + (N + 1) + 1);
     int wpb = 8;
@@ -292,6 +317,19 @@ int launch_red(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
 }
 
 }  // namespace
+
+// Reduced source weights of every node at order p (into ws.wred).
+int launch_reduce_moments(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
+    const int M = t.num_nodes, nq = nT(p), nr = (p + 1) * (p + 1);
+    FMM_TRY(ws.wred.ensure(sizeof(double) * (size_t)M * nr));
+    const int wpb = 4;
+    const size_t sm = sizeof(double) * wpb * nq;
+    FMM_TRY(set_smem((const void*)k_reduce_moments, sm));
+    count_launches(1);
+    k_reduce_moments<<<grid_for(M, wpb), 32 * wpb, sm, st>>>(M, p, ws.mom.as<double>(), ws.wred.as<double>());
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
 
 // Exact-mode M2L: reduced moments, reduced M2L (FP32 or FP64), completion of
 // the local expansions.

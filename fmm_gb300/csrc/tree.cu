@@ -288,7 +288,7 @@ __global__ void k_pos_of(int64_t n, const uint32_t* __restrict__ perm, int32_t* 
 // counters: [0] next frontier size, [1] far count, [2] near count, [3] overflow flag
 __global__ void k_list_iter(const int2* __restrict__ in, int nin, int2* __restrict__ out, int64_t cap_out,
                             uint64_t* __restrict__ far, int64_t cap_far, uint64_t* __restrict__ nearp,
-                            int64_t cap_near, const TreeDev t, double theta, double rdamp,
+                            int64_t cap_near, const TreeDev t, double theta, double rdamp, int order,
                             unsigned long long* counters) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nin) return;
@@ -308,7 +308,7 @@ __global__ void k_list_iter(const int2* __restrict__ in, int nin, int2* __restri
     if (accept) {
         const unsigned long long k = atomicAdd(&counters[1], 1ull);
         if (k < (unsigned long long)cap_far)
-            far[k] = ((uint64_t)(uint32_t)i << 32) | (uint32_t)j;
+            far[k] = ((uint64_t)(uint32_t)i << 36) | ((uint64_t)(order & 15) << 32) | (uint32_t)j;
         else
             counters[3] = 1;
     } else if (li && lj) {
@@ -333,15 +333,19 @@ __global__ void k_list_iter(const int2* __restrict__ in, int nin, int2* __restri
     }
 }
 
-__global__ void k_split_pairs(int64_t m, const uint64_t* __restrict__ sorted, int32_t* __restrict__ src) {
+__global__ void k_split_pairs(int64_t m, const uint64_t* __restrict__ sorted, int32_t* __restrict__ src,
+                              uint8_t* __restrict__ ord) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k < m) src[k] = (int32_t)(sorted[k] & 0xffffffffull);
+    if (k >= m) return;
+    src[k] = (int32_t)(sorted[k] & 0xffffffffull);
+    if (ord) ord[k] = (uint8_t)((sorted[k] >> 32) & 15ull);
 }
 
-__global__ void k_csr_offsets(int M, int64_t m, const uint64_t* __restrict__ sorted, int32_t* __restrict__ off) {
+__global__ void k_csr_offsets(int M, int64_t m, const uint64_t* __restrict__ sorted, int32_t* __restrict__ off,
+                              int shift) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i > M) return;
-    const uint64_t key = (uint64_t)(uint32_t)i << 32;
+    const uint64_t key = (uint64_t)(uint32_t)i << shift;
     int64_t a = 0, h = m;
     while (a < h) {
         const int64_t mid = (a + h) >> 1;
@@ -622,7 +626,7 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
             k_list_iter<<<grid_for(nin, 256), 256, 0, st>>>(fin, (int)nin, fout, cap_front,
                                                              ws.far_pairs.as<uint64_t>(), cap_far,
                                                              ws.near_pairs.as<uint64_t>(), cap_near, t, tp.theta,
-                                                             tp.mac_mode == 1 ? tp.rdamp : 0.0, ctr);
+                                                             tp.mac_mode == 1 ? tp.rdamp : 0.0, tp.order, ctr);
             FMM_CUDA_TRY(cudaMemcpyAsync(h, ctr, sizeof(h), cudaMemcpyDeviceToHost, st));
             FMM_CUDA_TRY(cudaStreamSynchronize(st));
             if (h[3]) {
@@ -660,20 +664,24 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
         FMM_TRY(ws.near_src.ensure(sizeof(int32_t) * (std::max<int64_t>(1, t.nnear) + (M + 1))));
         t.far_src = ws.far_src.as<int32_t>();
         t.far_off = t.far_src + std::max<int64_t>(1, t.nfar);
+        FMM_TRY(ws.far_ord.ensure(std::max<int64_t>(1, t.nfar)));
+        t.far_ord = ws.far_ord.as<uint8_t>();
         t.near_src = ws.near_src.as<int32_t>();
         t.near_off = t.near_src + std::max<int64_t>(1, t.nnear);
         if (t.nfar > 0) {
             count_launches(1);
-            k_split_pairs<<<grid_for(t.nfar, 256), 256, 0, st>>>(t.nfar, ws.far_sorted.as<uint64_t>(), t.far_src);
+            k_split_pairs<<<grid_for(t.nfar, 256), 256, 0, st>>>(t.nfar, ws.far_sorted.as<uint64_t>(), t.far_src,
+                                                                  t.far_ord);
         }
         if (t.nnear > 0) {
             count_launches(1);
-            k_split_pairs<<<grid_for(t.nnear, 256), 256, 0, st>>>(t.nnear, ws.near_sorted.as<uint64_t>(), t.near_src);
+            k_split_pairs<<<grid_for(t.nnear, 256), 256, 0, st>>>(t.nnear, ws.near_sorted.as<uint64_t>(), t.near_src,
+                                                                   nullptr);
         }
         count_launches(1);
-        k_csr_offsets<<<grid_for(M + 1, 256), 256, 0, st>>>(M, t.nfar, ws.far_sorted.as<uint64_t>(), t.far_off);
+        k_csr_offsets<<<grid_for(M + 1, 256), 256, 0, st>>>(M, t.nfar, ws.far_sorted.as<uint64_t>(), t.far_off, 36);
         count_launches(1);
-        k_csr_offsets<<<grid_for(M + 1, 256), 256, 0, st>>>(M, t.nnear, ws.near_sorted.as<uint64_t>(), t.near_off);
+        k_csr_offsets<<<grid_for(M + 1, 256), 256, 0, st>>>(M, t.nnear, ws.near_sorted.as<uint64_t>(), t.near_off, 32);
         unsigned long long* pc = ctr + 4;
         FMM_CUDA_TRY(cudaMemsetAsync(pc, 0, sizeof(unsigned long long), st));
         if (t.nnear > 0) {
