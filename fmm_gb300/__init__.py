@@ -16,8 +16,8 @@ import numpy as np
 from . import _lib
 from ._lib import FmmError
 
-__all__ = ["field_direct", "field_fmm", "field_direct_device", "field_fmm_device", "Options", "last_stats",
-           "n_components", "FmmError", "version"]
+__all__ = ["field_direct", "field_fmm", "field_fmm_batched", "field_direct_device", "field_fmm_device", "Options",
+           "last_stats", "n_components", "FmmError", "version", "load_selector"]
 
 
 def n_components(order):
@@ -59,6 +59,33 @@ class Options:
         o.target_rel_err = float(self.target_rel_err)
         o.stream = int(self.stream) or None
         return o
+
+
+import os
+import threading
+
+SELECTOR_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "selector_v1.bin")
+_sel_local = threading.local()
+
+
+def load_selector(path=None):
+    """Loads the expansion-order selector's network parameters (float32 blob
+    written by fmm_gb300.selector_train) for the calling thread."""
+    path = path or SELECTOR_WEIGHTS
+    if not os.path.exists(path):
+        raise FmmError(_lib.FMM_ENOTSUP, "learned selector (no weights at %s; run fmm_gb300.selector_train)" % path)
+    p = np.fromfile(path, dtype="<f4")
+    L = _lib.lib()
+    L.fmm_selector_load.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+    _lib.check(L.fmm_selector_load(p.ctypes.data, p.size), "fmm_selector_load")
+    _sel_local.loaded = path
+
+
+def _options_c(options):
+    opts = options or Options()
+    if opts.selector == "learned" and getattr(_sel_local, "loaded", None) is None:
+        load_selector()
+    return opts.to_c()
 
 
 def _damp_bytes(damp_type):
@@ -119,7 +146,7 @@ def field_fmm(comm, coordinates, multipoles, exclusions, theta, ncrit, expansion
     n = X.shape[0]
     F = np.zeros((n, n_components(field_order)), order="F")
     ds, dl = _damp_bytes(damp_type)
-    o = (options or Options()).to_c()
+    o = _options_c(options)
     box = None
     if box_matrix is not None:
         box = np.asfortranarray(box_matrix, dtype=np.float64)
@@ -130,6 +157,39 @@ def field_fmm(comm, coordinates, multipoles, exclusions, theta, ncrit, expansion
                                   _dptr(box) if box is not None else None, ctypes.byref(o))
     _lib.check(st, "field_fmm")
     return F
+
+
+def field_fmm_batched(systems_list, theta, ncrit, expansion_order, field_order, damp_type="", *, options=None):
+    """Many independent systems in one call (fmm_field_fmm_batched).
+
+    `systems_list` is a sequence of dicts with the keys of fmm_gb300.systems
+    (coordinates, multipoles, exclusions, damping_factors); exclusion indices
+    are 1-based within each system.  Returns a list of per-system field
+    arrays."""
+    sizes = [np.asarray(s["coordinates"]).shape[0] for s in systems_list]
+    offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    n = int(offsets[-1])
+    X = np.asfortranarray(np.concatenate([np.asarray(s["coordinates"], dtype=np.float64) for s in systems_list]))
+    M = np.asfortranarray(np.concatenate([np.asarray(s["multipoles"], dtype=np.float64) for s in systems_list]))
+    width = max(np.asarray(s["exclusions"]).reshape(sizes[k], -1).shape[1] for k, s in enumerate(systems_list))
+    E = np.zeros((n, width), dtype=np.int32, order="F")
+    for k, s in enumerate(systems_list):
+        e = np.asarray(s["exclusions"], dtype=np.int32).reshape(sizes[k], -1)
+        E[offsets[k]:offsets[k + 1], :e.shape[1]] = e
+    d = None
+    if damp_type:
+        d = np.ascontiguousarray(np.concatenate([np.asarray(s["damping_factors"], dtype=np.float64)
+                                                 for s in systems_list]))
+    F = np.zeros((n, n_components(field_order)), order="F")
+    ds, dl = _damp_bytes(damp_type)
+    o = _options_c(options)
+    st = _lib.lib().fmm_field_fmm_batched(len(systems_list), offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                          _dptr(X), M.shape[1], _dptr(M), E.shape[1],
+                                          E.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), float(theta), int(ncrit),
+                                          int(expansion_order), int(field_order), _dptr(F), ds, dl,
+                                          _dptr(d) if d is not None else None, ctypes.byref(o))
+    _lib.check(st, "field_fmm_batched")
+    return [F[offsets[k]:offsets[k + 1]] for k in range(len(systems_list))]
 
 
 def _ptr(t):
@@ -155,7 +215,7 @@ def field_fmm_device(coordinates, multipoles, exclusions, theta, ncrit, expansio
     """Device-resident FMM (see ``field_direct_device``)."""
     n = coordinates.shape[0]
     ds, dl = _damp_bytes(damp_type)
-    o = (options or Options()).to_c()
+    o = _options_c(options)
     st = _lib.lib().fmm_field_fmm_device(n, _ptr(coordinates), multipoles.shape[1], _ptr(multipoles),
                                          exclusions.shape[1], _ptr(exclusions), float(theta), int(ncrit),
                                          int(expansion_order), int(field_order), _ptr(field), ds, dl,
@@ -164,7 +224,8 @@ def field_fmm_device(coordinates, multipoles, exclusions, theta, ncrit, expansio
 
 
 STAT_NAMES = ["num_nodes", "num_leaves", "max_depth", "m2l_pairs", "p2p_leaf_pairs", "p2p_particle_pairs", "t_tree",
-              "t_lists", "t_p2m_m2m", "t_p2p", "t_m2l", "t_l2l_l2p", "t_total"]
+              "t_p2m_m2m", "t_lists", "t_p2p", "t_m2l", "t_l2l_l2p", "t_total", "selector_fallback",
+              "sampled_rms_err", "m2l_order_mean"] + ["m2l_pairs_q%d" % q for q in range(13)]
 
 
 def last_stats():

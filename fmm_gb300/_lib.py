@@ -44,12 +44,20 @@ EXPORTED = [
     "fmm_field_fmm",
     "fmm_field_direct_device",
     "fmm_field_fmm_device",
+    "fmm_field_fmm_batched",
     "fmm_field_direct_targets_device",
     "fmm_field_direct_targets_noalloc",
     "fmm_last_stats",
     "fmm_debug_tree",
     "fmm_measure_fma_peak",
     "fmm_launch_count",
+    "fmm_selector_load",
+    "fmm_selector_param_count",
+    "fmm_mlp_param_count",
+    "fmm_mlp_forward",
+    "fmm_mlp_grad",
+    "fmm_mlp_train",
+    "fmm_selector_collect",
     "fmm_strerror",
     "fmm_version",
 ]
@@ -88,6 +96,9 @@ def lib():
                                                   i64, ctypes.c_void_p, c, ctypes.c_void_p, cs, c,
                                                   ctypes.c_void_p, op]
     L.fmm_field_direct_targets_noalloc.argtypes = L.fmm_field_direct_targets_device.argtypes
+    L.fmm_field_fmm_batched.argtypes = [c, ctypes.POINTER(ctypes.c_int64), d, c, d, c, i32, ctypes.c_double, c, c, c,
+                                        d, cs, c, d, op]
+    L.fmm_field_fmm_batched.restype = c
     L.fmm_last_stats.argtypes = [d, c]
     L.fmm_measure_fma_peak.argtypes = [c, d]
     L.fmm_launch_count.restype = ctypes.c_int64

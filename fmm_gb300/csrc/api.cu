@@ -1,6 +1,7 @@
 // C ABI (include/fmm_gpu.h): argument checking, device workspaces and the
 // field_fmm / field_direct pipelines.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -37,7 +38,7 @@ Workspace::~Workspace() {
                      &node_val2, &counters,  &scalars,     &front_a,    &front_b,    &far_pairs,  &near_pairs,
                      &far_sorted, &near_sorted, &node_dfs, &far_src,    &near_src,   &sx,         &sy,
                      &sz,        &smc,       &sd,          &fsorted,    &mom,        &loc,        &partial,
-                     &term_off,  &term_abc,  &term_c, &f32buf, &wred, &far_ord, &sel_norms, &sel_params, &sel_scratch};
+                     &term_off,  &term_abc,  &term_c, &f32buf, &wred, &far_ord, &sel_norms, &sel_params, &sel_scratch, &sysbuf};
     for (DevBuf* b : all) b->release();
     if (events_ready)
         for (auto& e : ev) cudaEventDestroy(e);
@@ -57,8 +58,9 @@ Workspace& thread_workspace() {
 
 namespace {
 
+constexpr int kNumStats = 16 + kMaxP + 1;
 struct Stats {
-    double v[13] = {0};
+    double v[kNumStats] = {0};
 };
 thread_local Stats g_stats;
 
@@ -184,16 +186,57 @@ int upload(Workspace& ws, int64_t n, const double* X, int mdim, const double* mp
     return FMM_OK;
 }
 
+__global__ void k_gather_rows(int64_t n, int nf, const double* __restrict__ field, const int64_t* __restrict__ rows,
+                              int nr, double* __restrict__ out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nr * nf) return;
+    const int r = q % nr, f = q / nr;
+    out[(size_t)f * nr + r] = field[(size_t)f * n + rows[r]];
+}
+
+// Far pairs per expansion order (0..15) into hist.
+__global__ void k_order_hist(int64_t m, const uint8_t* __restrict__ ord, unsigned long long* __restrict__ hist) {
+    __shared__ unsigned int h[16];
+    if (threadIdx.x < 16) h[threadIdx.x] = 0;
+    __syncthreads();
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < m; q += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&h[ord[q] & 15], 1u);
+    __syncthreads();
+    if (threadIdx.x < 16 && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], (unsigned long long)h[threadIdx.x]);
+}
+
+constexpr int kCheckTargets = 16;  // sampled particles of the learned-selector check
+constexpr double kSelThetaLoose = 0.6;
+constexpr double kSelPairsPerTarget = 150.0;
+
+// Relative RMS error (field columns of order >= 1) of F against R, both
+// (ntgt x nf) column-major on the host.
+double sampled_rms(const std::vector<double>& F, const std::vector<double>& R, int ntgt, int nf) {
+    double acc = 0.0;
+    for (int t = 0; t < ntgt; ++t) {
+        double d = 0.0, g = 0.0;
+        for (int f = 1; f < nf; ++f) {
+            const double a = F[(size_t)f * ntgt + t], b = R[(size_t)f * ntgt + t];
+            d += (a - b) * (a - b);
+            g += b * b;
+        }
+        acc += g > 0 ? d / g : 0.0;
+    }
+    return std::sqrt(acc / ntgt);
+}
+
 int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, int f, const Opts& o,
             const TreeParams& tp, double* d_field, cudaStream_t st) {
     ensure_events(ws);
-    if (o.selector == 1) return FMM_ENOTSUP;  // learned selector: not built yet
+    const bool learned = o.selector == 1;
+    if (learned && !ws.sel_ready) return FMM_ENOTSUP;  // no selector weights loaded
     Modes md{o.coef_mode, o.excl_mode, o.precision};
-    if (md.precision != 0) {
-        // the mixed paths mask exclusions in the FP32 loop and use exact tensors
+    if (md.precision != 0 || learned) {
+        // the mixed and learned paths mask exclusions and use exact tensors
         md.excl_mode = 1;
         md.coef_mode = 1;
     }
+    if (learned && (p < 10 || dim_to_order(P.dim) > 2 || f < 1)) return FMM_ENOTSUP;
     TreeParams tpl = tp;
     if (o.mac_mode == 1 && P.damp_type != DAMP_NONE && P.damp) {
         const double dmin = min_damping_factor(ws, P.damp, P.n, st);
@@ -203,24 +246,92 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     const int nf = nT(f);
     cudaEventRecord(ws.ev[0], st);
     FMM_TRY(build_tree(ws, P.x, P.n, tp, t, st));
+    // learned selector: FP64 direct sum at sampled particles (field scale of
+    // the per-pair budget, and the check of the result)
+    std::vector<double> ref_rows;
+    std::vector<int64_t> rows;
+    if (learned) {
+        const int nt = (int)std::min<int64_t>(kCheckTargets, P.n);
+        for (int k = 0; k < nt; ++k) rows.push_back((int64_t)(((uint64_t)k * 2654435761ull + 12345ull) % (uint64_t)P.n));
+        FMM_TRY(ws.sel_scratch.ensure(sizeof(double) * (size_t)nt * nf * 2 + sizeof(int64_t) * nt));
+        int64_t* d_rows = reinterpret_cast<int64_t*>(ws.sel_scratch.as<double>() + (size_t)nt * nf * 2);
+        double* d_ref = ws.sel_scratch.as<double>();
+        FMM_CUDA_TRY(cudaMemcpyAsync(d_rows, rows.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, st));
+        Modes mdir{1, 1, 0};
+        FMM_TRY(launch_direct_f64(ws, P, f, mdir, d_ref, st, nt, d_rows));
+        ref_rows.resize((size_t)nt * nf);
+        FMM_CUDA_TRY(cudaMemcpyAsync(ref_rows.data(), d_ref, sizeof(double) * nt * nf, cudaMemcpyDeviceToHost, st));
+        FMM_CUDA_TRY(cudaStreamSynchronize(st));
+        std::vector<double> mag(nt);
+        for (int k = 0; k < nt; ++k) {
+            double g = 0.0;
+            for (int c = 1; c < 4; ++c) g += ref_rows[(size_t)c * nt + k] * ref_rows[(size_t)c * nt + k];
+            mag[k] = std::sqrt(g);
+        }
+        std::sort(mag.begin(), mag.end());
+        const double scale = 0.5 * mag[nt / 2];
+        // truncation budget: what the FP32 near field leaves of the target
+        const double floor_fp32 = md.precision == 0 ? 0.0 : 9e-7;
+        const double trunc = std::sqrt(std::max(o.target * o.target - floor_fp32 * floor_fp32, 0.04 * o.target * o.target));
+        tpl.sel_log_budget = (float)(std::log10(trunc * scale / std::sqrt(kSelPairsPerTarget)) - 0.3);
+        tpl.sel_theta = kSelThetaLoose;
+    }
     cudaEventRecord(ws.ev[1], st);
-    FMM_TRY(build_lists(ws, t, tpl, st));
-    cudaEventRecord(ws.ev[2], st);
     FMM_TRY(gather_sorted(ws, P, t, st));
     FMM_TRY(launch_p2m_m2m(ws, P, t, p, st));
-    cudaEventRecord(ws.ev[3], st);
-    if (md.precision == 1 || md.precision == 2)
-        FMM_TRY(launch_p2p_f32(ws, P, t, f, st));
-    else
-        FMM_TRY(launch_p2p_f64(ws, P, t, f, md, st));
-    FMM_TRY(launch_excl_correction(ws, P, &t, f, md, ws.fsorted.as<double>(), st));
-    cudaEventRecord(ws.ev[4], st);
-    FMM_TRY(launch_m2l(ws, t, p, md, st));
-    cudaEventRecord(ws.ev[5], st);
-    FMM_TRY(launch_l2l_l2p(ws, P, t, p, f, st));
-    FMM_TRY(scatter_field(ws, t, P.n, nf, d_field, st));
+    if (learned) {
+        FMM_TRY(launch_reduce_moments(ws, t, p, st));
+        FMM_TRY(selector_node_norms(ws, t, p, P.damp ? ws.sd.as<double>() : nullptr, st));
+        tpl.sel_params = ws.sel_params.as<float>();
+        tpl.sel_lnorm = ws.sel_norms.as<float>();
+        tpl.sel_dmin = ws.sel_norms.as<float>() + (size_t)t.num_nodes * (p + 1);
+        tpl.sel_P = p;
+    }
+    cudaEventRecord(ws.ev[2], st);
+    bool fallback = false;
+    double check_rms = -1.0;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        FMM_TRY(build_lists(ws, t, tpl, st));
+        cudaEventRecord(ws.ev[3], st);
+        if (md.precision == 1 || md.precision == 2)
+            FMM_TRY(launch_p2p_f32(ws, P, t, f, st));
+        else
+            FMM_TRY(launch_p2p_f64(ws, P, t, f, md, st));
+        FMM_TRY(launch_excl_correction(ws, P, &t, f, md, ws.fsorted.as<double>(), st));
+        cudaEventRecord(ws.ev[4], st);
+        FMM_TRY(launch_m2l(ws, t, p, md, st));
+        cudaEventRecord(ws.ev[5], st);
+        FMM_TRY(launch_l2l_l2p(ws, P, t, p, f, st));
+        FMM_TRY(scatter_field(ws, t, P.n, nf, d_field, st));
+        if (!learned || attempt == 1) break;
+        // check at the sampled particles; fall back to the fixed rule if the
+        // measured error is above the target
+        const int nt = (int)rows.size();
+        double* d_got = ws.sel_scratch.as<double>() + (size_t)nt * nf;
+        const int64_t* d_rows = reinterpret_cast<const int64_t*>(ws.sel_scratch.as<double>() + (size_t)nt * nf * 2);
+        count_launches(1);
+        k_gather_rows<<<(nt * nf + 127) / 128, 128, 0, st>>>(P.n, nf, d_field, d_rows, nt, d_got);
+        std::vector<double> got((size_t)nt * nf);
+        FMM_CUDA_TRY(cudaMemcpyAsync(got.data(), d_got, sizeof(double) * nt * nf, cudaMemcpyDeviceToHost, st));
+        FMM_CUDA_TRY(cudaStreamSynchronize(st));
+        check_rms = sampled_rms(got, ref_rows, nt, nf);
+        if (check_rms <= o.target) break;
+        fallback = true;
+        tpl.sel_params = nullptr;  // fixed rule (theta, expansion order of the call)
+    }
     cudaEventRecord(ws.ev[6], st);
-    FMM_CUDA_TRY(cudaEventSynchronize(ws.ev[6]));
+    // far pairs per expansion order (outside the timed phases)
+    unsigned long long hist[16] = {0};
+    FMM_TRY(ws.counters.ensure(sizeof(unsigned long long) * 32));
+    unsigned long long* d_hist = ws.counters.as<unsigned long long>() + 16;
+    FMM_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(hist), st));
+    if (t.nfar > 0 && t.far_ord) {
+        count_launches(1);
+        k_order_hist<<<(unsigned)std::min<int64_t>(1024, (t.nfar + 255) / 256), 256, 0, st>>>(t.nfar, t.far_ord,
+                                                                                                    d_hist);
+    }
+    FMM_CUDA_TRY(cudaMemcpyAsync(hist, d_hist, sizeof(hist), cudaMemcpyDeviceToHost, st));
+    FMM_CUDA_TRY(cudaStreamSynchronize(st));
     FMM_CUDA_TRY(cudaGetLastError());
     Stats s;
     s.v[0] = t.num_nodes;
@@ -236,6 +347,14 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     }
     cudaEventElapsedTime(&ms, ws.ev[0], ws.ev[6]);
     s.v[12] = ms;
+    s.v[13] = fallback ? 1.0 : 0.0;
+    s.v[14] = check_rms;
+    double osum = 0.0;
+    for (int q = 0; q <= kMaxP; ++q) {
+        s.v[16 + q] = (double)hist[q];
+        osum += (double)q * (double)hist[q];
+    }
+    s.v[15] = t.nfar > 0 ? osum / (double)t.nfar : 0.0;
     g_stats = s;
     return FMM_OK;
 }
@@ -263,9 +382,18 @@ const char* fmm_strerror(int s) {
     }
 }
 
+int fmm_selector_load(const float* params, int64_t count) {
+    if (!params || count != fmm_selector_param_count()) return FMM_EINVAL;
+    Workspace& ws = thread_workspace();
+    FMM_TRY(ws.sel_params.ensure(sizeof(float) * (size_t)count));
+    FMM_CUDA_TRY(cudaMemcpy(ws.sel_params.p, params, sizeof(float) * (size_t)count, cudaMemcpyHostToDevice));
+    ws.sel_ready = true;
+    return FMM_OK;
+}
+
 int fmm_last_stats(double* out, int len) {
     int k = 0;
-    for (; k < len && k < 13; ++k) out[k] = g_stats.v[k];
+    for (; k < len && k < kNumStats; ++k) out[k] = g_stats.v[k];
     return k;
 }
 
@@ -376,6 +504,90 @@ int fmm_field_fmm(int comm, int64_t n, const double* X, int mdim, const double* 
     FMM_CUDA_TRY(cudaMemcpyAsync(field, ws.out_field.p, sizeof(double) * (size_t)nf * n, cudaMemcpyDeviceToHost, st));
     FMM_CUDA_TRY(cudaStreamSynchronize(st));
     return FMM_OK;
+}
+
+// Many independent systems in one call (see include/fmm_gpu.h).
+int fmm_field_fmm_batched(int nsys, const int64_t* offsets, const double* X, int mdim, const double* mp, int exw,
+                          const int32_t* ex, double theta, int ncrit, int p, int field_order, double* field,
+                          const char* damp, int damp_len, const double* dampf, const fmm_opts* opts) {
+    if (nsys < 1 || !offsets || offsets[0] != 0) return FMM_EINVAL;
+    const int64_t n = offsets[nsys];
+    int dt = 0;
+    FMM_TRY(parse_damp(damp, damp_len, &dt));
+    FMM_TRY(check_common(n, mdim, exw, field_order, dt, dampf));
+    Opts o;
+    FMM_TRY(parse_opts(opts, &o));
+    if (ncrit < 1 || p < 0 || !(theta > 0.0)) return FMM_EINVAL;
+    if (p > kMaxP) return FMM_ENOTSUP;
+    if (exw > 0 && !ex) return FMM_EINVAL;
+    // per system: sizes, exclusion ranges, bounding-box centre and half-extent
+    std::vector<double> cen(3 * (size_t)nsys), half((size_t)nsys);
+    double hmax = 0.0;
+    for (int k = 0; k < nsys; ++k) {
+        const int64_t a = offsets[k], b = offsets[k + 1];
+        if (b - a <= ncrit) return FMM_EINVAL;  // every system must need a tree of its own
+        for (int64_t i = a; i < b; ++i)
+            for (int w = 0; w < exw; ++w) {
+                const int32_t e = ex[(size_t)w * n + i];
+                if (e < 0 || e > b - a) return FMM_EINVAL;
+            }
+        double h = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            double lo = X[d * n + a], hi = lo;
+            for (int64_t i = a; i < b; ++i) {
+                lo = std::min(lo, X[d * n + i]);
+                hi = std::max(hi, X[d * n + i]);
+            }
+            cen[3 * (size_t)k + d] = 0.5 * (lo + hi);
+            h = std::max(h, 0.5 * (hi - lo));
+        }
+        half[k] = h;
+        hmax = std::max(hmax, h);
+    }
+    // packing: a G^3 grid (G a power of two) of cells of side S, one system
+    // centred in each; cell boundaries are octree node boundaries
+    int G = 1;
+    while ((int64_t)G * G * G < nsys) G *= 2;
+    const double S = 2.0 * hmax * 1.05 + 1e-6;
+    std::vector<double> Xp((size_t)3 * n);
+    std::vector<int32_t> exg((size_t)std::max(exw, 0) * n), sys((size_t)n);
+    for (int k = 0; k < nsys; ++k) {
+        const int ix = k % G, iy = (k / G) % G, iz = k / (G * G);
+        const double cc[3] = {(ix - 0.5 * (G - 1)) * S, (iy - 0.5 * (G - 1)) * S, (iz - 0.5 * (G - 1)) * S};
+        for (int64_t i = offsets[k]; i < offsets[k + 1]; ++i) {
+            for (int d = 0; d < 3; ++d) Xp[d * n + i] = (X[d * n + i] - cen[3 * (size_t)k + d]) + cc[d];
+            sys[i] = k;
+            for (int w = 0; w < exw; ++w) {
+                const int32_t e = ex[(size_t)w * n + i];
+                exg[(size_t)w * n + i] = e == 0 ? 0 : (int32_t)(e + offsets[k]);
+            }
+        }
+    }
+    Workspace& ws = thread_workspace();
+    cudaStream_t st = o.stream;
+    const int nf = nT(field_order);
+    Particles P;
+    FMM_TRY(upload(ws, n, Xp.data(), mdim, mp, exw, exg.data(), dt != DAMP_NONE ? dampf : nullptr, nf, &P, st));
+    P.damp_type = dt;
+    FMM_TRY(ws.sysbuf.ensure(sizeof(int32_t) * (size_t)n));
+    // the node system ids reuse sysbuf after the tree is built, so keep the
+    // per-particle ids in the scalars-independent buffer below
+    DevBuf dsys;
+    FMM_TRY(dsys.ensure(sizeof(int32_t) * (size_t)n));
+    FMM_CUDA_TRY(cudaMemcpyAsync(dsys.p, sys.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    TreeParams tp{ncrit, theta, 1, 1, {0, 0, 0}, o.mac_mode, 0.0, p};
+    tp.root_r = 0.5 * G * S;
+    tp.d_sys = dsys.as<int32_t>();
+    int rc = run_fmm(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st);
+    if (rc == FMM_OK) {
+        if (cudaMemcpyAsync(field, ws.out_field.p, sizeof(double) * (size_t)nf * n, cudaMemcpyDeviceToHost, st) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            rc = FMM_ECUDA;
+    }
+    cudaStreamSynchronize(st);
+    dsys.release();
+    return rc;
 }
 
 }  // extern "C"

@@ -18,6 +18,13 @@ The closed-form AMOEBA numerator is (-1)^j (2j-1)!! + e^{-u} Q_j(u) with
 Q_1 = 1 and Q_{j+1} = 3u (Q_j' - Q_j) - (2j+1) Q_j; its coefficients are
 emitted too.
 
+FP32 kernels also use re-centred Taylor expansions of N_j on unit intervals
+between the small-argument series and the closed form (both lose digits
+there: the series to alternating terms, the closed form to cancellation):
+    N_j(c + t) = sum_n b_n t^n,  b_n = sum_k a_k C(k, n) c^(k - n),  |t| <= 1/2
+with the exact series coefficients a_k; centres THOLE_CENTRES in x = a r,
+AMOEBA_CENTRES in u = (a r)^3.
+
 Run:  python gen_tables.py > series_tables.h
 """
 from fractions import Fraction
@@ -26,6 +33,10 @@ from math import factorial
 JMAX = 8      # highest radial derivative (tensor order) of the damped kernels
 KT = 24       # Thole series length (powers of x)
 KA = 30       # AMOEBA series length (powers of u)
+NTAY = 14     # terms of the re-centred expansions (|t| <= 1/2)
+THOLE_CENTRES = (Fraction(3, 2), Fraction(5, 2))
+AMOEBA_CENTRES = (Fraction(3, 2), Fraction(5, 2), Fraction(7, 2))
+KFULL = 160   # series terms summed exactly for the re-centred coefficients
 
 
 def power_rule(m, j):
@@ -65,6 +76,16 @@ def amoeba_q():
     return Q
 
 
+def binom(k, n):
+    return factorial(k) // (factorial(n) * factorial(k - n))
+
+
+def recentred(fn, j, c):
+    """b_n, n < NTAY, of N_j(c + t) from the exact series fn(j, k)."""
+    a = [fn(j, k) for k in range(KFULL)]
+    return [sum(a[k] * binom(k, n) * c ** (k - n) for k in range(n, KFULL)) for n in range(NTAY)]
+
+
 def fmt(fr):
     return repr(float(fr)) if fr != 0 else "0.0"
 
@@ -94,6 +115,15 @@ def main():
                 row[d] = c
         out.append("  {" + ", ".join(fmt(c) for c in row) + "}, \\")
     out.append("}")
+    out.append(f"#define FMM_TAY_N {NTAY}")
+    out.append(f"#define FMM_THOLE_NC {len(THOLE_CENTRES)}")
+    out.append(f"#define FMM_AMOEBA_NC {len(AMOEBA_CENTRES)}")
+    for name, fn, cs in (("THOLE", thole, THOLE_CENTRES), ("AMOEBA", amoeba, AMOEBA_CENTRES)):
+        out.append(f"#define FMM_{name}_TAY_INIT {{ \\")
+        for j in range(JMAX + 1):
+            rows = ["{" + ", ".join(fmt(b) for b in recentred(fn, j, c)) + "}" for c in cs]
+            out.append("  {" + ", ".join(rows) + "}, \\")
+        out.append("}")
     print("\n".join(out))
 
 

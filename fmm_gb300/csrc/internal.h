@@ -45,6 +45,7 @@ struct TreeDev {
     int32_t* child = nullptr;        // 8 per node, -1 where empty
     int32_t* level_nodes = nullptr;  // node ids grouped by depth
     int32_t* leaves = nullptr;       // ids of the leaves
+    int32_t* sysid = nullptr;        // batched systems: system of each node (-1: spans several), or null
     // interaction lists, CSR by target node, sources ascending
     int64_t nfar = 0, nnear = 0;
     int64_t near_particle_pairs = 0;
@@ -72,6 +73,8 @@ struct TreeParams {
     int sel_P = 0;                      // order of the stored norms
     float sel_log_budget = 0.0f;        // log10 of the per-pair error budget
     double sel_theta = 0.0;             // loose acceptance test applied before the network
+    double root_r = 0.0;                // > 0: root half-width given (batched packing box)
+    const int32_t* d_sys = nullptr;     // batched systems: system id of each particle (input order)
 };
 
 // Distance beyond which the damped kernel's radial derivatives g_j (j <= nmax)
@@ -95,7 +98,7 @@ struct Workspace {
     DevBuf node_d, node_i, child, level_nodes, leaves, node_key, node_val, node_key2, node_val2;
     DevBuf counters, scalars;
     DevBuf front_a, front_b, far_pairs, near_pairs, far_sorted, near_sorted;
-    DevBuf node_dfs, far_src, near_src, far_ord;
+    DevBuf node_dfs, far_src, near_src, far_ord, sysbuf;
     DevBuf sel_norms, sel_params, sel_scratch;
     // sorted particle data
     DevBuf sx, sy, sz, smc, sd;
@@ -108,6 +111,7 @@ struct Workspace {
     // ref-mode closed-form tensor tables
     DevBuf term_off, term_abc, term_c;
     int term_order = -1;
+    bool sel_ready = false;  // selector weights loaded
     // timing
     cudaEvent_t ev[16] = {};
     bool events_ready = false;

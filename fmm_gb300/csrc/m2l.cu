@@ -21,6 +21,7 @@
 #include <algorithm>
 
 #include "internal.h"
+#include "m2l_basis.cuh"
 #include "pair.cuh"
 
 namespace fmm {
@@ -31,30 +32,6 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 
 constexpr int kMaxR = (kMaxP + 1) * (kMaxP + 1);  // reduced components at the highest order
 constexpr int kMaxRPL = (kMaxR + 31) / 32;        // per-lane outputs
-
-// Restricted tensor layout: components (t,u,v) with v <= 2, ordered by total
-// order n, then v, then u.
-__host__ __device__ constexpr int rbase(int n) { return n == 0 ? 0 : 1 + 3 * (n - 1) * n / 2; }
-__host__ __device__ constexpr int ridx(int t, int u, int v) {
-    const int n = t + u + v;
-    return rbase(n) + (v == 0 ? 0 : (v == 1 ? n + 1 : 2 * n + 1)) + u;
-}
-// Reduced basis (s_z <= 1): order k block of 2k+1 entries starting at k^2.
-__host__ __device__ constexpr int qidx(int x, int y, int z) {
-    const int k = x + y + z;
-    return k * k + (z == 0 ? y : k + 1 + y);
-}
-
-// Per reduced index q: packed (x, y, z, k).
-__device__ __forceinline__ int qcomp(int q) {
-    int k = 0;
-    while ((k + 1) * (k + 1) <= q) ++k;
-    const int l = q - k * k;
-    const int z = l <= k ? 0 : 1;
-    const int y = z == 0 ? l : l - (k + 1);
-    const int x = k - y - z;
-    return x | (y << 8) | (z << 16) | (k << 24);
-}
 
 // Fold w_s (full basis, in shared memory, length nT(p)) onto s_z <= 1.
 __device__ void fold_moments(double* w, int p, int lane) {
@@ -127,8 +104,8 @@ struct Acc<double> {
     static constexpr int kBlock = 1;
 };
 
-template <typename R>
-__global__ void __launch_bounds__(256) k_m2l_red(const TreeDev t, const double* __restrict__ wred,
+template <typename R, int RPL>
+__global__ void __launch_bounds__(128) k_m2l_red(const TreeDev t, const double* __restrict__ wred,
                                                  double* __restrict__ loc, int p) {
     extern __shared__ double sm_raw[];
     const int N = 2 * p, nTr = rbase(N + 1), nr = (p + 1) * (p + 1), nq = nT(p);
@@ -144,40 +121,24 @@ __global__ void __launch_bounds__(256) k_m2l_red(const TreeDev t, const double* 
     R* ws = TB + nTr;
     R* gsh = ws + nr;
     // recursion rules of the restricted tensor entries
-    for (int e = threadIdx.x; e < nTr; e += blockDim.x) {
-        int n = 0;
-        while (rbase(n + 1) <= e) ++n;
-        const int l = e - rbase(n);
-        const int v = l <= n ? 0 : (l <= 2 * n ? 1 : 2);
-        const int u = l - (v == 0 ? 0 : (v == 1 ? n + 1 : 2 * n + 1));
-        const int tt = n - v - u;
-        int dir = 0, par = 0, gp = 0, cnt = 0;
-        if (tt > 0) {
-            dir = 0; par = ridx(tt - 1, u, v); cnt = tt - 1; gp = tt > 1 ? ridx(tt - 2, u, v) : 0;
-        } else if (u > 0) {
-            dir = 1; par = ridx(0, u - 1, v); cnt = u - 1; gp = u > 1 ? ridx(0, u - 2, v) : 0;
-        } else if (v > 0) {
-            dir = 2; par = ridx(0, 0, v - 1); cnt = v - 1; gp = v > 1 ? ridx(0, 0, v - 2) : 0;
-        }
-        rule[e] = make_int2(par | (dir << 16), gp | (cnt << 16));
-    }
+    for (int e = threadIdx.x; e < nTr; e += blockDim.x) rule[e] = restricted_rule(e);
     __syncthreads();
     const int i = blockIdx.x * (blockDim.x >> 5) + wib;
     if (i >= t.num_nodes) return;
     const double cxi = t.cx[i], cyi = t.cy[i], czi = t.cz[i];
     const double ih = 1.0 / t.r[i];
     const int q0 = t.far_off[i], q1 = t.far_off[i + 1];
-    double acc[kMaxRPL];
-    R part[kMaxRPL];
+    double acc[RPL];
+    R part[RPL];
 #pragma unroll
-    for (int r = 0; r < kMaxRPL; ++r) {
+    for (int r = 0; r < RPL; ++r) {
         acc[r] = 0.0;
         part[r] = (R)0;
     }
     // per-lane scale factors (1/h)^k for the reduced source entries it loads
-    R sc[(kMaxR + 31) / 32];
+    R sc[RPL];
 #pragma unroll
-    for (int r = 0; r < (kMaxR + 31) / 32; ++r) {
+    for (int r = 0; r < RPL; ++r) {
         const int s = lane + 32 * r;
         double v = 1.0;
         if (s < nr) {
@@ -186,6 +147,15 @@ __global__ void __launch_bounds__(256) k_m2l_red(const TreeDev t, const double* 
         }
         sc[r] = (R)v;
     }
+    int fx_[RPL], fy_[RPL], fz_[RPL], fk_[RPL];
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) {
+        const int c = (lane + 32 * r < nr) ? qcomp(lane + 32 * r) : 0;
+        fx_[r] = c & 0xff;
+        fy_[r] = (c >> 8) & 0xff;
+        fz_[r] = (c >> 16) & 0xff;
+        fk_[r] = c >> 24;
+    }
     for (int q = q0; q < q1; ++q) {
         const int j = t.far_src[q];
         // per-pair expansion order (the far list stores it; at most p)
@@ -193,7 +163,7 @@ __global__ void __launch_bounds__(256) k_m2l_red(const TreeDev t, const double* 
         const int Nq = 2 * pq, nrq = (pq + 1) * (pq + 1);
         const R X = (R)((cxi - t.cx[j]) * ih), Y = (R)((cyi - t.cy[j]) * ih), Z = (R)((czi - t.cz[j]) * ih);
 #pragma unroll
-        for (int r = 0; r < (kMaxR + 31) / 32; ++r) {
+        for (int r = 0; r < RPL; ++r) {
             const int s = lane + 32 * r;
             if (s < nrq) ws[s] = (R)wred[(size_t)j * nr + s] * sc[r];
         }
@@ -238,44 +208,35 @@ __global__ void __launch_bounds__(256) k_m2l_red(const TreeDev t, const double* 
         // contiguously along y, and each source weight is loaded once for all
         // of the lane's outputs
         {
-            int fx_[kMaxRPL], fy_[kMaxRPL], fz_[kMaxRPL], fk_[kMaxRPL];
+            R a[RPL];
 #pragma unroll
-            for (int r = 0; r < kMaxRPL; ++r) {
-                const int c = (lane + 32 * r < nr) ? qcomp(lane + 32 * r) : 0;
-                fx_[r] = c & 0xff;
-                fy_[r] = (c >> 8) & 0xff;
-                fz_[r] = (c >> 16) & 0xff;
-                fk_[r] = c >> 24;
-            }
-            R a[kMaxRPL];
-#pragma unroll
-            for (int r = 0; r < kMaxRPL; ++r) a[r] = (R)0;
+            for (int r = 0; r < RPL; ++r) a[r] = (R)0;
             for (int k = 0; k <= pq; ++k) {
 #pragma unroll
                 for (int sz = 0; sz <= 1; ++sz) {
                     const int len = k + 1 - sz;
                     if (len <= 0) continue;
                     const int soff = k * k + (sz == 0 ? 0 : k + 1);
-                    int base[kMaxRPL];
+                    int base[RPL];
 #pragma unroll
-                    for (int r = 0; r < kMaxRPL; ++r) {
+                    for (int r = 0; r < RPL; ++r) {
                         const int n = k + fk_[r], v = sz + fz_[r];
                         base[r] = rbase(n) + (v == 0 ? 0 : (v == 1 ? n + 1 : 2 * n + 1)) + fy_[r];
                     }
                     for (int sy = 0; sy < len; ++sy) {
                         const R w = ws[soff + sy];
 #pragma unroll
-                        for (int r = 0; r < kMaxRPL; ++r)
+                        for (int r = 0; r < RPL; ++r)
                             if (lane + 32 * r < nrq) a[r] += w * A[base[r] + sy];
                     }
                 }
             }
 #pragma unroll
-            for (int r = 0; r < kMaxRPL; ++r) part[r] += a[r];
+            for (int r = 0; r < RPL; ++r) part[r] += a[r];
         }
         if (Acc<R>::kBlock == 1 || ((q - q0) % Acc<R>::kBlock) == Acc<R>::kBlock - 1) {
 #pragma unroll
-            for (int r = 0; r < kMaxRPL; ++r) {
+            for (int r = 0; r < RPL; ++r) {
                 acc[r] += (double)part[r];
                 part[r] = (R)0;
             }
@@ -284,7 +245,7 @@ __global__ void __launch_bounds__(256) k_m2l_red(const TreeDev t, const double* 
     }
     double* L = loc + (size_t)i * nq;
 #pragma unroll
-    for (int r = 0; r < kMaxRPL; ++r) {
+    for (int r = 0; r < RPL; ++r) {
         const int f = lane + 32 * r;
         if (f < nr) {
             const int c = qcomp(f);
@@ -301,19 +262,31 @@ int set_smem(const void* fn, size_t bytes) {
     return FMM_OK;
 }
 
-template <typename R>
-int launch_red(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
+template <typename R, int RPL>
+int launch_red_rpl(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
     const int N = 2 * p, nTr = rbase(N + 1), nr = (p + 1) * (p + 1);
     size_t tab = sizeof(int2) * nTr;
     tab = (tab + 15) & ~(size_t)15;
     const size_t per_warp = sizeof(R) * (2 * nTr + nr + (N + 1) + 1);
-    int wpb = 8;
+    int wpb = 4;
     while (wpb > 1 && tab + wpb * per_warp > 160 * 1024) wpb /= 2;
     const size_t sm = tab + wpb * per_warp;
-    FMM_TRY(set_smem((const void*)k_m2l_red<R>, sm));
+    FMM_TRY(set_smem((const void*)k_m2l_red<R, RPL>, sm));
     count_launches(1);
-    k_m2l_red<R><<<grid_for(t.num_nodes, wpb), 32 * wpb, sm, st>>>(t, ws.wred.as<double>(), ws.loc.as<double>(), p);
+    k_m2l_red<R, RPL><<<grid_for(t.num_nodes, wpb), 32 * wpb, sm, st>>>(t, ws.wred.as<double>(), ws.loc.as<double>(),
+                                                                        p);
     return FMM_OK;
+}
+
+// Outputs per lane: ceil((p+1)^2 / 32).
+template <typename R>
+int launch_red(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
+    const int rpl = ((p + 1) * (p + 1) + 31) / 32;
+    if (rpl <= 1) return launch_red_rpl<R, 1>(ws, t, p, st);
+    if (rpl <= 2) return launch_red_rpl<R, 2>(ws, t, p, st);
+    if (rpl <= 3) return launch_red_rpl<R, 3>(ws, t, p, st);
+    if (rpl <= 4) return launch_red_rpl<R, 4>(ws, t, p, st);
+    return launch_red_rpl<R, 6>(ws, t, p, st);
 }
 
 }  // namespace

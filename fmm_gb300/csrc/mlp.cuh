@@ -10,6 +10,8 @@
 //   W4[Q][H], b4[Q]
 #pragma once
 
+#include "internal.h"
+
 namespace fmm {
 
 constexpr int kMlpIn = 17;
@@ -53,6 +55,25 @@ __device__ __forceinline__ void mlp_forward(const float* __restrict__ P, const f
     mlp_layer<kMlpH, kMlpH, true>(P + kOffW2, P + kOffB2, h1, h2);
     mlp_layer<kMlpH, kMlpH, true>(P + kOffW3, P + kOffB3, h2, h1);
     mlp_layer<kMlpOut, kMlpH, false>(P + kOffW4, P + kOffB4, h1, y);
+}
+
+// Features of the pair (target i, source j); P = order of the stored norms.
+// Source norms of orders above kFeatOrders are not used (fixed at -40), so
+// training (moments to order 12) and use (moments to the call's expansion
+// order, at least kFeatOrders) see the same inputs.
+constexpr int kFeatOrders = 10;
+__device__ __forceinline__ void selector_features(const TreeDev& t, const float* __restrict__ lnorm,
+                                                  const float* __restrict__ dmin, int P, int i, int j, float* x) {
+    const double dx = t.cx[i] - t.cx[j], dy = t.cy[i] - t.cy[j], dz = t.cz[i] - t.cz[j];
+    const double R = sqrt(dx * dx + dy * dy + dz * dz);
+    const float lR = (float)log10(R);
+    x[0] = (float)(1.7320508075688772 * (t.r[i] + t.r[j]) / R);
+    x[1] = log2f((float)(t.r[j] / t.r[i]));
+    x[2] = log2f((float)t.count[i]);
+    for (int k = 0; k <= kQmax; ++k)
+        x[3 + k] = (k <= P && k <= kFeatOrders) ? fmaxf(lnorm[(size_t)j * (P + 1) + k] - (float)(k + 2) * lR, -40.0f)
+                                                : -40.0f;
+    x[16] = fminf(dmin[i] * dmin[j] * (float)R, 30.0f) * (1.0f / 30.0f);
 }
 
 }  // namespace fmm

@@ -151,6 +151,46 @@ __global__ void __launch_bounds__(128) k_direct_f64(int64_t n, const int64_t* __
     }
 }
 
+// Direct sum for a few targets: one block per (target, source split), the
+// block's threads stride over the sources; block reduction of the partial
+// field into partial[split][f][target].
+template <int M, int F>
+__global__ void __launch_bounds__(128) k_direct_few(int64_t n, const int64_t* __restrict__ targets, int64_t ntgt,
+                                                    const double* __restrict__ X, const double* __restrict__ mc,
+                                                    const double* __restrict__ damp, int damp_type, int64_t chunk,
+                                                    double* __restrict__ partial) {
+    constexpr int NF = nT(F), NM = nT(M);
+    __shared__ double red[NF][4];
+    const int64_t ti = blockIdx.x;
+    const int64_t i = targets ? targets[ti] : ti;
+    const double xi = X[i], yi = X[n + i], zi = X[2 * n + i];
+    const double di = damp ? damp[i] : 0.0;
+    double acc[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) acc[f] = 0.0;
+    const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+    for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+        if (j == i) continue;
+        double m[NM];
+#pragma unroll
+        for (int s = 0; s < NM; ++s) m[s] = mc[(size_t)s * n + j];
+        pair_field<M, F, double>(xi - X[j], yi - X[n + j], zi - X[2 * n + j], di * (damp ? damp[j] : 0.0), damp_type,
+                                 m, acc);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        double v = acc[f];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[f][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NF) {
+        const int f = threadIdx.x;
+        partial[((size_t)blockIdx.y * NF + f) * ntgt + ti] = (red[f][0] + red[f][1]) + (red[f][2] + red[f][3]);
+    }
+}
+
 __global__ void k_direct_reduce(int64_t ntgt, int nf, int ks, const double* __restrict__ partial,
                                 const int64_t* __restrict__ targets, int64_t ld, double* __restrict__ field) {
     const int64_t ti = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -259,16 +299,24 @@ int launch_direct_f64(Workspace& ws, const Particles& P, int field_order, const 
     double* mc = ws.smc.as<double>();
     count_launches(1);
     k_scale_mp<<<grid_for(n, 256), 256, 0, st>>>(n, P.dim, P.mp, mc);
-    const int64_t tblocks = (ntgt + 127) / 128;
-    int64_t ks = std::max<int64_t>(1, (8LL * num_sms() + tblocks - 1) / tblocks);
-    ks = std::min<int64_t>(ks, std::max<int64_t>(1, n / 256));
+    // few targets (sampled checks): a block per target and source split
+    const bool few = ntgt <= 64;
+    const int64_t tblocks = few ? ntgt : (ntgt + 127) / 128;
+    int64_t ks = std::max<int64_t>(1, ((few ? 16LL : 8LL) * num_sms() + tblocks - 1) / tblocks);
+    ks = std::min<int64_t>(ks, std::max<int64_t>(1, n / (few ? 1024 : 256)));
     ks = std::min<int64_t>(ks, 65535);
     const int64_t chunk = (n + ks - 1) / ks;
     FMM_TRY(ws.partial.ensure(sizeof(double) * (size_t)ks * nf * ntgt));
     dim3 grid((unsigned)tblocks, (unsigned)ks);
-    FMM_MF_SWITCH(m, field_order, (k_direct_f64<MM, FF><<<grid, 128, 0, st>>>(n, d_targets, ntgt, P.x, mc, P.damp,
-                                                                               P.damp_type, chunk,
-                                                                               ws.partial.as<double>())));
+    if (few) {
+        FMM_MF_SWITCH(m, field_order, (k_direct_few<MM, FF><<<grid, 128, 0, st>>>(n, d_targets, ntgt, P.x, mc, P.damp,
+                                                                                   P.damp_type, chunk,
+                                                                                   ws.partial.as<double>())));
+    } else {
+        FMM_MF_SWITCH(m, field_order, (k_direct_f64<MM, FF><<<grid, 128, 0, st>>>(n, d_targets, ntgt, P.x, mc,
+                                                                                   P.damp, P.damp_type, chunk,
+                                                                                   ws.partial.as<double>())));
+    }
     count_launches(1);
     k_direct_reduce<<<grid_for(ntgt, 256), 256, 0, st>>>(ntgt, nf, (int)ks, ws.partial.as<double>(), nullptr, ntgt,
                                                          d_field);

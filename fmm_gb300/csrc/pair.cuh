@@ -41,7 +41,13 @@ __constant__ double cAmoebaQ[FMM_SER_JMAX + 1][FMM_SER_JMAX] = FMM_AMOEBA_Q_INIT
 __constant__ float cTholeSeriesF[FMM_SER_JMAX + 1][FMM_SER_KT + 1] = FMM_THOLE_SERIES_INIT;
 __constant__ float cAmoebaSeriesF[FMM_SER_JMAX + 1][FMM_SER_KA + 1] = FMM_AMOEBA_SERIES_INIT;
 __constant__ float cAmoebaQF[FMM_SER_JMAX + 1][FMM_SER_JMAX] = FMM_AMOEBA_Q_INIT;
+// re-centred expansions (FP32 kernels): lanes index them by their own
+// interval, so they live in global memory rather than the constant bank
+__device__ const float gTholeTay[FMM_SER_JMAX + 1][FMM_THOLE_NC][FMM_TAY_N] = FMM_THOLE_TAY_INIT;
+__device__ const float gAmoebaTay[FMM_SER_JMAX + 1][FMM_AMOEBA_NC][FMM_TAY_N] = FMM_AMOEBA_TAY_INIT;
 #endif
+static const double hTholeTay[FMM_SER_JMAX + 1][FMM_THOLE_NC][FMM_TAY_N] = FMM_THOLE_TAY_INIT;
+static const double hAmoebaTay[FMM_SER_JMAX + 1][FMM_AMOEBA_NC][FMM_TAY_N] = FMM_AMOEBA_TAY_INIT;
 static const double hTholeSeries[FMM_SER_JMAX + 1][FMM_SER_KT + 1] = FMM_THOLE_SERIES_INIT;
 static const double hAmoebaSeries[FMM_SER_JMAX + 1][FMM_SER_KA + 1] = FMM_AMOEBA_SERIES_INIT;
 static const double hAmoebaQ[FMM_SER_JMAX + 1][FMM_SER_JMAX] = FMM_AMOEBA_Q_INIT;
@@ -60,6 +66,9 @@ struct Real<double> {
     static constexpr int kAmoebaK = 16;
     static constexpr double kErfS = 3.0;     // Boys series for a r^2 below this
     static constexpr int kErfK = 40;
+    static constexpr bool kTay = false;      // re-centred expansions unused in FP64
+    __host__ __device__ static __forceinline__ double thole_tay(int, int, int) { return 0.0; }
+    __host__ __device__ static __forceinline__ double amoeba_tay(int, int, int) { return 0.0; }
     __host__ __device__ static __forceinline__ double rsqrt_(double x) {
 #ifdef __CUDA_ARCH__
         return ::rsqrt(x);
@@ -102,10 +111,29 @@ struct Real<double> {
 
 template <>
 struct Real<float> {
-    static constexpr float kTholeX = 2.0f;
-    static constexpr int kTholeK = 20;
-    static constexpr float kAmoebaU = 2.0f;
-    static constexpr int kAmoebaK = 24;
+    // series below 1, re-centred expansions on [1, 3) (Thole, x = a r) and
+    // [1, 4) (AMOEBA, u = (a r)^3), closed forms above
+    static constexpr float kTholeX = 1.0f;
+    static constexpr int kTholeK = 18;
+    static constexpr float kAmoebaU = 1.0f;
+    static constexpr int kAmoebaK = 18;
+    static constexpr bool kTay = true;
+    static constexpr float kTholeHi = 1.0f + FMM_THOLE_NC;
+    static constexpr float kAmoebaHi = 1.0f + FMM_AMOEBA_NC;
+    __host__ __device__ static __forceinline__ float thole_tay(int j, int c, int n) {
+#ifdef __CUDA_ARCH__
+        return __ldg(&gTholeTay[j][c][n]);
+#else
+        return (float)hTholeTay[j][c][n];
+#endif
+    }
+    __host__ __device__ static __forceinline__ float amoeba_tay(int j, int c, int n) {
+#ifdef __CUDA_ARCH__
+        return __ldg(&gAmoebaTay[j][c][n]);
+#else
+        return (float)hAmoebaTay[j][c][n];
+#endif
+    }
     static constexpr float kErfS = 6.0f;
     static constexpr int kErfK = 36;
     __host__ __device__ static __forceinline__ float rsqrt_(float x) {
@@ -154,25 +182,46 @@ __host__ __device__ constexpr double dfact_odd(int j) {  // (2j-1)!!, (-1)!! = 1
     return p;
 }
 
+// Whether v lies in the re-centred-expansion range [lo, hi) (FP32 only).
+template <typename R>
+__host__ __device__ __forceinline__ bool tay_interval(R v, R lo, R hi) {
+    return Real<R>::kTay && v >= lo && v < hi;
+}
+template <typename R>
+__host__ __device__ constexpr R thole_hi() {
+    if constexpr (Real<R>::kTay) return Real<R>::kTholeHi;
+    else return (R)0;
+}
+template <typename R>
+__host__ __device__ constexpr R amoeba_hi() {
+    if constexpr (Real<R>::kTay) return Real<R>::kAmoebaHi;
+    else return (R)0;
+}
+
 // g_j(r), j = 0..N, of the kernel `damp` at squared distance r2 and pair
 // damping factor a (the product of the two particles' factors).
 template <int N, typename R>
-__host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, R* g);
+__host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, R* g, R eps = (R)0);
 
 template <int N, typename R>
 __host__ __device__ __forceinline__ void radial_g(int damp, R r2, R a, R* g) {
     radial_g_ir<N, R>(damp, r2, Real<R>::rsqrt_(r2), a, g);
 }
 
-// Same, with 1/r supplied by the caller (e.g. a refined FP32 value).
+// Same, with 1/r supplied by the caller (e.g. a refined FP32 value) and,
+// optionally, the relative error eps of that value (1/r = ir (1 + eps)):
+// the powers r^-(2j+1) then carry the correction (2j+1) eps, which keeps the
+// error of a rounded ir from growing with the tensor order.
 template <int N, typename R>
-__host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, R* g) {
+__host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, R* g, R eps) {
     using RT = Real<R>;
     const R ir2 = ir * ir;
     if (damp == DAMP_NONE) {
         g[0] = ir;
 #pragma unroll
         for (int j = 1; j <= N; ++j) g[j] = -(R)(2 * j - 1) * g[j - 1] * ir2;
+#pragma unroll
+        for (int j = 0; j <= N; ++j) g[j] += g[j] * ((R)(2 * j + 1) * eps);
         return;
     }
     if (damp == DAMP_ERF) {
@@ -218,6 +267,16 @@ __host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, 
                 for (int k = RT::kTholeK - 1; k >= 0; --k) acc = acc * x + RT::thole(j, k);
                 num[j] = acc;
             }
+        } else if (tay_interval<R>(x, RT::kTholeX, thole_hi<R>())) {
+            const int c = (int)(x - RT::kTholeX);
+            const R t = x - ((R)c + (R)1.5);
+#pragma unroll
+            for (int j = 0; j <= N; ++j) {
+                R acc = RT::thole_tay(j, c, FMM_TAY_N - 1);
+#pragma unroll 1
+                for (int k = FMM_TAY_N - 2; k >= 0; --k) acc = acc * t + RT::thole_tay(j, c, k);
+                num[j] = acc;
+            }
         } else {
             const R e = RT::exp_(-x);
             const R x2 = x * x;
@@ -244,6 +303,16 @@ __host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, 
                 for (int k = RT::kAmoebaK - 1; k >= 0; --k) acc = acc * u + RT::amoeba(j, k);
                 num[j] = acc;
             }
+        } else if (tay_interval<R>(u, RT::kAmoebaU, amoeba_hi<R>())) {
+            const int c = (int)(u - RT::kAmoebaU);
+            const R t = u - ((R)c + (R)1.5);
+#pragma unroll
+            for (int j = 1; j <= N; ++j) {
+                R acc = RT::amoeba_tay(j, c, FMM_TAY_N - 1);
+#pragma unroll 1
+                for (int k = FMM_TAY_N - 2; k >= 0; --k) acc = acc * t + RT::amoeba_tay(j, c, k);
+                num[j] = acc;
+            }
         } else {
             const R e = RT::exp_(-u);
 #pragma unroll
@@ -258,7 +327,8 @@ __host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, 
     R irp = ir;
 #pragma unroll
     for (int j = 0; j <= N; ++j) {
-        g[j] = num[j] * irp;
+        const R v = num[j] * irp;
+        g[j] = v + v * ((R)(2 * j + 1) * eps);
         irp *= ir2;
     }
 }
@@ -355,9 +425,11 @@ __device__ __forceinline__ void pair_field_f32acc(float dx, float dy, float dz, 
     const float h = r2 * y0;
     const float hl = fmaf(r2, y0, -h);
     const float res = fmaf(-h, y0, 1.0f) - (hl + r2lo * y0) * y0;
-    const float ir = fmaf(0.5f * y0, res, y0);
+    const float c = 0.5f * y0 * res;
+    const float ir = y0 + c;
+    const float ir_lo = c - (ir - y0);  // exact: |c| << y0
     float g[N + 1];
-    radial_g_ir<N, float>(damp, r2, ir, a, g);
+    radial_g_ir<N, float>(damp, r2, ir, a, g, ir_lo * (r2 * ir));
     float T[nT(N)];
     md_tensor<N, float>(dx, dy, dz, g, T);
     contract<M, F, float>(T, Mc, acc);

@@ -55,29 +55,28 @@ __global__ void k_node_norms(int M, int P, const double* __restrict__ wred, cons
         }
         lnorm[(size_t)node * (P + 1) + k] = (float)log10(sqrt(s) + 1e-300);
     }
-    double dm = 1e300;
-    if (sd) {
+    // leaves: smallest damping factor of their particles; internal nodes
+    // start at +inf and take the minimum of their leaves (k_dmin_up)
+    float dm = sd ? __int_as_float(0x7f800000) : 0.0f;
+    if (sd && t.is_leaf[node]) {
+        double v = 1e300;
         const int s0 = t.start[node], c = t.count[node];
-        for (int q = s0; q < s0 + c; ++q) dm = fmin(dm, sd[q]);
+        for (int q = s0; q < s0 + c; ++q) v = fmin(v, sd[q]);
+        dm = (float)v;
     }
-    dmin[node] = sd ? (float)dm : 0.0f;
+    dmin[node] = dm;
+}
+
+// Propagates leaf minima to all ancestors.  Damping factors are positive, so
+// the order of their float bit patterns as signed integers is their order.
+__global__ void k_dmin_up(int M, const TreeDev t, float* __restrict__ dmin) {
+    const int node = blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= M || !t.is_leaf[node]) return;
+    const int v = __float_as_int(dmin[node]);
+    for (int a = t.parent[node]; a >= 0; a = t.parent[a]) atomicMin(reinterpret_cast<int*>(dmin + a), v);
 }
 
 }  // namespace
-
-// Features of the pair (target i, source j); P = order of the stored norms.
-__device__ void selector_features(const TreeDev& t, const float* __restrict__ lnorm, const float* __restrict__ dmin,
-                                  int P, int i, int j, float* x) {
-    const double dx = t.cx[i] - t.cx[j], dy = t.cy[i] - t.cy[j], dz = t.cz[i] - t.cz[j];
-    const double R = sqrt(dx * dx + dy * dy + dz * dz);
-    const float lR = (float)log10(R);
-    x[0] = (float)(1.7320508075688772 * (t.r[i] + t.r[j]) / R);
-    x[1] = log2f((float)(t.r[j] / t.r[i]));
-    x[2] = log2f((float)t.count[i]);
-    for (int k = 0; k <= kQmax; ++k)
-        x[3 + k] = (k <= P) ? fmaxf(lnorm[(size_t)j * (P + 1) + k] - (float)(k + 2) * lR, -40.0f) : -40.0f;
-    x[16] = fminf(dmin[i] * dmin[j] * (float)R, 30.0f) * (1.0f / 30.0f);
-}
 
 namespace {
 
@@ -260,7 +259,8 @@ __global__ void k_pair_errors(const TreeDev t, int P, const int2* __restrict__ p
                 }
         }
         for (int off = 4; off < 32; off <<= 1) err2 += __shfl_xor_sync(0xffffffffu, err2, off);
-        if (lane == 0) labels[(size_t)pr * kMlpOut + (q - kQmin)] = (float)log10(sqrt(err2 / nt) + 1e-30);
+        // errors below 1e-14 (field units) are rounding noise of the FP64 sums
+        if (lane == 0) labels[(size_t)pr * kMlpOut + (q - kQmin)] = (float)log10(fmax(sqrt(err2 / nt), 1e-14));
         __syncwarp();
     }
 }
@@ -412,6 +412,10 @@ int selector_node_norms(Workspace& ws, const TreeDev& t, int P, const double* d_
     k_node_norms<<<grid_for(M, 128), 128, 0, st>>>(M, P, ws.wred.as<double>(), t, d_sorted_damp,
                                                    ws.sel_norms.as<float>(),
                                                    ws.sel_norms.as<float>() + (size_t)M * (P + 1));
+    if (d_sorted_damp) {
+        count_launches(1);
+        k_dmin_up<<<grid_for(M, 128), 128, 0, st>>>(M, t, ws.sel_norms.as<float>() + (size_t)M * (P + 1));
+    }
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
@@ -473,6 +477,7 @@ using namespace fmm;
 extern "C" {
 
 int fmm_mlp_param_count(void) { return kMlpParams; }
+int fmm_selector_param_count(void) { return kMlpParams; }
 
 // Training data of the selector for one system: features and log10 errors
 // at orders 2..12 of up to max_pairs far pairs sampled uniformly from the

@@ -32,6 +32,7 @@
 #include <cstring>
 
 #include "internal.h"
+#include "mlp.cuh"
 #include "pair.cuh"
 
 namespace fmm {
@@ -133,8 +134,8 @@ __global__ void k_radius(const double* __restrict__ X, int64_t n, double* __rest
     if (threadIdx.x == 0) atomicMax(reinterpret_cast<unsigned long long*>(scalars + 5), __double_as_longlong(bm));
 }
 
-__global__ void k_root(double* scalars, int64_t n, int ncrit, double* bd, int32_t* bi, int64_t cap) {
-    const double r = __dmul_rn(scalars[5], 1.0001);
+__global__ void k_root(double* scalars, int64_t n, int ncrit, double* bd, int32_t* bi, int64_t cap, double root_r) {
+    const double r = root_r > 0.0 ? root_r : __dmul_rn(scalars[5], 1.0001);
     const double rmax = __dsqrt_rn(__dmul_rn(__dmul_rn(1.5, r), r));
     scalars[3] = r;
     scalars[4] = rmax;
@@ -280,6 +281,17 @@ __global__ void k_leaf_of(int nleaves, const int32_t* __restrict__ leaves, const
     for (int q = lane; q < c; q += 32) leaf_of[s + q] = k;
 }
 
+// System of each node from its first and last particle (key-sorted order);
+// -1 when they differ (the node spans several packed systems).
+__global__ void k_node_sys(int M, const int32_t* __restrict__ start, const int32_t* __restrict__ count,
+                           const uint32_t* __restrict__ perm, const int32_t* __restrict__ sys,
+                           int32_t* __restrict__ sysid) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= M) return;
+    const int a = sys[perm[start[k]]], b = sys[perm[start[k] + count[k] - 1]];
+    sysid[k] = a == b ? a : -1;
+}
+
 __global__ void k_pos_of(int64_t n, const uint32_t* __restrict__ perm, int32_t* __restrict__ pos_of) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k < n) pos_of[perm[k]] = (int32_t)k;
@@ -299,7 +311,15 @@ __global__ void k_list_iter(const int2* __restrict__ in, int nin, int2* __restri
     const double r = norm2_3(dx, dy, dz);
     const double ri = t.rmax[i], rj = t.rmax[j];
     const bool li = t.is_leaf[i] != 0, lj = t.is_leaf[j] != 0;
-    bool accept = __dmul_rn(r, theta) > __dadd_rn(ri, rj);
+    // batched systems: no pairs across systems; nodes spanning several
+    // systems are always refined
+    bool mixed = false;
+    if (t.sysid) {
+        const int si = t.sysid[i], sj = t.sysid[j];
+        if (si >= 0 && sj >= 0 && si != sj) return;
+        mixed = si < 0 || sj < 0;
+    }
+    bool accept = !mixed && __dmul_rn(r, theta) > __dadd_rn(ri, rj);
     if (accept && rdamp > 0.0) {
         // closest possible particle distance: centre distance minus the cube circumradii
         const double gap = __dsub_rn(r, __dmul_rn(1.7320508075688772, __dadd_rn(t.r[i], t.r[j])));
@@ -311,7 +331,81 @@ __global__ void k_list_iter(const int2* __restrict__ in, int nin, int2* __restri
             far[k] = ((uint64_t)(uint32_t)i << 36) | ((uint64_t)(order & 15) << 32) | (uint32_t)j;
         else
             counters[3] = 1;
-    } else if (li && lj) {
+    } else if (li && lj && !mixed) {
+        const unsigned long long k = atomicAdd(&counters[2], 1ull);
+        if (k < (unsigned long long)cap_near)
+            nearp[k] = ((uint64_t)(uint32_t)i << 32) | (uint32_t)j;
+        else
+            counters[3] = 1;
+    } else {
+        const bool descend_i = lj || ((ri > rj) && !li);
+        const int* ch = t.child + 8 * (descend_i ? i : j);
+        int c[8], nc = 0;
+#pragma unroll
+        for (int o = 0; o < 8; ++o)
+            if (ch[o] >= 0) c[nc++] = ch[o];
+        const unsigned long long base = atomicAdd(&counters[0], (unsigned long long)nc);
+        if (base + nc > (unsigned long long)cap_out) {
+            counters[3] = 1;
+            return;
+        }
+        for (int o = 0; o < nc; ++o) out[base + o] = descend_i ? make_int2(c[o], j) : make_int2(i, c[o]);
+    }
+}
+
+// Learned acceptance (selector): a pair that passes the loose geometric test
+// (theta_loose) and the damping-range test is accepted at the lowest order q
+// (2..qmax) whose predicted log10 truncation error is within the per-pair
+// budget; otherwise it is refined exactly like a pair the test rejects.
+__global__ void __launch_bounds__(128) k_list_iter_learned(
+    const int2* __restrict__ in, int nin, int2* __restrict__ out, int64_t cap_out, uint64_t* __restrict__ far,
+    int64_t cap_far, uint64_t* __restrict__ nearp, int64_t cap_near, const TreeDev t, double theta_loose, double rdamp,
+    int qmax, const float* __restrict__ params, const float* __restrict__ lnorm, const float* __restrict__ dmin,
+    int P, float log_budget, unsigned long long* counters) {
+    __shared__ float Psh[kMlpParams];
+    for (int e = threadIdx.x; e < kMlpParams; e += blockDim.x) Psh[e] = params[e];
+    __syncthreads();
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nin) return;
+    const int i = in[q].x, j = in[q].y;
+    const double dx = __dsub_rn(t.cx[i], __dadd_rn(t.cx[j], 0.0));
+    const double dy = __dsub_rn(t.cy[i], __dadd_rn(t.cy[j], 0.0));
+    const double dz = __dsub_rn(t.cz[i], __dadd_rn(t.cz[j], 0.0));
+    const double r = norm2_3(dx, dy, dz);
+    const double ri = t.rmax[i], rj = t.rmax[j];
+    const bool li = t.is_leaf[i] != 0, lj = t.is_leaf[j] != 0;
+    // batched systems: no pairs across systems; nodes spanning several
+    // systems are always refined
+    bool mixed = false;
+    if (t.sysid) {
+        const int si = t.sysid[i], sj = t.sysid[j];
+        if (si >= 0 && sj >= 0 && si != sj) return;
+        mixed = si < 0 || sj < 0;
+    }
+    bool accept = !mixed && __dmul_rn(r, theta_loose) > __dadd_rn(ri, rj);
+    if (accept && rdamp > 0.0) {
+        const double gap = __dsub_rn(r, __dmul_rn(1.7320508075688772, __dadd_rn(t.r[i], t.r[j])));
+        accept = gap >= rdamp;
+    }
+    int order = 0;
+    if (accept) {
+        float x[kMlpIn], y[kMlpOut];
+        selector_features(t, lnorm, dmin, P, i, j, x);
+        mlp_forward(Psh, x, y);
+        for (int o = kQmin; o <= qmax; ++o)
+            if (y[o - kQmin] <= log_budget) {
+                order = o;
+                break;
+            }
+        accept = order > 0;
+    }
+    if (accept) {
+        const unsigned long long k = atomicAdd(&counters[1], 1ull);
+        if (k < (unsigned long long)cap_far)
+            far[k] = ((uint64_t)(uint32_t)i << 36) | ((uint64_t)(order & 15) << 32) | (uint32_t)j;
+        else
+            counters[3] = 1;
+    } else if (li && lj && !mixed) {
         const unsigned long long k = atomicAdd(&counters[2], 1ull);
         if (k < (unsigned long long)cap_near)
             nearp[k] = ((uint64_t)(uint32_t)i << 32) | (uint32_t)j;
@@ -459,7 +553,8 @@ int build_tree(Workspace& ws, const double* d_X, int64_t n, const TreeParams& tp
     int64_t want = std::max<int64_t>(1024, 4 * (n / std::max(1, tp.ncrit)) + 64);
     FMM_TRY(grow_nodes(ws, want, 0, st));
     count_launches(1);
-    k_root<<<1, 1, 0, st>>>(scal, n, tp.ncrit, ws.node_d.as<double>(), ws.node_i.as<int32_t>(), ws.node_cap);
+    k_root<<<1, 1, 0, st>>>(scal, n, tp.ncrit, ws.node_d.as<double>(), ws.node_i.as<int32_t>(), ws.node_cap,
+                            tp.root_r);
     // keys and sort
     FMM_TRY(ws.keys_a.ensure(sizeof(uint64_t) * n));
     FMM_TRY(ws.keys_b.ensure(sizeof(uint64_t) * n));
@@ -578,6 +673,13 @@ int build_tree(Workspace& ws, const double* d_X, int64_t n, const TreeParams& tp
     k_leaf_of<<<grid_for((int64_t)nl * 32, 256), 256, 0, st>>>(nl, t.leaves, t.start, t.count, t.leaf_of);
     count_launches(1);
     k_pos_of<<<grid_for(n, 256), 256, 0, st>>>(n, t.perm, t.pos_of);
+    t.sysid = nullptr;
+    if (tp.d_sys) {
+        FMM_TRY(ws.sysbuf.ensure(sizeof(int32_t) * (size_t)M));
+        t.sysid = ws.sysbuf.as<int32_t>();
+        count_launches(1);
+        k_node_sys<<<grid_for(M, 256), 256, 0, st>>>(M, t.start, t.count, t.perm, tp.d_sys, t.sysid);
+    }
     double sc[5];
     FMM_CUDA_TRY(cudaMemcpyAsync(sc, scal, sizeof(sc), cudaMemcpyDeviceToHost, st));
     FMM_CUDA_TRY(cudaStreamSynchronize(st));
@@ -623,6 +725,12 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
         while (nin > 0) {
             FMM_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
             count_launches(1);
+            if (tp.sel_params) {
+                k_list_iter_learned<<<grid_for(nin, 128), 128, 0, st>>>(
+                    fin, (int)nin, fout, cap_front, ws.far_pairs.as<uint64_t>(), cap_far, ws.near_pairs.as<uint64_t>(),
+                    cap_near, t, tp.sel_theta, tp.mac_mode == 1 ? tp.rdamp : 0.0, tp.order, tp.sel_params,
+                    tp.sel_lnorm, tp.sel_dmin, tp.sel_P, tp.sel_log_budget, ctr);
+            } else
             k_list_iter<<<grid_for(nin, 256), 256, 0, st>>>(fin, (int)nin, fout, cap_front,
                                                              ws.far_pairs.as<uint64_t>(), cap_far,
                                                              ws.near_pairs.as<uint64_t>(), cap_near, t, tp.theta,

@@ -86,6 +86,22 @@ int fmm_field_fmm(int comm, int64_t n, const double *coordinates, int mdim, cons
                   double *field, const char *damp, int damp_len, const double *damping_factors, int is_periodic,
                   const double *box_matrix, const fmm_opts *opts);
 
+/* Many independent systems in one call (no counterpart in the reference,
+ * which handles one system per call).  System k owns particles
+ * offsets[k] .. offsets[k+1]-1 of the concatenated arrays (same layouts as
+ * fmm_field_fmm, n = offsets[nsys]); its exclusion indices are 1-based within
+ * the system.  Systems do not interact.  They are packed into one octree
+ * whose top levels form a grid with one system per cell; list generation
+ * drops cross-system pairs, so every phase runs once for all systems.  Each
+ * system must have more than ncrit particles.  The per-system trees differ
+ * from those of separate calls (their root box is the grid cell), so results
+ * agree with separate calls to within the FMM truncation error, not bitwise.
+ * Host pointers; blocks until `field` holds the result. */
+int fmm_field_fmm_batched(int nsys, const int64_t *offsets, const double *coordinates, int mdim,
+                          const double *multipoles, int exw, const int32_t *exclusions, double theta, int ncrit,
+                          int expansion_order, int field_order, double *field, const char *damp, int damp_len,
+                          const double *damping_factors, const fmm_opts *opts);
+
 /* Same computations on arrays already resident in device memory (same
  * layouts), enqueued on opts->stream.  No host<->device copies of particle
  * data; the call returns after enqueueing all work except where it must read
@@ -134,8 +150,13 @@ int fmm_field_direct_targets_noalloc(int64_t n, const double *d_coordinates, int
 /* Statistics of the last fmm_field_fmm* call on this thread: tree and list
  * sizes and per-phase device times in milliseconds.  `out` receives up to
  * `len` doubles in this order: num_nodes, num_leaves, max_depth, m2l_pairs,
- * p2p_leaf_pairs, p2p_particle_pairs, t_tree, t_lists, t_p2m_m2m, t_p2p,
- * t_m2l, t_l2l_l2p, t_total.  Returns the number written. */
+ * p2p_leaf_pairs, p2p_particle_pairs, t_tree (with the learned selector's
+ * sampled direct sum), t_p2m_m2m, t_lists, t_p2p, t_m2l, t_l2l_l2p (with the
+ * selector's check), t_total, selector_fallback (1 if the learned selector's
+ * sampled check failed and the fixed rule was used), sampled_rms_err (learned
+ * selector only, else -1), mean expansion order of the far pairs, then the
+ * number of far pairs at each expansion order 0..12.  Returns the number
+ * written (at most 29). */
 int fmm_last_stats(double *out, int len);
 
 /* Diagnostics (no counterpart in the reference): builds the octree and
@@ -156,6 +177,30 @@ int fmm_measure_fma_peak(int precision, double *tflops);
 
 /* Number of kernels this library launched on the calling thread so far. */
 int64_t fmm_launch_count(void);
+
+/* Learned expansion-order selector (no counterpart in the reference): loads
+ * the network parameters (count = fmm_selector_param_count() floats, the
+ * layout written by fmm_gb300/selector_train.py) for the calling thread.
+ * opts->selector = 1 then makes fmm_field_fmm* accept far pairs by the
+ * network's predicted truncation error (orders 2..expansion_order, which must
+ * be >= 10), check the result at sampled particles against an FP64 direct sum
+ * and fall back to the fixed rule (theta, expansion_order) if the check
+ * fails.  Without loaded weights opts->selector = 1 returns FMM_ENOTSUP. */
+int fmm_selector_load(const float *params, int64_t count);
+int fmm_selector_param_count(void);
+
+/* Selector network kernels (training and checks): parameter count, batched
+ * forward pass, gradient of the mean squared error, Adam training; and
+ * training-data collection for one system (features and log10 errors at
+ * orders 2..12 of sampled far pairs).  Host pointers. */
+int fmm_mlp_param_count(void);
+int fmm_mlp_forward(const float *params, const float *x, int64_t n, float *y);
+int fmm_mlp_grad(const float *params, const float *x, const float *y, int64_t n, float *grad, float *loss);
+int fmm_mlp_train(float *params, const float *x, const float *y, int64_t n, int epochs, int batch, float lr,
+                  uint64_t seed, float *losses);
+int fmm_selector_collect(int64_t n, const double *coordinates, int mdim, const double *multipoles,
+                         const double *damping_factors, int ncrit, double theta, int max_pairs, uint64_t seed,
+                         float *features, float *labels, int *npairs);
 
 /* Human-readable text for a status code. */
 const char *fmm_strerror(int status);

@@ -1,0 +1,84 @@
+"""Learned expansion-order selector at run time on the GPU: the shipped
+network meets the accuracy target, does less M2L work than the fixed rule,
+follows the requested target, and a network that under-predicts errors is
+caught by the sampled check (fixed-rule fallback)."""
+import numpy as np
+import pytest
+
+import fmm_gb300
+from fmm_gb300 import Options, systems
+from helpers import per_target_rel
+
+pytestmark = pytest.mark.gpu
+
+N_MOL = 20000
+BOX = 270.0 * (N_MOL / 333333.0) ** (1.0 / 3.0)  # density of the 1M-particle water workload
+
+
+@pytest.fixture(scope="module")
+def water():
+    s = systems.water(N_MOL, BOX, order=2, seed=11)
+    D = fmm_gb300.field_direct(0, s["coordinates"], s["multipoles"], s["exclusions"], 1, "AMOEBA",
+                               s["damping_factors"], options=Options(excl_mode="mask"))
+    return s, D
+
+
+def _run(s, selector, **kw):
+    opt = Options.exact(precision="mixed", mac_mode="damping", selector=selector, **kw)
+    F = fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"], 0.3, 64, 10, 1, "AMOEBA",
+                            s["damping_factors"], options=opt)
+    return F, fmm_gb300.last_stats()
+
+
+def _rms(F, D):
+    e = per_target_rel(F, D, slice(1, 4))
+    return float(np.sqrt(np.mean(e ** 2)))
+
+
+def _m2l_work(st):
+    return sum(st["m2l_pairs_q%d" % q] * (q + 1) ** 4 for q in range(13))
+
+
+def test_learned_meets_target(water):
+    s, D = water
+    F, st = _run(s, "learned", target_rel_err=1e-6)
+    assert st["selector_fallback"] == 0
+    assert 0.0 <= st["sampled_rms_err"] <= 1e-6
+    assert _rms(F, D) <= 1e-6
+
+
+def test_learned_cheaper_than_fixed(water):
+    s, D = water
+    _, sf = _run(s, "fixed")
+    _, sl = _run(s, "learned")
+    assert sf["m2l_order_mean"] == 10.0
+    assert sl["m2l_order_mean"] < 10.0
+    assert _m2l_work(sl) < 0.8 * _m2l_work(sf)
+
+
+def test_looser_target_lowers_orders(water):
+    s, D = water
+    Fa, a = _run(s, "learned", target_rel_err=1e-5)
+    _, b = _run(s, "learned", target_rel_err=1e-6)
+    assert a["m2l_order_mean"] < b["m2l_order_mean"]
+    assert _rms(Fa, D) <= 1e-5
+
+
+def test_underestimating_network_falls_back(water, tmp_path):
+    s, D = water
+    w = np.fromfile(fmm_gb300.SELECTOR_WEIGHTS, dtype="<f4").copy()
+    # last layer: zero weights, bias -30 (predicts 1e-30 at every order, so
+    # every accepted pair would get order 2)
+    nout, nh = 11, 64
+    w[-nout:] = -30.0
+    w[-nout - nout * nh:-nout] = 0.0
+    bad = tmp_path / "bad.bin"
+    w.tofile(bad)
+    fmm_gb300.load_selector(str(bad))
+    try:
+        F, st = _run(s, "learned")
+    finally:
+        fmm_gb300.load_selector()
+    assert st["selector_fallback"] == 1
+    assert st["m2l_order_mean"] == 10.0
+    assert _rms(F, D) <= 1e-6
