@@ -100,6 +100,9 @@ struct Workspace {
     DevBuf front_a, front_b, far_pairs, near_pairs, far_sorted, near_sorted;
     DevBuf node_dfs, far_src, near_src, far_ord, sysbuf;
     DevBuf sel_norms, sel_params, sel_scratch;
+    // grouped M2L
+    DevBuf m2l_tgt, m2l_keys, m2l_keys2, m2l_vals, m2l_vals2, m2l_ukeys, m2l_cnt, m2l_gstart, m2l_tcnt, m2l_toff,
+        m2l_tasks, m2l_T, m2l_gq, m2l_gab, m2l_wsc, m2l_out;
     // sorted particle data
     DevBuf sx, sy, sz, smc, sd;
     DevBuf f32buf;  // FP32 particle data of the mixed-precision near field
@@ -153,6 +156,7 @@ int launch_p2p_f64(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
 int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, cudaStream_t st);
 int launch_m2l(Workspace& ws, const TreeDev& t, int p, const Modes& md, cudaStream_t st);
 int launch_m2l_reduced(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaStream_t st);
+int launch_m2l_grouped(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaStream_t st);
 int launch_reduce_moments(Workspace& ws, const TreeDev& t, int p, cudaStream_t st);
 // selector.cu
 int selector_node_norms(Workspace& ws, const TreeDev& t, int P, const double* d_sorted_damp, cudaStream_t st);

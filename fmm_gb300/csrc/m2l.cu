@@ -317,10 +317,16 @@ int launch_m2l_reduced(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaSt
         count_launches(1);
         k_reduce_moments<<<grid_for(M, wpb), 32 * wpb, sm, st>>>(M, p, ws.mom.as<double>(), ws.wred.as<double>());
     }
-    if (fp32)
-        FMM_TRY(launch_red<float>(ws, t, p, st));
-    else
-        FMM_TRY(launch_red<double>(ws, t, p, st));
+    const int gst = launch_m2l_grouped(ws, t, p, fp32, st);
+    if (gst == FMM_ENOTSUP) {
+        // FP64 operator too large for shared memory: per-pair kernel
+        if (fp32)
+            FMM_TRY(launch_red<float>(ws, t, p, st));
+        else
+            FMM_TRY(launch_red<double>(ws, t, p, st));
+    } else {
+        FMM_TRY(gst);
+    }
     count_launches(1);
     k_complete_locals<<<grid_for(M, 4), 128, 0, st>>>(M, p, ws.loc.as<double>());
     FMM_CUDA_TRY(cudaGetLastError());

@@ -1,0 +1,509 @@
+// M2L as dense matrix products grouped by displacement (exact-coefficient
+// modes; the reference's per-pair M2L is src/fmm.F90:826-882).
+//
+// Octree cells are cubes on a grid: the centre displacement of two cells is an
+// integer multiple D of the smaller cell's half-width, and a pair's
+// reduced-basis M2L operator depends only on D, the level difference and the
+// pair's expansion order q.  The far pairs are sorted by that key; each group
+// shares one operator G ((q+1)^2 x (q+1)^2, from the restricted tensor T of
+// the group's displacement, computed once per group in FP64), and the group's
+// pairs are the columns of one product C = G W, evaluated by register-tiled
+// blocks on the CUDA cores.  Per-pair columns go to a buffer in target-sorted
+// order and are summed per target in FP64.
+//
+// Units: per-node weights w'_s = w^_s / h_j^|s|, per-target locals
+// L'_f = h_i^(|f|+1) L_f, tensor T(D_c) at the displacement in units of the
+// coarser cell's half-width h_c; then G_fs = a^(|f|+1) b^|s| T_{s+f}(D_c)
+// with a = h_i/h_c, b = h_j/h_c (powers of two, at most 1), so all operands
+// are O(1) and the FP32 products stay in range.
+#include <algorithm>
+
+#include <cub/cub.cuh>
+
+#include "internal.h"
+#include "m2l_basis.cuh"
+
+namespace fmm {
+
+namespace {
+
+inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+constexpr int kFallback = 63;            // key code of pairs without a grid displacement
+constexpr int64_t kDOff = 1 << 17;       // offset of the 18-bit displacement fields
+constexpr int kTaskCols = 256;           // pairs (columns) per product block
+constexpr int kGemmThreads = 128;        // 16 row groups x 8 column groups
+constexpr int kMaxRed = (kMaxP + 1) * (kMaxP + 1);  // reduced components at the highest order
+
+__global__ void k_far_targets(int M, const int32_t* __restrict__ off, int32_t* __restrict__ tgt) {
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= M) return;
+    for (int q = off[i] + lane; q < off[i + 1]; q += 32) tgt[q] = i;
+}
+
+// w'_s = w^_s / h^|s| per node (h the node's half-width).
+template <typename R>
+__global__ void k_scale_weights(int64_t total, int nr, const double* __restrict__ wred, const double* __restrict__ h,
+                                R* __restrict__ wsc) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = e / nr;
+        const int s = (int)(e - node * nr);
+        int k = 0;
+        while ((k + 1) * (k + 1) <= s) ++k;
+        const double ih = 1.0 / h[node];
+        double sc = 1.0;
+        for (int u = 0; u < k; ++u) sc *= ih;
+        wsc[e] = (R)(wred[e] * sc);
+    }
+}
+
+// Group key of every far pair: level difference, expansion order and integer
+// displacement in units of the smaller half-width; pairs off the grid (or
+// with out-of-range fields) get unique keys of their own.
+__global__ void k_m2l_keys(int64_t nfar, const TreeDev t, const int32_t* __restrict__ tgt, int p,
+                           uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= nfar) return;
+    const int i = tgt[q], j = t.far_src[q];
+    const int ord = t.far_ord ? min((int)t.far_ord[q], p) : p;
+    const double hf = fmin(t.r[i], t.r[j]);
+    const double dx = (t.cx[i] - t.cx[j]) / hf, dy = (t.cy[i] - t.cy[j]) / hf, dz = (t.cz[i] - t.cz[j]) / hf;
+    const double rx = rint(dx), ry = rint(dy), rz = rint(dz);
+    const int dl = t.depth[i] - t.depth[j];
+    const double lim = (double)(kDOff - 1);
+    const bool grid = fabs(dx - rx) < 1e-6 && fabs(dy - ry) < 1e-6 && fabs(dz - rz) < 1e-6 && fabs(rx) <= lim &&
+                      fabs(ry) <= lim && fabs(rz) <= lim && dl > -31 && dl < 31;
+    uint64_t key;
+    if (grid)
+        key = ((uint64_t)(dl + 31) << 58) | ((uint64_t)ord << 54) | ((uint64_t)((int64_t)rx + kDOff) << 36) |
+              ((uint64_t)((int64_t)ry + kDOff) << 18) | (uint64_t)((int64_t)rz + kDOff);
+    else
+        key = ((uint64_t)kFallback << 58) | (uint64_t)q;
+    keys[q] = key;
+    vals[q] = (int32_t)q;
+}
+
+// One warp per group: restricted tensor T(D_c) of orders <= 2q in FP64 by the
+// Hermite recursion (two level buffers in shared memory), stored as R, with
+// the group's order and unit ratios a, b.
+template <typename R>
+__global__ void __launch_bounds__(128) k_group_tensor(int ngroups, const uint64_t* __restrict__ ukeys,
+                                                      const int32_t* __restrict__ gstart,
+                                                      const int32_t* __restrict__ svals,
+                                                      const int32_t* __restrict__ tgt, const TreeDev t, int p,
+                                                      int ldT, R* __restrict__ gT, int32_t* __restrict__ gq,
+                                                      float2* __restrict__ gab) {
+    extern __shared__ double smg[];
+    const int N = 2 * p, nTr = rbase(N + 1);
+    int2* rule = reinterpret_cast<int2*>(smg);
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* TA = smg + nTr + wib * (2 * nTr + N + 1);
+    double* TB = TA + nTr;
+    double* gsh = TB + nTr;
+    for (int e = threadIdx.x; e < nTr; e += blockDim.x) rule[e] = restricted_rule(e);
+    __syncthreads();
+    const int g = blockIdx.x * (blockDim.x >> 5) + wib;
+    if (g >= ngroups) return;
+    const uint64_t key = ukeys[g];
+    const int pos0 = svals[gstart[g]];
+    const int i = tgt[pos0], j = t.far_src[pos0];
+    const int q = (int)(key >> 58) == kFallback ? (t.far_ord ? min((int)t.far_ord[pos0], p) : p)
+                                                 : (int)((key >> 54) & 15);
+    const double hi = t.r[i], hj = t.r[j], hc = fmax(hi, hj);
+    const double X = (t.cx[i] - t.cx[j]) / hc, Y = (t.cy[i] - t.cy[j]) / hc, Z = (t.cz[i] - t.cz[j]) / hc;
+    const int Nq = 2 * q;
+    const double r2 = X * X + Y * Y + Z * Z;
+    const double rinv = 1.0 / sqrt(r2), rinv2 = rinv * rinv;
+    if (lane <= Nq) {
+        double v = rinv, c = 1.0;
+        for (int jj = 1; jj <= lane; ++jj) {
+            v *= rinv2;
+            c *= -(double)(2 * jj - 1);
+        }
+        gsh[lane] = c * v;
+    }
+    __syncwarp();
+    double* A = TA;
+    double* B = TB;
+    if (lane == 0) A[0] = gsh[Nq];
+    __syncwarp();
+    for (int lev = Nq - 1; lev >= 0; --lev) {
+        const int lim = rbase(Nq - lev + 1);
+        for (int e = lane; e < lim; e += 32) {
+            double v;
+            if (e == 0) {
+                v = gsh[lev];
+            } else {
+                const int2 ru = rule[e];
+                const int dir = ru.x >> 16, cnt = ru.y >> 16;
+                const double crd = dir == 0 ? X : (dir == 1 ? Y : Z);
+                v = crd * A[ru.x & 0xffff];
+                if (cnt > 0) v += (double)cnt * A[ru.y & 0xffff];
+            }
+            B[e] = v;
+        }
+        __syncwarp();
+        double* tmp = A;
+        A = B;
+        B = tmp;
+    }
+    R* out = gT + (size_t)g * ldT;
+    for (int e = lane; e < rbase(Nq + 1); e += 32) out[e] = (R)A[e];
+    if (lane == 0) {
+        gq[g] = q;
+        gab[g] = make_float2((float)(hi / hc), (float)(hj / hc));
+    }
+}
+
+__global__ void k_task_counts(int ng, const int32_t* __restrict__ gstart, int32_t* __restrict__ tcnt) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g > ng) return;
+    tcnt[g] = g < ng ? (gstart[g + 1] - gstart[g] + kTaskCols - 1) / kTaskCols : 0;
+}
+
+__global__ void k_fill_tasks(int ng, const int32_t* __restrict__ gstart, const int32_t* __restrict__ toff,
+                             int2* __restrict__ tasks) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    const int n = toff[g + 1] - toff[g];
+    for (int k = 0; k < n; ++k) tasks[toff[g] + k] = make_int2(g, k * kTaskCols);
+}
+
+// Loads a thread's CPT consecutive weight entries (16-byte aligned) as vectors.
+template <typename R, int CPT>
+__device__ __forceinline__ void load_row(const R* p, R* v);
+template <>
+__device__ __forceinline__ void load_row<float, 8>(const float* p, float* v) {
+    const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+template <>
+__device__ __forceinline__ void load_row<double, 4>(const double* p, double* v) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+
+// Shared-memory plan of the product kernel (elements of R unless noted).
+template <typename R, int CPT>
+struct GemmSmem {
+    static constexpr int TN = 8 * CPT;  // columns per tile
+    static constexpr int LDW = TN + 4;  // padded row stride of the weight tile
+    int nrmax, rmmax, nTr;
+    size_t off_dec, off_pow, off_T, off_G, off_W, off_col, bytes;
+    __host__ __device__ GemmSmem(int p) {
+        nrmax = (p + 1) * (p + 1);
+        rmmax = 16 * ((nrmax + 15) / 16);
+        nTr = rbase(2 * p + 1);
+        size_t o = 0;
+        off_dec = o;
+        o += sizeof(int) * nrmax;
+        o = (o + 15) & ~(size_t)15;
+        off_pow = o;
+        o += sizeof(R) * 32;
+        off_T = o;
+        o += sizeof(R) * nTr;
+        o = (o + 15) & ~(size_t)15;
+        off_G = o;
+        o += sizeof(R) * (size_t)nrmax * rmmax;
+        off_W = o;
+        o += sizeof(R) * (size_t)nrmax * LDW;
+        off_col = o;
+        o += sizeof(int) * 2 * TN;
+        bytes = o;
+    }
+};
+
+// Columns [c_begin, c_begin + kTaskCols) of one group: C = G W for tiles of
+// TN pairs; thread (rg, cg) owns rows rg + 16k (k < RT) and columns
+// cg*CPT .. cg*CPT + CPT - 1 of each tile.
+template <typename R, int RT, int CPT>
+__device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, int g, int c_begin, int nrq, int cnt,
+                                          int gs, const int32_t* __restrict__ svals,
+                                          const int32_t* __restrict__ far_src, const R* __restrict__ wsc, int nr,
+                                          R* __restrict__ out, int ldo) {
+    constexpr int TN = GemmSmem<R, CPT>::TN;
+    constexpr int LDW = GemmSmem<R, CPT>::LDW;
+    constexpr int RM = 16 * RT;
+    const int tid = threadIdx.x;
+    const int rg = tid & 15, cg = tid >> 4;
+    const int* dec = reinterpret_cast<const int*>(sm + L.off_dec);
+    const R* apow = reinterpret_cast<const R*>(sm + L.off_pow);
+    const R* bpow = apow + 16;
+    const R* Tsh = reinterpret_cast<const R*>(sm + L.off_T);
+    R* G = reinterpret_cast<R*>(sm + L.off_G);
+    R* W = reinterpret_cast<R*>(sm + L.off_W);
+    int* colpos = reinterpret_cast<int*>(sm + L.off_col);
+    int* colsrc = colpos + TN;
+    // operator G^T (s-major, RM rows per s; rows >= nrq are zero)
+    for (int e = tid; e < nrq * RM; e += kGemmThreads) {
+        const int s = e / RM, f = e - s * RM;
+        R v = (R)0;
+        if (f < nrq) {
+            const int cs = dec[s], cf = dec[f];
+            const int x = (cs & 0xff) + (cf & 0xff), y = ((cs >> 8) & 0xff) + ((cf >> 8) & 0xff),
+                      z = ((cs >> 16) & 0xff) + ((cf >> 16) & 0xff);
+            v = apow[(cf >> 24) + 1] * bpow[cs >> 24] * Tsh[ridx(x, y, z)];
+        }
+        G[e] = v;
+    }
+    const int c_end = min(cnt, c_begin + kTaskCols);
+    for (int cb = c_begin; cb < c_end; cb += TN) {
+        const int ncol = min(TN, c_end - cb);
+        __syncthreads();  // G ready; previous tile's W and columns consumed
+        if (tid < TN) {
+            if (tid < ncol) {
+                const int pos = svals[gs + cb + tid];
+                colpos[tid] = pos;
+                colsrc[tid] = far_src[pos];
+            } else {
+                colpos[tid] = -1;
+                colsrc[tid] = -1;
+            }
+        }
+        __syncthreads();
+        // weight tile W[s][c] (coalesced along s)
+        for (int e = tid; e < nrq * TN; e += kGemmThreads) {
+            const int c = e / nrq, s = e - c * nrq;
+            const int src = colsrc[c];
+            W[s * LDW + c] = src >= 0 ? wsc[(size_t)src * nr + s] : (R)0;
+        }
+        __syncthreads();
+        R acc[RT][CPT];
+#pragma unroll
+        for (int k = 0; k < RT; ++k)
+#pragma unroll
+            for (int l = 0; l < CPT; ++l) acc[k][l] = (R)0;
+        const R* Gp = G + rg;
+        const R* Wp = W + cg * CPT;
+#pragma unroll 2
+        for (int s = 0; s < nrq; ++s) {
+            R gv[RT], wv[CPT];
+#pragma unroll
+            for (int k = 0; k < RT; ++k) gv[k] = Gp[s * RM + 16 * k];
+            load_row<R, CPT>(Wp + s * LDW, wv);
+#pragma unroll
+            for (int k = 0; k < RT; ++k)
+#pragma unroll
+                for (int l = 0; l < CPT; ++l) acc[k][l] = fma(gv[k], wv[l], acc[k][l]);
+        }
+#pragma unroll
+        for (int l = 0; l < CPT; ++l) {
+            const int c = cg * CPT + l;
+            if (c < ncol) {
+                R* o = out + (size_t)colpos[c] * ldo;
+#pragma unroll
+                for (int k = 0; k < RT; ++k) {
+                    const int f = rg + 16 * k;
+                    if (f < nrq) o[f] = acc[k][l];
+                }
+            }
+        }
+    }
+}
+
+template <typename R, int CPT>
+__global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restrict__ tasks, int p,
+                                                           const int32_t* __restrict__ gstart,
+                                                           const int32_t* __restrict__ gq,
+                                                           const float2* __restrict__ gab, const R* __restrict__ gT,
+                                                           int ldT, const int32_t* __restrict__ svals,
+                                                           const int32_t* __restrict__ far_src,
+                                                           const R* __restrict__ wsc, R* __restrict__ out) {
+    extern __shared__ __align__(16) char sm_gemm[];
+    const GemmSmem<R, CPT> L(p);
+    const int nr = (p + 1) * (p + 1);
+    const int2 task = tasks[blockIdx.x];
+    const int g = task.x;
+    const int q = gq[g], nrq = (q + 1) * (q + 1);
+    const int gs = gstart[g], cnt = gstart[g + 1] - gs;
+    int* dec = reinterpret_cast<int*>(sm_gemm + L.off_dec);
+    R* apow = reinterpret_cast<R*>(sm_gemm + L.off_pow);
+    R* bpow = apow + 16;
+    R* Tsh = reinterpret_cast<R*>(sm_gemm + L.off_T);
+    for (int e = threadIdx.x; e < nrq; e += kGemmThreads) dec[e] = qcomp(e);
+    if (threadIdx.x < 16) {
+        const float2 ab = gab[g];
+        R a = (R)1, b = (R)1;
+        for (int u = 0; u < (int)threadIdx.x; ++u) {
+            a *= (R)ab.x;
+            b *= (R)ab.y;
+        }
+        apow[threadIdx.x] = a;
+        bpow[threadIdx.x] = b;
+    }
+    const int nTq = rbase(2 * q + 1);
+    for (int e = threadIdx.x; e < nTq; e += kGemmThreads) Tsh[e] = gT[(size_t)g * ldT + e];
+    __syncthreads();
+    const int rt = (nrq + 15) / 16;
+    switch (rt) {
+#define FMM_GEMM_CASE(K)                                                                                     \
+    case K:                                                                                                  \
+        gemm_task<R, K, CPT>(L, sm_gemm, g, task.y, nrq, cnt, gs, svals, far_src, wsc, nr, out, nr); \
+        break;
+        FMM_GEMM_CASE(1)
+        FMM_GEMM_CASE(2)
+        FMM_GEMM_CASE(3)
+        FMM_GEMM_CASE(4)
+        FMM_GEMM_CASE(5)
+        FMM_GEMM_CASE(6)
+        FMM_GEMM_CASE(7)
+        FMM_GEMM_CASE(8)
+        FMM_GEMM_CASE(9)
+        FMM_GEMM_CASE(10)
+        FMM_GEMM_CASE(11)
+#undef FMM_GEMM_CASE
+        default:
+            break;
+    }
+}
+
+// Warp per target: FP64 sum of its pairs' columns, back to physical units,
+// into the reduced components of the local expansion.
+template <typename R>
+__global__ void k_m2l_sum(const TreeDev t, int p, const R* __restrict__ out, double* __restrict__ loc) {
+    constexpr int RPL = (kMaxRed + 31) / 32;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= t.num_nodes) return;
+    const int nr = (p + 1) * (p + 1);
+    double acc[RPL];
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) acc[r] = 0.0;
+    const int q0 = t.far_off[i], q1 = t.far_off[i + 1];
+    for (int q = q0; q < q1; ++q) {
+        const int ord = t.far_ord ? min((int)t.far_ord[q], p) : p;
+        const int nrq = (ord + 1) * (ord + 1);
+        const R* o = out + (size_t)q * nr;
+#pragma unroll
+        for (int r = 0; r < RPL; ++r) {
+            const int f = lane + 32 * r;
+            if (f < nrq) acc[r] += (double)o[f];
+        }
+    }
+    const double ih = 1.0 / t.r[i];
+    double* L = loc + (size_t)i * nT(p);
+#pragma unroll
+    for (int r = 0; r < RPL; ++r) {
+        const int f = lane + 32 * r;
+        if (f < nr) {
+            const int c = qcomp(f);
+            const int k = c >> 24;
+            double s = ih;
+            for (int e = 0; e < k; ++e) s *= ih;
+            L[pidx(c & 0xff, (c >> 8) & 0xff, (c >> 16) & 0xff)] = acc[r] * s;
+        }
+    }
+}
+
+template <typename R, int CPT>
+int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
+    const int M = t.num_nodes, nr = (p + 1) * (p + 1), N = 2 * p, nTr = rbase(N + 1);
+    const int64_t nf = t.nfar;
+    FMM_TRY(ws.m2l_out.ensure(sizeof(R) * (size_t)std::max<int64_t>(1, nf) * nr));
+    if (nf > 0) {
+        FMM_TRY(ws.m2l_tgt.ensure(sizeof(int32_t) * nf));
+        FMM_TRY(ws.m2l_keys.ensure(sizeof(uint64_t) * nf));
+        FMM_TRY(ws.m2l_keys2.ensure(sizeof(uint64_t) * nf));
+        FMM_TRY(ws.m2l_vals.ensure(sizeof(int32_t) * nf));
+        FMM_TRY(ws.m2l_vals2.ensure(sizeof(int32_t) * nf));
+        FMM_TRY(ws.m2l_ukeys.ensure(sizeof(uint64_t) * nf));
+        FMM_TRY(ws.m2l_cnt.ensure(sizeof(int32_t) * (nf + 1)));
+        FMM_TRY(ws.m2l_gstart.ensure(sizeof(int32_t) * (nf + 1)));
+        FMM_TRY(ws.m2l_wsc.ensure(sizeof(R) * (size_t)M * nr));
+        FMM_TRY(ws.counters.ensure(sizeof(unsigned long long) * 32));
+        int32_t* tgt = ws.m2l_tgt.as<int32_t>();
+        count_launches(1);
+        k_far_targets<<<grid_for(M, 4), 128, 0, st>>>(M, t.far_off, tgt);
+        count_launches(1);
+        k_scale_weights<R><<<grid_for((int64_t)M * nr, 256), 256, 0, st>>>((int64_t)M * nr, nr, ws.wred.as<double>(),
+                                                                          t.r, ws.m2l_wsc.as<R>());
+        count_launches(1);
+        k_m2l_keys<<<grid_for(nf, 256), 256, 0, st>>>(nf, t, tgt, p, ws.m2l_keys.as<uint64_t>(),
+                                                       ws.m2l_vals.as<int32_t>());
+        // sort by key, run-length encode into groups
+        int* d_nruns = reinterpret_cast<int*>(ws.counters.as<unsigned long long>() + 14);
+        size_t tb1 = 0, tb2 = 0, tb3 = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, tb1, ws.m2l_keys.as<uint64_t>(), ws.m2l_keys2.as<uint64_t>(),
+                                        ws.m2l_vals.as<int32_t>(), ws.m2l_vals2.as<int32_t>(), (int)nf, 0, 64, st);
+        cub::DeviceRunLengthEncode::Encode(nullptr, tb2, ws.m2l_keys2.as<uint64_t>(), ws.m2l_ukeys.as<uint64_t>(),
+                                           ws.m2l_cnt.as<int32_t>(), d_nruns, (int)nf, st);
+        cub::DeviceScan::ExclusiveSum(nullptr, tb3, ws.m2l_cnt.as<int32_t>(), ws.m2l_gstart.as<int32_t>(),
+                                      (int)nf + 1, st);
+        FMM_TRY(ws.cub_tmp.ensure(std::max(tb1, std::max(tb2, tb3))));
+        FMM_CUDA_TRY(cub::DeviceRadixSort::SortPairs(ws.cub_tmp.p, tb1, ws.m2l_keys.as<uint64_t>(),
+                                                     ws.m2l_keys2.as<uint64_t>(), ws.m2l_vals.as<int32_t>(),
+                                                     ws.m2l_vals2.as<int32_t>(), (int)nf, 0, 64, st));
+        FMM_CUDA_TRY(cub::DeviceRunLengthEncode::Encode(ws.cub_tmp.p, tb2, ws.m2l_keys2.as<uint64_t>(),
+                                                        ws.m2l_ukeys.as<uint64_t>(), ws.m2l_cnt.as<int32_t>(),
+                                                        d_nruns, (int)nf, st));
+        int ng = 0;
+        FMM_CUDA_TRY(cudaMemcpyAsync(&ng, d_nruns, sizeof(int), cudaMemcpyDeviceToHost, st));
+        FMM_CUDA_TRY(cudaStreamSynchronize(st));
+        FMM_CUDA_TRY(cudaMemsetAsync(ws.m2l_cnt.as<int32_t>() + ng, 0, sizeof(int32_t), st));
+        size_t tb4 = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tb4, ws.m2l_cnt.as<int32_t>(), ws.m2l_gstart.as<int32_t>(), ng + 1, st);
+        FMM_TRY(ws.cub_tmp.ensure(tb4));
+        FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb4, ws.m2l_cnt.as<int32_t>(),
+                                                   ws.m2l_gstart.as<int32_t>(), ng + 1, st));
+        // per-group tensors
+        const int ldT = nTr;
+        FMM_TRY(ws.m2l_T.ensure(sizeof(R) * (size_t)ng * ldT));
+        FMM_TRY(ws.m2l_gq.ensure(sizeof(int32_t) * ng));
+        FMM_TRY(ws.m2l_gab.ensure(sizeof(float2) * ng));
+        {
+            const int wpb = 4;
+            const size_t sm = sizeof(double) * (nTr + (size_t)wpb * (2 * nTr + N + 1));
+            if (sm > 48 * 1024)
+                FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_group_tensor<R>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            count_launches(1);
+            k_group_tensor<R><<<grid_for(ng, wpb), 32 * wpb, sm, st>>>(
+                ng, ws.m2l_ukeys.as<uint64_t>(), ws.m2l_gstart.as<int32_t>(), ws.m2l_vals2.as<int32_t>(), tgt, t, p,
+                ldT, ws.m2l_T.as<R>(), ws.m2l_gq.as<int32_t>(), ws.m2l_gab.as<float2>());
+        }
+        // tasks: up to kTaskCols pairs of one group each
+        FMM_TRY(ws.m2l_tcnt.ensure(sizeof(int32_t) * (ng + 1)));
+        FMM_TRY(ws.m2l_toff.ensure(sizeof(int32_t) * (ng + 1)));
+        count_launches(1);
+        k_task_counts<<<grid_for(ng + 1, 256), 256, 0, st>>>(ng, ws.m2l_gstart.as<int32_t>(),
+                                                              ws.m2l_tcnt.as<int32_t>());
+        size_t tb5 = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tb5, ws.m2l_tcnt.as<int32_t>(), ws.m2l_toff.as<int32_t>(), ng + 1, st);
+        FMM_TRY(ws.cub_tmp.ensure(tb5));
+        FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb5, ws.m2l_tcnt.as<int32_t>(),
+                                                   ws.m2l_toff.as<int32_t>(), ng + 1, st));
+        int ntasks = 0;
+        FMM_CUDA_TRY(cudaMemcpyAsync(&ntasks, ws.m2l_toff.as<int32_t>() + ng, sizeof(int), cudaMemcpyDeviceToHost, st));
+        FMM_CUDA_TRY(cudaStreamSynchronize(st));
+        FMM_TRY(ws.m2l_tasks.ensure(sizeof(int2) * std::max(1, ntasks)));
+        count_launches(1);
+        k_fill_tasks<<<grid_for(ng, 256), 256, 0, st>>>(ng, ws.m2l_gstart.as<int32_t>(), ws.m2l_toff.as<int32_t>(),
+                                                        ws.m2l_tasks.as<int2>());
+        const GemmSmem<R, CPT> L(p);
+        FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_m2l_gemm<R, CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)L.bytes));
+        count_launches(1);
+        k_m2l_gemm<R, CPT><<<(unsigned)ntasks, kGemmThreads, L.bytes, st>>>(
+            ws.m2l_tasks.as<int2>(), p, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(),
+            ws.m2l_gab.as<float2>(), ws.m2l_T.as<R>(), ldT, ws.m2l_vals2.as<int32_t>(), t.far_src,
+            ws.m2l_wsc.as<R>(), ws.m2l_out.as<R>());
+    }
+    count_launches(1);
+    k_m2l_sum<R><<<grid_for(M, 4), 128, 0, st>>>(t, p, ws.m2l_out.as<R>(), ws.loc.as<double>());
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
+}  // namespace
+
+// Grouped reduced-basis M2L into the reduced components of ws.loc (the
+// weights ws.wred must be current).  FP32 products for `fp32`, else FP64;
+// returns FMM_ENOTSUP where the FP64 operator does not fit shared memory.
+int launch_m2l_grouped(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaStream_t st) {
+    if (fp32) return grouped<float, 8>(ws, t, p, st);
+    if (GemmSmem<double, 4>(p).bytes > 227 * 1024) return FMM_ENOTSUP;
+    return grouped<double, 4>(ws, t, p, st);
+}
+
+}  // namespace fmm
