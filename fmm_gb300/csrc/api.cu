@@ -60,7 +60,7 @@ Workspace& thread_workspace() {
 
 namespace {
 
-constexpr int kNumStats = 16 + kMaxP + 1;
+constexpr int kNumStats = 16 + kMaxP + 1 + 3;
 struct Stats {
     double v[kNumStats] = {0};
 };
@@ -230,6 +230,8 @@ double sampled_rms(const std::vector<double>& F, const std::vector<double>& R, i
 int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, int f, const Opts& o,
             const TreeParams& tp, double* d_field, cudaStream_t st) {
     ensure_events(ws);
+    ws.product_timed = false;
+    ws.m2l_groups = 0;
     const bool learned = o.selector == 1;
     if (learned && !ws.sel_ready) return FMM_ENOTSUP;  // no selector weights loaded
     Modes md{o.coef_mode, o.excl_mode, o.precision};
@@ -299,6 +301,7 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
             FMM_TRY(launch_p2p_f32(ws, P, t, f, st));
         else
             FMM_TRY(launch_p2p_f64(ws, P, t, f, md, st));
+        cudaEventRecord(ws.ev[7], st);  // end of the near-field kernel proper
         FMM_TRY(launch_excl_correction(ws, P, &t, f, md, ws.fsorted.as<double>(), st));
         cudaEventRecord(ws.ev[4], st);
         FMM_TRY(launch_m2l(ws, t, p, md, st));
@@ -357,6 +360,12 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         osum += (double)q * (double)hist[q];
     }
     s.v[15] = t.nfar > 0 ? osum / (double)t.nfar : 0.0;
+    cudaEventElapsedTime(&ms, ws.ev[3], ws.ev[7]);
+    s.v[16 + kMaxP + 1] = ms;
+    ms = -1.0f;
+    if (ws.product_timed) cudaEventElapsedTime(&ms, ws.ev[8], ws.ev[9]);
+    s.v[16 + kMaxP + 2] = ms;
+    s.v[16 + kMaxP + 3] = (double)ws.m2l_groups;
     g_stats = s;
     return FMM_OK;
 }

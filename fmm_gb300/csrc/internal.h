@@ -118,6 +118,8 @@ struct Workspace {
     // timing
     cudaEvent_t ev[16] = {};
     bool events_ready = false;
+    bool product_timed = false;  // ev[8], ev[9] bracket the grouped M2L product kernel of the last call
+    int64_t m2l_groups = 0;      // displacement groups of the last grouped M2L
     int device = -1;
     int64_t node_cap = 0;
     ~Workspace();

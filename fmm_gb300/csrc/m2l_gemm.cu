@@ -371,15 +371,26 @@ __global__ void k_m2l_sum(const TreeDev t, int p, const R* __restrict__ out, dou
 #pragma unroll
     for (int r = 0; r < RPL; ++r) acc[r] = 0.0;
     const int q0 = t.far_off[i], q1 = t.far_off[i + 1];
-    for (int q = q0; q < q1; ++q) {
-        const int ord = t.far_ord ? min((int)t.far_ord[q], p) : p;
-        const int nrq = (ord + 1) * (ord + 1);
-        const R* o = out + (size_t)q * nr;
+    // four pairs per step: independent loads in flight
+    constexpr int U = 4;
+    for (int qb = q0; qb < q1; qb += U) {
+        R v[U][RPL];
 #pragma unroll
-        for (int r = 0; r < RPL; ++r) {
-            const int f = lane + 32 * r;
-            if (f < nrq) acc[r] += (double)o[f];
+        for (int u = 0; u < U; ++u) {
+            const int q = qb + u;
+            const int ord = q < q1 ? (t.far_ord ? min((int)t.far_ord[q], p) : p) : -1;
+            const int nrq = (ord + 1) * (ord + 1);
+            const R* o = out + (size_t)q * nr;
+#pragma unroll
+            for (int r = 0; r < RPL; ++r) {
+                const int f = lane + 32 * r;
+                v[u][r] = f < nrq ? o[f] : (R)0;
+            }
         }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int r = 0; r < RPL; ++r) acc[r] += (double)v[u][r];
     }
     const double ih = 1.0 / t.r[i];
     double* L = loc + (size_t)i * nT(p);
@@ -440,6 +451,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         int ng = 0;
         FMM_CUDA_TRY(cudaMemcpyAsync(&ng, d_nruns, sizeof(int), cudaMemcpyDeviceToHost, st));
         FMM_CUDA_TRY(cudaStreamSynchronize(st));
+        ws.m2l_groups = ng;
         FMM_CUDA_TRY(cudaMemsetAsync(ws.m2l_cnt.as<int32_t>() + ng, 0, sizeof(int32_t), st));
         size_t tb4 = 0;
         cub::DeviceScan::ExclusiveSum(nullptr, tb4, ws.m2l_cnt.as<int32_t>(), ws.m2l_gstart.as<int32_t>(), ng + 1, st);
@@ -483,11 +495,16 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         const GemmSmem<R, CPT> L(p);
         FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_m2l_gemm<R, CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)L.bytes));
+        if (ws.events_ready) {
+            cudaEventRecord(ws.ev[8], st);
+            ws.product_timed = true;
+        }
         count_launches(1);
         k_m2l_gemm<R, CPT><<<(unsigned)ntasks, kGemmThreads, L.bytes, st>>>(
             ws.m2l_tasks.as<int2>(), p, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(),
             ws.m2l_gab.as<float2>(), ws.m2l_T.as<R>(), ldT, ws.m2l_vals2.as<int32_t>(), t.far_src,
             ws.m2l_wsc.as<R>(), ws.m2l_out.as<R>());
+        if (ws.product_timed) cudaEventRecord(ws.ev[9], st);
     }
     count_launches(1);
     k_m2l_sum<R><<<grid_for(M, 4), 128, 0, st>>>(t, p, ws.m2l_out.as<R>(), ws.loc.as<double>());

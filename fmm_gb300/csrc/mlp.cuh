@@ -57,6 +57,104 @@ __device__ __forceinline__ void mlp_forward(const float* __restrict__ P, const f
     mlp_layer<kMlpOut, kMlpH, false>(P + kOffW4, P + kOffB4, h1, y);
 }
 
+// Inference layout of the parameters in shared memory (floats): the blob
+// with W1's rows padded from kMlpIn to kMlpInP entries so that every weight
+// row starts on a 16-byte boundary and is read as float4, and W4/b4 padded to
+// kMlpOutP rows (zeros) so outputs come in blocks of four.
+constexpr int kMlpInP = 20;
+constexpr int kMlpOutP = 12;
+constexpr int kSOffMean = 0;
+constexpr int kSOffIstd = kSOffMean + kMlpIn;
+constexpr int kSOffW1 = 36;
+constexpr int kSOffB1 = kSOffW1 + kMlpH * kMlpInP;
+constexpr int kSOffW2 = kSOffB1 + kMlpH;
+constexpr int kSOffB2 = kSOffW2 + kMlpH * kMlpH;
+constexpr int kSOffW3 = kSOffB2 + kMlpH;
+constexpr int kSOffB3 = kSOffW3 + kMlpH * kMlpH;
+constexpr int kSOffW4 = kSOffB3 + kMlpH;
+constexpr int kSOffB4 = kSOffW4 + kMlpOutP * kMlpH;
+constexpr int kMlpSmem = kSOffB4 + kMlpOutP;
+static_assert(kSOffW2 % 4 == 0 && kSOffW3 % 4 == 0 && kSOffW4 % 4 == 0 && kMlpSmem % 4 == 0, "float4 rows");
+static_assert(kSOffW4 - kSOffB1 == kOffW4 - kOffB1, "b1 .. b3 keep the blob's relative layout");
+
+// Block-cooperative copy of the parameter blob into the inference layout.
+__device__ __forceinline__ void mlp_stage(const float* __restrict__ P, float* S) {
+    for (int e = threadIdx.x; e < kMlpSmem; e += blockDim.x) {
+        float v = 0.0f;
+        if (e < 2 * kMlpIn) {
+            v = P[kOffMean + e];
+        } else if (e >= kSOffW1 && e < kSOffB1) {
+            const int o = (e - kSOffW1) / kMlpInP, k = (e - kSOffW1) % kMlpInP;
+            v = k < kMlpIn ? P[kOffW1 + o * kMlpIn + k] : 0.0f;
+        } else if (e >= kSOffB1 && e < kSOffW4) {
+            v = P[kOffB1 + (e - kSOffB1)];
+        } else if (e >= kSOffW4 && e < kSOffW4 + kMlpOut * kMlpH) {
+            v = P[kOffW4 + (e - kSOffW4)];
+        } else if (e >= kSOffB4 && e < kSOffB4 + kMlpOut) {
+            v = P[kOffB4 + (e - kSOffB4)];
+        }
+        S[e] = v;
+    }
+}
+
+// One dense layer out[o] = act(b[o] + W[o] . in), four outputs at a time
+// (eight independent FMA chains), with `in` in registers (compile-time
+// indices) and the outputs stored to this thread's column of the shared
+// activation buffer (act[o * stride]), the only dynamically indexed array.
+template <int NIN, bool RELU>
+__device__ __forceinline__ void mlp_layer_smem(const float* W, const float* b, int nout, const float (&in)[NIN],
+                                               float* act, int stride) {
+#pragma unroll 1
+    for (int o = 0; o < nout; o += 4) {
+        const float4* w0 = reinterpret_cast<const float4*>(W + o * NIN);
+        float a[4][2];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            a[r][0] = b[o + r];
+            a[r][1] = 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < NIN / 4; ++k) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const float4 w = w0[r * (NIN / 4) + k];
+                a[r][0] = fmaf(w.x, in[4 * k], a[r][0]);
+                a[r][1] = fmaf(w.y, in[4 * k + 1], a[r][1]);
+                a[r][0] = fmaf(w.z, in[4 * k + 2], a[r][0]);
+                a[r][1] = fmaf(w.w, in[4 * k + 3], a[r][1]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const float v = a[r][0] + a[r][1];
+            act[(o + r) * stride] = RELU ? fmaxf(v, 0.0f) : v;
+        }
+    }
+}
+
+template <int N>
+__device__ __forceinline__ void mlp_load_act(const float* act, int stride, float (&v)[N]) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = act[k * stride];
+}
+
+// Forward pass with the weights in the inference layout S and a per-thread
+// activation column act (kMlpH entries at stride `stride`); the kMlpOut
+// outputs are left in act[0 .. kMlpOut-1] (same stride).
+__device__ __forceinline__ void mlp_forward_smem(const float* S, float* act, int stride, const float* x) {
+    float in[kMlpInP];
+#pragma unroll
+    for (int k = 0; k < kMlpInP; ++k) in[k] = k < kMlpIn ? (x[k] - S[kSOffMean + k]) * S[kSOffIstd + k] : 0.0f;
+    mlp_layer_smem<kMlpInP, true>(S + kSOffW1, S + kSOffB1, kMlpH, in, act, stride);
+    float h[kMlpH];
+    mlp_load_act(act, stride, h);
+    mlp_layer_smem<kMlpH, true>(S + kSOffW2, S + kSOffB2, kMlpH, h, act, stride);
+    mlp_load_act(act, stride, h);
+    mlp_layer_smem<kMlpH, true>(S + kSOffW3, S + kSOffB3, kMlpH, h, act, stride);
+    mlp_load_act(act, stride, h);
+    mlp_layer_smem<kMlpH, false>(S + kSOffW4, S + kSOffB4, kMlpOutP, h, act, stride);
+}
+
 // Features of the pair (target i, source j); P = order of the stored norms.
 // Source norms of orders above kFeatOrders are not used (fixed at -40), so
 // training (moments to order 12) and use (moments to the call's expansion

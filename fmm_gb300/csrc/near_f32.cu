@@ -24,39 +24,94 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 
 constexpr int kExwRegs = 8;  // exclusion entries held in registers per target
 
-// Positions relative to the particle's leaf centre as double-float pairs
-// (hi = rounded value, lo = rounded remainder): differences of positions in
-// two leaves then lose nothing beyond the final FP32 rounding.
+// Per sorted particle, one record of float4s: (x, y, z, d), (x_lo, y_lo, z_lo,
+// original index + 1 as int bits), then the FP32 scaled multipoles padded to
+// a multiple of 4.  Positions are relative to the particle's own leaf centre
+// as double-float pairs (hi = rounded value, lo = rounded remainder), so
+// differences of positions in two leaves lose nothing beyond the final FP32
+// rounding.  A source is then read with a handful of 16-byte loads from one
+// base address.
+__host__ __device__ constexpr int rec_vec(int dim) { return 2 + (dim + 3) / 4; }
+
 __global__ void k_gather_f32(int64_t n, int dim, const TreeDev t, const double* __restrict__ sx,
                              const double* __restrict__ sy, const double* __restrict__ sz,
-                             const double* __restrict__ sd, const double* __restrict__ smc, float* __restrict__ fx,
-                             float* __restrict__ fy, float* __restrict__ fz, float* __restrict__ fxl,
-                             float* __restrict__ fyl, float* __restrict__ fzl, float* __restrict__ fd,
-                             float* __restrict__ fmc, int32_t* __restrict__ forig) {
+                             const double* __restrict__ sd, const double* __restrict__ smc,
+                             float4* __restrict__ rec) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= n) return;
+    const int nv = rec_vec(dim);
     const int leaf = t.leaf_of[k];
     const double rx = sx[k] - t.cx[leaf], ry = sy[k] - t.cy[leaf], rz = sz[k] - t.cz[leaf];
-    fx[k] = (float)rx;
-    fy[k] = (float)ry;
-    fz[k] = (float)rz;
-    fxl[k] = (float)(rx - (double)fx[k]);
-    fyl[k] = (float)(ry - (double)fy[k]);
-    fzl[k] = (float)(rz - (double)fz[k]);
-    fd[k] = (float)sd[k];
-    for (int c = 0; c < dim; ++c) fmc[(size_t)c * n + k] = (float)smc[(size_t)c * n + k];
-    forig[k] = (int32_t)t.perm[k] + 1;  // 1-based, as in the exclusion lists
+    const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
+    float4* r = rec + (size_t)k * nv;
+    r[0] = make_float4(hx, hy, hz, (float)sd[k]);
+    r[1] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz),
+                       __int_as_float((int32_t)t.perm[k] + 1));  // 1-based, as in the exclusion lists
+    for (int v = 2; v < nv; ++v) {
+        float m[4];
+        for (int c = 0; c < 4; ++c) {
+            const int s = 4 * (v - 2) + c;
+            m[c] = s < dim ? (float)smc[(size_t)s * n + k] : 0.0f;
+        }
+        r[v] = make_float4(m[0], m[1], m[2], m[3]);
+    }
 }
 
+// Sum over the sources [js, je) of one leaf (lane group grp of ngr) for the
+// lane's target: compensated FP32 (TwoSum hi + lo), since the per-atom terms
+// are much larger than their neutral total.  CHECK: the leaf may hold the
+// target itself or one of its excluded partners.
+template <int M, int F, bool CHECK>
+__device__ __forceinline__ void p2p_leaf(const float4* __restrict__ rec, int js, int je, int grp, int ngr, int tgt,
+                                         float xt, float yt, float zt, float dt, float ox, float oy, float oz,
+                                         float oxl, float oyl, float ozl, const int32_t* __restrict__ excl,
+                                         int exw, int64_t n, int ot, int damp, float* hi, float* lo) {
+    constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
+    for (int k = js + grp; k < je; k += ngr) {
+        const float4* r = rec + (size_t)k * NV;
+        const float4 a = r[0], b = r[1];
+        if (CHECK) {
+            if (k == tgt) continue;
+            const int o = __float_as_int(b.w);
+            bool skip = false;
+            for (int e = 0; e < exw; ++e) skip |= (excl[(size_t)e * n + ot] == o);
+            if (skip) continue;
+        }
+        float mc[4 * (NV - 2)];
+#pragma unroll
+        for (int v = 0; v < NV - 2; ++v) {
+            const float4 w = r[2 + v];
+            mc[4 * v] = w.x;
+            mc[4 * v + 1] = w.y;
+            mc[4 * v + 2] = w.z;
+            mc[4 * v + 3] = w.w;
+        }
+        const float dx = ((xt - a.x) + ox) + (oxl - b.x);
+        const float dy = ((yt - a.y) + oy) + (oyl - b.y);
+        const float dz = ((zt - a.z) + oz) + (ozl - b.z);
+        float c[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) c[f] = 0.0f;
+        pair_field_f32acc<M, F>(dx, dy, dz, dt * a.w, damp, mc, c);
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            const float s = hi[f] + c[f];
+            const float bb = s - hi[f];
+            lo[f] += (hi[f] - (s - bb)) + (c[f] - bb);
+            hi[f] = s;
+        }
+    }
+}
+
+// One warp per target leaf, its particles across the lanes (for leaves of
+// fewer than 32 particles, groups of lanes split each source leaf).  Source
+// leaves that hold neither the target nor an excluded partner of any of the
+// warp's targets run without the exclusion test.
 template <int M, int F>
-__global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float* __restrict__ fx,
-                                                 const float* __restrict__ fy, const float* __restrict__ fz,
-                                                 const float* __restrict__ fxl, const float* __restrict__ fyl,
-                                                 const float* __restrict__ fzl, const float* __restrict__ fd,
-                                                 const float* __restrict__ fmc,
-                                                 const int32_t* __restrict__ forig, const int32_t* __restrict__ excl,
-                                                 int exw, int64_t n, int damp, double* __restrict__ fs) {
-    constexpr int NF = nT(F), NM = nT(M);
+__global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* __restrict__ rec,
+                                                 const int32_t* __restrict__ excl, int exw, int64_t n, int damp,
+                                                 double* __restrict__ fs) {
+    constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= t.num_leaves) return;
@@ -71,13 +126,17 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float* _
         const int ngr = 32 / g;
         const int tl = lane & (g - 1), grp = lane / g;
         const bool valid = tl < nt;
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
         const int tgt = s0 + chunk + (valid ? tl : 0);
-        const float xt = fx[tgt], yt = fy[tgt], zt = fz[tgt], dt = fd[tgt];
-        const float xtl = fxl[tgt], ytl = fyl[tgt], ztl = fzl[tgt];
-        const int ot = forig[tgt] - 1;
-        int ex[kExwRegs];
+        const float4 ta = rec[(size_t)tgt * NV], tb = rec[(size_t)tgt * NV + 1];
+        const int ot = __float_as_int(tb.w) - 1;
+        // leaves of the target's excluded partners (-1: none)
+        int exl[kExwRegs];
 #pragma unroll
-        for (int q = 0; q < kExwRegs; ++q) ex[q] = (q < exw) ? excl[(size_t)q * n + ot] : 0;
+        for (int e = 0; e < kExwRegs; ++e) {
+            int o = (e < exw) ? excl[(size_t)e * n + ot] : 0;
+            exl[e] = o > 0 ? t.leaf_of[t.pos_of[o - 1]] : -1;
+        }
         double acc[NF];
 #pragma unroll
         for (int f = 0; f < NF; ++f) acc[f] = 0.0;
@@ -88,39 +147,20 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float* _
                 const double odx = cxa - t.cx[j], ody = cya - t.cy[j], odz = cza - t.cz[j];
                 const float ox = (float)odx, oy = (float)ody, oz = (float)odz;
                 // low parts of the offset folded with the target's low parts
-                const float oxl = (float)(odx - (double)ox) + xtl, oyl = (float)(ody - (double)oy) + ytl,
-                            ozl = (float)(odz - (double)oz) + ztl;
-                // per source leaf: compensated FP32 sums (hi + lo, TwoSum), since
-                // the per-atom terms are much larger than their (neutral) total
+                const float oxl = (float)(odx - (double)ox) + tb.x, oyl = (float)(ody - (double)oy) + tb.y,
+                            ozl = (float)(odz - (double)oz) + tb.z;
+                bool need = (j == leaf) || exw > kExwRegs;
+#pragma unroll
+                for (int e = 0; e < kExwRegs; ++e) need |= (exl[e] == j);
                 float hi[NF], lo[NF];
 #pragma unroll
                 for (int f = 0; f < NF; ++f) hi[f] = lo[f] = 0.0f;
-                for (int k = js + grp; k < je; k += ngr) {
-                    if (k == tgt) continue;
-                    const int o = forig[k];
-                    bool skip = false;
-#pragma unroll
-                    for (int e = 0; e < kExwRegs; ++e) skip |= (ex[e] == o);
-                    for (int e = kExwRegs; e < exw; ++e) skip |= (excl[(size_t)e * n + ot] == o);
-                    if (skip) continue;
-                    float mc[NM];
-#pragma unroll
-                    for (int s = 0; s < NM; ++s) mc[s] = fmc[(size_t)s * n + k];
-                    const float dx = ((xt - fx[k]) + ox) + (oxl - fxl[k]);
-                    const float dy = ((yt - fy[k]) + oy) + (oyl - fyl[k]);
-                    const float dz = ((zt - fz[k]) + oz) + (ozl - fzl[k]);
-                    float c[NF];
-#pragma unroll
-                    for (int f = 0; f < NF; ++f) c[f] = 0.0f;
-                    pair_field_f32acc<M, F>(dx, dy, dz, dt * fd[k], damp, mc, c);
-#pragma unroll
-                    for (int f = 0; f < NF; ++f) {
-                        const float s = hi[f] + c[f];
-                        const float bb = s - hi[f];
-                        lo[f] += (hi[f] - (s - bb)) + (c[f] - bb);
-                        hi[f] = s;
-                    }
-                }
+                if (__any_sync(vmask, need))
+                    p2p_leaf<M, F, true>(rec, js, je, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy, oz, oxl, oyl,
+                                         ozl, excl, exw, n, ot, damp, hi, lo);
+                else
+                    p2p_leaf<M, F, false>(rec, js, je, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy, oz, oxl, oyl,
+                                          ozl, excl, exw, n, ot, damp, hi, lo);
 #pragma unroll
                 for (int f = 0; f < NF; ++f) acc[f] += (double)hi[f] + (double)lo[f];
             }
@@ -142,26 +182,17 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
     const int m = dim_to_order(P.dim);
     const int64_t n = P.n;
     const int nf = nT(field_order);
-    FMM_TRY(ws.f32buf.ensure(sizeof(float) * (size_t)n * (7 + P.dim) + sizeof(int32_t) * n));
-    float* fx = ws.f32buf.as<float>();
-    float* fy = fx + n;
-    float* fz = fy + n;
-    float* fxl = fz + n;
-    float* fyl = fxl + n;
-    float* fzl = fyl + n;
-    float* fd = fzl + n;
-    float* fmc = fd + n;
-    int32_t* forig = reinterpret_cast<int32_t*>(fmc + (size_t)n * P.dim);
+    const int nv = rec_vec(P.dim);
+    FMM_TRY(ws.f32buf.ensure(sizeof(float4) * (size_t)n * nv));
+    float4* rec = ws.f32buf.as<float4>();
     count_launches(1);
     k_gather_f32<<<grid_for(n, 256), 256, 0, st>>>(n, P.dim, t, ws.sx.as<double>(), ws.sy.as<double>(),
-                                                    ws.sz.as<double>(), ws.sd.as<double>(), ws.smc.as<double>(), fx,
-                                                    fy, fz, fxl, fyl, fzl, fd, fmc, forig);
+                                                    ws.sz.as<double>(), ws.sd.as<double>(), ws.smc.as<double>(), rec);
     FMM_TRY(ws.fsorted.ensure(sizeof(double) * (size_t)n * nf));
     const unsigned blocks = grid_for((int64_t)t.num_leaves * 32, 128);
     FMM_MF_SWITCH(m, field_order,
-                  (k_p2p_f32<MM, FF><<<blocks, 128, 0, st>>>(t, fx, fy, fz, fxl, fyl, fzl, fd, fmc, forig, P.excl,
-                                                              P.exw, n,
-                                                              P.damp_type, ws.fsorted.as<double>())));
+                  (k_p2p_f32<MM, FF><<<blocks, 128, 0, st>>>(t, rec, P.excl, P.exw, n, P.damp_type,
+                                                              ws.fsorted.as<double>())));
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }

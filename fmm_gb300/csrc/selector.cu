@@ -379,17 +379,22 @@ __global__ void k_adam(int nparam, int first, float* __restrict__ p, const float
     p[k] -= lr * mh / (sqrtf(vh) + 1e-8f);
 }
 
+// Batched inference with the same routine the list kernel uses.
 __global__ void k_mlp_infer(const float* __restrict__ params, const float* __restrict__ X, int n, float* __restrict__ Y) {
-    __shared__ float P[kMlpParams];
-    for (int e = threadIdx.x; e < kMlpParams; e += blockDim.x) P[e] = params[e];
+    extern __shared__ __align__(16) float sm_inf[];
+    float* S = sm_inf;
+    float* act = sm_inf + kMlpSmem + threadIdx.x;
+    mlp_stage(params, S);
     __syncthreads();
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
-    float x[kMlpIn], y[kMlpOut];
+    float x[kMlpIn];
     for (int k = 0; k < kMlpIn; ++k) x[k] = X[(size_t)q * kMlpIn + k];
-    mlp_forward(P, x, y);
-    for (int o = 0; o < kMlpOut; ++o) Y[(size_t)q * kMlpOut + o] = y[o];
+    mlp_forward_smem(S, act, blockDim.x, x);
+    for (int o = 0; o < kMlpOut; ++o) Y[(size_t)q * kMlpOut + o] = act[o * blockDim.x];
 }
+
+size_t infer_smem(int threads) { return sizeof(float) * (kMlpSmem + (size_t)kMlpH * threads); }
 
 size_t train_smem() {
     return sizeof(float) * (kMlpParams + kTB * (kMlpIn + 3 * kMlpH + kMlpOut + 3 * kMlpH));
@@ -544,8 +549,10 @@ int fmm_mlp_forward(const float* params, const float* x, int64_t n, float* y) {
     if (!dp || !dx || !dy) return FMM_ENOMEM;
     FMM_CUDA_TRY(cudaMemcpy(dp, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice));
     FMM_CUDA_TRY(cudaMemcpy(dx, x, sizeof(float) * n * kMlpIn, cudaMemcpyHostToDevice));
+    FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)infer_smem(128)));
     count_launches(1);
-    k_mlp_infer<<<grid_for(n, 128), 128>>>(dp, dx, (int)n, dy);
+    k_mlp_infer<<<grid_for(n, 128), 128, infer_smem(128)>>>(dp, dx, (int)n, dy);
     FMM_CUDA_TRY(cudaMemcpy(y, dy, sizeof(float) * n * kMlpOut, cudaMemcpyDeviceToHost));
     return FMM_OK;
 }

@@ -362,8 +362,9 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
     int64_t cap_far, uint64_t* __restrict__ nearp, int64_t cap_near, const TreeDev t, double theta_loose, double rdamp,
     int qmax, const float* __restrict__ params, const float* __restrict__ lnorm, const float* __restrict__ dmin,
     int P, float log_budget, unsigned long long* counters) {
-    __shared__ float Psh[kMlpParams];
-    for (int e = threadIdx.x; e < kMlpParams; e += blockDim.x) Psh[e] = params[e];
+    extern __shared__ __align__(16) float sm_sel[];
+    float* S = sm_sel;  // weights (inference layout), then one activation column per thread
+    mlp_stage(params, S);
     __syncthreads();
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nin) return;
@@ -389,11 +390,12 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
     }
     int order = 0;
     if (accept) {
-        float x[kMlpIn], y[kMlpOut];
+        float x[kMlpIn];
         selector_features(t, lnorm, dmin, P, i, j, x);
-        mlp_forward(Psh, x, y);
+        float* act = sm_sel + kMlpSmem + threadIdx.x;
+        mlp_forward_smem(S, act, blockDim.x, x);
         for (int o = kQmin; o <= qmax; ++o)
-            if (y[o - kQmin] <= log_budget) {
+            if (act[(o - kQmin) * blockDim.x] <= log_budget) {
                 order = o;
                 break;
             }
@@ -705,9 +707,15 @@ double min_damping_factor(Workspace& ws, const double* d, int64_t n, cudaStream_
 
 int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st) {
     const int M = t.num_nodes;
-    int64_t cap_front = std::max<int64_t>(4096, 64LL * M);
-    int64_t cap_far = std::max<int64_t>(4096, 200LL * M);
-    int64_t cap_near = std::max<int64_t>(4096, 100LL * t.num_leaves);
+    // capacities: pair counts grow like theta^-3; never below what the
+    // workspace already holds (buffers only grow), so repeated calls on
+    // similar systems do not retry
+    const double th = std::max(0.05, std::min(tp.theta, tp.sel_params ? tp.sel_theta : tp.theta));
+    const double per = std::min(4000.0, 25.0 / (th * th * th));
+    int64_t cap_far = std::max<int64_t>({4096, (int64_t)(per * M), (int64_t)(ws.far_pairs.cap / sizeof(uint64_t))});
+    int64_t cap_near = std::max<int64_t>(
+        {4096, (int64_t)(0.4 * per * t.num_leaves), (int64_t)(ws.near_pairs.cap / sizeof(uint64_t))});
+    int64_t cap_front = std::max<int64_t>({4096, cap_far, (int64_t)(ws.front_a.cap / sizeof(int2))});
     unsigned long long* ctr = ws.counters.as<unsigned long long>();
     for (int attempt = 0; attempt < 8; ++attempt) {
         FMM_TRY(ws.front_a.ensure(sizeof(int2) * cap_front));
@@ -726,7 +734,10 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
             FMM_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
             count_launches(1);
             if (tp.sel_params) {
-                k_list_iter_learned<<<grid_for(nin, 128), 128, 0, st>>>(
+                const size_t smem = sizeof(float) * (kMlpSmem + (size_t)kMlpH * 128);
+                FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_list_iter_learned,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                k_list_iter_learned<<<grid_for(nin, 128), 128, smem, st>>>(
                     fin, (int)nin, fout, cap_front, ws.far_pairs.as<uint64_t>(), cap_far, ws.near_pairs.as<uint64_t>(),
                     cap_near, t, tp.sel_theta, tp.mac_mode == 1 ? tp.rdamp : 0.0, tp.order, tp.sel_params,
                     tp.sel_lnorm, tp.sel_dmin, tp.sel_P, tp.sel_log_budget, ctr);

@@ -154,9 +154,11 @@ int fmm_field_direct_targets_noalloc(int64_t n, const double *d_coordinates, int
  * sampled direct sum), t_p2m_m2m, t_lists, t_p2p, t_m2l, t_l2l_l2p (with the
  * selector's check), t_total, selector_fallback (1 if the learned selector's
  * sampled check failed and the fixed rule was used), sampled_rms_err (learned
- * selector only, else -1), mean expansion order of the far pairs, then the
- * number of far pairs at each expansion order 0..12.  Returns the number
- * written (at most 29). */
+ * selector only, else -1), mean expansion order of the far pairs, the
+ * number of far pairs at each expansion order 0..12, the device time of the
+ * near-field kernel alone and of the grouped M2L product kernel alone (-1 if
+ * that kernel did not run), the number of displacement groups of the grouped
+ * M2L.  Returns the number written (at most 32). */
 int fmm_last_stats(double *out, int len);
 
 /* Diagnostics (no counterpart in the reference): builds the octree and
