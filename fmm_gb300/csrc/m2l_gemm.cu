@@ -33,7 +33,6 @@ constexpr int kFallback = 63;            // key code of pairs without a grid dis
 constexpr int64_t kDOff = 1 << 17;       // offset of the 18-bit displacement fields
 constexpr int kTaskCols = 256;           // pairs (columns) per product block
 constexpr int kGemmThreads = 128;        // 16 row groups x 8 column groups
-constexpr int kMaxRed = (kMaxP + 1) * (kMaxP + 1);  // reduced components at the highest order
 
 __global__ void k_far_targets(int M, const int32_t* __restrict__ off, int32_t* __restrict__ tgt) {
     const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -287,6 +286,8 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
 #pragma unroll
                 for (int l = 0; l < CPT; ++l) acc[k][l] = fma(gv[k], wv[l], acc[k][l]);
         }
+        // full rows of ldo entries (zeros above the pair's order), so the
+        // per-target sum reads them without knowing the order
 #pragma unroll
         for (int l = 0; l < CPT; ++l) {
             const int c = cg * CPT + l;
@@ -295,8 +296,12 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
 #pragma unroll
                 for (int k = 0; k < RT; ++k) {
                     const int f = rg + 16 * k;
-                    if (f < nrq) o[f] = acc[k][l];
+                    if (f < nrq)
+                        o[f] = acc[k][l];
+                    else if (f < ldo)
+                        o[f] = (R)0;
                 }
+                for (int f = RM + rg; f < ldo; f += 16) o[f] = (R)0;
             }
         }
     }
@@ -358,52 +363,34 @@ __global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restric
     }
 }
 
-// Warp per target: FP64 sum of its pairs' columns, back to physical units,
-// into the reduced components of the local expansion.
+// Block per target, thread per reduced component: FP64 sum of the target's
+// pair rows (contiguous in target order, eight loads in flight per thread),
+// back to physical units, into the reduced components of the local expansion.
 template <typename R>
-__global__ void k_m2l_sum(const TreeDev t, int p, const R* __restrict__ out, double* __restrict__ loc) {
-    constexpr int RPL = (kMaxRed + 31) / 32;
-    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (i >= t.num_nodes) return;
+__global__ void __launch_bounds__(128) k_m2l_sum(const TreeDev t, int p, const R* __restrict__ out,
+                                                 double* __restrict__ loc) {
+    const int i = blockIdx.x;
     const int nr = (p + 1) * (p + 1);
-    double acc[RPL];
-#pragma unroll
-    for (int r = 0; r < RPL; ++r) acc[r] = 0.0;
     const int q0 = t.far_off[i], q1 = t.far_off[i + 1];
-    // four pairs per step: independent loads in flight
-    constexpr int U = 4;
-    for (int qb = q0; qb < q1; qb += U) {
-        R v[U][RPL];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int q = qb + u;
-            const int ord = q < q1 ? (t.far_ord ? min((int)t.far_ord[q], p) : p) : -1;
-            const int nrq = (ord + 1) * (ord + 1);
-            const R* o = out + (size_t)q * nr;
-#pragma unroll
-            for (int r = 0; r < RPL; ++r) {
-                const int f = lane + 32 * r;
-                v[u][r] = f < nrq ? o[f] : (R)0;
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-#pragma unroll
-            for (int r = 0; r < RPL; ++r) acc[r] += (double)v[u][r];
-    }
     const double ih = 1.0 / t.r[i];
     double* L = loc + (size_t)i * nT(p);
+    for (int f = threadIdx.x; f < nr; f += blockDim.x) {
+        constexpr int U = 8;
+        double acc = 0.0;
+        int q = q0;
+        for (; q + U <= q1; q += U) {
+            R v[U];
 #pragma unroll
-    for (int r = 0; r < RPL; ++r) {
-        const int f = lane + 32 * r;
-        if (f < nr) {
-            const int c = qcomp(f);
-            const int k = c >> 24;
-            double s = ih;
-            for (int e = 0; e < k; ++e) s *= ih;
-            L[pidx(c & 0xff, (c >> 8) & 0xff, (c >> 16) & 0xff)] = acc[r] * s;
+            for (int u = 0; u < U; ++u) v[u] = out[(size_t)(q + u) * nr + f];
+#pragma unroll
+            for (int u = 0; u < U; ++u) acc += (double)v[u];
         }
+        for (; q < q1; ++q) acc += (double)out[(size_t)q * nr + f];
+        const int c = qcomp(f);
+        const int k = c >> 24;
+        double s = ih;
+        for (int e = 0; e < k; ++e) s *= ih;
+        L[pidx(c & 0xff, (c >> 8) & 0xff, (c >> 16) & 0xff)] = acc * s;
     }
 }
 
@@ -507,7 +494,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         if (ws.product_timed) cudaEventRecord(ws.ev[9], st);
     }
     count_launches(1);
-    k_m2l_sum<R><<<grid_for(M, 4), 128, 0, st>>>(t, p, ws.m2l_out.as<R>(), ws.loc.as<double>());
+    k_m2l_sum<R><<<(unsigned)M, 128, 0, st>>>(t, p, ws.m2l_out.as<R>(), ws.loc.as<double>());
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
