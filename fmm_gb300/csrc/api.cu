@@ -40,7 +40,7 @@ Workspace::~Workspace() {
                      &sz,        &smc,       &sd,          &fsorted,    &mom,        &loc,        &partial,
                      &term_off,  &term_abc,  &term_c, &f32buf, &wred, &far_ord, &sel_norms, &sel_params, &sel_scratch, &sysbuf,
                      &m2l_tgt, &m2l_keys, &m2l_keys2, &m2l_vals, &m2l_vals2, &m2l_ukeys, &m2l_cnt, &m2l_gstart,
-                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out};
+                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &xlate};
     for (DevBuf* b : all) b->release();
     if (events_ready)
         for (auto& e : ev) cudaEventDestroy(e);
@@ -306,7 +306,7 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         cudaEventRecord(ws.ev[4], st);
         FMM_TRY(launch_m2l(ws, t, p, md, st));
         cudaEventRecord(ws.ev[5], st);
-        FMM_TRY(launch_l2l_l2p(ws, P, t, p, f, st));
+        FMM_TRY(launch_l2l_l2p(ws, P, t, p, f, md.precision == 1 || md.precision == 3, st));
         FMM_TRY(scatter_field(ws, t, P.n, nf, d_field, st));
         if (!learned || attempt == 1) break;
         // check at the sampled particles; fall back to the fixed rule if the

@@ -1,17 +1,9 @@
-// Multipole and local expansions, FP64: P2M, M2M, M2L, L2L, L2P.
-//
-// Cell multipoles are kept scaled, M'_t = M_t / t! (t! = tx! ty! tz!), where
-// M_t are the reference's raw Cartesian moments sum q (r - c)^t.  Then every
-// translation is a plain convolution with d^u / u!:
-//   P2M  M'_t(leaf)   = sum_i sum_{s<=t} (d_i^(t-s)/(t-s)!) M'_s(i)   (src/fmm.F90:437-472)
-//   M2M  M'_t(parent) = sum_c sum_{u<=t} (d_c^u/u!) M'_{t-u}(c)       (src/fmm.F90:387-435;
-//        the reference shifts each leaf straight into every ancestor, which is
-//        the same sum since the shifts compose exactly; here level by level)
-//   M2L  L_f(i)      += sum_s (-1)^(|s|+1) M'_s(j) T_{s+f}(c_i - c_j)  (src/fmm.F90:826-882)
-//   L2L  L_t(child)  += sum_u L_{t+u}(parent) d^u/u!                   (src/fmm.F90:981-1044)
-//   L2P  F_t(i)      += sum_u L_{t+u}(leaf) d_i^u/u!, |t| <= f         (src/fmm.F90:1046-1132)
-// Expansions are node-major: node k's coefficients are contiguous.
-// All kernels use one warp per node; orders are runtime values up to 12.
+// Reference-mode M2L (FP64): the reference's own closed-form tensors with the
+// int32 Cnij table (src/tensors_recursive.F90:29-135) over the full Cartesian
+// bases, L_f(i) += sum_s (-1)^(|s|+1) M'_s(j) T_{s+f}(c_i - c_j)
+// (src/fmm.F90:826-882), with M'_s = M_s / s! the scaled moments of
+// translate.cu.  The exact-coefficient modes use the reduced-basis M2L
+// (m2l.cu, m2l_gemm.cu) instead.
 #include <algorithm>
 #include <vector>
 
@@ -33,126 +25,6 @@ __device__ __forceinline__ int cz_(int c) { return (c >> 16) & 0xff; }
 
 __device__ __forceinline__ void fill_comp(int* sh, int nq) {
     for (int q = threadIdx.x; q < nq; q += blockDim.x) sh[q] = pack_comp(q);
-}
-
-// e[a] = d^a / a!, a = 0..p
-__device__ __forceinline__ void scaled_powers(double d, int p, double* e) {
-    e[0] = 1.0;
-    for (int a = 1; a <= p; ++a) e[a] = e[a - 1] * d / (double)a;
-}
-
-// dp[u] = dx^ux dy^uy dz^uz / u! for |u| <= p, computed by one warp.
-__device__ __forceinline__ void warp_dpow(int lane, double dx, double dy, double dz, int p, const int* comp,
-                                          double* e3, double* dp) {
-    if (lane < 3) scaled_powers(lane == 0 ? dx : (lane == 1 ? dy : dz), p, e3 + lane * (kMaxP + 1));
-    __syncwarp();
-    for (int u = lane; u < nT(p); u += 32) {
-        const int c = comp[u];
-        dp[u] = e3[cx_(c)] * e3[(kMaxP + 1) + cy_(c)] * e3[2 * (kMaxP + 1) + cz_(c)];
-    }
-    __syncwarp();
-}
-
-// ---------------------------------------------------------------- P2M
-__global__ void k_p2m(const TreeDev t, const double* __restrict__ sx, const double* __restrict__ sy,
-                      const double* __restrict__ sz, const double* __restrict__ smc, int64_t n, int m, int p,
-                      double* __restrict__ mom) {
-    extern __shared__ double smem[];
-    const int nq = nT(p);
-    int* comp = reinterpret_cast<int*>(smem);
-    double* base = smem + (nq + 1) / 2 + 1;
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int per_warp = nq + 3 * (kMaxP + 1) + 32;
-    double* dp = base + wib * per_warp;
-    double* e3 = dp + nq;
-    double* ms = e3 + 3 * (kMaxP + 1);
-    fill_comp(comp, nq);
-    __syncthreads();
-    const int w = blockIdx.x * (blockDim.x >> 5) + wib;
-    if (w >= t.num_leaves) return;
-    const int leaf = t.leaves[w];
-    const double cx = t.cx[leaf], cy = t.cy[leaf], cz = t.cz[leaf];
-    const int s0 = t.start[leaf], cnt = t.count[leaf];
-    const int nm = nT(m);
-    double acc[kMaxNPL];
-#pragma unroll
-    for (int r = 0; r < kMaxNPL; ++r) acc[r] = 0.0;
-    for (int k = s0; k < s0 + cnt; ++k) {
-        if (lane < nm) {
-            const double c = smc[(size_t)lane * n + k];
-            ms[lane] = ((order_of(lane) + 1) % 2) ? -c : c;  // back to M_s / s!
-        }
-        warp_dpow(lane, sx[k] - cx, sy[k] - cy, sz[k] - cz, p, comp, e3, dp);
-#pragma unroll
-        for (int r = 0; r < kMaxNPL; ++r) {
-            const int tq = lane + 32 * r;
-            if (tq < nq) {
-                const int ct = comp[tq];
-                double a = 0.0;
-                for (int s = 0; s < nm; ++s) {
-                    const int cs = comp[s];
-                    const int ux = cx_(ct) - cx_(cs), uy = cy_(ct) - cy_(cs), uz = cz_(ct) - cz_(cs);
-                    if (ux < 0 || uy < 0 || uz < 0) continue;
-                    a += dp[pidx(ux, uy, uz)] * ms[s];
-                }
-                acc[r] += a;
-            }
-        }
-        __syncwarp();
-    }
-#pragma unroll
-    for (int r = 0; r < kMaxNPL; ++r) {
-        const int tq = lane + 32 * r;
-        if (tq < nq) mom[(size_t)leaf * nq + tq] = acc[r];
-    }
-}
-
-// ---------------------------------------------------------------- M2M
-__global__ void k_m2m(const TreeDev t, const int32_t* __restrict__ nodes, int cnt, int p, double* __restrict__ mom) {
-    extern __shared__ double smem[];
-    const int nq = nT(p);
-    int* comp = reinterpret_cast<int*>(smem);
-    double* base = smem + (nq + 1) / 2 + 1;
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int per_warp = 2 * nq + 3 * (kMaxP + 1);
-    double* dp = base + wib * per_warp;
-    double* mc = dp + nq;
-    double* e3 = mc + nq;
-    fill_comp(comp, nq);
-    __syncthreads();
-    const int w = blockIdx.x * (blockDim.x >> 5) + wib;
-    if (w >= cnt) return;
-    const int node = nodes[w];
-    if (t.is_leaf[node]) return;
-    const double px = t.cx[node], py = t.cy[node], pz = t.cz[node];
-    double acc[kMaxNPL];
-#pragma unroll
-    for (int r = 0; r < kMaxNPL; ++r) acc[r] = 0.0;
-    for (int o = 0; o < 8; ++o) {
-        const int c = t.child[8 * node + o];
-        if (c < 0) continue;
-        for (int q = lane; q < nq; q += 32) mc[q] = mom[(size_t)c * nq + q];
-        warp_dpow(lane, t.cx[c] - px, t.cy[c] - py, t.cz[c] - pz, p, comp, e3, dp);
-#pragma unroll
-        for (int r = 0; r < kMaxNPL; ++r) {
-            const int tq = lane + 32 * r;
-            if (tq < nq) {
-                const int ct = comp[tq];
-                const int tx = cx_(ct), ty = cy_(ct), tz = cz_(ct);
-                double a = 0.0;
-                for (int ux = 0; ux <= tx; ++ux)
-                    for (int uy = 0; uy <= ty; ++uy)
-                        for (int uz = 0; uz <= tz; ++uz) a += dp[pidx(ux, uy, uz)] * mc[pidx(tx - ux, ty - uy, tz - uz)];
-                acc[r] += a;
-            }
-        }
-        __syncwarp();
-    }
-#pragma unroll
-    for (int r = 0; r < kMaxNPL; ++r) {
-        const int tq = lane + 32 * r;
-        if (tq < nq) mom[(size_t)node * nq + tq] = acc[r];
-    }
 }
 
 // ---------------------------------------------------------------- M2L
@@ -302,79 +174,6 @@ __global__ void k_m2l_f64(const TreeDev t, const double* __restrict__ mom, doubl
 }
 
 
-// ---------------------------------------------------------------- L2L
-__global__ void k_l2l(const TreeDev t, const int32_t* __restrict__ nodes, int cnt, int p, double* __restrict__ loc) {
-    extern __shared__ double smem[];
-    const int nq = nT(p);
-    int* comp = reinterpret_cast<int*>(smem);
-    double* base = smem + (nq + 1) / 2 + 1;
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int per_warp = 2 * nq + 3 * (kMaxP + 1);
-    double* dp = base + wib * per_warp;
-    double* lp = dp + nq;
-    double* e3 = lp + nq;
-    fill_comp(comp, nq);
-    __syncthreads();
-    const int w = blockIdx.x * (blockDim.x >> 5) + wib;
-    if (w >= cnt) return;
-    const int c = nodes[w];
-    const int par = t.parent[c];
-    for (int q = lane; q < nq; q += 32) lp[q] = loc[(size_t)par * nq + q];
-    warp_dpow(lane, t.cx[c] - t.cx[par], t.cy[c] - t.cy[par], t.cz[c] - t.cz[par], p, comp, e3, dp);
-    for (int tq = lane; tq < nq; tq += 32) {
-        const int ct = comp[tq];
-        const int tx = cx_(ct), ty = cy_(ct), tz = cz_(ct);
-        const int rem = p - (tx + ty + tz);
-        double a = 0.0;
-        for (int u = 0; u < nT(rem); ++u) {
-            const int cu = comp[u];
-            a += lp[pidx(tx + cx_(cu), ty + cy_(cu), tz + cz_(cu))] * dp[u];
-        }
-        loc[(size_t)c * nq + tq] += a;
-    }
-}
-
-// ---------------------------------------------------------------- L2P
-__global__ void k_l2p(const TreeDev t, const double* __restrict__ sx, const double* __restrict__ sy,
-                      const double* __restrict__ sz, int64_t n, int p, int f, const double* __restrict__ loc,
-                      double* __restrict__ fs) {
-    extern __shared__ double smem[];
-    const int nq = nT(p);
-    int* comp = reinterpret_cast<int*>(smem);
-    double* base = smem + (nq + 1) / 2 + 1;
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int per_warp = nq + 32 * 3 * (kMaxP + 1);
-    double* lsh = base + wib * per_warp;
-    double* e = lsh + nq + lane * 3 * (kMaxP + 1);
-    fill_comp(comp, nq);
-    __syncthreads();
-    const int w = blockIdx.x * (blockDim.x >> 5) + wib;
-    if (w >= t.num_leaves) return;
-    const int leaf = t.leaves[w];
-    for (int q = lane; q < nq; q += 32) lsh[q] = loc[(size_t)leaf * nq + q];
-    __syncwarp();
-    const double cx = t.cx[leaf], cy = t.cy[leaf], cz = t.cz[leaf];
-    const int s0 = t.start[leaf], cnt = t.count[leaf];
-    const int nf = nT(f);
-    for (int k = s0 + lane; k < s0 + cnt; k += 32) {
-        scaled_powers(sx[k] - cx, p, e);
-        scaled_powers(sy[k] - cy, p, e + (kMaxP + 1));
-        scaled_powers(sz[k] - cz, p, e + 2 * (kMaxP + 1));
-        for (int tq = 0; tq < nf; ++tq) {
-            const int ct = comp[tq];
-            const int tx = cx_(ct), ty = cy_(ct), tz = cz_(ct);
-            const int rem = p - (tx + ty + tz);
-            double a = 0.0;
-            for (int u = 0; u < nT(rem); ++u) {
-                const int cu = comp[u];
-                a += lsh[pidx(tx + cx_(cu), ty + cy_(cu), tz + cz_(cu))] * e[cx_(cu)] * e[(kMaxP + 1) + cy_(cu)] *
-                     e[2 * (kMaxP + 1) + cz_(cu)];
-            }
-            fs[(size_t)tq * n + k] += a;
-        }
-    }
-}
-
 size_t comp_bytes(int nq) { return sizeof(double) * ((nq + 1) / 2 + 1); }
 
 // Terms of the reference's closed-form tensors (src/tensors_recursive.F90:29-62)
@@ -438,35 +237,6 @@ int set_smem(const void* fn, size_t bytes) {
 
 }  // namespace
 
-int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, cudaStream_t st) {
-    const int nq = nT(p);
-    const int m = dim_to_order(P.dim);
-    FMM_TRY(ws.mom.ensure(sizeof(double) * (size_t)t.num_nodes * nq));
-    double* mom = ws.mom.as<double>();
-    {
-        const int wpb = 4;
-        const size_t sm = comp_bytes(nq) + sizeof(double) * wpb * (nq + 3 * (kMaxP + 1) + 32);
-        FMM_TRY(set_smem((const void*)k_p2m, sm));
-        count_launches(1);
-        k_p2m<<<grid_for(t.num_leaves, wpb), 32 * wpb, sm, st>>>(t, ws.sx.as<double>(), ws.sy.as<double>(),
-                                                                  ws.sz.as<double>(), ws.smc.as<double>(), P.n, m, p,
-                                                                  mom);
-    }
-    {
-        const int wpb = 4;
-        const size_t sm = comp_bytes(nq) + sizeof(double) * wpb * (2 * nq + 3 * (kMaxP + 1));
-        FMM_TRY(set_smem((const void*)k_m2m, sm));
-        for (int d = t.max_depth - 1; d >= 1; --d) {
-            const int lo = t.level_start[d], hi = t.level_start[d + 1];
-            if (hi <= lo) continue;
-            count_launches(1);
-            k_m2m<<<grid_for(hi - lo, wpb), 32 * wpb, sm, st>>>(t, t.level_nodes + lo, hi - lo, p, mom);
-        }
-    }
-    FMM_CUDA_TRY(cudaGetLastError());
-    return FMM_OK;
-}
-
 int launch_m2l(Workspace& ws, const TreeDev& t, int p, const Modes& md, cudaStream_t st) {
     const int nq = nT(p), N = 2 * p, nqT = nT(N);
     FMM_TRY(ws.loc.ensure(sizeof(double) * (size_t)t.num_nodes * nq));
@@ -494,33 +264,6 @@ int launch_m2l(Workspace& ws, const TreeDev& t, int p, const Modes& md, cudaStre
     k_m2l_f64<<<grid_for(t.num_nodes, wpb), 32 * wpb, sm, st>>>(t, ws.mom.as<double>(), ws.loc.as<double>(), p, ref,
                                                                 ws.term_off.as<int32_t>(), ws.term_abc.as<uchar4>(),
                                                                 ws.term_c.as<double>());
-    FMM_CUDA_TRY(cudaGetLastError());
-    return FMM_OK;
-}
-
-int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, int field_order, cudaStream_t st) {
-    const int nq = nT(p);
-    double* loc = ws.loc.as<double>();
-    {
-        const int wpb = 4;
-        const size_t sm = comp_bytes(nq) + sizeof(double) * wpb * (2 * nq + 3 * (kMaxP + 1));
-        FMM_TRY(set_smem((const void*)k_l2l, sm));
-        for (int d = 2; d <= t.max_depth; ++d) {
-            const int lo = t.level_start[d], hi = t.level_start[d + 1];
-            if (hi <= lo) continue;
-            count_launches(1);
-            k_l2l<<<grid_for(hi - lo, wpb), 32 * wpb, sm, st>>>(t, t.level_nodes + lo, hi - lo, p, loc);
-        }
-    }
-    {
-        const int wpb = 2;
-        const size_t sm = comp_bytes(nq) + sizeof(double) * wpb * (nq + 32 * 3 * (kMaxP + 1));
-        FMM_TRY(set_smem((const void*)k_l2p, sm));
-        count_launches(1);
-        k_l2p<<<grid_for(t.num_leaves, wpb), 32 * wpb, sm, st>>>(t, ws.sx.as<double>(), ws.sy.as<double>(),
-                                                                  ws.sz.as<double>(), P.n, p, field_order, loc,
-                                                                  ws.fsorted.as<double>());
-    }
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }

@@ -114,6 +114,10 @@ struct Workspace {
     // ref-mode closed-form tensor tables
     DevBuf term_off, term_abc, term_c;
     int term_order = -1;
+    // index tables of P2M / M2M / L2L at (xlate_p, xlate_m)
+    DevBuf xlate;
+    int xlate_p = -1, xlate_m = -1;
+    int xlate_n[3] = {0, 0, 0};
     bool sel_ready = false;  // selector weights loaded
     // timing
     cudaEvent_t ev[16] = {};
@@ -165,7 +169,8 @@ int selector_node_norms(Workspace& ws, const TreeDev& t, int P, const double* d_
 int selector_pair_data(Workspace& ws, const Particles& Pt, const TreeDev& t, int P, const int2* d_pairs, int npairs,
                        float* d_feats, float* d_labels, cudaStream_t st);
 int selector_unpack_far(Workspace& ws, const TreeDev& t, int2* d_out, cudaStream_t st);
-int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, int field_order, cudaStream_t st);
+int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, int field_order, bool fp32,
+                   cudaStream_t st);
 int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, cudaStream_t st);
 int launch_excl_correction(Workspace& ws, const Particles& P, const TreeDev* t, int field_order, const Modes& md,
                            double* d_field_sorted_or_orig, cudaStream_t st);
