@@ -3,11 +3,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "internal.h"
+#include "mlp.cuh"
 
 namespace fmm {
 
@@ -40,10 +42,11 @@ Workspace::~Workspace() {
                      &sz,        &smc,       &sd,          &fsorted,    &mom,        &loc,        &partial,
                      &term_off,  &term_abc,  &term_c, &f32buf, &wred, &far_ord, &sel_norms, &sel_params, &sel_scratch, &sysbuf,
                      &m2l_tgt, &m2l_keys, &m2l_keys2, &m2l_vals, &m2l_vals2, &m2l_ukeys, &m2l_cnt, &m2l_gstart,
-                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &xlate};
+                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &xlate, &dsmc, &f32node};
     for (DevBuf* b : all) b->release();
     if (events_ready)
         for (auto& e : ev) cudaEventDestroy(e);
+    if (aux) cudaStreamDestroy(aux);
 }
 
 Workspace& thread_workspace() {
@@ -208,7 +211,18 @@ __global__ void k_order_hist(int64_t m, const uint8_t* __restrict__ ord, unsigne
 }
 
 constexpr int kCheckTargets = 16;  // sampled particles of the learned-selector check
-constexpr double kSelThetaLoose = 0.6;
+constexpr double kSelThetaLoose = 0.6;  // default loose acceptance test of the learned selector
+
+// Loose acceptance test of the learned selector: FMM_GB300_SEL_THETA
+// overrides the default (tuning; values outside (0, 1) are ignored).
+double sel_theta_loose() {
+    static const double v = [] {
+        const char* e = std::getenv("FMM_GB300_SEL_THETA");
+        const double x = e ? std::atof(e) : 0.0;
+        return (x > 0.0 && x < 1.0) ? x : kSelThetaLoose;
+    }();
+    return v;
+}
 constexpr double kSelPairsPerTarget = 150.0;
 
 // Relative RMS error (field columns of order >= 1) of F against R, both
@@ -249,23 +263,41 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     TreeDev t;
     const int nf = nT(f);
     cudaEventRecord(ws.ev[0], st);
-    FMM_TRY(build_tree(ws, P.x, P.n, tp, t, st));
     // learned selector: FP64 direct sum at sampled particles (field scale of
-    // the per-pair budget, and the check of the result)
+    // the per-pair budget, and the check of the result), on a second stream
+    // so that it overlaps the tree build and the upward pass
     std::vector<double> ref_rows;
     std::vector<int64_t> rows;
+    const int nt = learned ? (int)std::min<int64_t>(kCheckTargets, P.n) : 0;
     if (learned) {
-        const int nt = (int)std::min<int64_t>(kCheckTargets, P.n);
+        if (!ws.aux) FMM_CUDA_TRY(cudaStreamCreateWithFlags(&ws.aux, cudaStreamNonBlocking));
         for (int k = 0; k < nt; ++k) rows.push_back((int64_t)(((uint64_t)k * 2654435761ull + 12345ull) % (uint64_t)P.n));
         FMM_TRY(ws.sel_scratch.ensure(sizeof(double) * (size_t)nt * nf * 2 + sizeof(int64_t) * nt));
         int64_t* d_rows = reinterpret_cast<int64_t*>(ws.sel_scratch.as<double>() + (size_t)nt * nf * 2);
         double* d_ref = ws.sel_scratch.as<double>();
-        FMM_CUDA_TRY(cudaMemcpyAsync(d_rows, rows.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, st));
+        cudaEventRecord(ws.ev[10], st);  // inputs in place
+        FMM_CUDA_TRY(cudaStreamWaitEvent(ws.aux, ws.ev[10], 0));
+        FMM_CUDA_TRY(cudaMemcpyAsync(d_rows, rows.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, ws.aux));
         Modes mdir{1, 1, 0};
-        FMM_TRY(launch_direct_f64(ws, P, f, mdir, d_ref, st, nt, d_rows));
+        FMM_TRY(launch_direct_f64(ws, P, f, mdir, d_ref, ws.aux, nt, d_rows));
+        cudaEventRecord(ws.ev[11], ws.aux);
+    }
+    FMM_TRY(build_tree(ws, P.x, P.n, tp, t, st));
+    cudaEventRecord(ws.ev[1], st);
+    FMM_TRY(gather_sorted(ws, P, t, st));
+    FMM_TRY(launch_p2m_m2m(ws, P, t, p, st));
+    if (learned) {
+        FMM_TRY(launch_reduce_moments(ws, t, p, st));
+        FMM_TRY(selector_node_norms(ws, t, p, P.damp ? ws.sd.as<double>() : nullptr, st));
+        tpl.sel_params = ws.sel_params.as<float>();
+        tpl.sel_lnorm = ws.sel_norms.as<float>();
+        tpl.sel_dmin = ws.sel_norms.as<float>() + (size_t)t.num_nodes * (p + 1);
+        tpl.sel_P = p;
+        // per-pair error budget from the sampled field scale
+        FMM_CUDA_TRY(cudaEventSynchronize(ws.ev[11]));
         ref_rows.resize((size_t)nt * nf);
-        FMM_CUDA_TRY(cudaMemcpyAsync(ref_rows.data(), d_ref, sizeof(double) * nt * nf, cudaMemcpyDeviceToHost, st));
-        FMM_CUDA_TRY(cudaStreamSynchronize(st));
+        FMM_CUDA_TRY(cudaMemcpy(ref_rows.data(), ws.sel_scratch.as<double>(), sizeof(double) * nt * nf,
+                                cudaMemcpyDeviceToHost));
         std::vector<double> mag(nt);
         for (int k = 0; k < nt; ++k) {
             double g = 0.0;
@@ -278,18 +310,7 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         const double floor_fp32 = md.precision == 0 ? 0.0 : 9e-7;
         const double trunc = std::sqrt(std::max(o.target * o.target - floor_fp32 * floor_fp32, 0.04 * o.target * o.target));
         tpl.sel_log_budget = (float)(std::log10(trunc * scale / std::sqrt(kSelPairsPerTarget)) - 0.3);
-        tpl.sel_theta = kSelThetaLoose;
-    }
-    cudaEventRecord(ws.ev[1], st);
-    FMM_TRY(gather_sorted(ws, P, t, st));
-    FMM_TRY(launch_p2m_m2m(ws, P, t, p, st));
-    if (learned) {
-        FMM_TRY(launch_reduce_moments(ws, t, p, st));
-        FMM_TRY(selector_node_norms(ws, t, p, P.damp ? ws.sd.as<double>() : nullptr, st));
-        tpl.sel_params = ws.sel_params.as<float>();
-        tpl.sel_lnorm = ws.sel_norms.as<float>();
-        tpl.sel_dmin = ws.sel_norms.as<float>() + (size_t)t.num_nodes * (p + 1);
-        tpl.sel_P = p;
+        tpl.sel_theta = sel_theta_loose();
     }
     cudaEventRecord(ws.ev[2], st);
     bool fallback = false;
@@ -396,8 +417,11 @@ const char* fmm_strerror(int s) {
 int fmm_selector_load(const float* params, int64_t count) {
     if (!params || count != fmm_selector_param_count()) return FMM_EINVAL;
     Workspace& ws = thread_workspace();
-    FMM_TRY(ws.sel_params.ensure(sizeof(float) * (size_t)count));
+    FMM_TRY(ws.sel_params.ensure(sizeof(float) * (size_t)kMlpBufFloats));
     FMM_CUDA_TRY(cudaMemcpy(ws.sel_params.p, params, sizeof(float) * (size_t)count, cudaMemcpyHostToDevice));
+    count_launches(1);
+    k_mlp_stage_global<<<1, 256>>>(ws.sel_params.as<float>());  // inference layout after the blob
+    FMM_CUDA_TRY(cudaDeviceSynchronize());
     ws.sel_ready = true;
     return FMM_OK;
 }

@@ -105,12 +105,15 @@ struct Workspace {
         m2l_tasks, m2l_T, m2l_gq, m2l_gab, m2l_wsc, m2l_out;
     // sorted particle data
     DevBuf sx, sy, sz, smc, sd;
-    DevBuf f32buf;  // FP32 particle data of the mixed-precision near field
+    DevBuf f32buf;   // FP32 particle records of the mixed-precision near field
+    DevBuf f32node;  // node centres as FP32 hi/lo pairs
     DevBuf fsorted;
     // expansions
     DevBuf mom, loc, wred;
-    // direct-sum partial sums
-    DevBuf partial;
+    // direct sum: scaled multipoles and partial sums
+    DevBuf dsmc, partial;
+    // second stream (the learned selector's sampled direct sum overlaps the tree phases)
+    cudaStream_t aux = nullptr;
     // ref-mode closed-form tensor tables
     DevBuf term_off, term_abc, term_c;
     int term_order = -1;

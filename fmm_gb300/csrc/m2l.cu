@@ -30,7 +30,6 @@ namespace {
 
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
-constexpr int kMaxR = (kMaxP + 1) * (kMaxP + 1);  // reduced components at the highest order
 
 // Fold w_s (full basis, in shared memory, length nT(p)) onto s_z <= 1.
 __device__ void fold_moments(double* w, int p, int lane) {

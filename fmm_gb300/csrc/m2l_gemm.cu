@@ -42,18 +42,23 @@ __global__ void k_far_targets(int M, const int32_t* __restrict__ off, int32_t* _
 }
 
 // w'_s = w^_s / h^|s| per node (h the node's half-width).
+// (rows of ld >= nr entries, zero padded)
 template <typename R>
-__global__ void k_scale_weights(int64_t total, int nr, const double* __restrict__ wred, const double* __restrict__ h,
-                                R* __restrict__ wsc) {
+__global__ void k_scale_weights(int64_t total, int nr, int ld, const double* __restrict__ wred,
+                                const double* __restrict__ h, R* __restrict__ wsc) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t node = e / nr;
-        const int s = (int)(e - node * nr);
+        const int64_t node = e / ld;
+        const int s = (int)(e - node * ld);
+        if (s >= nr) {
+            wsc[e] = (R)0;
+            continue;
+        }
         int k = 0;
         while ((k + 1) * (k + 1) <= s) ++k;
         const double ih = 1.0 / h[node];
         double sc = 1.0;
         for (int u = 0; u < k; ++u) sc *= ih;
-        wsc[e] = (R)(wred[e] * sc);
+        wsc[e] = (R)(wred[node * nr + s] * sc);
     }
 }
 
@@ -169,27 +174,13 @@ __global__ void k_fill_tasks(int ng, const int32_t* __restrict__ gstart, const i
     for (int k = 0; k < n; ++k) tasks[toff[g] + k] = make_int2(g, k * kTaskCols);
 }
 
-// Loads a thread's CPT consecutive weight entries (16-byte aligned) as vectors.
-template <typename R, int CPT>
-__device__ __forceinline__ void load_row(const R* p, R* v);
-template <>
-__device__ __forceinline__ void load_row<float, 8>(const float* p, float* v) {
-    const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
-    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-}
-template <>
-__device__ __forceinline__ void load_row<double, 4>(const double* p, double* v) {
-    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
-    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
-}
-
 // Shared-memory plan of the product kernel (elements of R unless noted).
 template <typename R, int CPT>
 struct GemmSmem {
-    static constexpr int TN = 8 * CPT;  // columns per tile
-    static constexpr int LDW = TN + 4;  // padded row stride of the weight tile
+    static constexpr int TN = 8 * CPT;                // columns per tile
+    static constexpr int VS = 16 / (int)sizeof(R);    // weights per 16-byte load
     int nrmax, rmmax, nTr;
-    size_t off_dec, off_pow, off_T, off_G, off_W, off_col, bytes;
+    size_t off_dec, off_pow, off_T, off_G, bytes;
     __host__ __device__ GemmSmem(int p) {
         nrmax = (p + 1) * (p + 1);
         rmmax = 16 * ((nrmax + 15) / 16);
@@ -204,26 +195,48 @@ struct GemmSmem {
         o += sizeof(R) * nTr;
         o = (o + 15) & ~(size_t)15;
         off_G = o;
-        o += sizeof(R) * (size_t)nrmax * rmmax;
-        off_W = o;
-        o += sizeof(R) * (size_t)nrmax * LDW;
-        off_col = o;
-        o += sizeof(int) * 2 * TN;
+        o += sizeof(R) * (size_t)((nrmax + VS - 1) / VS * VS) * rmmax;
         bytes = o;
+    }
+};
+
+// Row stride of the per-node weights: (p+1)^2 rounded up to 16 bytes.
+template <typename R>
+__host__ __device__ constexpr int wsc_ld(int nr) {
+    return (nr + 16 / (int)sizeof(R) - 1) / (16 / (int)sizeof(R)) * (16 / (int)sizeof(R));
+}
+
+template <typename R>
+struct Vec;
+template <>
+struct Vec<float> {
+    using T = float4;
+    __device__ static __forceinline__ void get(const T& v, float* o) {
+        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    }
+};
+template <>
+struct Vec<double> {
+    using T = double2;
+    __device__ static __forceinline__ void get(const T& v, double* o) {
+        o[0] = v.x; o[1] = v.y;
     }
 };
 
 // Columns [c_begin, c_begin + kTaskCols) of one group: C = G W for tiles of
 // TN pairs; thread (rg, cg) owns rows rg + 16k (k < RT) and columns
-// cg*CPT .. cg*CPT + CPT - 1 of each tile.
+// cg*CPT .. cg*CPT + CPT - 1 of each tile.  G^T sits in shared memory
+// (s-major); each thread streams its columns' weights straight from global
+// memory (L1/L2-resident), VS consecutive s per 16-byte load, so the tile loop
+// needs no block barrier.
 template <typename R, int RT, int CPT>
-__device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, int g, int c_begin, int nrq, int cnt,
-                                          int gs, const int32_t* __restrict__ svals,
-                                          const int32_t* __restrict__ far_src, const R* __restrict__ wsc, int nr,
-                                          R* __restrict__ out, int ldo) {
+__device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, int c_begin, int nrq, int cnt, int gs,
+                                          const int32_t* __restrict__ svals, const int32_t* __restrict__ far_src,
+                                          const R* __restrict__ wsc, int ldw, R* __restrict__ out, int ldo) {
     constexpr int TN = GemmSmem<R, CPT>::TN;
-    constexpr int LDW = GemmSmem<R, CPT>::LDW;
+    constexpr int VS = GemmSmem<R, CPT>::VS;
     constexpr int RM = 16 * RT;
+    using V = typename Vec<R>::T;
     const int tid = threadIdx.x;
     const int rg = tid & 15, cg = tid >> 4;
     const int* dec = reinterpret_cast<const int*>(sm + L.off_dec);
@@ -231,14 +244,12 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
     const R* bpow = apow + 16;
     const R* Tsh = reinterpret_cast<const R*>(sm + L.off_T);
     R* G = reinterpret_cast<R*>(sm + L.off_G);
-    R* W = reinterpret_cast<R*>(sm + L.off_W);
-    int* colpos = reinterpret_cast<int*>(sm + L.off_col);
-    int* colsrc = colpos + TN;
-    // operator G^T (s-major, RM rows per s; rows >= nrq are zero)
-    for (int e = tid; e < nrq * RM; e += kGemmThreads) {
+    const int nrv = (nrq + VS - 1) / VS * VS;
+    // operator G^T (s-major, RM rows per s; rows f >= nrq and s >= nrq zero)
+    for (int e = tid; e < nrv * RM; e += kGemmThreads) {
         const int s = e / RM, f = e - s * RM;
         R v = (R)0;
-        if (f < nrq) {
+        if (f < nrq && s < nrq) {
             const int cs = dec[s], cf = dec[f];
             const int x = (cs & 0xff) + (cf & 0xff), y = ((cs >> 8) & 0xff) + ((cf >> 8) & 0xff),
                       z = ((cs >> 16) & 0xff) + ((cf >> 16) & 0xff);
@@ -246,53 +257,51 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
         }
         G[e] = v;
     }
+    __syncthreads();
     const int c_end = min(cnt, c_begin + kTaskCols);
     for (int cb = c_begin; cb < c_end; cb += TN) {
-        const int ncol = min(TN, c_end - cb);
-        __syncthreads();  // G ready; previous tile's W and columns consumed
-        if (tid < TN) {
-            if (tid < ncol) {
-                const int pos = svals[gs + cb + tid];
-                colpos[tid] = pos;
-                colsrc[tid] = far_src[pos];
-            } else {
-                colpos[tid] = -1;
-                colsrc[tid] = -1;
-            }
+        int pos[CPT];
+        const V* wp[CPT];
+#pragma unroll
+        for (int l = 0; l < CPT; ++l) {
+            const int c = cb + cg * CPT + l;
+            pos[l] = c < c_end ? svals[gs + c] : -1;
+            wp[l] = pos[l] >= 0 ? reinterpret_cast<const V*>(wsc + (size_t)far_src[pos[l]] * ldw) : nullptr;
         }
-        __syncthreads();
-        // weight tile W[s][c] (coalesced along s)
-        for (int e = tid; e < nrq * TN; e += kGemmThreads) {
-            const int c = e / nrq, s = e - c * nrq;
-            const int src = colsrc[c];
-            W[s * LDW + c] = src >= 0 ? wsc[(size_t)src * nr + s] : (R)0;
-        }
-        __syncthreads();
         R acc[RT][CPT];
 #pragma unroll
         for (int k = 0; k < RT; ++k)
 #pragma unroll
             for (int l = 0; l < CPT; ++l) acc[k][l] = (R)0;
         const R* Gp = G + rg;
-        const R* Wp = W + cg * CPT;
-#pragma unroll 2
-        for (int s = 0; s < nrq; ++s) {
-            R gv[RT], wv[CPT];
+        for (int s0 = 0; s0 < nrv; s0 += VS) {
+            R wv[CPT][VS];
 #pragma unroll
-            for (int k = 0; k < RT; ++k) gv[k] = Gp[s * RM + 16 * k];
-            load_row<R, CPT>(Wp + s * LDW, wv);
+            for (int l = 0; l < CPT; ++l) {
+                if (wp[l]) {
+                    Vec<R>::get(wp[l][s0 / VS], wv[l]);
+                } else {
 #pragma unroll
-            for (int k = 0; k < RT; ++k)
+                    for (int u = 0; u < VS; ++u) wv[l][u] = (R)0;
+                }
+            }
 #pragma unroll
-                for (int l = 0; l < CPT; ++l) acc[k][l] = fma(gv[k], wv[l], acc[k][l]);
+            for (int u = 0; u < VS; ++u) {
+                R gv[RT];
+#pragma unroll
+                for (int k = 0; k < RT; ++k) gv[k] = Gp[(s0 + u) * RM + 16 * k];
+#pragma unroll
+                for (int k = 0; k < RT; ++k)
+#pragma unroll
+                    for (int l = 0; l < CPT; ++l) acc[k][l] = fma(gv[k], wv[l][u], acc[k][l]);
+            }
         }
         // full rows of ldo entries (zeros above the pair's order), so the
         // per-target sum reads them without knowing the order
 #pragma unroll
         for (int l = 0; l < CPT; ++l) {
-            const int c = cg * CPT + l;
-            if (c < ncol) {
-                R* o = out + (size_t)colpos[c] * ldo;
+            if (pos[l] >= 0) {
+                R* o = out + (size_t)pos[l] * ldo;
 #pragma unroll
                 for (int k = 0; k < RT; ++k) {
                     const int f = rg + 16 * k;
@@ -344,7 +353,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restric
     switch (rt) {
 #define FMM_GEMM_CASE(K)                                                                                     \
     case K:                                                                                                  \
-        gemm_task<R, K, CPT>(L, sm_gemm, g, task.y, nrq, cnt, gs, svals, far_src, wsc, nr, out, nr); \
+        gemm_task<R, K, CPT>(L, sm_gemm, task.y, nrq, cnt, gs, svals, far_src, wsc, wsc_ld<R>(nr), out, nr); \
         break;
         FMM_GEMM_CASE(1)
         FMM_GEMM_CASE(2)
@@ -408,14 +417,16 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_TRY(ws.m2l_ukeys.ensure(sizeof(uint64_t) * nf));
         FMM_TRY(ws.m2l_cnt.ensure(sizeof(int32_t) * (nf + 1)));
         FMM_TRY(ws.m2l_gstart.ensure(sizeof(int32_t) * (nf + 1)));
-        FMM_TRY(ws.m2l_wsc.ensure(sizeof(R) * (size_t)M * nr));
+        const int ldw = wsc_ld<R>(nr);
+        FMM_TRY(ws.m2l_wsc.ensure(sizeof(R) * (size_t)M * ldw));
         FMM_TRY(ws.counters.ensure(sizeof(unsigned long long) * 32));
         int32_t* tgt = ws.m2l_tgt.as<int32_t>();
         count_launches(1);
         k_far_targets<<<grid_for(M, 4), 128, 0, st>>>(M, t.far_off, tgt);
         count_launches(1);
-        k_scale_weights<R><<<grid_for((int64_t)M * nr, 256), 256, 0, st>>>((int64_t)M * nr, nr, ws.wred.as<double>(),
-                                                                          t.r, ws.m2l_wsc.as<R>());
+        k_scale_weights<R><<<grid_for((int64_t)M * ldw, 256), 256, 0, st>>>((int64_t)M * ldw, nr, ldw,
+                                                                           ws.wred.as<double>(), t.r,
+                                                                           ws.m2l_wsc.as<R>());
         count_launches(1);
         k_m2l_keys<<<grid_for(nf, 256), 256, 0, st>>>(nf, t, tgt, p, ws.m2l_keys.as<uint64_t>(),
                                                        ws.m2l_vals.as<int32_t>());

@@ -46,18 +46,7 @@ __device__ __forceinline__ void mlp_layer(const float* __restrict__ W, const flo
     }
 }
 
-// Forward pass of one sample; P points at the parameter blob.
-__device__ __forceinline__ void mlp_forward(const float* __restrict__ P, const float* x, float* y) {
-    float in[kMlpIn], h1[kMlpH], h2[kMlpH];
-#pragma unroll
-    for (int k = 0; k < kMlpIn; ++k) in[k] = (x[k] - P[kOffMean + k]) * P[kOffIstd + k];
-    mlp_layer<kMlpH, kMlpIn, true>(P + kOffW1, P + kOffB1, in, h1);
-    mlp_layer<kMlpH, kMlpH, true>(P + kOffW2, P + kOffB2, h1, h2);
-    mlp_layer<kMlpH, kMlpH, true>(P + kOffW3, P + kOffB3, h2, h1);
-    mlp_layer<kMlpOut, kMlpH, false>(P + kOffW4, P + kOffB4, h1, y);
-}
-
-// Inference layout of the parameters in shared memory (floats): the blob
+// Inference layout of the parameters (floats): the blob
 // with W1's rows padded from kMlpIn to kMlpInP entries so that every weight
 // row starts on a 16-byte boundary and is read as float4, and W4/b4 padded to
 // kMlpOutP rows (zeros) so outputs come in blocks of four.
@@ -97,62 +86,114 @@ __device__ __forceinline__ void mlp_stage(const float* __restrict__ P, float* S)
     }
 }
 
-// One dense layer out[o] = act(b[o] + W[o] . in), four outputs at a time
-// (eight independent FMA chains), with `in` in registers (compile-time
-// indices) and the outputs stored to this thread's column of the shared
-// activation buffer (act[o * stride]), the only dynamically indexed array.
-template <int NIN, bool RELU>
-__device__ __forceinline__ void mlp_layer_smem(const float* W, const float* b, int nout, const float (&in)[NIN],
-                                               float* act, int stride) {
-#pragma unroll 1
-    for (int o = 0; o < nout; o += 4) {
-        const float4* w0 = reinterpret_cast<const float4*>(W + o * NIN);
-        float a[4][2];
+// The device copy of the parameters holds the blob followed (at kMlpInfOff)
+// by the inference layout above, written once by k_mlp_stage_global.
+constexpr int kMlpInfOff = (kMlpParams + 3) / 4 * 4;
+constexpr int kMlpBufFloats = kMlpInfOff + kMlpSmem;
+
+namespace {
+__global__ void k_mlp_stage_global(float* buf) { mlp_stage(buf, buf + kMlpInfOff); }
+}  // namespace
+
+// Warp-cooperative inference on up to 32 samples (weights stationary in
+// registers): lane l owns hidden units 2l and 2l+1 of every layer and streams
+// the samples' input rows from shared memory (broadcast reads), so every
+// weight is read once per batch instead of once per sample.  Per-warp
+// scratch: X[32][kMlpInP] (normalised inputs, filled by the caller), two
+// activation buffers [32][kMlpH] and Y[32][kMlpOutP] (outputs).
+constexpr int kWarpMlpFloats = 32 * (kMlpInP + 2 * kMlpH + kMlpOutP);
+
+template <int NIN>
+__device__ __forceinline__ void warp_mlp_layer(const float* __restrict__ W, const float* __restrict__ b, const float* in,
+                                               float* outp, int cnt, int u0, bool relu) {
+    float wa[NIN], wb[NIN];
+    const float4* ra = reinterpret_cast<const float4*>(W + u0 * NIN);
+    const float4* rb = reinterpret_cast<const float4*>(W + (u0 + 1) * NIN);
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            a[r][0] = b[o + r];
-            a[r][1] = 0.0f;
-        }
+    for (int k = 0; k < NIN / 4; ++k) {
+        const float4 x = __ldg(ra + k), y = __ldg(rb + k);
+        wa[4 * k] = x.x; wa[4 * k + 1] = x.y; wa[4 * k + 2] = x.z; wa[4 * k + 3] = x.w;
+        wb[4 * k] = y.x; wb[4 * k + 1] = y.y; wb[4 * k + 2] = y.z; wb[4 * k + 3] = y.w;
+    }
+    const float ba = __ldg(b + u0), bb = __ldg(b + u0 + 1);
+    // two samples per step: eight independent FMA chains
+    for (int s = 0; s < cnt; s += 2) {
+        const bool two = s + 1 < cnt;
+        const float4* x4 = reinterpret_cast<const float4*>(in + s * NIN);
+        const float4* y4 = reinterpret_cast<const float4*>(in + (two ? s + 1 : s) * NIN);
+        float a0 = ba, c0 = 0.0f, a1 = bb, c1 = 0.0f;
+        float d0 = ba, e0 = 0.0f, d1 = bb, e1 = 0.0f;
 #pragma unroll
         for (int k = 0; k < NIN / 4; ++k) {
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                const float4 w = w0[r * (NIN / 4) + k];
-                a[r][0] = fmaf(w.x, in[4 * k], a[r][0]);
-                a[r][1] = fmaf(w.y, in[4 * k + 1], a[r][1]);
-                a[r][0] = fmaf(w.z, in[4 * k + 2], a[r][0]);
-                a[r][1] = fmaf(w.w, in[4 * k + 3], a[r][1]);
-            }
+            const float4 x = x4[k], y = y4[k];
+            a0 = fmaf(wa[4 * k], x.x, a0);
+            c0 = fmaf(wa[4 * k + 1], x.y, c0);
+            a1 = fmaf(wb[4 * k], x.x, a1);
+            c1 = fmaf(wb[4 * k + 1], x.y, c1);
+            d0 = fmaf(wa[4 * k], y.x, d0);
+            e0 = fmaf(wa[4 * k + 1], y.y, e0);
+            d1 = fmaf(wb[4 * k], y.x, d1);
+            e1 = fmaf(wb[4 * k + 1], y.y, e1);
+            a0 = fmaf(wa[4 * k + 2], x.z, a0);
+            c0 = fmaf(wa[4 * k + 3], x.w, c0);
+            a1 = fmaf(wb[4 * k + 2], x.z, a1);
+            c1 = fmaf(wb[4 * k + 3], x.w, c1);
+            d0 = fmaf(wa[4 * k + 2], y.z, d0);
+            e0 = fmaf(wa[4 * k + 3], y.w, e0);
+            d1 = fmaf(wb[4 * k + 2], y.z, d1);
+            e1 = fmaf(wb[4 * k + 3], y.w, e1);
         }
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const float v = a[r][0] + a[r][1];
-            act[(o + r) * stride] = RELU ? fmaxf(v, 0.0f) : v;
+        float v0 = a0 + c0, v1 = a1 + c1, w0 = d0 + e0, w1 = d1 + e1;
+        if (relu) {
+            v0 = fmaxf(v0, 0.0f);
+            v1 = fmaxf(v1, 0.0f);
+            w0 = fmaxf(w0, 0.0f);
+            w1 = fmaxf(w1, 0.0f);
         }
+        *reinterpret_cast<float2*>(outp + s * kMlpH + u0) = make_float2(v0, v1);
+        if (two) *reinterpret_cast<float2*>(outp + (s + 1) * kMlpH + u0) = make_float2(w0, w1);
     }
 }
 
-template <int N>
-__device__ __forceinline__ void mlp_load_act(const float* act, int stride, float (&v)[N]) {
+__device__ __forceinline__ void warp_mlp(const float* __restrict__ S, float* X, float* Ha, float* Hb, float* Y,
+                                         int cnt, int lane) {
+    const int u0 = 2 * lane;
+    warp_mlp_layer<kMlpInP>(S + kSOffW1, S + kSOffB1, X, Ha, cnt, u0, true);
+    __syncwarp();
+    warp_mlp_layer<kMlpH>(S + kSOffW2, S + kSOffB2, Ha, Hb, cnt, u0, true);
+    __syncwarp();
+    warp_mlp_layer<kMlpH>(S + kSOffW3, S + kSOffB3, Hb, Ha, cnt, u0, true);
+    __syncwarp();
+    if (lane < kMlpOut) {
+        float w[kMlpH];
+        const float4* r = reinterpret_cast<const float4*>(S + kSOffW4 + lane * kMlpH);
 #pragma unroll
-    for (int k = 0; k < N; ++k) v[k] = act[k * stride];
+        for (int k = 0; k < kMlpH / 4; ++k) {
+            const float4 x = __ldg(r + k);
+            w[4 * k] = x.x; w[4 * k + 1] = x.y; w[4 * k + 2] = x.z; w[4 * k + 3] = x.w;
+        }
+        const float b = __ldg(S + kSOffB4 + lane);
+        for (int s = 0; s < cnt; ++s) {
+            const float4* x4 = reinterpret_cast<const float4*>(Ha + s * kMlpH);
+            float a = b, c = 0.0f;
+#pragma unroll
+            for (int k = 0; k < kMlpH / 4; ++k) {
+                const float4 x = x4[k];
+                a = fmaf(w[4 * k], x.x, a);
+                c = fmaf(w[4 * k + 1], x.y, c);
+                a = fmaf(w[4 * k + 2], x.z, a);
+                c = fmaf(w[4 * k + 3], x.w, c);
+            }
+            Y[s * kMlpOutP + lane] = a + c;
+        }
+    }
+    __syncwarp();
 }
 
-// Forward pass with the weights in the inference layout S and a per-thread
-// activation column act (kMlpH entries at stride `stride`); the kMlpOut
-// outputs are left in act[0 .. kMlpOut-1] (same stride).
-__device__ __forceinline__ void mlp_forward_smem(const float* S, float* act, int stride, const float* x) {
-    float in[kMlpInP];
+// Normalised, padded network input of one sample (kMlpInP floats).
+__device__ __forceinline__ void mlp_input(const float* __restrict__ S, const float* x, float* row) {
 #pragma unroll
-    for (int k = 0; k < kMlpInP; ++k) in[k] = k < kMlpIn ? (x[k] - S[kSOffMean + k]) * S[kSOffIstd + k] : 0.0f;
-    mlp_layer_smem<kMlpInP, true>(S + kSOffW1, S + kSOffB1, kMlpH, in, act, stride);
-    float h[kMlpH];
-    mlp_load_act(act, stride, h);
-    mlp_layer_smem<kMlpH, true>(S + kSOffW2, S + kSOffB2, kMlpH, h, act, stride);
-    mlp_load_act(act, stride, h);
-    mlp_layer_smem<kMlpH, true>(S + kSOffW3, S + kSOffB3, kMlpH, h, act, stride);
-    mlp_load_act(act, stride, h);
-    mlp_layer_smem<kMlpH, false>(S + kSOffW4, S + kSOffB4, kMlpOutP, h, act, stride);
+    for (int k = 0; k < kMlpInP; ++k) row[k] = k < kMlpIn ? (x[k] - __ldg(S + kSOffMean + k)) * __ldg(S + kSOffIstd + k) : 0.0f;
 }
 
 // Features of the pair (target i, source j); P = order of the stored norms.
@@ -162,16 +203,18 @@ __device__ __forceinline__ void mlp_forward_smem(const float* S, float* act, int
 constexpr int kFeatOrders = 10;
 __device__ __forceinline__ void selector_features(const TreeDev& t, const float* __restrict__ lnorm,
                                                   const float* __restrict__ dmin, int P, int i, int j, float* x) {
-    const double dx = t.cx[i] - t.cx[j], dy = t.cy[i] - t.cy[j], dz = t.cz[i] - t.cz[j];
-    const double R = sqrt(dx * dx + dy * dy + dz * dz);
-    const float lR = (float)log10(R);
-    x[0] = (float)(1.7320508075688772 * (t.r[i] + t.r[j]) / R);
-    x[1] = log2f((float)(t.r[j] / t.r[i]));
+    // FP32 is ample for network inputs (the FP64 pipe is the scarce one)
+    const float dx = (float)(t.cx[i] - t.cx[j]), dy = (float)(t.cy[i] - t.cy[j]), dz = (float)(t.cz[i] - t.cz[j]);
+    const float R = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float lR = log10f(R);
+    const float ri = (float)t.r[i], rj = (float)t.r[j];
+    x[0] = 1.7320508f * (ri + rj) / R;
+    x[1] = log2f(rj / ri);
     x[2] = log2f((float)t.count[i]);
     for (int k = 0; k <= kQmax; ++k)
         x[3 + k] = (k <= P && k <= kFeatOrders) ? fmaxf(lnorm[(size_t)j * (P + 1) + k] - (float)(k + 2) * lR, -40.0f)
                                                 : -40.0f;
-    x[16] = fminf(dmin[i] * dmin[j] * (float)R, 30.0f) * (1.0f / 30.0f);
+    x[16] = fminf(dmin[i] * dmin[j] * R, 30.0f) * (1.0f / 30.0f);
 }
 
 }  // namespace fmm

@@ -295,8 +295,8 @@ int launch_direct_f64(Workspace& ws, const Particles& P, int field_order, const 
     const int64_t n = P.n;
     if (!d_targets) ntgt = n;
     const int nf = nT(field_order);
-    FMM_TRY(ws.smc.ensure(sizeof(double) * (size_t)n * P.dim));
-    double* mc = ws.smc.as<double>();
+    FMM_TRY(ws.dsmc.ensure(sizeof(double) * (size_t)n * P.dim));  // own buffer: may overlap the FMM phases
+    double* mc = ws.dsmc.as<double>();
     count_launches(1);
     k_scale_mp<<<grid_for(n, 256), 256, 0, st>>>(n, P.dim, P.mp, mc);
     // few targets (sampled checks): a block per target and source split

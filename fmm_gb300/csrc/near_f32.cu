@@ -57,6 +57,25 @@ __global__ void k_gather_f32(int64_t n, int dim, const TreeDev t, const double* 
     }
 }
 
+// Node centres as double-float pairs (hi = rounded centre, lo = rounded
+// remainder), so leaf-centre offsets are formed in FP32 without losing bits.
+__global__ void k_node_centres_f32(int M, const TreeDev t, float4* __restrict__ hi, float4* __restrict__ lo) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= M) return;
+    const float hx = (float)t.cx[k], hy = (float)t.cy[k], hz = (float)t.cz[k];
+    hi[k] = make_float4(hx, hy, hz, 0.0f);
+    lo[k] = make_float4((float)(t.cx[k] - (double)hx), (float)(t.cy[k] - (double)hy), (float)(t.cz[k] - (double)hz),
+                        0.0f);
+}
+
+// a - b as an unevaluated pair s + e (Knuth's TwoSum with b negated).
+__device__ __forceinline__ float two_diff(float a, float b, float& e) {
+    const float s = a - b;
+    const float bb = s - a;
+    e = (a - (s - bb)) - (b + bb);
+    return s;
+}
+
 // Sum over the sources [js, je) of one leaf (lane group grp of ngr) for the
 // lane's target: compensated FP32 (TwoSum hi + lo), since the per-atom terms
 // are much larger than their neutral total.  CHECK: the leaf may hold the
@@ -109,6 +128,7 @@ __device__ __forceinline__ void p2p_leaf(const float4* __restrict__ rec, int js,
 // warp's targets run without the exclusion test.
 template <int M, int F>
 __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* __restrict__ rec,
+                                                 const float4* __restrict__ chi, const float4* __restrict__ clo,
                                                  const int32_t* __restrict__ excl, int exw, int64_t n, int damp,
                                                  double* __restrict__ fs) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
@@ -118,7 +138,7 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
     const int leaf = t.leaves[w];
     const int s0 = t.start[leaf], cnt = t.count[leaf];
     const int q0 = t.near_off[leaf], q1 = t.near_off[leaf + 1];
-    const double cxa = t.cx[leaf], cya = t.cy[leaf], cza = t.cz[leaf];
+    const float4 ca = chi[leaf], cal = clo[leaf];
     for (int chunk = 0; chunk < cnt; chunk += 32) {
         const int nt = min(32, cnt - chunk);
         int g = 1;
@@ -137,18 +157,22 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
             int o = (e < exw) ? excl[(size_t)e * n + ot] : 0;
             exl[e] = o > 0 ? t.leaf_of[t.pos_of[o - 1]] : -1;
         }
-        double acc[NF];
+        // per-target sums over all source leaves as double-float pairs (FP32
+        // arithmetic; the FP64 pipe is the scarce one)
+        float AH[NF], AL[NF];
 #pragma unroll
-        for (int f = 0; f < NF; ++f) acc[f] = 0.0;
+        for (int f = 0; f < NF; ++f) AH[f] = AL[f] = 0.0f;
         if (valid) {
             for (int q = q0; q < q1; ++q) {
                 const int j = t.near_src[q];
                 const int js = t.start[j], je = js + t.count[j];
-                const double odx = cxa - t.cx[j], ody = cya - t.cy[j], odz = cza - t.cz[j];
-                const float ox = (float)odx, oy = (float)ody, oz = (float)odz;
-                // low parts of the offset folded with the target's low parts
-                const float oxl = (float)(odx - (double)ox) + tb.x, oyl = (float)(ody - (double)oy) + tb.y,
-                            ozl = (float)(odz - (double)oz) + tb.z;
+                // leaf-centre offset c_A - c_B as hi + lo; the low parts are
+                // folded with the target's low parts
+                const float4 cb = chi[j], cbl = clo[j];
+                float ex, ey, ez;
+                const float ox = two_diff(ca.x, cb.x, ex), oy = two_diff(ca.y, cb.y, ey), oz = two_diff(ca.z, cb.z, ez);
+                const float oxl = (ex + (cal.x - cbl.x)) + tb.x, oyl = (ey + (cal.y - cbl.y)) + tb.y,
+                            ozl = (ez + (cal.z - cbl.z)) + tb.z;
                 bool need = (j == leaf) || exw > kExwRegs;
 #pragma unroll
                 for (int e = 0; e < kExwRegs; ++e) need |= (exl[e] == j);
@@ -162,9 +186,19 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
                     p2p_leaf<M, F, false>(rec, js, je, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy, oz, oxl, oyl,
                                           ozl, excl, exw, n, ot, damp, hi, lo);
 #pragma unroll
-                for (int f = 0; f < NF; ++f) acc[f] += (double)hi[f] + (double)lo[f];
+                for (int f = 0; f < NF; ++f) {
+                    // (AH, AL) += (hi, lo)
+                    const float sum = AH[f] + hi[f];
+                    const float bb = sum - AH[f];
+                    const float err = (AH[f] - (sum - bb)) + (hi[f] - bb);
+                    AH[f] = sum;
+                    AL[f] += err + lo[f];
+                }
             }
         }
+        double acc[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) acc[f] = (double)AH[f] + (double)AL[f];
         for (int off = g; off < 32; off <<= 1) {
 #pragma unroll
             for (int f = 0; f < NF; ++f) acc[f] += __shfl_xor_sync(0xffffffffu, acc[f], off);
@@ -188,10 +222,15 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
     count_launches(1);
     k_gather_f32<<<grid_for(n, 256), 256, 0, st>>>(n, P.dim, t, ws.sx.as<double>(), ws.sy.as<double>(),
                                                     ws.sz.as<double>(), ws.sd.as<double>(), ws.smc.as<double>(), rec);
+    FMM_TRY(ws.f32node.ensure(sizeof(float4) * 2 * (size_t)t.num_nodes));
+    float4* chi = ws.f32node.as<float4>();
+    float4* clo = chi + t.num_nodes;
+    count_launches(1);
+    k_node_centres_f32<<<grid_for(t.num_nodes, 256), 256, 0, st>>>(t.num_nodes, t, chi, clo);
     FMM_TRY(ws.fsorted.ensure(sizeof(double) * (size_t)n * nf));
     const unsigned blocks = grid_for((int64_t)t.num_leaves * 32, 128);
     FMM_MF_SWITCH(m, field_order,
-                  (k_p2p_f32<MM, FF><<<blocks, 128, 0, st>>>(t, rec, P.excl, P.exw, n, P.damp_type,
+                  (k_p2p_f32<MM, FF><<<blocks, 128, 0, st>>>(t, rec, chi, clo, P.excl, P.exw, n, P.damp_type,
                                                               ws.fsorted.as<double>())));
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;

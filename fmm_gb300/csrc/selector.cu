@@ -379,22 +379,34 @@ __global__ void k_adam(int nparam, int first, float* __restrict__ p, const float
     p[k] -= lr * mh / (sqrtf(vh) + 1e-8f);
 }
 
-// Batched inference with the same routine the list kernel uses.
-__global__ void k_mlp_infer(const float* __restrict__ params, const float* __restrict__ X, int n, float* __restrict__ Y) {
+// Batched inference with the routine the list kernel uses: a warp per 32
+// samples, weights (inference layout after the blob in `params`) in
+// registers.
+__global__ void __launch_bounds__(128) k_mlp_infer(const float* __restrict__ params, const float* __restrict__ X,
+                                                   int n, float* __restrict__ Y) {
     extern __shared__ __align__(16) float sm_inf[];
-    float* S = sm_inf;
-    float* act = sm_inf + kMlpSmem + threadIdx.x;
-    mlp_stage(params, S);
-    __syncthreads();
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    float x[kMlpIn];
-    for (int k = 0; k < kMlpIn; ++k) x[k] = X[(size_t)q * kMlpIn + k];
-    mlp_forward_smem(S, act, blockDim.x, x);
-    for (int o = 0; o < kMlpOut; ++o) Y[(size_t)q * kMlpOut + o] = act[o * blockDim.x];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* Xs = sm_inf + wib * kWarpMlpFloats;
+    float* Ha = Xs + 32 * kMlpInP;
+    float* Hb = Ha + 32 * kMlpH;
+    float* Ys = Hb + 32 * kMlpH;
+    const float* S = params + kMlpInfOff;
+    const int base = (blockIdx.x * blockDim.x) + wib * 32;
+    const int cnt = max(0, min(32, n - base));
+    if (cnt == 0) return;  // whole warp
+    const int q = base + lane;
+    if (lane < cnt) {
+        float x[kMlpIn];
+        for (int k = 0; k < kMlpIn; ++k) x[k] = X[(size_t)q * kMlpIn + k];
+        mlp_input(S, x, Xs + lane * kMlpInP);
+    }
+    __syncwarp();
+    warp_mlp(S, Xs, Ha, Hb, Ys, cnt, lane);
+    if (lane < cnt)
+        for (int o = 0; o < kMlpOut; ++o) Y[(size_t)q * kMlpOut + o] = Ys[lane * kMlpOutP + o];
 }
 
-size_t infer_smem(int threads) { return sizeof(float) * (kMlpSmem + (size_t)kMlpH * threads); }
+size_t infer_smem(int threads) { return sizeof(float) * (size_t)(threads / 32) * kWarpMlpFloats; }
 
 size_t train_smem() {
     return sizeof(float) * (kMlpParams + kTB * (kMlpIn + 3 * kMlpH + kMlpOut + 3 * kMlpH));
@@ -543,12 +555,14 @@ int fmm_selector_collect(int64_t n, const double* X, int mdim, const double* mp,
 int fmm_mlp_forward(const float* params, const float* x, int64_t n, float* y) {
     if (!params || !x || !y || n < 1) return FMM_EINVAL;
     DevF P, X, Y;
-    float* dp = P.p(kMlpParams);
+    float* dp = P.p(kMlpBufFloats);  // blob, then its inference layout
     float* dx = X.p((size_t)n * kMlpIn);
     float* dy = Y.p((size_t)n * kMlpOut);
     if (!dp || !dx || !dy) return FMM_ENOMEM;
     FMM_CUDA_TRY(cudaMemcpy(dp, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice));
     FMM_CUDA_TRY(cudaMemcpy(dx, x, sizeof(float) * n * kMlpIn, cudaMemcpyHostToDevice));
+    count_launches(1);
+    k_mlp_stage_global<<<1, 256>>>(dp);
     FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)infer_smem(128)));
     count_launches(1);

@@ -298,59 +298,107 @@ __global__ void k_pos_of(int64_t n, const uint32_t* __restrict__ perm, int32_t* 
 }
 
 // counters: [0] next frontier size, [1] far count, [2] near count, [3] overflow flag
+// Slots for this lane's `cnt` entries in a list shared by the whole grid: one
+// atomic per warp (warp-wide inclusive scan of the counts); every lane of
+// the warp must call it.  Returns the first slot of the lane's entries.
+__device__ __forceinline__ unsigned long long warp_alloc(unsigned long long* ctr, unsigned cnt, int lane) {
+    unsigned x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    const unsigned total = __shfl_sync(0xffffffffu, x, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total) base = atomicAdd(ctr, (unsigned long long)total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + (x - cnt);
+}
+
+// Outcome of one candidate pair (i, j): far (at `order`), near (two leaves),
+// or refined into the children of the larger node; entries are appended to
+// the far list, the near list or the next frontier.  Called by every lane of
+// the warp (skip: no candidate).
+__device__ __forceinline__ void emit_pair(bool skip, bool accept, int order, int i, int j, bool li, bool lj,
+                                          bool mixed, double ri, double rj, const TreeDev& t, int2* __restrict__ out,
+                                          int64_t cap_out, uint64_t* __restrict__ far, int64_t cap_far,
+                                          uint64_t* __restrict__ nearp, int64_t cap_near,
+                                          unsigned long long* counters, int lane) {
+    const bool isfar = !skip && accept;
+    const bool isnear = !skip && !accept && li && lj && !mixed;
+    const bool refine = !skip && !accept && !isnear;
+    int c[8], nc = 0;
+    bool descend_i = false;
+    if (refine) {
+        descend_i = lj || ((ri > rj) && !li);
+        const int* ch = t.child + 8 * (descend_i ? i : j);
+#pragma unroll
+        for (int o = 0; o < 8; ++o) {
+            const int v = ch[o];
+            if (v >= 0) c[nc++] = v;
+        }
+    }
+    const unsigned long long kf = warp_alloc(&counters[1], isfar ? 1u : 0u, lane);
+    const unsigned long long kn = warp_alloc(&counters[2], isnear ? 1u : 0u, lane);
+    const unsigned long long kr = warp_alloc(&counters[0], (unsigned)nc, lane);
+    if (isfar) {
+        if (kf < (unsigned long long)cap_far)
+            far[kf] = ((uint64_t)(uint32_t)i << 36) | ((uint64_t)(order & 15) << 32) | (uint32_t)j;
+        else
+            counters[3] = 1;
+    }
+    if (isnear) {
+        if (kn < (unsigned long long)cap_near)
+            nearp[kn] = ((uint64_t)(uint32_t)i << 32) | (uint32_t)j;
+        else
+            counters[3] = 1;
+    }
+    if (refine) {
+        if (kr + nc > (unsigned long long)cap_out) {
+            counters[3] = 1;
+        } else {
+            for (int o = 0; o < nc; ++o) out[kr + o] = descend_i ? make_int2(c[o], j) : make_int2(i, c[o]);
+        }
+    }
+}
+
 __global__ void k_list_iter(const int2* __restrict__ in, int nin, int2* __restrict__ out, int64_t cap_out,
                             uint64_t* __restrict__ far, int64_t cap_far, uint64_t* __restrict__ nearp,
                             int64_t cap_near, const TreeDev t, double theta, double rdamp, int order,
                             unsigned long long* counters) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nin) return;
-    const int i = in[q].x, j = in[q].y;
-    const double dx = __dsub_rn(t.cx[i], __dadd_rn(t.cx[j], 0.0));
-    const double dy = __dsub_rn(t.cy[i], __dadd_rn(t.cy[j], 0.0));
-    const double dz = __dsub_rn(t.cz[i], __dadd_rn(t.cz[j], 0.0));
-    const double r = norm2_3(dx, dy, dz);
-    const double ri = t.rmax[i], rj = t.rmax[j];
-    const bool li = t.is_leaf[i] != 0, lj = t.is_leaf[j] != 0;
-    // batched systems: no pairs across systems; nodes spanning several
-    // systems are always refined
-    bool mixed = false;
-    if (t.sysid) {
-        const int si = t.sysid[i], sj = t.sysid[j];
-        if (si >= 0 && sj >= 0 && si != sj) return;
-        mixed = si < 0 || sj < 0;
-    }
-    bool accept = !mixed && __dmul_rn(r, theta) > __dadd_rn(ri, rj);
-    if (accept && rdamp > 0.0) {
-        // closest possible particle distance: centre distance minus the cube circumradii
-        const double gap = __dsub_rn(r, __dmul_rn(1.7320508075688772, __dadd_rn(t.r[i], t.r[j])));
-        accept = gap >= rdamp;
-    }
-    if (accept) {
-        const unsigned long long k = atomicAdd(&counters[1], 1ull);
-        if (k < (unsigned long long)cap_far)
-            far[k] = ((uint64_t)(uint32_t)i << 36) | ((uint64_t)(order & 15) << 32) | (uint32_t)j;
-        else
-            counters[3] = 1;
-    } else if (li && lj && !mixed) {
-        const unsigned long long k = atomicAdd(&counters[2], 1ull);
-        if (k < (unsigned long long)cap_near)
-            nearp[k] = ((uint64_t)(uint32_t)i << 32) | (uint32_t)j;
-        else
-            counters[3] = 1;
-    } else {
-        const bool descend_i = lj || ((ri > rj) && !li);
-        const int* ch = t.child + 8 * (descend_i ? i : j);
-        int c[8], nc = 0;
-#pragma unroll
-        for (int o = 0; o < 8; ++o)
-            if (ch[o] >= 0) c[nc++] = ch[o];
-        const unsigned long long base = atomicAdd(&counters[0], (unsigned long long)nc);
-        if (base + nc > (unsigned long long)cap_out) {
-            counters[3] = 1;
-            return;
+    const int lane = threadIdx.x & 31;
+    bool skip = q >= nin;
+    int i = 0, j = 0;
+    double ri = 0.0, rj = 0.0;
+    bool li = false, lj = false, mixed = false, accept = false;
+    if (!skip) {
+        i = in[q].x;
+        j = in[q].y;
+        const double dx = __dsub_rn(t.cx[i], __dadd_rn(t.cx[j], 0.0));
+        const double dy = __dsub_rn(t.cy[i], __dadd_rn(t.cy[j], 0.0));
+        const double dz = __dsub_rn(t.cz[i], __dadd_rn(t.cz[j], 0.0));
+        const double r = norm2_3(dx, dy, dz);
+        ri = t.rmax[i];
+        rj = t.rmax[j];
+        li = t.is_leaf[i] != 0;
+        lj = t.is_leaf[j] != 0;
+        // batched systems: no pairs across systems; nodes spanning several
+        // systems are always refined
+        if (t.sysid) {
+            const int si = t.sysid[i], sj = t.sysid[j];
+            if (si >= 0 && sj >= 0 && si != sj) skip = true;
+            mixed = si < 0 || sj < 0;
         }
-        for (int o = 0; o < nc; ++o) out[base + o] = descend_i ? make_int2(c[o], j) : make_int2(i, c[o]);
+        accept = !mixed && __dmul_rn(r, theta) > __dadd_rn(ri, rj);
+        if (accept && rdamp > 0.0) {
+            // closest possible particle distance: centre distance minus the cube circumradii
+            const double gap = __dsub_rn(r, __dmul_rn(1.7320508075688772, __dadd_rn(t.r[i], t.r[j])));
+            accept = gap >= rdamp;
+        }
     }
+    emit_pair(skip, accept, order, i, j, li, lj, mixed, ri, rj, t, out, cap_out, far, cap_far, nearp, cap_near,
+              counters, lane);
 }
 
 // Learned acceptance (selector): a pair that passes the loose geometric test
@@ -363,70 +411,64 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
     int qmax, const float* __restrict__ params, const float* __restrict__ lnorm, const float* __restrict__ dmin,
     int P, float log_budget, unsigned long long* counters) {
     extern __shared__ __align__(16) float sm_sel[];
-    float* S = sm_sel;  // weights (inference layout), then one activation column per thread
-    mlp_stage(params, S);
-    __syncthreads();
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* X = sm_sel + wib * kWarpMlpFloats;  // this warp's network scratch
+    float* Ha = X + 32 * kMlpInP;
+    float* Hb = Ha + 32 * kMlpH;
+    float* Y = Hb + 32 * kMlpH;
+    const float* S = params + kMlpInfOff;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nin) return;
-    const int i = in[q].x, j = in[q].y;
-    const double dx = __dsub_rn(t.cx[i], __dadd_rn(t.cx[j], 0.0));
-    const double dy = __dsub_rn(t.cy[i], __dadd_rn(t.cy[j], 0.0));
-    const double dz = __dsub_rn(t.cz[i], __dadd_rn(t.cz[j], 0.0));
-    const double r = norm2_3(dx, dy, dz);
-    const double ri = t.rmax[i], rj = t.rmax[j];
-    const bool li = t.is_leaf[i] != 0, lj = t.is_leaf[j] != 0;
-    // batched systems: no pairs across systems; nodes spanning several
-    // systems are always refined
-    bool mixed = false;
-    if (t.sysid) {
-        const int si = t.sysid[i], sj = t.sysid[j];
-        if (si >= 0 && sj >= 0 && si != sj) return;
-        mixed = si < 0 || sj < 0;
-    }
-    bool accept = !mixed && __dmul_rn(r, theta_loose) > __dadd_rn(ri, rj);
-    if (accept && rdamp > 0.0) {
-        const double gap = __dsub_rn(r, __dmul_rn(1.7320508075688772, __dadd_rn(t.r[i], t.r[j])));
-        accept = gap >= rdamp;
-    }
-    int order = 0;
-    if (accept) {
-        float x[kMlpIn];
-        selector_features(t, lnorm, dmin, P, i, j, x);
-        float* act = sm_sel + kMlpSmem + threadIdx.x;
-        mlp_forward_smem(S, act, blockDim.x, x);
-        for (int o = kQmin; o <= qmax; ++o)
-            if (act[(o - kQmin) * blockDim.x] <= log_budget) {
-                order = o;
-                break;
-            }
-        accept = order > 0;
-    }
-    if (accept) {
-        const unsigned long long k = atomicAdd(&counters[1], 1ull);
-        if (k < (unsigned long long)cap_far)
-            far[k] = ((uint64_t)(uint32_t)i << 36) | ((uint64_t)(order & 15) << 32) | (uint32_t)j;
-        else
-            counters[3] = 1;
-    } else if (li && lj && !mixed) {
-        const unsigned long long k = atomicAdd(&counters[2], 1ull);
-        if (k < (unsigned long long)cap_near)
-            nearp[k] = ((uint64_t)(uint32_t)i << 32) | (uint32_t)j;
-        else
-            counters[3] = 1;
-    } else {
-        const bool descend_i = lj || ((ri > rj) && !li);
-        const int* ch = t.child + 8 * (descend_i ? i : j);
-        int c[8], nc = 0;
-#pragma unroll
-        for (int o = 0; o < 8; ++o)
-            if (ch[o] >= 0) c[nc++] = ch[o];
-        const unsigned long long base = atomicAdd(&counters[0], (unsigned long long)nc);
-        if (base + nc > (unsigned long long)cap_out) {
-            counters[3] = 1;
-            return;
+    bool skip = q >= nin;
+    int i = 0, j = 0;
+    double ri = 0.0, rj = 0.0;
+    bool li = false, lj = false, mixed = false, accept = false;
+    if (!skip) {
+        i = in[q].x;
+        j = in[q].y;
+        const double dx = __dsub_rn(t.cx[i], __dadd_rn(t.cx[j], 0.0));
+        const double dy = __dsub_rn(t.cy[i], __dadd_rn(t.cy[j], 0.0));
+        const double dz = __dsub_rn(t.cz[i], __dadd_rn(t.cz[j], 0.0));
+        const double r = norm2_3(dx, dy, dz);
+        ri = t.rmax[i];
+        rj = t.rmax[j];
+        li = t.is_leaf[i] != 0;
+        lj = t.is_leaf[j] != 0;
+        // batched systems: no pairs across systems; nodes spanning several
+        // systems are always refined
+        if (t.sysid) {
+            const int si = t.sysid[i], sj = t.sysid[j];
+            if (si >= 0 && sj >= 0 && si != sj) skip = true;
+            mixed = si < 0 || sj < 0;
         }
-        for (int o = 0; o < nc; ++o) out[base + o] = descend_i ? make_int2(c[o], j) : make_int2(i, c[o]);
+        accept = !skip && !mixed && __dmul_rn(r, theta_loose) > __dadd_rn(ri, rj);
+        if (accept && rdamp > 0.0) {
+            const double gap = __dsub_rn(r, __dmul_rn(1.7320508075688772, __dadd_rn(t.r[i], t.r[j])));
+            accept = gap >= rdamp;
+        }
     }
+    // the network runs once per warp on the pairs that passed the loose test
+    const unsigned need = __ballot_sync(0xffffffffu, accept);
+    int order = 0;
+    if (need) {
+        const int slot = __popc(need & ((1u << lane) - 1u));
+        if (accept) {
+            float x[kMlpIn];
+            selector_features(t, lnorm, dmin, P, i, j, x);
+            mlp_input(S, x, X + slot * kMlpInP);
+        }
+        __syncwarp();
+        warp_mlp(S, X, Ha, Hb, Y, __popc(need), lane);
+        if (accept) {
+            for (int o = kQmin; o <= qmax; ++o)
+                if (Y[slot * kMlpOutP + (o - kQmin)] <= log_budget) {
+                    order = o;
+                    break;
+                }
+            accept = order > 0;
+        }
+    }
+    emit_pair(skip, accept, order, i, j, li, lj, mixed, ri, rj, t, out, cap_out, far, cap_far, nearp, cap_near,
+              counters, lane);
 }
 
 __global__ void k_split_pairs(int64_t m, const uint64_t* __restrict__ sorted, int32_t* __restrict__ src,
@@ -734,7 +776,7 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
             FMM_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
             count_launches(1);
             if (tp.sel_params) {
-                const size_t smem = sizeof(float) * (kMlpSmem + (size_t)kMlpH * 128);
+                const size_t smem = sizeof(float) * 4 * (size_t)kWarpMlpFloats;
                 FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_list_iter_learned,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
                 k_list_iter_learned<<<grid_for(nin, 128), 128, smem, st>>>(

@@ -127,6 +127,19 @@ def test_fmm_exact_mode_matches_oracle(damp):
     assert rel_err(G, O) <= TOL
 
 
+@pytest.mark.parametrize("p", [2, 9, 11, 12])
+def test_fmm_exact_mode_all_orders(p):
+    """Grouped reduced-basis M2L at low and high orders (FP64 products up to
+    p = 11, the per-pair FP64 kernel at p = 12; FP32 products at all orders)."""
+    from fmm_gb300 import systems
+    s = systems.water(1200, 45.0, seed=16)
+    O = oracle.field_fmm(*_fmm_args(s), 0.5, 32, p, 1, coef_mode="exact", excl_mode="mask", centroid_mode="blocked")
+    G = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, p, 1, options=Options.exact())
+    assert rel_err(G, O) <= TOL
+    Gm = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, p, 1, options=Options.exact(precision="mixed"))
+    assert rel_err(Gm, O, slice(1, None)) < 5e-6
+
+
 def test_theta_to_zero_is_direct():
     s = small_system(700, 20.0, seed=7)
     G = fmm_gb300.field_fmm(*_fmm_args(s), 1e-3, 16, 4, 1)
