@@ -397,7 +397,8 @@ def main():
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
         "tree": {k: stats[k] for k in ("num_nodes", "num_leaves", "max_depth", "m2l_pairs", "m2l_groups",
-                                       "m2l_order_mean", "p2p_leaf_pairs", "p2p_particle_pairs")},
+                                       "m2l_order_mean", "p2p_leaf_pairs", "p2p_particle_pairs", "list_candidates",
+                                       "list_evals")},
     }
     print(json.dumps(line), flush=True)
     if dist:

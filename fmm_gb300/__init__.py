@@ -226,7 +226,7 @@ def field_fmm_device(coordinates, multipoles, exclusions, theta, ncrit, expansio
 STAT_NAMES = ["num_nodes", "num_leaves", "max_depth", "m2l_pairs", "p2p_leaf_pairs", "p2p_particle_pairs", "t_tree",
               "t_p2m_m2m", "t_lists", "t_p2p", "t_m2l", "t_l2l_l2p", "t_total", "selector_fallback",
               "sampled_rms_err", "m2l_order_mean"] + ["m2l_pairs_q%d" % q for q in range(13)] + \
-             ["t_p2p_kernel", "t_m2l_product", "m2l_groups"]
+             ["t_p2p_kernel", "t_m2l_product", "m2l_groups", "list_candidates", "list_evals"]
 
 
 def last_stats():

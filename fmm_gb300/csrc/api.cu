@@ -63,7 +63,7 @@ Workspace& thread_workspace() {
 
 namespace {
 
-constexpr int kNumStats = 16 + kMaxP + 1 + 3;
+constexpr int kNumStats = 16 + kMaxP + 1 + 5;
 struct Stats {
     double v[kNumStats] = {0};
 };
@@ -387,6 +387,8 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     if (ws.product_timed) cudaEventElapsedTime(&ms, ws.ev[8], ws.ev[9]);
     s.v[16 + kMaxP + 2] = ms;
     s.v[16 + kMaxP + 3] = (double)ws.m2l_groups;
+    s.v[16 + kMaxP + 4] = (double)ws.list_candidates;
+    s.v[16 + kMaxP + 5] = (double)ws.list_evals;
     g_stats = s;
     return FMM_OK;
 }

@@ -127,6 +127,8 @@ struct Workspace {
     bool events_ready = false;
     bool product_timed = false;  // ev[8], ev[9] bracket the grouped M2L product kernel of the last call
     int64_t m2l_groups = 0;      // displacement groups of the last grouped M2L
+    int64_t list_candidates = 0; // cell pairs examined by the last list build
+    int64_t list_evals = 0;      // of which evaluated by the selector network
     int device = -1;
     int64_t node_cap = 0;
     ~Workspace();

@@ -71,8 +71,10 @@ __global__ void k_m2l_keys(int64_t nfar, const TreeDev t, const int32_t* __restr
     if (q >= nfar) return;
     const int i = tgt[q], j = t.far_src[q];
     const int ord = t.far_ord ? min((int)t.far_ord[q], p) : p;
-    const double hf = fmin(t.r[i], t.r[j]);
-    const double dx = (t.cx[i] - t.cx[j]) / hf, dy = (t.cy[i] - t.cy[j]) / hf, dz = (t.cz[i] - t.cz[j]) / hf;
+    // half-widths are the root's divided by powers of two: 1/h times an
+    // integer multiple of h stays within rounding of that integer
+    const double ihf = 1.0 / fmin(t.r[i], t.r[j]);
+    const double dx = (t.cx[i] - t.cx[j]) * ihf, dy = (t.cy[i] - t.cy[j]) * ihf, dz = (t.cz[i] - t.cz[j]) * ihf;
     const double rx = rint(dx), ry = rint(dy), rz = rint(dz);
     const int dl = t.depth[i] - t.depth[j];
     const double lim = (double)(kDOff - 1);
@@ -372,8 +374,30 @@ __global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restric
     }
 }
 
-// Block per target, thread per reduced component: FP64 sum of the target's
-// pair rows (contiguous in target order, eight loads in flight per thread),
+// Running sum of one output: FP32 values as a double-float pair (TwoSum, on
+// the FP32 pipe), FP64 values in FP64.
+template <typename R>
+struct Sum;
+template <>
+struct Sum<float> {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float v) {
+        const float s = hi + v;
+        const float bb = s - hi;
+        lo += (hi - (s - bb)) + (v - bb);
+        hi = s;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+template <>
+struct Sum<double> {
+    double v = 0.0;
+    __device__ __forceinline__ void add(double x) { v += x; }
+    __device__ __forceinline__ double value() const { return v; }
+};
+
+// Block per target, thread per reduced component: compensated sum of the
+// target's pair rows (contiguous in target order, eight loads in flight),
 // back to physical units, into the reduced components of the local expansion.
 template <typename R>
 __global__ void __launch_bounds__(128) k_m2l_sum(const TreeDev t, int p, const R* __restrict__ out,
@@ -385,21 +409,21 @@ __global__ void __launch_bounds__(128) k_m2l_sum(const TreeDev t, int p, const R
     double* L = loc + (size_t)i * nT(p);
     for (int f = threadIdx.x; f < nr; f += blockDim.x) {
         constexpr int U = 8;
-        double acc = 0.0;
+        Sum<R> acc;
         int q = q0;
         for (; q + U <= q1; q += U) {
             R v[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) v[u] = out[(size_t)(q + u) * nr + f];
 #pragma unroll
-            for (int u = 0; u < U; ++u) acc += (double)v[u];
+            for (int u = 0; u < U; ++u) acc.add(v[u]);
         }
-        for (; q < q1; ++q) acc += (double)out[(size_t)q * nr + f];
+        for (; q < q1; ++q) acc.add(out[(size_t)q * nr + f]);
         const int c = qcomp(f);
         const int k = c >> 24;
         double s = ih;
         for (int e = 0; e < k; ++e) s *= ih;
-        L[pidx(c & 0xff, (c >> 8) & 0xff, (c >> 16) & 0xff)] = acc * s;
+        L[pidx(c & 0xff, (c >> 8) & 0xff, (c >> 16) & 0xff)] = acc.value() * s;
     }
 }
 

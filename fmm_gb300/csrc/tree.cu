@@ -425,10 +425,6 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
     if (!skip) {
         i = in[q].x;
         j = in[q].y;
-        const double dx = __dsub_rn(t.cx[i], __dadd_rn(t.cx[j], 0.0));
-        const double dy = __dsub_rn(t.cy[i], __dadd_rn(t.cy[j], 0.0));
-        const double dz = __dsub_rn(t.cz[i], __dadd_rn(t.cz[j], 0.0));
-        const double r = norm2_3(dx, dy, dz);
         ri = t.rmax[i];
         rj = t.rmax[j];
         li = t.is_leaf[i] != 0;
@@ -440,14 +436,19 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
             if (si >= 0 && sj >= 0 && si != sj) skip = true;
             mixed = si < 0 || sj < 0;
         }
-        accept = !skip && !mixed && __dmul_rn(r, theta_loose) > __dadd_rn(ri, rj);
+        // loose geometric gate in FP32 (the network decides; no parity with
+        // the reference's rule is involved here)
+        const float dx = (float)(t.cx[i] - t.cx[j]), dy = (float)(t.cy[i] - t.cy[j]), dz = (float)(t.cz[i] - t.cz[j]);
+        const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+        accept = !skip && !mixed && r * (float)theta_loose > (float)(ri + rj);
         if (accept && rdamp > 0.0) {
-            const double gap = __dsub_rn(r, __dmul_rn(1.7320508075688772, __dadd_rn(t.r[i], t.r[j])));
-            accept = gap >= rdamp;
+            const float gap = r - 1.7320508f * (float)(t.r[i] + t.r[j]);
+            accept = gap >= (float)rdamp;
         }
     }
     // the network runs once per warp on the pairs that passed the loose test
     const unsigned need = __ballot_sync(0xffffffffu, accept);
+    if (need && lane == 0) atomicAdd(&counters[4], (unsigned long long)__popc(need));
     int order = 0;
     if (need) {
         const int slot = __popc(need & ((1u << lane) - 1u));
@@ -766,13 +767,15 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
         FMM_TRY(ws.near_pairs.ensure(sizeof(uint64_t) * cap_near));
         const int2 root = make_int2(0, 0);
         FMM_CUDA_TRY(cudaMemcpyAsync(ws.front_a.p, &root, sizeof(int2), cudaMemcpyHostToDevice, st));
-        unsigned long long h[4] = {0, 0, 0, 0};
+        unsigned long long h[5] = {0, 0, 0, 0, 0};  // frontier, far, near, overflow flag, network evaluations
         FMM_CUDA_TRY(cudaMemcpyAsync(ctr, h, sizeof(h), cudaMemcpyHostToDevice, st));
         int64_t nin = 1;
+        int64_t candidates = 0;
         int2* fin = ws.front_a.as<int2>();
         int2* fout = ws.front_b.as<int2>();
         bool overflow = false;
         while (nin > 0) {
+            candidates += nin;
             FMM_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
             count_launches(1);
             if (tp.sel_params) {
@@ -806,6 +809,8 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
         }
         t.nfar = (int64_t)h[1];
         t.nnear = (int64_t)h[2];
+        ws.list_candidates = candidates;
+        ws.list_evals = (int64_t)h[4];
         // sort both lists by (target, source) and build CSR offsets
         FMM_TRY(ws.far_sorted.ensure(sizeof(uint64_t) * std::max<int64_t>(1, t.nfar)));
         FMM_TRY(ws.near_sorted.ensure(sizeof(uint64_t) * std::max<int64_t>(1, t.nnear)));

@@ -158,7 +158,9 @@ int fmm_field_direct_targets_noalloc(int64_t n, const double *d_coordinates, int
  * number of far pairs at each expansion order 0..12, the device time of the
  * near-field kernel alone and of the grouped M2L product kernel alone (-1 if
  * that kernel did not run), the number of displacement groups of the grouped
- * M2L.  Returns the number written (at most 32). */
+ * M2L, the cell pairs examined by the list build and how many of them the
+ * learned selector's network evaluated.  Returns the number written (at most
+ * 34). */
 int fmm_last_stats(double *out, int len);
 
 /* Diagnostics (no counterpart in the reference): builds the octree and
