@@ -353,6 +353,16 @@ def main():
     kernels = {k: {"ms": round(v[1], 3), "algorithmic_flops": v[0], "achieved_tflops": v[0] / (v[1] * 1e-3) / 1e12,
                    "frac": v[0] / (v[1] * 1e-3) / 1e12 / peak.value, "convention": v[2]} for k, v in kern.items()
                if v[1] > 0}
+    # DRAM bytes per unit from one ncu capture of each kernel on the 100k case
+    # (profiles/), scaled to this launch by its units (pairs): the kernels are
+    # compute-bound and their traffic grows in proportion to the pairs
+    per_unit = {"k_p2p_f32": (12.84e6 / 415.6e6, p2p_pairs, "profiles/k_p2p_f32_water100k.md"),
+                "k_m2l_gemm<float>": ((62.88e6 + 947.37e6) / 2.027e6, stats["m2l_pairs"],
+                                      "profiles/k_m2l_gemm_f32_water100k.md")}
+    for k, (b, units, src) in per_unit.items():
+        if k in kernels:
+            kernels[k]["traffic_bytes"] = b * units
+            kernels[k]["traffic_source"] = src + " (DRAM read+write per unit x units of this launch)"
     dom = max(kernels, key=lambda k: kernels[k]["ms"])
     roofline = {"bound": "fp64" if prec == 0 else "fp32", "kernel": dom,
                 "achieved": kernels[dom]["achieved_tflops"], "peak": peak.value, "unit": "TFLOP/s",
@@ -361,7 +371,7 @@ def main():
                                "MEASURED_PEAKS.json has only HBM copy and bf16 tensor figures, and neither bounds "
                                "these CUDA-core kernels",
                 "algorithmic_flops_per_launch": kernels[dom]["algorithmic_flops"],
-                "traffic": None, "kernels": kernels, "phase_ms": {k: round(v, 3) for k, v in phase.items()}}
+                "traffic": kernels[dom].get("traffic_bytes"), "kernels": kernels, "phase_ms": {k: round(v, 3) for k, v in phase.items()}}
 
     compare = None
     if args.arm != "fp64" and not args.no_compare:

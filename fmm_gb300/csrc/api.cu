@@ -278,14 +278,18 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         cudaEventRecord(ws.ev[10], st);  // inputs in place
         FMM_CUDA_TRY(cudaStreamWaitEvent(ws.aux, ws.ev[10], 0));
         FMM_CUDA_TRY(cudaMemcpyAsync(d_rows, rows.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, ws.aux));
+        // few source splits: the FP64 sum runs beside the FP32-bound phases
+        // on the otherwise idle FP64 pipes and is only awaited by the check
         Modes mdir{1, 1, 0};
-        FMM_TRY(launch_direct_f64(ws, P, f, mdir, d_ref, ws.aux, nt, d_rows));
+        FMM_TRY(launch_direct_f64(ws, P, f, mdir, d_ref, ws.aux, nt, d_rows, 16));
         cudaEventRecord(ws.ev[11], ws.aux);
     }
     FMM_TRY(build_tree(ws, P.x, P.n, tp, t, st));
     cudaEventRecord(ws.ev[1], st);
     FMM_TRY(gather_sorted(ws, P, t, st));
-    FMM_TRY(launch_p2m_m2m(ws, P, t, p, st));
+    const bool f32_near = md.precision == 1 || md.precision == 2;
+    if (f32_near || learned) FMM_TRY(prepare_f32_records(ws, P, t, st));
+    FMM_TRY(launch_p2m_m2m(ws, P, t, p, st, md.precision != 0));
     if (learned) {
         FMM_TRY(launch_reduce_moments(ws, t, p, st));
         FMM_TRY(selector_node_norms(ws, t, p, P.damp ? ws.sd.as<double>() : nullptr, st));
@@ -293,15 +297,18 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         tpl.sel_lnorm = ws.sel_norms.as<float>();
         tpl.sel_dmin = ws.sel_norms.as<float>() + (size_t)t.num_nodes * (p + 1);
         tpl.sel_P = p;
-        // per-pair error budget from the sampled field scale
-        FMM_CUDA_TRY(cudaEventSynchronize(ws.ev[11]));
-        ref_rows.resize((size_t)nt * nf);
-        FMM_CUDA_TRY(cudaMemcpy(ref_rows.data(), ws.sel_scratch.as<double>(), sizeof(double) * nt * nf,
-                                cudaMemcpyDeviceToHost));
+        // per-pair error budget from the sampled field scale (FP32 estimate)
+        double* d_est = ws.sel_scratch.as<double>() + (size_t)nt * nf;
+        const int64_t* d_rows = reinterpret_cast<const int64_t*>(ws.sel_scratch.as<double>() + (size_t)nt * nf * 2);
+        FMM_CUDA_TRY(cudaStreamWaitEvent(st, ws.ev[10], 0));
+        FMM_TRY(launch_direct_scale_f32(ws, P, t, f, d_est, st, nt, d_rows));
+        std::vector<double> est((size_t)nt * nf);
+        FMM_CUDA_TRY(cudaMemcpyAsync(est.data(), d_est, sizeof(double) * nt * nf, cudaMemcpyDeviceToHost, st));
+        FMM_CUDA_TRY(cudaStreamSynchronize(st));
         std::vector<double> mag(nt);
         for (int k = 0; k < nt; ++k) {
             double g = 0.0;
-            for (int c = 1; c < 4; ++c) g += ref_rows[(size_t)c * nt + k] * ref_rows[(size_t)c * nt + k];
+            for (int c = 1; c < 4; ++c) g += est[(size_t)c * nt + k] * est[(size_t)c * nt + k];
             mag[k] = std::sqrt(g);
         }
         std::sort(mag.begin(), mag.end());
@@ -318,7 +325,7 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     for (int attempt = 0; attempt < 2; ++attempt) {
         FMM_TRY(build_lists(ws, t, tpl, st));
         cudaEventRecord(ws.ev[3], st);
-        if (md.precision == 1 || md.precision == 2)
+        if (f32_near)
             FMM_TRY(launch_p2p_f32(ws, P, t, f, st));
         else
             FMM_TRY(launch_p2p_f64(ws, P, t, f, md, st));
@@ -340,6 +347,13 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         std::vector<double> got((size_t)nt * nf);
         FMM_CUDA_TRY(cudaMemcpyAsync(got.data(), d_got, sizeof(double) * nt * nf, cudaMemcpyDeviceToHost, st));
         FMM_CUDA_TRY(cudaStreamSynchronize(st));
+        if (ref_rows.empty()) {
+            // the FP64 reference sums (second stream)
+            FMM_CUDA_TRY(cudaEventSynchronize(ws.ev[11]));
+            ref_rows.resize((size_t)nt * nf);
+            FMM_CUDA_TRY(cudaMemcpy(ref_rows.data(), ws.sel_scratch.as<double>(), sizeof(double) * nt * nf,
+                                    cudaMemcpyDeviceToHost));
+        }
         check_rms = sampled_rms(got, ref_rows, nt, nf);
         if (check_rms <= o.target) break;
         fallback = true;

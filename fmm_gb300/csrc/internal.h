@@ -157,14 +157,24 @@ struct Modes {
     int precision;
 };
 
+// split_cap > 0 bounds the source splits per target (fewer, longer blocks:
+// used when the sum runs beside other work on a second stream).
 int launch_direct_f64(Workspace& ws, const Particles& P, int field_order, const Modes& md, double* d_field,
-                      cudaStream_t st, int64_t ntgt = 0, const int64_t* d_targets = nullptr);
+                      cudaStream_t st, int64_t ntgt = 0, const int64_t* d_targets = nullptr, int split_cap = 0);
+// FP32 particle records and node centres of the mixed-precision near field
+// (near_f32.cu; after gather_sorted).
+int prepare_f32_records(Workspace& ws, const Particles& P, const TreeDev& t, cudaStream_t st);
+// FP32 field estimate at a few targets (exclusions masked) from those
+// records, into d_out (ntgt x nT(field_order), FP64, column-major).
+int launch_direct_scale_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, double* d_out,
+                            cudaStream_t st, int64_t ntgt, const int64_t* d_targets);
 
 // FMM phases (near.cu / expansions.cu)
 int gather_sorted(Workspace& ws, const Particles& P, const TreeDev& t, cudaStream_t st);
 int launch_p2p_f64(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, const Modes& md,
                    cudaStream_t st);
-int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, cudaStream_t st);
+// df: P2M sums in double-float (FP32 pipe) instead of FP64 (mixed path)
+int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, cudaStream_t st, bool df = false);
 int launch_m2l(Workspace& ws, const TreeDev& t, int p, const Modes& md, cudaStream_t st);
 int launch_m2l_reduced(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaStream_t st);
 int launch_m2l_grouped(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaStream_t st);

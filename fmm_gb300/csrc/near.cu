@@ -289,7 +289,7 @@ __global__ void k_scatter(int64_t n, int nf, const uint32_t* __restrict__ perm, 
 bool near_orders_supported(int m, int f) { return m >= 0 && m <= 2 && f >= 0 && f <= 2; }
 
 int launch_direct_f64(Workspace& ws, const Particles& P, int field_order, const Modes& md, double* d_field,
-                      cudaStream_t st, int64_t ntgt, const int64_t* d_targets) {
+                      cudaStream_t st, int64_t ntgt, const int64_t* d_targets, int split_cap) {
     const int m = dim_to_order(P.dim);
     if (!near_orders_supported(m, field_order)) return FMM_ENOTSUP;
     const int64_t n = P.n;
@@ -305,6 +305,7 @@ int launch_direct_f64(Workspace& ws, const Particles& P, int field_order, const 
     int64_t ks = std::max<int64_t>(1, ((few ? 16LL : 8LL) * num_sms() + tblocks - 1) / tblocks);
     ks = std::min<int64_t>(ks, std::max<int64_t>(1, n / (few ? 1024 : 256)));
     ks = std::min<int64_t>(ks, 65535);
+    if (split_cap > 0) ks = std::min<int64_t>(ks, split_cap);
     const int64_t chunk = (n + ks - 1) / ks;
     FMM_TRY(ws.partial.ensure(sizeof(double) * (size_t)ks * nf * ntgt));
     dim3 grid((unsigned)tblocks, (unsigned)ks);

@@ -76,6 +76,62 @@ __device__ __forceinline__ float two_diff(float a, float b, float& e) {
     return s;
 }
 
+// FP32 field estimate at a few targets over all sources (exclusions masked),
+// from the sorted FP32 records; only a magnitude is wanted (the learned
+// selector's error budget).  Block per (target, source split); block sums
+// added into out (ntgt x nF, column-major, zeroed by the caller).
+template <int M, int F>
+__global__ void __launch_bounds__(128) k_direct_scale(const TreeDev t, const float4* __restrict__ rec,
+                                                      const float4* __restrict__ chi,
+                                                      const int64_t* __restrict__ targets, int64_t ntgt, int64_t n,
+                                                      int damp, int exw, const int32_t* __restrict__ excl,
+                                                      int64_t chunk, double* __restrict__ out) {
+    constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
+    __shared__ float red[NF][4];
+    const int64_t ti = blockIdx.x;
+    const int64_t i = targets[ti];
+    const int it = t.pos_of[i];
+    const float4 ta = rec[(size_t)it * NV], ca = chi[t.leaf_of[it]];
+    const float tx = ta.x + ca.x, ty = ta.y + ca.y, tz = ta.z + ca.z;
+    float acc[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) acc[f] = 0.0f;
+    const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+    for (int64_t k = j0 + threadIdx.x; k < j1; k += blockDim.x) {
+        if (k == it) continue;
+        const float4* r = rec + (size_t)k * NV;
+        const float4 sa = r[0], sb = r[1];
+        const int o = __float_as_int(sb.w);
+        bool ex = false;
+        for (int e = 0; e < exw; ++e) ex |= (excl[(size_t)e * n + i] == o);
+        if (ex) continue;
+        const float4 cb = chi[t.leaf_of[k]];
+        float mc[4 * (NV - 2)];
+#pragma unroll
+        for (int v = 0; v < NV - 2; ++v) {
+            const float4 w = r[2 + v];
+            mc[4 * v] = w.x;
+            mc[4 * v + 1] = w.y;
+            mc[4 * v + 2] = w.z;
+            mc[4 * v + 3] = w.w;
+        }
+        pair_field<M, F, float>(tx - (sa.x + cb.x), ty - (sa.y + cb.y), tz - (sa.z + cb.z), ta.w * sa.w, damp, mc,
+                                acc);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        float v = acc[f];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[f][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NF) {
+        const int f = threadIdx.x;
+        atomicAdd(&out[(size_t)f * ntgt + ti], (double)((red[f][0] + red[f][1]) + (red[f][2] + red[f][3])));
+    }
+}
+
 // Sum over the sources [js, je) of one leaf (lane group grp of ngr) for the
 // lane's target: compensated FP32 (TwoSum hi + lo), since the per-atom terms
 // are much larger than their neutral total.  CHECK: the leaf may hold the
@@ -212,21 +268,46 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
 
 }  // namespace
 
+int prepare_f32_records(Workspace& ws, const Particles& P, const TreeDev& t, cudaStream_t st) {
+    const int64_t n = P.n;
+    const int nv = rec_vec(P.dim);
+    FMM_TRY(ws.f32buf.ensure(sizeof(float4) * (size_t)n * nv));
+    count_launches(1);
+    k_gather_f32<<<grid_for(n, 256), 256, 0, st>>>(n, P.dim, t, ws.sx.as<double>(), ws.sy.as<double>(),
+                                                    ws.sz.as<double>(), ws.sd.as<double>(), ws.smc.as<double>(),
+                                                    ws.f32buf.as<float4>());
+    FMM_TRY(ws.f32node.ensure(sizeof(float4) * 2 * (size_t)t.num_nodes));
+    float4* chi = ws.f32node.as<float4>();
+    count_launches(1);
+    k_node_centres_f32<<<grid_for(t.num_nodes, 256), 256, 0, st>>>(t.num_nodes, t, chi, chi + t.num_nodes);
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
+int launch_direct_scale_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, double* d_out,
+                            cudaStream_t st, int64_t ntgt, const int64_t* d_targets) {
+    const int m = dim_to_order(P.dim);
+    const int nf = nT(field_order);
+    FMM_CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(double) * (size_t)nf * ntgt, st));
+    int64_t ks = std::max<int64_t>(1, (16LL * 152 + ntgt - 1) / ntgt);
+    ks = std::min<int64_t>(ks, std::max<int64_t>(1, P.n / 1024));
+    const int64_t chunk = (P.n + ks - 1) / ks;
+    const float4* chi = ws.f32node.as<float4>();
+    dim3 grid((unsigned)ntgt, (unsigned)ks);
+    FMM_MF_SWITCH(m, field_order,
+                  (k_direct_scale<MM, FF><<<grid, 128, 0, st>>>(t, ws.f32buf.as<float4>(), chi, d_targets, ntgt, P.n,
+                                                                 P.damp_type, P.exw, P.excl, chunk, d_out)));
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
 int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, cudaStream_t st) {
     const int m = dim_to_order(P.dim);
     const int64_t n = P.n;
     const int nf = nT(field_order);
-    const int nv = rec_vec(P.dim);
-    FMM_TRY(ws.f32buf.ensure(sizeof(float4) * (size_t)n * nv));
-    float4* rec = ws.f32buf.as<float4>();
-    count_launches(1);
-    k_gather_f32<<<grid_for(n, 256), 256, 0, st>>>(n, P.dim, t, ws.sx.as<double>(), ws.sy.as<double>(),
-                                                    ws.sz.as<double>(), ws.sd.as<double>(), ws.smc.as<double>(), rec);
-    FMM_TRY(ws.f32node.ensure(sizeof(float4) * 2 * (size_t)t.num_nodes));
-    float4* chi = ws.f32node.as<float4>();
-    float4* clo = chi + t.num_nodes;
-    count_launches(1);
-    k_node_centres_f32<<<grid_for(t.num_nodes, 256), 256, 0, st>>>(t.num_nodes, t, chi, clo);
+    const float4* rec = ws.f32buf.as<float4>();  // prepare_f32_records
+    const float4* chi = ws.f32node.as<float4>();
+    const float4* clo = chi + t.num_nodes;
     FMM_TRY(ws.fsorted.ensure(sizeof(double) * (size_t)n * nf));
     const unsigned blocks = grid_for((int64_t)t.num_leaves * 32, 128);
     FMM_MF_SWITCH(m, field_order,

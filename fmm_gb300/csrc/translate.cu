@@ -122,10 +122,26 @@ __device__ __forceinline__ void copy_ints(int* dst, const int* __restrict__ src,
     for (int e = threadIdx.x; e < n; e += blockDim.x) dst[e] = src[e];
 }
 
+// 1/a and 1/a! for a = 0..2 kMaxP (no divisions on the FP64 pipe)
+__constant__ double cInvInt[2 * kMaxP + 2] = {
+#define FMM_X(a) ((a) == 0 ? 0.0 : 1.0 / (a)),
+    FMM_X(0) FMM_X(1) FMM_X(2) FMM_X(3) FMM_X(4) FMM_X(5) FMM_X(6) FMM_X(7) FMM_X(8) FMM_X(9) FMM_X(10) FMM_X(11)
+    FMM_X(12) FMM_X(13) FMM_X(14) FMM_X(15) FMM_X(16) FMM_X(17) FMM_X(18) FMM_X(19) FMM_X(20) FMM_X(21) FMM_X(22)
+    FMM_X(23) FMM_X(24) FMM_X(25)
+#undef FMM_X
+};
+__constant__ double cInvFact[kMaxP + 1] = {
+#define FMM_F(a) (1.0 / cfact(a)),
+    FMM_F(0) FMM_F(1) FMM_F(2) FMM_F(3) FMM_F(4) FMM_F(5) FMM_F(6) FMM_F(7) FMM_F(8) FMM_F(9) FMM_F(10) FMM_F(11)
+    FMM_F(12)
+#undef FMM_F
+};
+static_assert(kMaxP == 12, "inverse tables cover orders up to 12");
+
 // e[a] = d^a / a!, a = 0..p
 __device__ __forceinline__ void scaled_powers(double d, int p, double* e) {
     e[0] = 1.0;
-    for (int a = 1; a <= p; ++a) e[a] = e[a - 1] * d / (double)a;
+    for (int a = 1; a <= p; ++a) e[a] = e[a - 1] * d * cInvInt[a];
 }
 
 // ---------------------------------------------------------------- P2M
@@ -133,6 +149,10 @@ constexpr int kP2mThreads = 128;
 constexpr int kP2mBatch = 8;
 constexpr int kMaxOut = (nT(kMaxP) + kP2mThreads - 1) / kP2mThreads;
 
+// DF: accumulate in double-float pairs (FP32 arithmetic, exact products by
+// FMA, ~48-bit sums) instead of FP64; used by the mixed-precision path, where
+// the FP64 pipe is the bottleneck of this kernel.
+template <bool DF>
 __global__ void __launch_bounds__(kP2mThreads) k_p2m(const TreeDev t, const double* __restrict__ sx,
                                                      const double* __restrict__ sy, const double* __restrict__ sz,
                                                      const double* __restrict__ smc, int64_t n, int m, int p,
@@ -140,12 +160,14 @@ __global__ void __launch_bounds__(kP2mThreads) k_p2m(const TreeDev t, const doub
                                                      double* __restrict__ mom) {
     extern __shared__ __align__(16) double sm_p2m[];
     const int nq = v.nq, nm = nT(m), P1 = p + 1;
-    double* dp = sm_p2m;                        // [kP2mBatch][nq]
+    double* dp = sm_p2m;                        // [kP2mBatch][nq]  (DF: float2 hi/lo)
     double* e = dp + kP2mBatch * nq;            // [kP2mBatch][3][p+1]
-    double* ms = e + kP2mBatch * 3 * P1;        // [kP2mBatch][nm]
+    double* ms = e + kP2mBatch * 3 * P1;        // [kP2mBatch][nm]  (DF: float2 hi/lo)
     int* comp = reinterpret_cast<int*>(ms + kP2mBatch * nm);
     int* off = comp + nq;
     int* terms = off + nq + 1;
+    float2* dp2 = reinterpret_cast<float2*>(dp);
+    float2* ms2 = reinterpret_cast<float2*>(ms);
     copy_ints(comp, tab + v.comp, nq);
     copy_ints(off, tab + v.p2m_off, nq + 1);
     copy_ints(terms, tab + v.p2m, v.n_p2m);
@@ -153,8 +175,12 @@ __global__ void __launch_bounds__(kP2mThreads) k_p2m(const TreeDev t, const doub
     const double cx = t.cx[leaf], cy = t.cy[leaf], cz = t.cz[leaf];
     const int s0 = t.start[leaf], cnt = t.count[leaf];
     double acc[kMaxOut];
+    float ah[kMaxOut], al[kMaxOut];
 #pragma unroll
-    for (int r = 0; r < kMaxOut; ++r) acc[r] = 0.0;
+    for (int r = 0; r < kMaxOut; ++r) {
+        acc[r] = 0.0;
+        ah[r] = al[r] = 0.0f;
+    }
     __syncthreads();
     for (int b0 = 0; b0 < cnt; b0 += kP2mBatch) {
         const int nb = min(kP2mBatch, cnt - b0);
@@ -166,26 +192,58 @@ __global__ void __launch_bounds__(kP2mThreads) k_p2m(const TreeDev t, const doub
         for (int idx = threadIdx.x; idx < nb * nm; idx += blockDim.x) {
             const int b = idx / nm, s = idx % nm;
             const double c = smc[(size_t)s * n + s0 + b0 + b];
-            ms[b * nm + s] = ((order_of(s) + 1) % 2) ? -c : c;  // back to M_s / s!
+            const double w = ((order_of(s) + 1) % 2) ? -c : c;  // back to M_s / s!
+            if (DF) {
+                const float hi = (float)w;
+                ms2[b * nm + s] = make_float2(hi, (float)(w - (double)hi));
+            } else {
+                ms[b * nm + s] = w;
+            }
         }
         __syncthreads();
         for (int idx = threadIdx.x; idx < nb * nq; idx += blockDim.x) {
             const int b = idx / nq, u = idx % nq;
             const int c = comp[u];
             const double* eb = e + b * 3 * P1;
-            dp[b * nq + u] = eb[ux_(c)] * eb[P1 + uy_(c)] * eb[2 * P1 + uz_(c)];
+            const double w = eb[ux_(c)] * eb[P1 + uy_(c)] * eb[2 * P1 + uz_(c)];
+            if (DF) {
+                const float hi = (float)w;
+                dp2[b * nq + u] = make_float2(hi, (float)(w - (double)hi));
+            } else {
+                dp[b * nq + u] = w;
+            }
         }
         __syncthreads();
 #pragma unroll
         for (int r = 0; r < kMaxOut; ++r) {
             const int tq = threadIdx.x + kP2mThreads * r;
             if (tq < nq) {
-                double a = acc[r];
-                for (int j = off[tq]; j < off[tq + 1]; ++j) {
-                    const int s = terms[j] & 0xffff, u = terms[j] >> 16;
-                    for (int b = 0; b < nb; ++b) a = fma(dp[b * nq + u], ms[b * nm + s], a);
+                if (DF) {
+                    float h = ah[r], l = al[r];
+                    for (int j = off[tq]; j < off[tq + 1]; ++j) {
+                        const int s = terms[j] & 0xffff, u = terms[j] >> 16;
+                        for (int b = 0; b < nb; ++b) {
+                            const float2 d = dp2[b * nq + u], w = ms2[b * nm + s];
+                            const float pr = d.x * w.x;
+                            float er = fmaf(d.x, w.x, -pr);
+                            er = fmaf(d.x, w.y, er);
+                            er = fmaf(d.y, w.x, er);
+                            const float sum = h + pr;
+                            const float bb = sum - h;
+                            l += ((h - (sum - bb)) + (pr - bb)) + er;
+                            h = sum;
+                        }
+                    }
+                    ah[r] = h;
+                    al[r] = l;
+                } else {
+                    double a = acc[r];
+                    for (int j = off[tq]; j < off[tq + 1]; ++j) {
+                        const int s = terms[j] & 0xffff, u = terms[j] >> 16;
+                        for (int b = 0; b < nb; ++b) a = fma(dp[b * nq + u], ms[b * nm + s], a);
+                    }
+                    acc[r] = a;
                 }
-                acc[r] = a;
             }
         }
         __syncthreads();
@@ -193,7 +251,7 @@ __global__ void __launch_bounds__(kP2mThreads) k_p2m(const TreeDev t, const doub
 #pragma unroll
     for (int r = 0; r < kMaxOut; ++r) {
         const int tq = threadIdx.x + kP2mThreads * r;
-        if (tq < nq) mom[(size_t)leaf * nq + tq] = acc[r];
+        if (tq < nq) mom[(size_t)leaf * nq + tq] = DF ? (double)ah[r] + (double)al[r] : acc[r];
     }
 }
 
@@ -309,11 +367,20 @@ __global__ void __launch_bounds__(64) k_l2p(const TreeDev t, const double* __res
                                             const double* __restrict__ sy, const double* __restrict__ sz, int64_t n,
                                             int p, int f, const double* __restrict__ loc, double* __restrict__ fs) {
     extern __shared__ __align__(16) unsigned char sm_l2p_raw[];
+    __shared__ double hp[kMaxP + 1];  // h^k
     R* coef = reinterpret_cast<R*>(sm_l2p_raw);
     const int nq = nT(p), nf = nT(f);
     const int leaf = t.leaves[blockIdx.x];
     const double h = t.r[leaf], ih = 1.0 / h;
     const double* L = loc + (size_t)leaf * nq;
+    if (threadIdx.x == 0) {
+        double v = 1.0;
+        for (int k = 0; k <= p; ++k) {
+            hp[k] = v;
+            v *= h;
+        }
+    }
+    __syncthreads();
     // outputs tq of order k_t use nT(p - k_t) coefficients each, stored one
     // after the other
     int base = 0;
@@ -337,9 +404,7 @@ __global__ void __launch_bounds__(64) k_l2p(const TreeDev t, const double* __res
             }
             uz = rem - ux - uy - idx;
             const int w = pidx(tx + ux, ty + uy, tz + uz);
-            double s = 1.0;
-            for (int a = 0; a < kt + ux + uy + uz; ++a) s *= h;
-            s /= cfact(ux) * cfact(uy) * cfact(uz);
+            const double s = hp[kt + ux + uy + uz] * (cInvFact[ux] * cInvFact[uy] * cInvFact[uz]);
             coef[base + e] = (R)(L[w] * s);
         }
         base += cnt;
@@ -364,7 +429,7 @@ __global__ void __launch_bounds__(64) k_l2p(const TreeDev t, const double* __res
                 hx = hx * dx + hy;
             }
             double s = 1.0;
-            for (int a = 0; a < kt; ++a) s *= ih;
+            for (int a = 0; a < kt; ++a) s *= ih;  // kt <= 2
             fs[(size_t)tq * n + k] += (double)hx * s;
         }
     }
@@ -383,7 +448,7 @@ int set_smem(const void* fn, size_t bytes) {
 
 }  // namespace
 
-int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, cudaStream_t st) {
+int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, cudaStream_t st, bool df) {
     const int nq = nT(p);
     const int m = dim_to_order(P.dim);
     TabView v;
@@ -395,12 +460,18 @@ int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, c
         const int nm = nT(m);
         const size_t sm = sizeof(double) * (kP2mBatch * (size_t)nq + kP2mBatch * 3 * (p + 1) + kP2mBatch * nm) +
                           sizeof(int) * (2 * (size_t)nq + 1 + v.n_p2m);
-        FMM_TRY(set_smem((const void*)k_p2m, sm));
+        FMM_TRY(set_smem((const void*)k_p2m<false>, sm));
+        FMM_TRY(set_smem((const void*)k_p2m<true>, sm));
         if (t.num_leaves > 0) {
             count_launches(1);
-            k_p2m<<<(unsigned)t.num_leaves, kP2mThreads, sm, st>>>(t, ws.sx.as<double>(), ws.sy.as<double>(),
-                                                                   ws.sz.as<double>(), ws.smc.as<double>(), P.n, m, p,
-                                                                   tab, v, mom);
+            if (df)
+                k_p2m<true><<<(unsigned)t.num_leaves, kP2mThreads, sm, st>>>(
+                    t, ws.sx.as<double>(), ws.sy.as<double>(), ws.sz.as<double>(), ws.smc.as<double>(), P.n, m, p,
+                    tab, v, mom);
+            else
+                k_p2m<false><<<(unsigned)t.num_leaves, kP2mThreads, sm, st>>>(
+                    t, ws.sx.as<double>(), ws.sy.as<double>(), ws.sz.as<double>(), ws.smc.as<double>(), P.n, m, p,
+                    tab, v, mom);
         }
     }
     {
