@@ -10,6 +10,8 @@
 //   W4[Q][H], b4[Q]
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "internal.h"
 
 namespace fmm {
@@ -86,105 +88,151 @@ __device__ __forceinline__ void mlp_stage(const float* __restrict__ P, float* S)
     }
 }
 
+// Tensor-core inference (warp-level m16n8k16 MMA, FP16 operands, FP32
+// accumulation): per layer, the weights as B fragments in lane order (uint2
+// per lane and (k-tile, n-tile)), inputs padded to 32, outputs of the last
+// layer padded to 16; biases in FP32.
+constexpr int kTcK1 = 2, kTcKH = kMlpH / 16, kTcN = kMlpH / 8, kTcN4 = 2;  // k-tiles / n-tiles
+constexpr int kTcF1 = 0, kTcF2 = kTcF1 + kTcK1 * kTcN, kTcF3 = kTcF2 + kTcKH * kTcN, kTcF4 = kTcF3 + kTcKH * kTcN;
+constexpr int kTcFrags = kTcF4 + kTcKH * kTcN4;
+constexpr int kTcBias = 3 * kMlpH + 16;
+
 // The device copy of the parameters holds the blob followed (at kMlpInfOff)
-// by the inference layout above, written once by k_mlp_stage_global.
+// by the FP32 inference layout above, the FP32 biases and the FP16 weight
+// fragments; all written once by k_mlp_stage_global.
 constexpr int kMlpInfOff = (kMlpParams + 3) / 4 * 4;
-constexpr int kMlpBufFloats = kMlpInfOff + kMlpSmem;
+constexpr int kTcBiasOff = kMlpInfOff + kMlpSmem;
+constexpr int kTcFragOff = kTcBiasOff + kTcBias;  // uint2 entries from here
+constexpr int kMlpBufFloats = kTcFragOff + 2 * 32 * kTcFrags;
+static_assert(kTcFragOff % 2 == 0, "8-byte fragments");
+
+__device__ __forceinline__ uint32_t pack_half2(float lo, float hi) {
+    const __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
 
 namespace {
-__global__ void k_mlp_stage_global(float* buf) { mlp_stage(buf, buf + kMlpInfOff); }
+__global__ void k_mlp_stage_global(float* buf) {
+    mlp_stage(buf, buf + kMlpInfOff);
+    const float* P = buf;
+    float* bias = buf + kTcBiasOff;
+    for (int e = threadIdx.x; e < kTcBias; e += blockDim.x) {
+        float v = 0.0f;
+        if (e < kMlpH) v = P[kOffB1 + e];
+        else if (e < 2 * kMlpH) v = P[kOffB2 + e - kMlpH];
+        else if (e < 3 * kMlpH) v = P[kOffB3 + e - 2 * kMlpH];
+        else if (e - 3 * kMlpH < kMlpOut) v = P[kOffB4 + e - 3 * kMlpH];
+        bias[e] = v;
+    }
+    uint2* frag = reinterpret_cast<uint2*>(buf + kTcFragOff);
+    for (int e = threadIdx.x; e < 32 * kTcFrags; e += blockDim.x) {
+        const int fi = e >> 5, lane = e & 31, g = lane >> 2, t = lane & 3;
+        int layer, kt, nt;
+        if (fi < kTcF2) { layer = 1; kt = (fi - kTcF1) / kTcN; nt = (fi - kTcF1) % kTcN; }
+        else if (fi < kTcF3) { layer = 2; kt = (fi - kTcF2) / kTcN; nt = (fi - kTcF2) % kTcN; }
+        else if (fi < kTcF4) { layer = 3; kt = (fi - kTcF3) / kTcN; nt = (fi - kTcF3) % kTcN; }
+        else { layer = 4; kt = (fi - kTcF4) / kTcN4; nt = (fi - kTcF4) % kTcN4; }
+        const int nn = 8 * nt + g, k0 = 16 * kt + 2 * t;
+        auto w = [&](int k) -> float {
+            if (layer == 1) return (k < kMlpIn) ? P[kOffW1 + nn * kMlpIn + k] : 0.0f;
+            if (layer == 2) return P[kOffW2 + nn * kMlpH + k];
+            if (layer == 3) return P[kOffW3 + nn * kMlpH + k];
+            return nn < kMlpOut ? P[kOffW4 + nn * kMlpH + k] : 0.0f;
+        };
+        frag[e] = make_uint2(pack_half2(w(k0), w(k0 + 1)), pack_half2(w(k0 + 8), w(k0 + 9)));
+    }
+}
 }  // namespace
 
-// Warp-cooperative inference on up to 32 samples (weights stationary in
-// registers): lane l owns hidden units 2l and 2l+1 of every layer and streams
-// the samples' input rows from shared memory (broadcast reads), so every
-// weight is read once per batch instead of once per sample.  Per-warp
-// scratch: X[32][kMlpInP] (normalised inputs, filled by the caller), two
-// activation buffers [32][kMlpH] and Y[32][kMlpOutP] (outputs).
-constexpr int kWarpMlpFloats = 32 * (kMlpInP + 2 * kMlpH + kMlpOutP);
+__device__ __forceinline__ void mma_16816(float (&c)[4], const uint32_t (&a)[4], uint2 b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+}
 
-template <int NIN>
-__device__ __forceinline__ void warp_mlp_layer(const float* __restrict__ W, const float* __restrict__ b, const float* in,
-                                               float* outp, int cnt, int u0, bool relu) {
-    float wa[NIN], wb[NIN];
-    const float4* ra = reinterpret_cast<const float4*>(W + u0 * NIN);
-    const float4* rb = reinterpret_cast<const float4*>(W + (u0 + 1) * NIN);
+// One hidden layer on a 16-sample tile: A fragments in (KT k-tiles), ReLU'd
+// outputs packed as the next layer's A fragments (kTcKH k-tiles); the
+// m16n8 accumulator layout of n-tiles 2k and 2k+1 is exactly the m16k16 A
+// layout of k-tile k.
+template <int KT>
+__device__ __forceinline__ void tc_hidden(const uint2* __restrict__ frag, const float* __restrict__ bias,
+                                          const uint32_t (&a)[KT][4], uint32_t (&o)[kTcKH][4], int lane) {
+    const int t = lane & 3;
+    float c[kTcN][4];
 #pragma unroll
-    for (int k = 0; k < NIN / 4; ++k) {
-        const float4 x = __ldg(ra + k), y = __ldg(rb + k);
-        wa[4 * k] = x.x; wa[4 * k + 1] = x.y; wa[4 * k + 2] = x.z; wa[4 * k + 3] = x.w;
-        wb[4 * k] = y.x; wb[4 * k + 1] = y.y; wb[4 * k + 2] = y.z; wb[4 * k + 3] = y.w;
+    for (int nt = 0; nt < kTcN; ++nt) {
+        const float b0 = __ldg(bias + 8 * nt + 2 * t), b1 = __ldg(bias + 8 * nt + 2 * t + 1);
+        c[nt][0] = b0;
+        c[nt][1] = b1;
+        c[nt][2] = b0;
+        c[nt][3] = b1;
     }
-    const float ba = __ldg(b + u0), bb = __ldg(b + u0 + 1);
-    // two samples per step: eight independent FMA chains
-    for (int s = 0; s < cnt; s += 2) {
-        const bool two = s + 1 < cnt;
-        const float4* x4 = reinterpret_cast<const float4*>(in + s * NIN);
-        const float4* y4 = reinterpret_cast<const float4*>(in + (two ? s + 1 : s) * NIN);
-        float a0 = ba, c0 = 0.0f, a1 = bb, c1 = 0.0f;
-        float d0 = ba, e0 = 0.0f, d1 = bb, e1 = 0.0f;
 #pragma unroll
-        for (int k = 0; k < NIN / 4; ++k) {
-            const float4 x = x4[k], y = y4[k];
-            a0 = fmaf(wa[4 * k], x.x, a0);
-            c0 = fmaf(wa[4 * k + 1], x.y, c0);
-            a1 = fmaf(wb[4 * k], x.x, a1);
-            c1 = fmaf(wb[4 * k + 1], x.y, c1);
-            d0 = fmaf(wa[4 * k], y.x, d0);
-            e0 = fmaf(wa[4 * k + 1], y.y, e0);
-            d1 = fmaf(wb[4 * k], y.x, d1);
-            e1 = fmaf(wb[4 * k + 1], y.y, e1);
-            a0 = fmaf(wa[4 * k + 2], x.z, a0);
-            c0 = fmaf(wa[4 * k + 3], x.w, c0);
-            a1 = fmaf(wb[4 * k + 2], x.z, a1);
-            c1 = fmaf(wb[4 * k + 3], x.w, c1);
-            d0 = fmaf(wa[4 * k + 2], y.z, d0);
-            e0 = fmaf(wa[4 * k + 3], y.w, e0);
-            d1 = fmaf(wb[4 * k + 2], y.z, d1);
-            e1 = fmaf(wb[4 * k + 3], y.w, e1);
-        }
-        float v0 = a0 + c0, v1 = a1 + c1, w0 = d0 + e0, w1 = d1 + e1;
-        if (relu) {
-            v0 = fmaxf(v0, 0.0f);
-            v1 = fmaxf(v1, 0.0f);
-            w0 = fmaxf(w0, 0.0f);
-            w1 = fmaxf(w1, 0.0f);
-        }
-        *reinterpret_cast<float2*>(outp + s * kMlpH + u0) = make_float2(v0, v1);
-        if (two) *reinterpret_cast<float2*>(outp + (s + 1) * kMlpH + u0) = make_float2(w0, w1);
+    for (int kt = 0; kt < KT; ++kt)
+#pragma unroll
+        for (int nt = 0; nt < kTcN; ++nt) mma_16816(c[nt], a[kt], __ldg(frag + (kt * kTcN + nt) * 32 + lane));
+#pragma unroll
+    for (int k = 0; k < kTcKH; ++k) {
+        o[k][0] = pack_half2(fmaxf(c[2 * k][0], 0.0f), fmaxf(c[2 * k][1], 0.0f));
+        o[k][1] = pack_half2(fmaxf(c[2 * k][2], 0.0f), fmaxf(c[2 * k][3], 0.0f));
+        o[k][2] = pack_half2(fmaxf(c[2 * k + 1][0], 0.0f), fmaxf(c[2 * k + 1][1], 0.0f));
+        o[k][3] = pack_half2(fmaxf(c[2 * k + 1][2], 0.0f), fmaxf(c[2 * k + 1][3], 0.0f));
     }
 }
 
-__device__ __forceinline__ void warp_mlp(const float* __restrict__ S, float* X, float* Ha, float* Hb, float* Y,
-                                         int cnt, int lane) {
-    const int u0 = 2 * lane;
-    warp_mlp_layer<kMlpInP>(S + kSOffW1, S + kSOffB1, X, Ha, cnt, u0, true);
-    __syncwarp();
-    warp_mlp_layer<kMlpH>(S + kSOffW2, S + kSOffB2, Ha, Hb, cnt, u0, true);
-    __syncwarp();
-    warp_mlp_layer<kMlpH>(S + kSOffW3, S + kSOffB3, Hb, Ha, cnt, u0, true);
-    __syncwarp();
-    if (lane < kMlpOut) {
-        float w[kMlpH];
-        const float4* r = reinterpret_cast<const float4*>(S + kSOffW4 + lane * kMlpH);
+constexpr int kWarpTcFloats = 32 * (kMlpInP + kMlpOutP);  // per-warp scratch: X then Y
+
+// Warp-level tensor-core inference on up to 32 samples: X[32][kMlpInP]
+// normalised inputs (rows >= cnt ignored), outputs to Y[32][kMlpOutP]
+// (first kMlpOut columns).  buf is the device parameter buffer.
+__device__ __forceinline__ void warp_mlp_tc(const float* __restrict__ buf, const float* X, float* Y, int cnt,
+                                            int lane) {
+    const int g = lane >> 2, t = lane & 3;
+    const uint2* frag = reinterpret_cast<const uint2*>(buf + kTcFragOff);
+    const float* bias = buf + kTcBiasOff;
+    for (int m0 = 0; m0 < cnt; m0 += 16) {
+        const float* x0 = X + (m0 + g) * kMlpInP;
+        const float* x1 = X + (m0 + g + 8) * kMlpInP;
+        uint32_t a1[kTcK1][4];
 #pragma unroll
-        for (int k = 0; k < kMlpH / 4; ++k) {
-            const float4 x = __ldg(r + k);
-            w[4 * k] = x.x; w[4 * k + 1] = x.y; w[4 * k + 2] = x.z; w[4 * k + 3] = x.w;
+        for (int kt = 0; kt < kTcK1; ++kt) {
+            const int k = 16 * kt + 2 * t;
+            auto ld = [&](const float* x, int kk) { return kk < kMlpInP ? x[kk] : 0.0f; };
+            a1[kt][0] = pack_half2(ld(x0, k), ld(x0, k + 1));
+            a1[kt][1] = pack_half2(ld(x1, k), ld(x1, k + 1));
+            a1[kt][2] = pack_half2(ld(x0, k + 8), ld(x0, k + 9));
+            a1[kt][3] = pack_half2(ld(x1, k + 8), ld(x1, k + 9));
         }
-        const float b = __ldg(S + kSOffB4 + lane);
-        for (int s = 0; s < cnt; ++s) {
-            const float4* x4 = reinterpret_cast<const float4*>(Ha + s * kMlpH);
-            float a = b, c = 0.0f;
+        uint32_t h1[kTcKH][4], h2[kTcKH][4];
+        tc_hidden<kTcK1>(frag + kTcF1 * 32, bias, a1, h1, lane);
+        tc_hidden<kTcKH>(frag + kTcF2 * 32, bias + kMlpH, h1, h2, lane);
+        tc_hidden<kTcKH>(frag + kTcF3 * 32, bias + 2 * kMlpH, h2, h1, lane);
+        float c[kTcN4][4];
 #pragma unroll
-            for (int k = 0; k < kMlpH / 4; ++k) {
-                const float4 x = x4[k];
-                a = fmaf(w[4 * k], x.x, a);
-                c = fmaf(w[4 * k + 1], x.y, c);
-                a = fmaf(w[4 * k + 2], x.z, a);
-                c = fmaf(w[4 * k + 3], x.w, c);
+        for (int nt = 0; nt < kTcN4; ++nt) {
+            const float b0 = __ldg(bias + 3 * kMlpH + 8 * nt + 2 * t), b1 = __ldg(bias + 3 * kMlpH + 8 * nt + 2 * t + 1);
+            c[nt][0] = b0;
+            c[nt][1] = b1;
+            c[nt][2] = b0;
+            c[nt][3] = b1;
+        }
+#pragma unroll
+        for (int kt = 0; kt < kTcKH; ++kt)
+#pragma unroll
+            for (int nt = 0; nt < kTcN4; ++nt) mma_16816(c[nt], h1[kt], __ldg(frag + (kTcF4 + kt * kTcN4 + nt) * 32 + lane));
+#pragma unroll
+        for (int nt = 0; nt < kTcN4; ++nt) {
+            const int col = 8 * nt + 2 * t;
+            if (col < kMlpOutP) {
+                Y[(m0 + g) * kMlpOutP + col] = c[nt][0];
+                Y[(m0 + g + 8) * kMlpOutP + col] = c[nt][2];
             }
-            Y[s * kMlpOutP + lane] = a + c;
+            if (col + 1 < kMlpOutP) {
+                Y[(m0 + g) * kMlpOutP + col + 1] = c[nt][1];
+                Y[(m0 + g + 8) * kMlpOutP + col + 1] = c[nt][3];
+            }
         }
     }
     __syncwarp();

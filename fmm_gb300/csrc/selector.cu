@@ -380,16 +380,13 @@ __global__ void k_adam(int nparam, int first, float* __restrict__ p, const float
 }
 
 // Batched inference with the routine the list kernel uses: a warp per 32
-// samples, weights (inference layout after the blob in `params`) in
-// registers.
+// samples on the tensor cores (FP16 operands, FP32 accumulation).
 __global__ void __launch_bounds__(128) k_mlp_infer(const float* __restrict__ params, const float* __restrict__ X,
                                                    int n, float* __restrict__ Y) {
     extern __shared__ __align__(16) float sm_inf[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float* Xs = sm_inf + wib * kWarpMlpFloats;
-    float* Ha = Xs + 32 * kMlpInP;
-    float* Hb = Ha + 32 * kMlpH;
-    float* Ys = Hb + 32 * kMlpH;
+    float* Xs = sm_inf + wib * kWarpTcFloats;
+    float* Ys = Xs + 32 * kMlpInP;
     const float* S = params + kMlpInfOff;
     const int base = (blockIdx.x * blockDim.x) + wib * 32;
     const int cnt = max(0, min(32, n - base));
@@ -401,12 +398,12 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const float* __restrict__ par
         mlp_input(S, x, Xs + lane * kMlpInP);
     }
     __syncwarp();
-    warp_mlp(S, Xs, Ha, Hb, Ys, cnt, lane);
+    warp_mlp_tc(params, Xs, Ys, cnt, lane);
     if (lane < cnt)
         for (int o = 0; o < kMlpOut; ++o) Y[(size_t)q * kMlpOut + o] = Ys[lane * kMlpOutP + o];
 }
 
-size_t infer_smem(int threads) { return sizeof(float) * (size_t)(threads / 32) * kWarpMlpFloats; }
+size_t infer_smem(int threads) { return sizeof(float) * (size_t)(threads / 32) * kWarpTcFloats; }
 
 size_t train_smem() {
     return sizeof(float) * (kMlpParams + kTB * (kMlpIn + 3 * kMlpH + kMlpOut + 3 * kMlpH));

@@ -412,10 +412,8 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
     int P, float log_budget, unsigned long long* counters) {
     extern __shared__ __align__(16) float sm_sel[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float* X = sm_sel + wib * kWarpMlpFloats;  // this warp's network scratch
-    float* Ha = X + 32 * kMlpInP;
-    float* Hb = Ha + 32 * kMlpH;
-    float* Y = Hb + 32 * kMlpH;
+    float* X = sm_sel + wib * kWarpTcFloats;  // this warp's network scratch
+    float* Y = X + 32 * kMlpInP;
     const float* S = params + kMlpInfOff;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     bool skip = q >= nin;
@@ -458,7 +456,7 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
             mlp_input(S, x, X + slot * kMlpInP);
         }
         __syncwarp();
-        warp_mlp(S, X, Ha, Hb, Y, __popc(need), lane);
+        warp_mlp_tc(params, X, Y, __popc(need), lane);
         if (accept) {
             for (int o = kQmin; o <= qmax; ++o)
                 if (Y[slot * kMlpOutP + (o - kQmin)] <= log_budget) {
@@ -779,7 +777,7 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
             FMM_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st));
             count_launches(1);
             if (tp.sel_params) {
-                const size_t smem = sizeof(float) * 4 * (size_t)kWarpMlpFloats;
+                const size_t smem = sizeof(float) * 4 * (size_t)kWarpTcFloats;
                 FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_list_iter_learned,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
                 k_list_iter_learned<<<grid_for(nin, 128), 128, smem, st>>>(
