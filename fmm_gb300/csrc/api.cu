@@ -263,9 +263,10 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     TreeDev t;
     const int nf = nT(f);
     cudaEventRecord(ws.ev[0], st);
-    // learned selector: FP64 direct sum at sampled particles (field scale of
-    // the per-pair budget, and the check of the result), on a second stream
-    // so that it overlaps the tree build and the upward pass
+    FMM_TRY(build_tree(ws, P.x, P.n, tp, t, st));
+    cudaEventRecord(ws.ev[1], st);
+    // learned selector: FP64 direct sums at sampled particles, the check of
+    // the result; on a second stream beside the later, FP32-bound phases
     std::vector<double> ref_rows;
     std::vector<int64_t> rows;
     const int nt = learned ? (int)std::min<int64_t>(kCheckTargets, P.n) : 0;
@@ -284,8 +285,6 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         FMM_TRY(launch_direct_f64(ws, P, f, mdir, d_ref, ws.aux, nt, d_rows, 16));
         cudaEventRecord(ws.ev[11], ws.aux);
     }
-    FMM_TRY(build_tree(ws, P.x, P.n, tp, t, st));
-    cudaEventRecord(ws.ev[1], st);
     FMM_TRY(gather_sorted(ws, P, t, st));
     const bool f32_near = md.precision == 1 || md.precision == 2;
     if (f32_near || learned) FMM_TRY(prepare_f32_records(ws, P, t, st));

@@ -31,7 +31,7 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 
 constexpr int kFallback = 63;            // key code of pairs without a grid displacement
 constexpr int64_t kDOff = 1 << 17;       // offset of the 18-bit displacement fields
-constexpr int kTaskCols = 256;           // pairs (columns) per product block
+constexpr int kTaskCols = 512;           // pairs (columns) per product block
 constexpr int kGemmThreads = 128;        // 16 row groups x 8 column groups
 
 __global__ void k_far_targets(int M, const int32_t* __restrict__ off, int32_t* __restrict__ tgt) {
@@ -225,8 +225,30 @@ struct Vec<double> {
     }
 };
 
+// RT consecutive operator rows as 16-byte loads where the alignment allows
+// (row blocks of RT elements start at multiples of RT).
+template <typename R, int RT>
+__device__ __forceinline__ void load_rows(const R* p, R (&v)[RT]) {
+    constexpr int VS = 16 / (int)sizeof(R);
+    if constexpr (RT % VS == 0) {
+        using V = typename Vec<R>::T;
+#pragma unroll
+        for (int k = 0; k < RT / VS; ++k) Vec<R>::get(reinterpret_cast<const V*>(p)[k], v + VS * k);
+    } else if constexpr (sizeof(R) == 4 && RT % 2 == 0) {
+#pragma unroll
+        for (int k = 0; k < RT / 2; ++k) {
+            const float2 x = reinterpret_cast<const float2*>(p)[k];
+            v[2 * k] = x.x;
+            v[2 * k + 1] = x.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < RT; ++k) v[k] = p[k];
+    }
+}
+
 // Columns [c_begin, c_begin + kTaskCols) of one group: C = G W for tiles of
-// TN pairs; thread (rg, cg) owns rows rg + 16k (k < RT) and columns
+// TN pairs; thread (rg, cg) owns rows rg*RT + k (k < RT) and columns
 // cg*CPT .. cg*CPT + CPT - 1 of each tile.  G^T sits in shared memory
 // (s-major); each thread streams its columns' weights straight from global
 // memory (L1/L2-resident), VS consecutive s per 16-byte load, so the tile loop
@@ -275,7 +297,7 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
         for (int k = 0; k < RT; ++k)
 #pragma unroll
             for (int l = 0; l < CPT; ++l) acc[k][l] = (R)0;
-        const R* Gp = G + rg;
+        const R* Gp = G + rg * RT;  // this thread's RT consecutive rows
         for (int s0 = 0; s0 < nrv; s0 += VS) {
             R wv[CPT][VS];
 #pragma unroll
@@ -290,8 +312,7 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
 #pragma unroll
             for (int u = 0; u < VS; ++u) {
                 R gv[RT];
-#pragma unroll
-                for (int k = 0; k < RT; ++k) gv[k] = Gp[(s0 + u) * RM + 16 * k];
+                load_rows<R, RT>(Gp + (s0 + u) * RM, gv);
 #pragma unroll
                 for (int k = 0; k < RT; ++k)
 #pragma unroll
@@ -306,7 +327,7 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
                 R* o = out + (size_t)pos[l] * ldo;
 #pragma unroll
                 for (int k = 0; k < RT; ++k) {
-                    const int f = rg + 16 * k;
+                    const int f = rg * RT + k;
                     if (f < nrq)
                         o[f] = acc[k][l];
                     else if (f < ldo)

@@ -136,11 +136,11 @@ __global__ void __launch_bounds__(128) k_direct_scale(const TreeDev t, const flo
 // lane's target: compensated FP32 (TwoSum hi + lo), since the per-atom terms
 // are much larger than their neutral total.  CHECK: the leaf may hold the
 // target itself or one of its excluded partners.
-template <int M, int F, bool CHECK>
+template <int M, int F, int DAMP, bool CHECK>
 __device__ __forceinline__ void p2p_leaf(const float4* __restrict__ rec, int js, int je, int grp, int ngr, int tgt,
                                          float xt, float yt, float zt, float dt, float ox, float oy, float oz,
                                          float oxl, float oyl, float ozl, const int32_t* __restrict__ excl,
-                                         int exw, int64_t n, int ot, int damp, float* hi, float* lo) {
+                                         int exw, int64_t n, int ot, float* hi, float* lo) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
     for (int k = js + grp; k < je; k += ngr) {
         const float4* r = rec + (size_t)k * NV;
@@ -167,7 +167,7 @@ __device__ __forceinline__ void p2p_leaf(const float4* __restrict__ rec, int js,
         float c[NF];
 #pragma unroll
         for (int f = 0; f < NF; ++f) c[f] = 0.0f;
-        pair_field_f32acc<M, F>(dx, dy, dz, dt * a.w, damp, mc, c);
+        pair_field_f32acc<M, F>(dx, dy, dz, dt * a.w, DAMP, mc, c);
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
             const float s = hi[f] + c[f];
@@ -182,10 +182,12 @@ __device__ __forceinline__ void p2p_leaf(const float4* __restrict__ rec, int js,
 // fewer than 32 particles, groups of lanes split each source leaf).  Source
 // leaves that hold neither the target nor an excluded partner of any of the
 // warp's targets run without the exclusion test.
-template <int M, int F>
+// DAMP is the damping kind as a template parameter: one specialised kernel
+// per kind keeps the pair loop free of kind dispatch and its code small.
+template <int M, int F, int DAMP>
 __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* __restrict__ rec,
                                                  const float4* __restrict__ chi, const float4* __restrict__ clo,
-                                                 const int32_t* __restrict__ excl, int exw, int64_t n, int damp,
+                                                 const int32_t* __restrict__ excl, int exw, int64_t n,
                                                  double* __restrict__ fs) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -236,11 +238,11 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
 #pragma unroll
                 for (int f = 0; f < NF; ++f) hi[f] = lo[f] = 0.0f;
                 if (__any_sync(vmask, need))
-                    p2p_leaf<M, F, true>(rec, js, je, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy, oz, oxl, oyl,
-                                         ozl, excl, exw, n, ot, damp, hi, lo);
+                    p2p_leaf<M, F, DAMP, true>(rec, js, je, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy, oz, oxl,
+                                               oyl, ozl, excl, exw, n, ot, hi, lo);
                 else
-                    p2p_leaf<M, F, false>(rec, js, je, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy, oz, oxl, oyl,
-                                          ozl, excl, exw, n, ot, damp, hi, lo);
+                    p2p_leaf<M, F, DAMP, false>(rec, js, je, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy, oz, oxl,
+                                                oyl, ozl, excl, exw, n, ot, hi, lo);
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
                     // (AH, AL) += (hi, lo)
@@ -263,6 +265,25 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
 #pragma unroll
             for (int f = 0; f < NF; ++f) fs[(size_t)f * n + tgt] = acc[f];
         }
+    }
+}
+
+template <int M, int F>
+void launch_p2p_kind(unsigned blocks, cudaStream_t st, const TreeDev& t, const float4* rec, const float4* chi,
+                     const float4* clo, const int32_t* excl, int exw, int64_t n, int damp, double* fs) {
+    switch (damp) {
+        case DAMP_AMOEBA:
+            k_p2p_f32<M, F, DAMP_AMOEBA><<<blocks, 128, 0, st>>>(t, rec, chi, clo, excl, exw, n, fs);
+            break;
+        case DAMP_THOLE:
+            k_p2p_f32<M, F, DAMP_THOLE><<<blocks, 128, 0, st>>>(t, rec, chi, clo, excl, exw, n, fs);
+            break;
+        case DAMP_ERF:
+            k_p2p_f32<M, F, DAMP_ERF><<<blocks, 128, 0, st>>>(t, rec, chi, clo, excl, exw, n, fs);
+            break;
+        default:
+            k_p2p_f32<M, F, DAMP_NONE><<<blocks, 128, 0, st>>>(t, rec, chi, clo, excl, exw, n, fs);
+            break;
     }
 }
 
@@ -310,9 +331,8 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
     const float4* clo = chi + t.num_nodes;
     FMM_TRY(ws.fsorted.ensure(sizeof(double) * (size_t)n * nf));
     const unsigned blocks = grid_for((int64_t)t.num_leaves * 32, 128);
-    FMM_MF_SWITCH(m, field_order,
-                  (k_p2p_f32<MM, FF><<<blocks, 128, 0, st>>>(t, rec, chi, clo, P.excl, P.exw, n, P.damp_type,
-                                                              ws.fsorted.as<double>())));
+    FMM_MF_SWITCH(m, field_order, (launch_p2p_kind<MM, FF>(blocks, st, t, rec, chi, clo, P.excl, P.exw, n,
+                                                           P.damp_type, ws.fsorted.as<double>())));
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
