@@ -64,16 +64,23 @@ def pair_flops(m, f):
     return 2 * n_t(f) * n_t(m) + 2 * comb(m + f + 4, 4) + 12
 
 
-def workload_config(arm):
+WORKLOADS = {
+    "water": "water-like triplets N=999,999 in a 270 bohr cube, AMOEBA damping, multipoles order 2, field_order 1, "
+             "ncrit 64",
+    "blobs": "N=2,000,000 clustered particles (64 Gaussian blobs, sigma ~ U(5,30) bohr, centres in a 600 bohr cube, "
+             "Dirichlet(1) weights), AMOEBA damping, multipoles order 2, field_order 1, ncrit 64",
+}
+
+
+def workload_config(arm, system="water", n=3 * N_MOL):
     a = ARMS.get(arm, dict(theta=REF_SETTINGS["theta"], p=REF_SETTINGS["p"]))
     return {
-        "workload": "water-like triplets N=999,999 in a 270 bohr cube, AMOEBA damping, multipoles order 2, "
-                    "field_order 1, ncrit 64",
+        "workload": WORKLOADS[system] if n in (3 * N_MOL, 2_000_000) else WORKLOADS[system] + " (N=%d)" % n,
         "arm": arm,
         "theta": a["theta"],
         "expansion_order": a["p"],
         "settings": {k: v for k, v in a.items() if k not in ("theta", "p")},
-        "n_particles": 3 * N_MOL,
+        "n_particles": n,
         "l2": "inputs plus working set > 129 MB L2; a 256 MB buffer is also written between timed steps",
         "accuracy_oracle": "FP64 GPU direct sum on 8192 random particles, field columns of order >= 1",
     }
@@ -188,6 +195,47 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args):
+    """512 independent systems (N log-uniform in [1k, 64k], uniform at density
+    0.1 per bohr^3, erf damping, multipoles order 1, theta 0.5, p 6, f 1)
+    through fmm_gb300.field_fmm_batched: host arrays in, host field out, so
+    the time includes the host<->device copies.  Accuracy on 8 of the systems
+    against their FP64 direct sums."""
+    import fmm_gb300
+    from fmm_gb300 import Options, systems
+    sl = systems.batched_uniform(n_systems=512, seed=3)
+    n = sum(s["coordinates"].shape[0] for s in sl)
+    rng = np.random.default_rng(5)
+    check = sorted(rng.choice(len(sl), size=8, replace=False).tolist())
+    refs = {k: fmm_gb300.field_direct(0, sl[k]["coordinates"], sl[k]["multipoles"], sl[k]["exclusions"], 1, "ERF",
+                                      sl[k]["damping_factors"], options=Options(excl_mode="mask")) for k in check}
+    out = {}
+    for name, opt in (("mixed", Options.exact(precision="mixed")), ("fp64", Options.exact())):
+        for _ in range(args.warmup):
+            F = fmm_gb300.field_fmm_batched(sl, 0.5, NCRIT, 6, 1, "ERF", options=opt)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            F = fmm_gb300.field_fmm_batched(sl, 0.5, NCRIT, 6, 1, "ERF", options=opt)
+            times.append(time.perf_counter() - t0)
+        errs = []
+        for k in check:
+            d = np.linalg.norm(F[k][:, 1:] - refs[k][:, 1:], axis=1)
+            g = np.linalg.norm(refs[k][:, 1:], axis=1)
+            errs.append(d / g)
+        e = np.concatenate(errs)
+        out[name] = {"value": n / float(np.mean(times)), "ms_per_step": 1e3 * float(np.mean(times)),
+                     "rms_rel_err": float(np.sqrt(np.mean(e ** 2))), "max_rel_err": float(e.max())}
+    line = {"metric": "field_fmm_batched particles/s, 512 systems", "value": out["mixed"]["value"],
+            "unit": "particles/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": out["mixed"]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "512 systems, N log-uniform in [1k, 64k] (%d total), density 0.1, erf U(0.3,0.8), "
+                                   "multipoles order 1, theta 0.5, p 6, f 1, ncrit 64; host arrays (copies timed)" % n},
+            "arms": out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -200,6 +248,10 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=10_000, help="molecules in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-mol", type=int, default=N_MOL)
+    ap.add_argument("--system", default="water", choices=["water", "blobs"],
+                    help="water: the metric's workload; blobs: N=2M clustered particles (learned-selector workload)")
+    ap.add_argument("--batched", action="store_true",
+                    help="512 independent systems, N log-uniform in [1k, 64k], through the batched host call")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -207,6 +259,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.batched:
+        run_batched(args)
         return
 
     import torch
@@ -223,9 +278,13 @@ def main():
     stream = torch.cuda.current_stream()
     opts.stream = stream.cuda_stream
 
-    n_mol = args.n_mol
-    box = BOX * (n_mol / N_MOL) ** (1.0 / 3.0)
-    s = make_system(seed=rank, n_mol=n_mol, box=box)
+    if args.system == "blobs":
+        from fmm_gb300 import systems
+        s = systems.blobs(n=2_000_000, seed=rank)
+    else:
+        n_mol = args.n_mol
+        box = BOX * (n_mol / N_MOL) ** (1.0 / 3.0)
+        s = make_system(seed=rank, n_mol=n_mol, box=box)
     n = s["coordinates"].shape[0]
     dev = torch.device("cuda", local)
     tX = torch.from_numpy(np.ascontiguousarray(s["coordinates"].T).reshape(-1)).to(dev)  # column-major (n,3)
@@ -402,7 +461,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.arm == "fp64" else "f32+f64", "data": "synthetic", "config": workload_config(args.arm),
+        "dtype": "f64" if args.arm == "fp64" else "f32+f64", "data": "synthetic", "config": workload_config(args.arm, args.system, n),
         "accuracy": accuracy, "e2e": e2e, "roofline": roofline, "plain_fp64": compare, "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),

@@ -30,7 +30,10 @@ namespace {
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
 constexpr int kFallback = 63;            // key code of pairs without a grid displacement
-constexpr int64_t kDOff = 1 << 17;       // offset of the 18-bit displacement fields
+// Key layout (46 bits, so the radix sort needs 6 digit passes): level
+// difference + 31 (6 bits) | order (4) | Dx, Dy, Dz + kDOff (12 bits each).
+constexpr int kKeyBits = 46;
+constexpr int64_t kDOff = 1 << 11;       // offset of the 12-bit displacement fields
 constexpr int kTaskCols = 512;           // pairs (columns) per product block
 constexpr int kGemmThreads = 128;        // 16 row groups x 8 column groups
 
@@ -64,7 +67,7 @@ __global__ void k_scale_weights(int64_t total, int nr, int ld, const double* __r
 
 // Group key of every far pair: level difference, expansion order and integer
 // displacement in units of the smaller half-width; pairs off the grid (or
-// with out-of-range fields) get unique keys of their own.
+// with out-of-range fields) get unique keys of their own (code 63 | index).
 __global__ void k_m2l_keys(int64_t nfar, const TreeDev t, const int32_t* __restrict__ tgt, int p,
                            uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -82,10 +85,10 @@ __global__ void k_m2l_keys(int64_t nfar, const TreeDev t, const int32_t* __restr
                       fabs(ry) <= lim && fabs(rz) <= lim && dl > -31 && dl < 31;
     uint64_t key;
     if (grid)
-        key = ((uint64_t)(dl + 31) << 58) | ((uint64_t)ord << 54) | ((uint64_t)((int64_t)rx + kDOff) << 36) |
-              ((uint64_t)((int64_t)ry + kDOff) << 18) | (uint64_t)((int64_t)rz + kDOff);
+        key = ((uint64_t)(dl + 31) << 40) | ((uint64_t)ord << 36) | ((uint64_t)((int64_t)rx + kDOff) << 24) |
+              ((uint64_t)((int64_t)ry + kDOff) << 12) | (uint64_t)((int64_t)rz + kDOff);
     else
-        key = ((uint64_t)kFallback << 58) | (uint64_t)q;
+        key = ((uint64_t)kFallback << 40) | (uint64_t)q;
     keys[q] = key;
     vals[q] = (int32_t)q;
 }
@@ -114,8 +117,8 @@ __global__ void __launch_bounds__(128) k_group_tensor(int ngroups, const uint64_
     const uint64_t key = ukeys[g];
     const int pos0 = svals[gstart[g]];
     const int i = tgt[pos0], j = t.far_src[pos0];
-    const int q = (int)(key >> 58) == kFallback ? (t.far_ord ? min((int)t.far_ord[pos0], p) : p)
-                                                 : (int)((key >> 54) & 15);
+    const int q = (int)(key >> 40) == kFallback ? (t.far_ord ? min((int)t.far_ord[pos0], p) : p)
+                                                 : (int)((key >> 36) & 15);
     const double hi = t.r[i], hj = t.r[j], hc = fmax(hi, hj);
     const double X = (t.cx[i] - t.cx[j]) / hc, Y = (t.cy[i] - t.cy[j]) / hc, Z = (t.cz[i] - t.cz[j]) / hc;
     const int Nq = 2 * q;
@@ -479,7 +482,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         int* d_nruns = reinterpret_cast<int*>(ws.counters.as<unsigned long long>() + 14);
         size_t tb1 = 0, tb2 = 0, tb3 = 0;
         cub::DeviceRadixSort::SortPairs(nullptr, tb1, ws.m2l_keys.as<uint64_t>(), ws.m2l_keys2.as<uint64_t>(),
-                                        ws.m2l_vals.as<int32_t>(), ws.m2l_vals2.as<int32_t>(), (int)nf, 0, 64, st);
+                                        ws.m2l_vals.as<int32_t>(), ws.m2l_vals2.as<int32_t>(), (int)nf, 0, kKeyBits, st);
         cub::DeviceRunLengthEncode::Encode(nullptr, tb2, ws.m2l_keys2.as<uint64_t>(), ws.m2l_ukeys.as<uint64_t>(),
                                            ws.m2l_cnt.as<int32_t>(), d_nruns, (int)nf, st);
         cub::DeviceScan::ExclusiveSum(nullptr, tb3, ws.m2l_cnt.as<int32_t>(), ws.m2l_gstart.as<int32_t>(),
@@ -487,7 +490,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_TRY(ws.cub_tmp.ensure(std::max(tb1, std::max(tb2, tb3))));
         FMM_CUDA_TRY(cub::DeviceRadixSort::SortPairs(ws.cub_tmp.p, tb1, ws.m2l_keys.as<uint64_t>(),
                                                      ws.m2l_keys2.as<uint64_t>(), ws.m2l_vals.as<int32_t>(),
-                                                     ws.m2l_vals2.as<int32_t>(), (int)nf, 0, 64, st));
+                                                     ws.m2l_vals2.as<int32_t>(), (int)nf, 0, kKeyBits, st));
         FMM_CUDA_TRY(cub::DeviceRunLengthEncode::Encode(ws.cub_tmp.p, tb2, ws.m2l_keys2.as<uint64_t>(),
                                                         ws.m2l_ukeys.as<uint64_t>(), ws.m2l_cnt.as<int32_t>(),
                                                         d_nruns, (int)nf, st));
