@@ -185,7 +185,7 @@ struct GemmSmem {
     static constexpr int TN = 8 * CPT;                // columns per tile
     static constexpr int VS = 16 / (int)sizeof(R);    // weights per 16-byte load
     int nrmax, rmmax, nTr;
-    size_t off_dec, off_pow, off_T, off_G, bytes;
+    size_t off_dec, off_pow, off_T, off_col, off_G, bytes;
     __host__ __device__ GemmSmem(int p) {
         nrmax = (p + 1) * (p + 1);
         rmmax = 16 * ((nrmax + 15) / 16);
@@ -199,6 +199,8 @@ struct GemmSmem {
         off_T = o;
         o += sizeof(R) * nTr;
         o = (o + 15) & ~(size_t)15;
+        off_col = o;  // the task's pair positions and source nodes
+        o += sizeof(int) * 2 * kTaskCols;
         off_G = o;
         o += sizeof(R) * (size_t)((nrmax + VS - 1) / VS * VS) * rmmax;
         bytes = o;
@@ -271,7 +273,16 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
     const R* bpow = apow + 16;
     const R* Tsh = reinterpret_cast<const R*>(sm + L.off_T);
     R* G = reinterpret_cast<R*>(sm + L.off_G);
+    int* cpos = reinterpret_cast<int*>(sm + L.off_col);
+    int* csrc = cpos + kTaskCols;
     const int nrv = (nrq + VS - 1) / VS * VS;
+    const int c_end = min(cnt, c_begin + kTaskCols);
+    // the task's columns: pair positions and source nodes (loaded once)
+    for (int i = tid; i < c_end - c_begin; i += kGemmThreads) {
+        const int pos = svals[gs + c_begin + i];
+        cpos[i] = pos;
+        csrc[i] = far_src[pos];
+    }
     // operator G^T (s-major, RM rows per s; rows f >= nrq and s >= nrq zero)
     for (int e = tid; e < nrv * RM; e += kGemmThreads) {
         const int s = e / RM, f = e - s * RM;
@@ -285,15 +296,14 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
         G[e] = v;
     }
     __syncthreads();
-    const int c_end = min(cnt, c_begin + kTaskCols);
     for (int cb = c_begin; cb < c_end; cb += TN) {
         int pos[CPT];
         const V* wp[CPT];
 #pragma unroll
         for (int l = 0; l < CPT; ++l) {
             const int c = cb + cg * CPT + l;
-            pos[l] = c < c_end ? svals[gs + c] : -1;
-            wp[l] = pos[l] >= 0 ? reinterpret_cast<const V*>(wsc + (size_t)far_src[pos[l]] * ldw) : nullptr;
+            pos[l] = c < c_end ? cpos[c - c_begin] : -1;
+            wp[l] = pos[l] >= 0 ? reinterpret_cast<const V*>(wsc + (size_t)csrc[c - c_begin] * ldw) : nullptr;
         }
         R acc[RT][CPT];
 #pragma unroll

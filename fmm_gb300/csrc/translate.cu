@@ -149,6 +149,16 @@ constexpr int kP2mThreads = 128;
 constexpr int kP2mBatch = 8;
 constexpr int kMaxOut = (nT(kMaxP) + kP2mThreads - 1) / kP2mThreads;
 
+// Product of two double-float pairs (hi, lo), renormalised.
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    const float s = p + e;
+    return make_float2(s, e - (s - p));
+}
+
 // DF: accumulate in double-float pairs (FP32 arithmetic, exact products by
 // FMA, ~48-bit sums) instead of FP64; used by the mixed-precision path, where
 // the FP64 pipe is the bottleneck of this kernel.
@@ -201,16 +211,28 @@ __global__ void __launch_bounds__(kP2mThreads) k_p2m(const TreeDev t, const doub
             }
         }
         __syncthreads();
-        for (int idx = threadIdx.x; idx < nb * nq; idx += blockDim.x) {
-            const int b = idx / nq, u = idx % nq;
-            const int c = comp[u];
-            const double* eb = e + b * 3 * P1;
-            const double w = eb[ux_(c)] * eb[P1 + uy_(c)] * eb[2 * P1 + uz_(c)];
-            if (DF) {
+        if (DF) {
+            // scaled powers as double-float pairs, products on the FP32 pipe
+            float2* e2 = reinterpret_cast<float2*>(e);
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < nb * 3 * P1; idx += blockDim.x) {
+                const double w = e[idx];
                 const float hi = (float)w;
-                dp2[b * nq + u] = make_float2(hi, (float)(w - (double)hi));
-            } else {
-                dp[b * nq + u] = w;
+                e2[idx] = make_float2(hi, (float)(w - (double)hi));
+            }
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < nb * nq; idx += blockDim.x) {
+                const int b = idx / nq, u = idx % nq;
+                const int c = comp[u];
+                const float2* eb = e2 + b * 3 * P1;
+                dp2[b * nq + u] = df_mul(df_mul(eb[ux_(c)], eb[P1 + uy_(c)]), eb[2 * P1 + uz_(c)]);
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < nb * nq; idx += blockDim.x) {
+                const int b = idx / nq, u = idx % nq;
+                const int c = comp[u];
+                const double* eb = e + b * 3 * P1;
+                dp[b * nq + u] = eb[ux_(c)] * eb[P1 + uy_(c)] * eb[2 * P1 + uz_(c)];
             }
         }
         __syncthreads();
