@@ -265,25 +265,14 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     cudaEventRecord(ws.ev[0], st);
     FMM_TRY(build_tree(ws, P.x, P.n, tp, t, st));
     cudaEventRecord(ws.ev[1], st);
-    // learned selector: FP64 direct sums at sampled particles, the check of
-    // the result; on a second stream beside the later, FP32-bound phases
     std::vector<double> ref_rows;
     std::vector<int64_t> rows;
     const int nt = learned ? (int)std::min<int64_t>(kCheckTargets, P.n) : 0;
     if (learned) {
-        if (!ws.aux) FMM_CUDA_TRY(cudaStreamCreateWithFlags(&ws.aux, cudaStreamNonBlocking));
         for (int k = 0; k < nt; ++k) rows.push_back((int64_t)(((uint64_t)k * 2654435761ull + 12345ull) % (uint64_t)P.n));
         FMM_TRY(ws.sel_scratch.ensure(sizeof(double) * (size_t)nt * nf * 2 + sizeof(int64_t) * nt));
         int64_t* d_rows = reinterpret_cast<int64_t*>(ws.sel_scratch.as<double>() + (size_t)nt * nf * 2);
-        double* d_ref = ws.sel_scratch.as<double>();
-        cudaEventRecord(ws.ev[10], st);  // inputs in place
-        FMM_CUDA_TRY(cudaStreamWaitEvent(ws.aux, ws.ev[10], 0));
-        FMM_CUDA_TRY(cudaMemcpyAsync(d_rows, rows.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, ws.aux));
-        // few source splits: the FP64 sum runs beside the FP32-bound phases
-        // on the otherwise idle FP64 pipes and is only awaited by the check
-        Modes mdir{1, 1, 0};
-        FMM_TRY(launch_direct_f64(ws, P, f, mdir, d_ref, ws.aux, nt, d_rows, 16));
-        cudaEventRecord(ws.ev[11], ws.aux);
+        FMM_CUDA_TRY(cudaMemcpyAsync(d_rows, rows.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, st));
     }
     FMM_TRY(gather_sorted(ws, P, t, st));
     const bool f32_near = md.precision == 1 || md.precision == 2;
@@ -299,7 +288,6 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         // per-pair error budget from the sampled field scale (FP32 estimate)
         double* d_est = ws.sel_scratch.as<double>() + (size_t)nt * nf;
         const int64_t* d_rows = reinterpret_cast<const int64_t*>(ws.sel_scratch.as<double>() + (size_t)nt * nf * 2);
-        FMM_CUDA_TRY(cudaStreamWaitEvent(st, ws.ev[10], 0));
         FMM_TRY(launch_direct_scale_f32(ws, P, t, f, d_est, st, nt, d_rows));
         std::vector<double> est((size_t)nt * nf);
         FMM_CUDA_TRY(cudaMemcpyAsync(est.data(), d_est, sizeof(double) * nt * nf, cudaMemcpyDeviceToHost, st));
@@ -323,6 +311,17 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     double check_rms = -1.0;
     for (int attempt = 0; attempt < 2; ++attempt) {
         FMM_TRY(build_lists(ws, t, tpl, st));
+        if (learned && attempt == 0) {
+            // FP64 direct sums at the sampled particles (the check of the
+            // result) on a second stream, beside the FP32-bound near field
+            if (!ws.aux) FMM_CUDA_TRY(cudaStreamCreateWithFlags(&ws.aux, cudaStreamNonBlocking));
+            int64_t* d_rows = reinterpret_cast<int64_t*>(ws.sel_scratch.as<double>() + (size_t)nt * nf * 2);
+            cudaEventRecord(ws.ev[10], st);
+            FMM_CUDA_TRY(cudaStreamWaitEvent(ws.aux, ws.ev[10], 0));
+            Modes mdir{1, 1, 0};
+            FMM_TRY(launch_direct_f64(ws, P, f, mdir, ws.sel_scratch.as<double>(), ws.aux, nt, d_rows, 16));
+            cudaEventRecord(ws.ev[11], ws.aux);
+        }
         cudaEventRecord(ws.ev[3], st);
         if (f32_near)
             FMM_TRY(launch_p2p_f32(ws, P, t, f, st));

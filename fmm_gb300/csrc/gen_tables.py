@@ -18,12 +18,14 @@ The closed-form AMOEBA numerator is (-1)^j (2j-1)!! + e^{-u} Q_j(u) with
 Q_1 = 1 and Q_{j+1} = 3u (Q_j' - Q_j) - (2j+1) Q_j; its coefficients are
 emitted too.
 
-FP32 kernels also use re-centred Taylor expansions of N_j on unit intervals
-between the small-argument series and the closed form (both lose digits
-there: the series to alternating terms, the closed form to cancellation):
+FP32 kernels evaluate N_j below the closed form's range from one table of
+expansions on unit intervals: the series itself on [0, 1) (centre 0) and
+re-centred Taylor expansions on the intervals above it, where the series
+loses digits to alternating terms and the closed form to cancellation:
     N_j(c + t) = sum_n b_n t^n,  b_n = sum_k a_k C(k, n) c^(k - n),  |t| <= 1/2
 with the exact series coefficients a_k; centres THOLE_CENTRES in x = a r,
-AMOEBA_CENTRES in u = (a r)^3.
+AMOEBA_CENTRES in u = (a r)^3.  One table for the whole range keeps the
+lanes of a warp on one code path whichever interval each lane's pair is in.
 
 Run:  python gen_tables.py > series_tables.h
 """
@@ -33,9 +35,9 @@ from math import factorial
 JMAX = 8      # highest radial derivative (tensor order) of the damped kernels
 KT = 24       # Thole series length (powers of x)
 KA = 30       # AMOEBA series length (powers of u)
-NTAY = 14     # terms of the re-centred expansions (|t| <= 1/2)
-THOLE_CENTRES = (Fraction(3, 2), Fraction(5, 2))
-AMOEBA_CENTRES = (Fraction(3, 2), Fraction(5, 2), Fraction(7, 2))
+NTAY = 16     # terms of each interval's expansion (a multiple of 4: rows are read as float4)
+THOLE_CENTRES = (Fraction(0), Fraction(3, 2), Fraction(5, 2))
+AMOEBA_CENTRES = (Fraction(0), Fraction(3, 2), Fraction(5, 2), Fraction(7, 2))
 KFULL = 160   # series terms summed exactly for the re-centred coefficients
 
 

@@ -26,7 +26,8 @@ constexpr int kExwRegs = 8;  // exclusion entries held in registers per target
 
 // Per sorted particle, one record of float4s: (x, y, z, d), (x_lo, y_lo, z_lo,
 // original index + 1 as int bits), then the FP32 scaled multipoles padded to
-// a multiple of 4.  Positions are relative to the particle's own leaf centre
+// a multiple of 4 (for quadrupoles the first pad slot holds the trace of the
+// scaled second moments, used by the near-field contraction).  Positions are relative to the particle's own leaf centre
 // as double-float pairs (hi = rounded value, lo = rounded remainder), so
 // differences of positions in two leaves lose nothing beyond the final FP32
 // rounding.  A source is then read with a handful of 16-byte loads from one
@@ -52,6 +53,8 @@ __global__ void k_gather_f32(int64_t n, int dim, const TreeDev t, const double* 
         for (int c = 0; c < 4; ++c) {
             const int s = 4 * (v - 2) + c;
             m[c] = s < dim ? (float)smc[(size_t)s * n + k] : 0.0f;
+            if (dim == 10 && s == 10)
+                m[c] = (float)(smc[(size_t)4 * n + k] + smc[(size_t)7 * n + k] + smc[(size_t)9 * n + k]);
         }
         r[v] = make_float4(m[0], m[1], m[2], m[3]);
     }
@@ -132,21 +135,22 @@ __global__ void __launch_bounds__(128) k_direct_scale(const TreeDev t, const flo
     }
 }
 
-// Sum over the sources [js, je) of one leaf (lane group grp of ngr) for the
-// lane's target: compensated FP32 (TwoSum hi + lo), since the per-atom terms
-// are much larger than their neutral total.  CHECK: the leaf may hold the
+// Sum over the sources src[0, cnt) of one staged piece of a source leaf
+// (lane group grp of ngr) for the lane's target: compensated FP32 (TwoSum
+// hi + lo), since the per-atom terms are much larger than their neutral
+// total.  k0 is the sorted index of src[0].  CHECK: the piece may hold the
 // target itself or one of its excluded partners.
 template <int M, int F, int DAMP, bool CHECK>
-__device__ __forceinline__ void p2p_leaf(const float4* __restrict__ rec, int js, int je, int grp, int ngr, int tgt,
-                                         float xt, float yt, float zt, float dt, float ox, float oy, float oz,
-                                         float oxl, float oyl, float ozl, const int32_t* __restrict__ excl,
-                                         int exw, int64_t n, int ot, float* hi, float* lo) {
+__device__ __forceinline__ void p2p_leaf(const float4* src, int cnt, int k0, int grp, int ngr, int tgt, float xt,
+                                         float yt, float zt, float dt, float ox, float oy, float oz, float oxl,
+                                         float oyl, float ozl, const int32_t* __restrict__ excl, int exw, int64_t n,
+                                         int ot, float* hi, float* lo) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
-    for (int k = js + grp; k < je; k += ngr) {
-        const float4* r = rec + (size_t)k * NV;
+    for (int k = grp; k < cnt; k += ngr) {
+        const float4* r = src + k * NV;
         const float4 a = r[0], b = r[1];
         if (CHECK) {
-            if (k == tgt) continue;
+            if (k0 + k == tgt) continue;
             const int o = __float_as_int(b.w);
             bool skip = false;
             for (int e = 0; e < exw; ++e) skip |= (excl[(size_t)e * n + ot] == o);
@@ -178,10 +182,23 @@ __device__ __forceinline__ void p2p_leaf(const float4* __restrict__ rec, int js,
     }
 }
 
+// Source records are staged per warp in shared memory, double-buffered:
+// while one piece (a source leaf, or kStage / NV of its particles when it is
+// larger) is evaluated, the next is copied with cp.async.
+constexpr int kStage = 320;  // float4s per staging buffer
+
+__device__ __forceinline__ void cp_async16(float4* smem, const float4* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // One warp per target leaf, its particles across the lanes (for leaves of
-// fewer than 32 particles, groups of lanes split each source leaf).  Source
-// leaves that hold neither the target nor an excluded partner of any of the
-// warp's targets run without the exclusion test.
+// fewer than 32 particles, groups of lanes split each source piece).
+// Source leaves that hold neither the target nor an excluded partner of any
+// of the warp's targets run without the exclusion test.
 // DAMP is the damping kind as a template parameter: one specialised kernel
 // per kind keeps the pair loop free of kind dispatch and its code small.
 template <int M, int F, int DAMP>
@@ -190,9 +207,12 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
                                                  const int32_t* __restrict__ excl, int exw, int64_t n,
                                                  double* __restrict__ fs) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
+    constexpr int CAP = kStage / NV;  // particles per staged piece
+    __shared__ float4 sbuf[4][2][kStage];
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= t.num_leaves) return;
+    float4(*buf)[kStage] = sbuf[threadIdx.x >> 5];
     const int leaf = t.leaves[w];
     const int s0 = t.start[leaf], cnt = t.count[leaf];
     const int q0 = t.near_off[leaf], q1 = t.near_off[leaf + 1];
@@ -204,7 +224,6 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
         const int ngr = 32 / g;
         const int tl = lane & (g - 1), grp = lane / g;
         const bool valid = tl < nt;
-        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
         const int tgt = s0 + chunk + (valid ? tl : 0);
         const float4 ta = rec[(size_t)tgt * NV], tb = rec[(size_t)tgt * NV + 1];
         const int ot = __float_as_int(tb.w) - 1;
@@ -220,10 +239,39 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
         float AH[NF], AL[NF];
 #pragma unroll
         for (int f = 0; f < NF; ++f) AH[f] = AL[f] = 0.0f;
-        if (valid) {
-            for (int q = q0; q < q1; ++q) {
-                const int j = t.near_src[q];
-                const int js = t.start[j], je = js + t.count[j];
+        // current piece (q, off) of source leaf j = [js, js + jc); the first
+        // one is staged before the loop
+        int q = q0, off = 0, j = 0, js = 0, jc = 0;
+        if (q < q1) {
+            j = t.near_src[q];
+            js = t.start[j];
+            jc = t.count[j];
+            const int pc = min(CAP, jc);
+            for (int i = lane; i < pc * NV; i += 32) cp_async16(&buf[0][i], rec + (size_t)js * NV + i);
+        }
+        cp_async_commit();
+        int slot = 0;
+        while (q < q1) {
+            // stage the next piece
+            int nq = q, noff = off + CAP, nj = j, njs = js, njc = jc;
+            if (noff >= jc) {
+                nq = q + 1;
+                noff = 0;
+                if (nq < q1) {
+                    nj = t.near_src[nq];
+                    njs = t.start[nj];
+                    njc = t.count[nj];
+                }
+            }
+            if (nq < q1) {
+                const int npc = min(CAP, njc - noff);
+                const float4* gsrc = rec + (size_t)(njs + noff) * NV;
+                for (int i = lane; i < npc * NV; i += 32) cp_async16(&buf[slot ^ 1][i], gsrc + i);
+            }
+            cp_async_commit();
+            cp_async_wait_prev();
+            __syncwarp();
+            if (valid) {
                 // leaf-centre offset c_A - c_B as hi + lo; the low parts are
                 // folded with the target's low parts
                 const float4 cb = chi[j], cbl = clo[j];
@@ -234,15 +282,16 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
                 bool need = (j == leaf) || exw > kExwRegs;
 #pragma unroll
                 for (int e = 0; e < kExwRegs; ++e) need |= (exl[e] == j);
+                const int pc = min(CAP, jc - off);
                 float hi[NF], lo[NF];
 #pragma unroll
                 for (int f = 0; f < NF; ++f) hi[f] = lo[f] = 0.0f;
-                if (__any_sync(vmask, need))
-                    p2p_leaf<M, F, DAMP, true>(rec, js, je, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy, oz, oxl,
-                                               oyl, ozl, excl, exw, n, ot, hi, lo);
+                if (__any_sync(__activemask(), need))
+                    p2p_leaf<M, F, DAMP, true>(buf[slot], pc, js + off, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy,
+                                               oz, oxl, oyl, ozl, excl, exw, n, ot, hi, lo);
                 else
-                    p2p_leaf<M, F, DAMP, false>(rec, js, je, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy, oz, oxl,
-                                                oyl, ozl, excl, exw, n, ot, hi, lo);
+                    p2p_leaf<M, F, DAMP, false>(buf[slot], pc, js + off, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox,
+                                                oy, oz, oxl, oyl, ozl, excl, exw, n, ot, hi, lo);
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
                     // (AH, AL) += (hi, lo)
@@ -253,13 +302,21 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
                     AL[f] += err + lo[f];
                 }
             }
+            __syncwarp();
+            q = nq;
+            off = noff;
+            j = nj;
+            js = njs;
+            jc = njc;
+            slot ^= 1;
         }
+        cp_async_wait_all();
         double acc[NF];
 #pragma unroll
         for (int f = 0; f < NF; ++f) acc[f] = (double)AH[f] + (double)AL[f];
-        for (int off = g; off < 32; off <<= 1) {
+        for (int o = g; o < 32; o <<= 1) {
 #pragma unroll
-            for (int f = 0; f < NF; ++f) acc[f] += __shfl_xor_sync(0xffffffffu, acc[f], off);
+            for (int f = 0; f < NF; ++f) acc[f] += __shfl_xor_sync(0xffffffffu, acc[f], o);
         }
         if (grp == 0 && valid) {
 #pragma unroll

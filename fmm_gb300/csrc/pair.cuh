@@ -38,13 +38,12 @@ __constant__ double cInvOdd[FMM_INV_ODD_N] = {
 __constant__ double cTholeSeries[FMM_SER_JMAX + 1][FMM_SER_KT + 1] = FMM_THOLE_SERIES_INIT;
 __constant__ double cAmoebaSeries[FMM_SER_JMAX + 1][FMM_SER_KA + 1] = FMM_AMOEBA_SERIES_INIT;
 __constant__ double cAmoebaQ[FMM_SER_JMAX + 1][FMM_SER_JMAX] = FMM_AMOEBA_Q_INIT;
-__constant__ float cTholeSeriesF[FMM_SER_JMAX + 1][FMM_SER_KT + 1] = FMM_THOLE_SERIES_INIT;
-__constant__ float cAmoebaSeriesF[FMM_SER_JMAX + 1][FMM_SER_KA + 1] = FMM_AMOEBA_SERIES_INIT;
 __constant__ float cAmoebaQF[FMM_SER_JMAX + 1][FMM_SER_JMAX] = FMM_AMOEBA_Q_INIT;
-// re-centred expansions (FP32 kernels): lanes index them by their own
-// interval, so they live in global memory rather than the constant bank
-__device__ const float gTholeTay[FMM_SER_JMAX + 1][FMM_THOLE_NC][FMM_TAY_N] = FMM_THOLE_TAY_INIT;
-__device__ const float gAmoebaTay[FMM_SER_JMAX + 1][FMM_AMOEBA_NC][FMM_TAY_N] = FMM_AMOEBA_TAY_INIT;
+// interval expansions (FP32 kernels): lanes index them by their own
+// interval, so they live in global memory rather than the constant bank;
+// rows are read as float4s
+__device__ __align__(16) const float gTholeTay[FMM_SER_JMAX + 1][FMM_THOLE_NC][FMM_TAY_N] = FMM_THOLE_TAY_INIT;
+__device__ __align__(16) const float gAmoebaTay[FMM_SER_JMAX + 1][FMM_AMOEBA_NC][FMM_TAY_N] = FMM_AMOEBA_TAY_INIT;
 #endif
 static const double hTholeTay[FMM_SER_JMAX + 1][FMM_THOLE_NC][FMM_TAY_N] = FMM_THOLE_TAY_INIT;
 static const double hAmoebaTay[FMM_SER_JMAX + 1][FMM_AMOEBA_NC][FMM_TAY_N] = FMM_AMOEBA_TAY_INIT;
@@ -66,9 +65,9 @@ struct Real<double> {
     static constexpr int kAmoebaK = 16;
     static constexpr double kErfS = 3.0;     // Boys series for a r^2 below this
     static constexpr int kErfK = 40;
-    static constexpr bool kTay = false;      // re-centred expansions unused in FP64
-    __host__ __device__ static __forceinline__ double thole_tay(int, int, int) { return 0.0; }
-    __host__ __device__ static __forceinline__ double amoeba_tay(int, int, int) { return 0.0; }
+    static constexpr bool kTay = false;      // interval tables unused in FP64
+    __host__ __device__ static __forceinline__ void thole_row(int, int, double*) {}
+    __host__ __device__ static __forceinline__ void amoeba_row(int, int, double*) {}
     __host__ __device__ static __forceinline__ double rsqrt_(double x) {
 #ifdef __CUDA_ARCH__
         return ::rsqrt(x);
@@ -111,27 +110,41 @@ struct Real<double> {
 
 template <>
 struct Real<float> {
-    // series below 1, re-centred expansions on [1, 3) (Thole, x = a r) and
-    // [1, 4) (AMOEBA, u = (a r)^3), closed forms above
-    static constexpr float kTholeX = 1.0f;
-    static constexpr int kTholeK = 18;
-    static constexpr float kAmoebaU = 1.0f;
-    static constexpr int kAmoebaK = 18;
+    // interval tables below 3 (Thole, x = a r) and 4 (AMOEBA, u = (a r)^3):
+    // the series on [0, 1), re-centred expansions on the unit intervals
+    // above; closed forms beyond
     static constexpr bool kTay = true;
-    static constexpr float kTholeHi = 1.0f + FMM_THOLE_NC;
-    static constexpr float kAmoebaHi = 1.0f + FMM_AMOEBA_NC;
-    __host__ __device__ static __forceinline__ float thole_tay(int j, int c, int n) {
+    static constexpr float kTholeHi = (float)FMM_THOLE_NC;
+    static constexpr float kAmoebaHi = (float)FMM_AMOEBA_NC;
+    static_assert(FMM_TAY_N % 4 == 0, "interval rows are read as float4");
+    __host__ __device__ static __forceinline__ void thole_row(int j, int c, float* b) {
 #ifdef __CUDA_ARCH__
-        return __ldg(&gTholeTay[j][c][n]);
+        const float4* r = reinterpret_cast<const float4*>(&gTholeTay[j][c][0]);
+#pragma unroll
+        for (int v = 0; v < FMM_TAY_N / 4; ++v) {
+            const float4 w = __ldg(r + v);
+            b[4 * v] = w.x;
+            b[4 * v + 1] = w.y;
+            b[4 * v + 2] = w.z;
+            b[4 * v + 3] = w.w;
+        }
 #else
-        return (float)hTholeTay[j][c][n];
+        for (int n = 0; n < FMM_TAY_N; ++n) b[n] = (float)hTholeTay[j][c][n];
 #endif
     }
-    __host__ __device__ static __forceinline__ float amoeba_tay(int j, int c, int n) {
+    __host__ __device__ static __forceinline__ void amoeba_row(int j, int c, float* b) {
 #ifdef __CUDA_ARCH__
-        return __ldg(&gAmoebaTay[j][c][n]);
+        const float4* r = reinterpret_cast<const float4*>(&gAmoebaTay[j][c][0]);
+#pragma unroll
+        for (int v = 0; v < FMM_TAY_N / 4; ++v) {
+            const float4 w = __ldg(r + v);
+            b[4 * v] = w.x;
+            b[4 * v + 1] = w.y;
+            b[4 * v + 2] = w.z;
+            b[4 * v + 3] = w.w;
+        }
 #else
-        return (float)hAmoebaTay[j][c][n];
+        for (int n = 0; n < FMM_TAY_N; ++n) b[n] = (float)hAmoebaTay[j][c][n];
 #endif
     }
     static constexpr float kErfS = 6.0f;
@@ -153,20 +166,6 @@ struct Real<float> {
         return 1.0f / (2.0f * i + 1.0f);
 #endif
     }
-    __host__ __device__ static __forceinline__ float thole(int j, int k) {
-#ifdef __CUDA_ARCH__
-        return cTholeSeriesF[j][k];
-#else
-        return (float)hTholeSeries[j][k];
-#endif
-    }
-    __host__ __device__ static __forceinline__ float amoeba(int j, int k) {
-#ifdef __CUDA_ARCH__
-        return cAmoebaSeriesF[j][k];
-#else
-        return (float)hAmoebaSeries[j][k];
-#endif
-    }
     __host__ __device__ static __forceinline__ float amoebaQ(int j, int d) {
 #ifdef __CUDA_ARCH__
         return cAmoebaQF[j][d];
@@ -182,20 +181,21 @@ __host__ __device__ constexpr double dfact_odd(int j) {  // (2j-1)!!, (-1)!! = 1
     return p;
 }
 
-// Whether v lies in the re-centred-expansion range [lo, hi) (FP32 only).
+// Interval of v in the FP32 tables and the offset from its centre (the
+// series on [0, 1) has centre 0, the interval [c, c + 1) above it c + 1/2).
 template <typename R>
-__host__ __device__ __forceinline__ bool tay_interval(R v, R lo, R hi) {
-    return Real<R>::kTay && v >= lo && v < hi;
+__host__ __device__ __forceinline__ R table_offset(R v, int& c) {
+    c = (int)v;
+    return c == 0 ? v : v - ((R)c + (R)0.5);
 }
+
+// Horner sum of one table row at offset t.
 template <typename R>
-__host__ __device__ constexpr R thole_hi() {
-    if constexpr (Real<R>::kTay) return Real<R>::kTholeHi;
-    else return (R)0;
-}
-template <typename R>
-__host__ __device__ constexpr R amoeba_hi() {
-    if constexpr (Real<R>::kTay) return Real<R>::kAmoebaHi;
-    else return (R)0;
+__host__ __device__ __forceinline__ R table_horner(const R* b, R t) {
+    R acc = b[FMM_TAY_N - 1];
+#pragma unroll
+    for (int k = FMM_TAY_N - 2; k >= 0; --k) acc = acc * t + b[k];
+    return acc;
 }
 
 // g_j(r), j = 0..N, of the kernel `damp` at squared distance r2 and pair
@@ -259,25 +259,32 @@ __host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, 
     R num[N + 1];
     if (damp == DAMP_THOLE) {
         const R x = a * (r2 * ir);
-        if (x < RT::kTholeX) {
+        bool closed;
+        if constexpr (RT::kTay) {
+            closed = !(x < RT::kTholeHi);
+            if (!closed) {
+                int c;
+                const R t = table_offset(x, c);
 #pragma unroll
-            for (int j = 0; j <= N; ++j) {
-                R acc = RT::thole(j, RT::kTholeK);
-#pragma unroll 1
-                for (int k = RT::kTholeK - 1; k >= 0; --k) acc = acc * x + RT::thole(j, k);
-                num[j] = acc;
-            }
-        } else if (tay_interval<R>(x, RT::kTholeX, thole_hi<R>())) {
-            const int c = (int)(x - RT::kTholeX);
-            const R t = x - ((R)c + (R)1.5);
-#pragma unroll
-            for (int j = 0; j <= N; ++j) {
-                R acc = RT::thole_tay(j, c, FMM_TAY_N - 1);
-#pragma unroll 1
-                for (int k = FMM_TAY_N - 2; k >= 0; --k) acc = acc * t + RT::thole_tay(j, c, k);
-                num[j] = acc;
+                for (int j = 0; j <= N; ++j) {
+                    R b[FMM_TAY_N];
+                    RT::thole_row(j, c, b);
+                    num[j] = table_horner(b, t);
+                }
             }
         } else {
+            closed = !(x < RT::kTholeX);
+            if (!closed) {
+#pragma unroll
+                for (int j = 0; j <= N; ++j) {
+                    R acc = RT::thole(j, RT::kTholeK);
+#pragma unroll 1
+                    for (int k = RT::kTholeK - 1; k >= 0; --k) acc = acc * x + RT::thole(j, k);
+                    num[j] = acc;
+                }
+            }
+        }
+        if (closed) {
             const R e = RT::exp_(-x);
             const R x2 = x * x;
             R ym1 = (R)1, y0 = -((R)1 + x);  // y_0, y_1 (Yukawa numerators)
@@ -295,25 +302,32 @@ __host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, 
         const R x = a * (r2 * ir);
         const R u = x * x * x;
         num[0] = (R)0;
-        if (u < RT::kAmoebaU) {
+        bool closed;
+        if constexpr (RT::kTay) {
+            closed = !(u < RT::kAmoebaHi);
+            if (!closed) {
+                int c;
+                const R t = table_offset(u, c);
 #pragma unroll
-            for (int j = 1; j <= N; ++j) {
-                R acc = RT::amoeba(j, RT::kAmoebaK);
-#pragma unroll 1
-                for (int k = RT::kAmoebaK - 1; k >= 0; --k) acc = acc * u + RT::amoeba(j, k);
-                num[j] = acc;
-            }
-        } else if (tay_interval<R>(u, RT::kAmoebaU, amoeba_hi<R>())) {
-            const int c = (int)(u - RT::kAmoebaU);
-            const R t = u - ((R)c + (R)1.5);
-#pragma unroll
-            for (int j = 1; j <= N; ++j) {
-                R acc = RT::amoeba_tay(j, c, FMM_TAY_N - 1);
-#pragma unroll 1
-                for (int k = FMM_TAY_N - 2; k >= 0; --k) acc = acc * t + RT::amoeba_tay(j, c, k);
-                num[j] = acc;
+                for (int j = 1; j <= N; ++j) {
+                    R b[FMM_TAY_N];
+                    RT::amoeba_row(j, c, b);
+                    num[j] = table_horner(b, t);
+                }
             }
         } else {
+            closed = !(u < RT::kAmoebaU);
+            if (!closed) {
+#pragma unroll
+                for (int j = 1; j <= N; ++j) {
+                    R acc = RT::amoeba(j, RT::kAmoebaK);
+#pragma unroll 1
+                    for (int k = RT::kAmoebaK - 1; k >= 0; --k) acc = acc * u + RT::amoeba(j, k);
+                    num[j] = acc;
+                }
+            }
+        }
+        if (closed) {
             const R e = RT::exp_(-u);
 #pragma unroll
             for (int j = 1; j <= N; ++j) {
@@ -407,9 +421,37 @@ __host__ __device__ __forceinline__ void pair_field(R dx, R dy, R dz, R a, int d
     contract<M, F, R>(T, Mc, acc);
 }
 
+// contract<2, 1> written with dot products instead of the order-3 tensor:
+// with the source's quadratic form q(R) = sum_{|s|=2} Mc_s R^s, its gradient
+// v = grad q, d = sum_{|s|=1} Mc_s R^s and tr = Mc_xx + Mc_yy + Mc_zz,
+//     sum_s Mc_s T_s       = Mc_0 g_0 + (d + tr) g_1 + q g_2
+//     sum_s Mc_s T_{s+e_a} = R_a (Mc_0 g_1 + (d + tr) g_2 + q g_3)
+//                            + Mc_{e_a} g_1 + v_a g_2
+// (T_{s+e_a} = d/dR_a T_s and d/dR_a g_j = R_a g_{j+1}).  About 35 operations
+// instead of the 75 of the tensor recursion and the full contraction.  tr is
+// supplied by the caller (stored with the source); AMOEBA has g_0 = 0.
+template <typename R>
+__host__ __device__ __forceinline__ void contract_q1(R X, R Y, R Z, const R* g, const R* Mc, R tr, int damp,
+                                                     R* acc) {
+    const R X2 = X + X, Y2 = Y + Y, Z2 = Z + Z;
+    const R vx = Mc[4] * X2 + Mc[5] * Y + Mc[6] * Z;
+    const R vy = Mc[5] * X + Mc[7] * Y2 + Mc[8] * Z;
+    const R vz = Mc[6] * X + Mc[8] * Y + Mc[9] * Z2;
+    const R q = (R)0.5 * (X * vx + Y * vy + Z * vz);
+    const R dtr = Mc[1] * X + Mc[2] * Y + Mc[3] * Z + tr;
+    const R sc = Mc[0] * g[1] + dtr * g[2] + q * g[3];
+    R a0 = dtr * g[1] + q * g[2];
+    if (damp != DAMP_AMOEBA) a0 += Mc[0] * g[0];
+    acc[0] += a0;
+    acc[1] += X * sc + Mc[1] * g[1] + vx * g[2];
+    acc[2] += Y * sc + Mc[2] * g[1] + vy * g[2];
+    acc[3] += Z * sc + Mc[3] * g[1] + vz * g[2];
+}
+
 // FP32 pair with an accurate displacement: r^2 is formed with FMA-captured
 // rounding errors and 1/r refined by one Newton step on the compensated r^2,
 // so 1/r carries about one rounding instead of rsqrtf's few.
+// For M = 2, F = 1, Mc[10] holds the trace Mc_xx + Mc_yy + Mc_zz.
 template <int M, int F>
 __device__ __forceinline__ void pair_field_f32acc(float dx, float dy, float dz, float a, int damp, const float* Mc,
                                                   float* acc) {
@@ -430,9 +472,13 @@ __device__ __forceinline__ void pair_field_f32acc(float dx, float dy, float dz, 
     const float ir_lo = c - (ir - y0);  // exact: |c| << y0
     float g[N + 1];
     radial_g_ir<N, float>(damp, r2, ir, a, g, ir_lo * (r2 * ir));
-    float T[nT(N)];
-    md_tensor<N, float>(dx, dy, dz, g, T);
-    contract<M, F, float>(T, Mc, acc);
+    if constexpr (M == 2 && F == 1) {
+        contract_q1<float>(dx, dy, dz, g, Mc, Mc[10], damp, acc);
+    } else {
+        float T[nT(N)];
+        md_tensor<N, float>(dx, dy, dz, g, T);
+        contract<M, F, float>(T, Mc, acc);
+    }
 }
 
 // Out-of-line variant for cold paths (exclusion fix-ups) to keep code size down.
