@@ -7,9 +7,12 @@
 // pair's expansion order q.  The far pairs are sorted by that key; each group
 // shares one operator G ((q+1)^2 x (q+1)^2, from the restricted tensor T of
 // the group's displacement, computed once per group in FP64), and the group's
-// pairs are the columns of one product C = G W, evaluated by register-tiled
-// blocks on the CUDA cores.  Per-pair columns go to a buffer in target-sorted
-// order and are summed per target in FP64.
+// pairs are the columns of one product C = G W.  FP32 products run on the
+// tensor cores (tcgen05, kind::tf32 with operands split into two TF32 parts,
+// three products per term, FP32 accumulators in tensor memory); FP64
+// products, and FP32 ones on request, on the CUDA cores as register-tiled
+// blocks.  Per-pair columns go to a buffer in target-sorted order and are
+// summed per target with compensated sums.
 //
 // Units: per-node weights w'_s = w^_s / h_j^|s|, per-target locals
 // L'_f = h_i^(|f|+1) L_f, tensor T(D_c) at the displacement in units of the
@@ -20,8 +23,12 @@
 
 #include <cub/cub.cuh>
 
+#include <cstdlib>
+#include <cstring>
+
 #include "internal.h"
 #include "m2l_basis.cuh"
+#include "umma.cuh"
 
 namespace fmm {
 
@@ -165,18 +172,19 @@ __global__ void __launch_bounds__(128) k_group_tensor(int ngroups, const uint64_
     }
 }
 
-__global__ void k_task_counts(int ng, const int32_t* __restrict__ gstart, int32_t* __restrict__ tcnt) {
+// Tasks of up to `cols` pairs of one group: counts, then (group, first column).
+__global__ void k_task_counts(int ng, int cols, const int32_t* __restrict__ gstart, int32_t* __restrict__ tcnt) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g > ng) return;
-    tcnt[g] = g < ng ? (gstart[g + 1] - gstart[g] + kTaskCols - 1) / kTaskCols : 0;
+    tcnt[g] = g < ng ? (gstart[g + 1] - gstart[g] + cols - 1) / cols : 0;
 }
 
-__global__ void k_fill_tasks(int ng, const int32_t* __restrict__ gstart, const int32_t* __restrict__ toff,
+__global__ void k_fill_tasks(int ng, int cols, const int32_t* __restrict__ gstart, const int32_t* __restrict__ toff,
                              int2* __restrict__ tasks) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ng) return;
     const int n = toff[g + 1] - toff[g];
-    for (int k = 0; k < n; ++k) tasks[toff[g] + k] = make_int2(g, k * kTaskCols);
+    for (int k = 0; k < n; ++k) tasks[toff[g] + k] = make_int2(g, k * cols);
 }
 
 // Shared-memory plan of the product kernel (elements of R unless noted).
@@ -259,7 +267,8 @@ __device__ __forceinline__ void load_rows(const R* p, R (&v)[RT]) {
 // memory (L1/L2-resident), VS consecutive s per 16-byte load, so the tile loop
 // needs no block barrier.
 template <typename R, int RT, int CPT>
-__device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, int c_begin, int nrq, int cnt, int gs,
+__device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, int c_begin, int tcols, int nrq,
+                                          int cnt, int gs,
                                           const int32_t* __restrict__ svals, const int32_t* __restrict__ far_src,
                                           const R* __restrict__ wsc, int ldw, R* __restrict__ out, int ldo) {
     constexpr int TN = GemmSmem<R, CPT>::TN;
@@ -276,7 +285,7 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
     int* cpos = reinterpret_cast<int*>(sm + L.off_col);
     int* csrc = cpos + kTaskCols;
     const int nrv = (nrq + VS - 1) / VS * VS;
-    const int c_end = min(cnt, c_begin + kTaskCols);
+    const int c_end = min(cnt, c_begin + tcols);
     // the task's columns: pair positions and source nodes (loaded once)
     for (int i = tid; i < c_end - c_begin; i += kGemmThreads) {
         const int pos = svals[gs + c_begin + i];
@@ -302,7 +311,7 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
 #pragma unroll
         for (int l = 0; l < CPT; ++l) {
             const int c = cb + cg * CPT + l;
-            pos[l] = c < c_end ? cpos[c - c_begin] : -1;
+            pos[l] = c < c_end ? gs + c : -1;  // result row: the pair's place in group order
             wp[l] = pos[l] >= 0 ? reinterpret_cast<const V*>(wsc + (size_t)csrc[c - c_begin] * ldw) : nullptr;
         }
         R acc[RT][CPT];
@@ -352,20 +361,25 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
     }
 }
 
+// tcols: pairs per task (at most kTaskCols); tasks of order < qmin are left
+// to the tensor-core kernel.
 template <typename R, int CPT>
-__global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restrict__ tasks, int p,
+__global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restrict__ tasks, int tcols, int qmin,
+                                                           int p,
                                                            const int32_t* __restrict__ gstart,
                                                            const int32_t* __restrict__ gq,
                                                            const float2* __restrict__ gab, const R* __restrict__ gT,
                                                            int ldT, const int32_t* __restrict__ svals,
                                                            const int32_t* __restrict__ far_src,
-                                                           const R* __restrict__ wsc, R* __restrict__ out) {
+                                                           const R* __restrict__ wsc, R* __restrict__ out,
+                                                           int ldo) {
     extern __shared__ __align__(16) char sm_gemm[];
     const GemmSmem<R, CPT> L(p);
     const int nr = (p + 1) * (p + 1);
     const int2 task = tasks[blockIdx.x];
     const int g = task.x;
     const int q = gq[g], nrq = (q + 1) * (q + 1);
+    if (q < qmin) return;
     const int gs = gstart[g], cnt = gstart[g + 1] - gs;
     int* dec = reinterpret_cast<int*>(sm_gemm + L.off_dec);
     R* apow = reinterpret_cast<R*>(sm_gemm + L.off_pow);
@@ -389,7 +403,8 @@ __global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restric
     switch (rt) {
 #define FMM_GEMM_CASE(K)                                                                                     \
     case K:                                                                                                  \
-        gemm_task<R, K, CPT>(L, sm_gemm, task.y, nrq, cnt, gs, svals, far_src, wsc, wsc_ld<R>(nr), out, nr); \
+        gemm_task<R, K, CPT>(L, sm_gemm, task.y, tcols, nrq, cnt, gs, svals, far_src, wsc, wsc_ld<R>(nr), out, \
+                             ldo);                                                                            \
         break;
         FMM_GEMM_CASE(1)
         FMM_GEMM_CASE(2)
@@ -406,6 +421,335 @@ __global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restric
         default:
             break;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core product, for groups of order q <= 10 ((q+1)^2 <= 128).  A task
+// is up to 256 pairs of one group: D = G W^T with G the operator (f x s,
+// M = 128 rows f), W the pairs' weights (pairs x s, N = 256) and K = (q+1)^2
+// in chunks of 8 (one MMA K step).  Both operands are split into TF32 parts,
+// x = hi + lo, and D accumulates G_hi W_hi + G_hi W_lo + G_lo W_hi in FP32
+// (the dropped G_lo W_lo and the rounding of the parts leave about 2^-22 of
+// each term).  The parts are prepared once in global memory in the operand
+// layout: per node the weights, per group the operator, chunk by chunk.
+// Warp roles in a persistent block (one per SM):
+//   warps 0-1  producers: per chunk, one bulk (TMA) copy of the operator
+//              chunk and 16-byte cp.async gathers of the 256 pairs' weights
+//              into a ring of shared-memory stages, completing on the
+//              stage's full mbarrier; a stage is refilled once the MMAs that
+//              read it have committed to its empty mbarrier;
+//   warp 2     one thread issues the MMAs into one of two tensor-memory
+//              accumulators (256 columns each) and commits the finished task;
+//   warps 3-6  epilogue: each reads its 32 tensor-memory lanes (rows f) and
+//              writes, per pair, 32 consecutive entries of the pair's result
+//              row (128-byte stores), then frees the accumulator.
+// The two accumulators let the epilogue of one task overlap the MMAs of the
+// next.  Groups of higher order go to the CUDA-core kernel.
+constexpr int kTcMaxQ = 10;
+constexpr int kTcRows = 128;       // MMA M: operator rows f
+constexpr int kTcPairs = 256;      // MMA N: pairs per task
+constexpr int kTcKC = 8;           // reduced components per chunk (one MMA K step)
+constexpr int kTcStages = 8;
+constexpr int kTcProducers = 64;   // warps 0-1
+constexpr int kTcMmaWarp = 2;
+constexpr int kTcThreads = 224;
+constexpr uint32_t kTcCols = 512;  // two accumulators of kTcPairs columns
+constexpr long long kTcWaitCycles = 4000000000LL;  // about 2 s at 2 GHz
+
+// Float offset of element (r, k) in a K-major, unswizzled chunk kTcKC wide:
+// core matrices of 8 rows x 4 elements (128 bytes), K-adjacent ones 128 bytes
+// apart (LBO), row groups kTcKC / 4 * 128 bytes apart (SBO).
+__host__ __device__ __forceinline__ int tc_off(int r, int k) {
+    return (r >> 3) * (kTcKC * 8) + (k >> 2) * 32 + (r & 7) * 4 + (k & 3);
+}
+
+struct TcSmem {
+    static constexpr int g_floats = kTcRows * kTcKC;   // one TF32 part of an operator chunk
+    static constexpr int w_floats = kTcPairs * kTcKC;  // one TF32 part of a weight chunk
+    static constexpr size_t stage_bytes = sizeof(float) * 2 * (g_floats + w_floats);
+    static constexpr size_t off_bar = kTcStages * stage_bytes;
+    // full[S], empty[S], acc_full[2], acc_empty[2]
+    static constexpr size_t off_tmem = off_bar + sizeof(uint64_t) * (2 * kTcStages + 4);
+    static constexpr size_t bytes = off_tmem + 16;
+};
+
+// Per-node weights as TF32 parts, chunk by chunk: [chunk][hi KC | lo KC].
+__global__ void k_split_weights(int64_t total, int nr, int ldw, int ldk, const float* __restrict__ wsc,
+                                float* __restrict__ wsp) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = e / ldk;
+        const int s = (int)(e - node * ldk);
+        const float v = s < nr ? wsc[node * ldw + s] : 0.0f;
+        float h, l;
+        umma::split_tf32(v, h, l);
+        float* o = wsp + node * 2 * ldk + (s / kTcKC) * 2 * kTcKC + (s % kTcKC);
+        o[0] = h;
+        o[kTcKC] = l;
+    }
+}
+
+// Place of every far pair (target order) in group order: inv[svals[k]] = k.
+__global__ void k_inverse_perm(int64_t nf, const int32_t* __restrict__ svals, int32_t* __restrict__ inv) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k < nf) inv[svals[k]] = (int32_t)k;
+}
+
+// Source node of every far pair in group order: psrc[k] = far_src[svals[k]].
+__global__ void k_pair_sources(int64_t nf, const int32_t* __restrict__ svals, const int32_t* __restrict__ far_src,
+                               int32_t* __restrict__ psrc) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k < nf) psrc[k] = far_src[svals[k]];
+}
+
+// Size in floats of a group's split operator (chunks x (hi + lo) x 128 x KC);
+// zero for the groups the CUDA cores take.
+__global__ void k_gop_sizes(int ng, const int32_t* __restrict__ gq, int64_t* __restrict__ sz) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g > ng) return;
+    if (g == ng || gq[g] > kTcMaxQ) {
+        sz[g] = 0;
+        return;
+    }
+    const int nrq = (gq[g] + 1) * (gq[g] + 1), nch = (nrq + kTcKC - 1) / kTcKC;
+    sz[g] = (int64_t)nch * 2 * kTcRows * kTcKC;
+}
+
+// Block per group: G_fs = a^(|f|+1) b^|s| T_{f+s}(D_c) split into TF32 parts,
+// written chunk by chunk in the operand layout: [chunk][hi 128 x KC][lo 128 x KC].
+__global__ void __launch_bounds__(256) k_group_operator(int ldT, const float* __restrict__ gT,
+                                                        const int32_t* __restrict__ gq,
+                                                        const float2* __restrict__ gab,
+                                                        const int64_t* __restrict__ goff, float* __restrict__ gop) {
+    __shared__ int dec[(kTcMaxQ + 1) * (kTcMaxQ + 1)];
+    __shared__ float apow[32], bpow[32];
+    __shared__ float Tsh[1 + 3 * (2 * kTcMaxQ) * (2 * kTcMaxQ + 1) / 2];
+    const int g = blockIdx.x;
+    const int q = gq[g];
+    if (q > kTcMaxQ) return;
+    const int nrq = (q + 1) * (q + 1), nch = (nrq + kTcKC - 1) / kTcKC;
+    for (int e = threadIdx.x; e < nrq; e += blockDim.x) dec[e] = qcomp(e);
+    if (threadIdx.x < 32) {
+        const float2 ab = gab[g];
+        float a = 1.0f, b = 1.0f;
+        for (int u = 0; u < (int)threadIdx.x; ++u) {
+            a *= ab.x;
+            b *= ab.y;
+        }
+        apow[threadIdx.x] = a;
+        bpow[threadIdx.x] = b;
+    }
+    const int nTq = rbase(2 * q + 1);
+    for (int e = threadIdx.x; e < nTq; e += blockDim.x) Tsh[e] = gT[(size_t)g * ldT + e];
+    __syncthreads();
+    float* out = gop + goff[g];
+    const int kp = nch * kTcKC;
+    for (int e = threadIdx.x; e < kTcRows * kp; e += blockDim.x) {
+        const int n = e / kp, s = e - n * kp;
+        float v = 0.0f;
+        if (n < nrq && s < nrq) {
+            const int cs = dec[s], cf = dec[n];
+            const int x = (cs & 0xff) + (cf & 0xff), y = ((cs >> 8) & 0xff) + ((cf >> 8) & 0xff),
+                      z = ((cs >> 16) & 0xff) + ((cf >> 16) & 0xff);
+            v = apow[(cf >> 24) + 1] * bpow[cs >> 24] * Tsh[ridx(x, y, z)];
+        }
+        float h, l;
+        umma::split_tf32(v, h, l);
+        float* o = out + (size_t)(s / kTcKC) * 2 * kTcRows * kTcKC + tc_off(n, s % kTcKC);
+        o[0] = h;
+        o[kTcRows * kTcKC] = l;
+    }
+}
+
+// Next task index >= t of this block's stride that the tensor cores take.
+__device__ __forceinline__ int tc_next_task(int t, int ntasks, const int2* __restrict__ tasks,
+                                            const int32_t* __restrict__ gq) {
+    while (t < ntasks && gq[tasks[t].x] > kTcMaxQ) t += gridDim.x;
+    return t;
+}
+
+// Source nodes of a producer thread's rows 8 (rg0 + 2k) + rsub of task t.
+template <int RG>
+__device__ __forceinline__ void tc_load_rows(int t, const int2* __restrict__ tasks, const int32_t* __restrict__ gstart,
+                                             const int32_t* __restrict__ psrc, int rg0, int rsub, int (&r)[RG]) {
+    const int2 tk = tasks[t];
+    const int gs = gstart[tk.x] + tk.y, cnt = min(kTcPairs, gstart[tk.x + 1] - gs);
+#pragma unroll
+    for (int k = 0; k < RG; ++k) {
+        const int pr = 8 * (rg0 + 2 * k) + rsub;
+        r[k] = pr < cnt ? psrc[gs + pr] : -1;
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict__ tasks, int ntasks,
+                                                         const int32_t* __restrict__ gstart,
+                                                         const int32_t* __restrict__ gq,
+                                                         const int64_t* __restrict__ goff,
+                                                         const float* __restrict__ gop,
+                                                         const int32_t* __restrict__ psrc,
+                                                         const float* __restrict__ wsp, int ldk,
+                                                         float* __restrict__ out, int ldo, int* __restrict__ err) {
+    extern __shared__ __align__(1024) char sm_tc[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm_tc + TcSmem::off_bar);
+    uint64_t* empty = full + kTcStages;
+    uint64_t* acc_full = empty + kTcStages;
+    uint64_t* acc_empty = acc_full + 2;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm_tc + TcSmem::off_tmem);
+    if (warp == 0) {
+        umma::tmem_alloc(tslot, kTcCols);
+        umma::tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int st = 0; st < kTcStages; ++st) {
+            umma::mbar_init(&full[st], kTcProducers + 1);  // producers' cp.async arrivals + the bulk copy's
+            umma::mbar_init(&empty[st], 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            umma::mbar_init(&acc_full[a], 1);
+            umma::mbar_init(&acc_empty[a], 4);  // one arrival per epilogue warp
+        }
+        umma::mbar_fence_init();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    bool ok = true;
+    if (warp < kTcProducers / 32) {
+        // ---- producers.  Each gather instruction covers one 8-row group x
+        // (hi, lo) x two 16-byte pieces, which spreads its 512 bytes over all
+        // shared-memory banks; a thread keeps its 16 rows' source nodes (-1:
+        // no pair) in registers, loaded one task ahead.
+        const int pt = tid, plane = tid & 31;
+        const int part = plane >> 4, j = (plane >> 3) & 1, rsub = plane & 7;
+        constexpr int RG = kTcPairs / 8 / (kTcProducers / 32);  // row groups per thread
+        const int rg0 = pt >> 5;
+        const uint64_t keep = umma::l2_evict_last();  // the weights stay in L2 beside the result stream
+        uint32_t u = 0;
+        int task = tc_next_task(blockIdx.x, ntasks, tasks, gq);
+        int rows[RG], nrows[RG];
+        if (task < ntasks) tc_load_rows<RG>(task, tasks, gstart, psrc, rg0, rsub, rows);
+        while (task < ntasks && ok) {
+            const int g = tasks[task].x, q = gq[g];
+            const int nch = ((q + 1) * (q + 1) + kTcKC - 1) / kTcKC;
+            const int next = tc_next_task(task + gridDim.x, ntasks, tasks, gq);
+            if (next < ntasks) tc_load_rows<RG>(next, tasks, gstart, psrc, rg0, rsub, nrows);  // in flight
+            const float* G = gop + goff[g];
+            for (int ch = 0; ch < nch; ++ch, ++u) {
+                const int st = (int)(u % kTcStages);
+                if (u >= (uint32_t)kTcStages &&
+                    !umma::mbar_wait(&empty[st], ((u / kTcStages) - 1) & 1, kTcWaitCycles)) {
+                    ok = false;
+                    break;
+                }
+                float* Gs = reinterpret_cast<float*>(sm_tc + (size_t)st * TcSmem::stage_bytes);
+                float* Ws = Gs + 2 * TcSmem::g_floats;
+                if (pt == 0) {
+                    constexpr uint32_t gb = sizeof(float) * 2 * TcSmem::g_floats;
+                    umma::mbar_arrive_expect_tx(&full[st], gb);
+                    umma::bulk_g2s(Gs, G + (size_t)ch * 2 * TcSmem::g_floats, gb, &full[st]);
+                }
+                float* dst0 = Ws + part * TcSmem::w_floats + 4 * j * 8 + rsub * 4;  // tc_off(8 rg + rsub, 4 j)
+                const int coff = ch * 2 * kTcKC + part * kTcKC + 4 * j;
+#pragma unroll
+                for (int k = 0; k < RG; ++k) {
+                    const int src = rows[k];
+                    const float* gsrc = src >= 0 ? wsp + (size_t)src * 2 * ldk + coff : wsp;
+                    umma::cp16_keep(dst0 + (rg0 + 2 * k) * kTcKC * 8, gsrc, src >= 0, keep);
+                }
+                umma::cp_async_mbar_arrive(&full[st]);
+            }
+#pragma unroll
+            for (int k = 0; k < RG; ++k) rows[k] = nrows[k];
+            task = next;
+        }
+    } else if (warp == kTcMmaWarp) {
+        // ---- MMA issue (one thread)
+        if (lane == 0) {
+            uint32_t u = 0, tl = 0;
+            const uint32_t idesc = umma::idesc_tf32(kTcRows, kTcPairs);
+            constexpr uint32_t LBO = 128, SBO = kTcKC / 4 * 128;
+            for (int task = blockIdx.x; task < ntasks && ok; task += gridDim.x) {
+                const int g = tasks[task].x, q = gq[g];
+                if (q > kTcMaxQ) continue;
+                const int nch = ((q + 1) * (q + 1) + kTcKC - 1) / kTcKC;
+                const int acc = (int)(tl & 1);
+                if (tl >= 2 && !umma::mbar_wait(&acc_empty[acc], ((tl >> 1) - 1) & 1, kTcWaitCycles)) {
+                    ok = false;
+                    break;
+                }
+                umma::fence_after_sync();
+                const uint32_t d = tmem + (uint32_t)(acc * kTcPairs);
+                for (int ch = 0; ch < nch; ++ch, ++u) {
+                    const int st = (int)(u % kTcStages);
+                    if (!umma::mbar_wait(&full[st], (u / kTcStages) & 1, kTcWaitCycles)) {
+                        ok = false;
+                        break;
+                    }
+                    umma::fence_proxy_async();  // the cp.async data, for the tensor cores
+                    umma::fence_after_sync();
+                    const float* Gs = reinterpret_cast<const float*>(sm_tc + (size_t)st * TcSmem::stage_bytes);
+                    const float* Ws = Gs + 2 * TcSmem::g_floats;
+                    const uint64_t gh = umma::smem_desc(Gs, LBO, SBO);
+                    const uint64_t gl = umma::smem_desc(Gs + TcSmem::g_floats, LBO, SBO);
+                    const uint64_t wh = umma::smem_desc(Ws, LBO, SBO);
+                    const uint64_t wl = umma::smem_desc(Ws + TcSmem::w_floats, LBO, SBO);
+                    umma::mma_tf32(d, gh, wh, idesc, ch > 0 ? 1u : 0u);
+                    umma::mma_tf32(d, gh, wl, idesc, 1u);
+                    umma::mma_tf32(d, gl, wh, idesc, 1u);
+                    umma::commit(&empty[st]);
+                }
+                if (!ok) break;
+                umma::commit(&acc_full[acc]);
+                ++tl;
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31
+        const int sp = warp & 3;
+        const int f = 32 * sp + lane;
+        uint32_t tl = 0;
+        for (int task = blockIdx.x; task < ntasks && ok; task += gridDim.x) {
+            const int2 tk = tasks[task];
+            const int g = tk.x, q = gq[g];
+            if (q > kTcMaxQ) continue;
+            const int gs = gstart[g] + tk.y;
+            const int cnt = min(kTcPairs, gstart[g + 1] - gs);
+            const int acc = (int)(tl & 1);
+            if (!umma::mbar_wait(&acc_full[acc], (tl >> 1) & 1, kTcWaitCycles)) {
+                ok = false;
+                break;
+            }
+            umma::fence_after_sync();
+            const uint32_t base = tmem + ((uint32_t)(32 * sp) << 16) + (uint32_t)(acc * kTcPairs);
+            const bool tail = sp == 0 && ldo > kTcRows;  // entries beyond the 128 operator rows
+#pragma unroll 1
+            for (int c = 0; c < cnt; c += 16) {
+                float v[16];
+                umma::tmem_ld16(base + (uint32_t)c, v);
+                umma::tmem_ld_wait();
+                // the task's rows are consecutive (group order); streaming stores
+#pragma unroll
+                for (int jj = 0; jj < 16; ++jj) {
+                    if (c + jj < cnt) {
+                        float* row = out + (size_t)(gs + c + jj) * ldo;
+                        if (f < ldo) __stcs(row + f, v[jj]);
+                        if (tail)
+                            for (int e = kTcRows + lane; e < ldo; e += 32) __stcs(row + e, 0.0f);
+                    }
+                }
+            }
+            umma::fence_before_sync();
+            __syncwarp();  // also: spos is rewritten by the next task
+            if (lane == 0) umma::mbar_arrive(&acc_empty[acc]);
+            ++tl;
+        }
+    }
+    if (!ok) atomicExch(err, 1);
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, kTcCols);
 }
 
 // Running sum of one output: FP32 values as a double-float pair (TwoSum, on
@@ -431,11 +775,12 @@ struct Sum<double> {
 };
 
 // Block per target, thread per reduced component: compensated sum of the
-// target's pair rows (contiguous in target order, eight loads in flight),
-// back to physical units, into the reduced components of the local expansion.
+// target's pair rows (stored in group order; inv maps a pair's target-order
+// index to its row; eight loads in flight), back to physical units, into the
+// reduced components of the local expansion.
 template <typename R>
-__global__ void __launch_bounds__(128) k_m2l_sum(const TreeDev t, int p, const R* __restrict__ out,
-                                                 double* __restrict__ loc) {
+__global__ void __launch_bounds__(128) k_m2l_sum(const TreeDev t, int p, const R* __restrict__ out, int ldo,
+                                                 const int32_t* __restrict__ inv, double* __restrict__ loc) {
     const int i = blockIdx.x;
     const int nr = (p + 1) * (p + 1);
     const int q0 = t.far_off[i], q1 = t.far_off[i + 1];
@@ -448,11 +793,11 @@ __global__ void __launch_bounds__(128) k_m2l_sum(const TreeDev t, int p, const R
         for (; q + U <= q1; q += U) {
             R v[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) v[u] = out[(size_t)(q + u) * nr + f];
+            for (int u = 0; u < U; ++u) v[u] = out[(size_t)inv[q + u] * ldo + f];
 #pragma unroll
             for (int u = 0; u < U; ++u) acc.add(v[u]);
         }
-        for (; q < q1; ++q) acc.add(out[(size_t)q * nr + f]);
+        for (; q < q1; ++q) acc.add(out[(size_t)inv[q] * ldo + f]);
         const int c = qcomp(f);
         const int k = c >> 24;
         double s = ih;
@@ -461,11 +806,22 @@ __global__ void __launch_bounds__(128) k_m2l_sum(const TreeDev t, int p, const R
     }
 }
 
+// FP32 products on the CUDA cores instead of the tensor cores
+// (FMM_GB300_M2L_PRODUCT=cuda; read at every call).
+bool product_on_cuda_cores() {
+    const char* e = std::getenv("FMM_GB300_M2L_PRODUCT");
+    return e && std::strcmp(e, "cuda") == 0;
+}
+
 template <typename R, int CPT>
 int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
     const int M = t.num_nodes, nr = (p + 1) * (p + 1), N = 2 * p, nTr = rbase(N + 1);
+    const int ldo = (nr + 3) & ~3;  // result rows of 16-byte multiples
+    const bool tc = sizeof(R) == 4 && !product_on_cuda_cores();
+    const int cols = tc ? kTcPairs : kTaskCols;
     const int64_t nf = t.nfar;
-    FMM_TRY(ws.m2l_out.ensure(sizeof(R) * (size_t)std::max<int64_t>(1, nf) * nr));
+    FMM_TRY(ws.m2l_out.ensure(sizeof(R) * (size_t)std::max<int64_t>(1, nf) * ldo));
+    const int32_t* inv = nullptr;  // row of each far pair (target order) in group order
     if (nf > 0) {
         FMM_TRY(ws.m2l_tgt.ensure(sizeof(int32_t) * nf));
         FMM_TRY(ws.m2l_keys.ensure(sizeof(uint64_t) * nf));
@@ -504,6 +860,12 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_CUDA_TRY(cub::DeviceRunLengthEncode::Encode(ws.cub_tmp.p, tb2, ws.m2l_keys2.as<uint64_t>(),
                                                         ws.m2l_ukeys.as<uint64_t>(), ws.m2l_cnt.as<int32_t>(),
                                                         d_nruns, (int)nf, st));
+        // result rows are written in group order; the per-target sum reads
+        // them through the inverse permutation (in the free unsorted-keys buffer)
+        count_launches(1);
+        k_inverse_perm<<<grid_for(nf, 256), 256, 0, st>>>(nf, ws.m2l_vals2.as<int32_t>(),
+                                                          reinterpret_cast<int32_t*>(ws.m2l_keys.p));
+        inv = reinterpret_cast<const int32_t*>(ws.m2l_keys.p);
         int ng = 0;
         FMM_CUDA_TRY(cudaMemcpyAsync(&ng, d_nruns, sizeof(int), cudaMemcpyDeviceToHost, st));
         FMM_CUDA_TRY(cudaStreamSynchronize(st));
@@ -534,7 +896,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_TRY(ws.m2l_tcnt.ensure(sizeof(int32_t) * (ng + 1)));
         FMM_TRY(ws.m2l_toff.ensure(sizeof(int32_t) * (ng + 1)));
         count_launches(1);
-        k_task_counts<<<grid_for(ng + 1, 256), 256, 0, st>>>(ng, ws.m2l_gstart.as<int32_t>(),
+        k_task_counts<<<grid_for(ng + 1, 256), 256, 0, st>>>(ng, cols, ws.m2l_gstart.as<int32_t>(),
                                                               ws.m2l_tcnt.as<int32_t>());
         size_t tb5 = 0;
         cub::DeviceScan::ExclusiveSum(nullptr, tb5, ws.m2l_tcnt.as<int32_t>(), ws.m2l_toff.as<int32_t>(), ng + 1, st);
@@ -546,24 +908,87 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_CUDA_TRY(cudaStreamSynchronize(st));
         FMM_TRY(ws.m2l_tasks.ensure(sizeof(int2) * std::max(1, ntasks)));
         count_launches(1);
-        k_fill_tasks<<<grid_for(ng, 256), 256, 0, st>>>(ng, ws.m2l_gstart.as<int32_t>(), ws.m2l_toff.as<int32_t>(),
-                                                        ws.m2l_tasks.as<int2>());
-        const GemmSmem<R, CPT> L(p);
-        FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_m2l_gemm<R, CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)L.bytes));
-        if (ws.events_ready) {
-            cudaEventRecord(ws.ev[8], st);
-            ws.product_timed = true;
+        k_fill_tasks<<<grid_for(ng, 256), 256, 0, st>>>(ng, cols, ws.m2l_gstart.as<int32_t>(),
+                                                        ws.m2l_toff.as<int32_t>(), ws.m2l_tasks.as<int2>());
+        int* d_err = reinterpret_cast<int*>(ws.counters.as<unsigned long long>() + 13);
+        if (tc) {
+            // TF32 parts of the weights (per node) and of the operators (per group)
+            const int ldk = (nr + 15) / 16 * 16;
+            FMM_TRY(ws.m2l_wsplit.ensure(sizeof(float) * 2 * (size_t)M * ldk));
+            count_launches(1);
+            k_split_weights<<<grid_for((int64_t)M * ldk, 256), 256, 0, st>>>(
+                (int64_t)M * ldk, nr, ldw, ldk, reinterpret_cast<const float*>(ws.m2l_wsc.p), ws.m2l_wsplit.as<float>());
+            // source node per sorted pair (into the free unsorted-values buffer)
+            count_launches(1);
+            k_pair_sources<<<grid_for(nf, 256), 256, 0, st>>>(nf, ws.m2l_vals2.as<int32_t>(), t.far_src,
+                                                              ws.m2l_vals.as<int32_t>());
+            FMM_TRY(ws.m2l_gopoff.ensure(sizeof(int64_t) * (ng + 1)));
+            int64_t* goff = ws.m2l_gopoff.as<int64_t>();
+            count_launches(1);
+            k_gop_sizes<<<grid_for(ng + 1, 256), 256, 0, st>>>(ng, ws.m2l_gq.as<int32_t>(), goff);
+            size_t tb6 = 0;
+            cub::DeviceScan::ExclusiveSum(nullptr, tb6, goff, goff, ng + 1, st);
+            FMM_TRY(ws.cub_tmp.ensure(tb6));
+            FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb6, goff, goff, ng + 1, st));
+            int64_t gop_total = 0;
+            FMM_CUDA_TRY(cudaMemcpyAsync(&gop_total, goff + ng, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+            FMM_CUDA_TRY(cudaStreamSynchronize(st));
+            FMM_TRY(ws.m2l_gop.ensure(sizeof(float) * (size_t)std::max<int64_t>(1, gop_total)));
+            count_launches(1);
+            k_group_operator<<<(unsigned)ng, 256, 0, st>>>(ldT, reinterpret_cast<const float*>(ws.m2l_T.p),
+                                                           ws.m2l_gq.as<int32_t>(), ws.m2l_gab.as<float2>(), goff,
+                                                           ws.m2l_gop.as<float>());
+            FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)TcSmem::bytes));
+            int dev = 0, sms = 0;
+            FMM_CUDA_TRY(cudaGetDevice(&dev));
+            FMM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            const int grid = std::max(1, std::min(ntasks, sms));  // one block per SM (all tensor memory)
+            FMM_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+            if (ws.events_ready) {
+                cudaEventRecord(ws.ev[8], st);
+                ws.product_timed = true;
+            }
+            count_launches(1);
+            k_m2l_tc<<<(unsigned)grid, kTcThreads, TcSmem::bytes, st>>>(
+                ws.m2l_tasks.as<int2>(), ntasks, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(), goff,
+                ws.m2l_gop.as<float>(), ws.m2l_vals.as<int32_t>(), ws.m2l_wsplit.as<float>(), ldk,
+                reinterpret_cast<float*>(ws.m2l_out.p), ldo, d_err);
+            if (p > kTcMaxQ) {
+                // groups of order > 10 on the CUDA cores
+                const GemmSmem<float, CPT> L(p);
+                FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_m2l_gemm<float, CPT>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes));
+                count_launches(1);
+                k_m2l_gemm<float, CPT><<<(unsigned)ntasks, kGemmThreads, L.bytes, st>>>(
+                    ws.m2l_tasks.as<int2>(), cols, kTcMaxQ + 1, p, ws.m2l_gstart.as<int32_t>(),
+                    ws.m2l_gq.as<int32_t>(), ws.m2l_gab.as<float2>(), reinterpret_cast<const float*>(ws.m2l_T.p),
+                    ldT, ws.m2l_vals2.as<int32_t>(), t.far_src, reinterpret_cast<const float*>(ws.m2l_wsc.p),
+                    reinterpret_cast<float*>(ws.m2l_out.p), ldo);
+            }
+            if (ws.product_timed) cudaEventRecord(ws.ev[9], st);
+            int herr = 0;
+            FMM_CUDA_TRY(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+            FMM_CUDA_TRY(cudaStreamSynchronize(st));
+            if (herr) return FMM_ETIMEOUT;
+        } else {
+            const GemmSmem<R, CPT> L(p);
+            FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_m2l_gemm<R, CPT>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes));
+            if (ws.events_ready) {
+                cudaEventRecord(ws.ev[8], st);
+                ws.product_timed = true;
+            }
+            count_launches(1);
+            k_m2l_gemm<R, CPT><<<(unsigned)ntasks, kGemmThreads, L.bytes, st>>>(
+                ws.m2l_tasks.as<int2>(), cols, 0, p, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(),
+                ws.m2l_gab.as<float2>(), ws.m2l_T.as<R>(), ldT, ws.m2l_vals2.as<int32_t>(), t.far_src,
+                ws.m2l_wsc.as<R>(), ws.m2l_out.as<R>(), ldo);
+            if (ws.product_timed) cudaEventRecord(ws.ev[9], st);
         }
-        count_launches(1);
-        k_m2l_gemm<R, CPT><<<(unsigned)ntasks, kGemmThreads, L.bytes, st>>>(
-            ws.m2l_tasks.as<int2>(), p, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(),
-            ws.m2l_gab.as<float2>(), ws.m2l_T.as<R>(), ldT, ws.m2l_vals2.as<int32_t>(), t.far_src,
-            ws.m2l_wsc.as<R>(), ws.m2l_out.as<R>());
-        if (ws.product_timed) cudaEventRecord(ws.ev[9], st);
     }
     count_launches(1);
-    k_m2l_sum<R><<<(unsigned)M, 128, 0, st>>>(t, p, ws.m2l_out.as<R>(), ws.loc.as<double>());
+    k_m2l_sum<R><<<(unsigned)M, 128, 0, st>>>(t, p, ws.m2l_out.as<R>(), ldo, inv, ws.loc.as<double>());
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }

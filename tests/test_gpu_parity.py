@@ -205,6 +205,25 @@ def test_damping_aware_acceptance_matches_oracle(damp):
     assert rel_err(G, D, slice(1, 4)) < rel_err(G0, D, slice(1, 4))
 
 
+@pytest.mark.parametrize("p", [3, 10, 12])
+def test_m2l_tensor_core_product_matches_cuda_cores(p, monkeypatch):
+    """The FP32 M2L product on the tensor cores (operands split into TF32
+    parts, three products per term, FP32 accumulation in tensor memory) agrees
+    with the same product on the CUDA cores and with the FP64 path."""
+    from fmm_gb300 import systems
+    s = systems.water(4000, 70.0, order=2, seed=21)
+    d = s["damping_factors"]
+    mixed = Options.exact(precision="mixed")
+    F64 = fmm_gb300.field_fmm(*_fmm_args(s), 0.4, 64, p, 1, "AMOEBA", d, options=Options.exact())
+    Ftc = fmm_gb300.field_fmm(*_fmm_args(s), 0.4, 64, p, 1, "AMOEBA", d, options=mixed)
+    assert fmm_gb300.last_stats()["m2l_pairs"] > 0
+    monkeypatch.setenv("FMM_GB300_M2L_PRODUCT", "cuda")
+    Fcc = fmm_gb300.field_fmm(*_fmm_args(s), 0.4, 64, p, 1, "AMOEBA", d, options=mixed)
+    assert np.all(np.isfinite(Ftc))
+    assert rel_err(Ftc, Fcc, slice(1, None)) < 2e-6
+    assert rel_err(Ftc, F64, slice(1, None)) < 5e-6
+
+
 @pytest.mark.parametrize("damp,mf", [("AMOEBA", (2, 1)), ("", (2, 2)), ("ERF", (1, 1)), ("THOLE", (0, 1))])
 def test_mixed_precision_close_to_fp64(damp, mf):
     """FP32 near field and M2L with FP64 sums: within FP32 accuracy of the FP64
