@@ -440,9 +440,11 @@ __global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restric
 //              read it have committed to its empty mbarrier;
 //   warp 2     one thread issues the MMAs into one of two tensor-memory
 //              accumulators (256 columns each) and commits the finished task;
-//   warps 3-6  epilogue: each reads its 32 tensor-memory lanes (rows f) and
-//              writes, per pair, 32 consecutive entries of the pair's result
-//              row (128-byte stores), then frees the accumulator.
+//   warps 3+   epilogue (four per tensor-memory sub-partition, each a
+//              quarter of the columns): each reads its 32 lanes (rows f),
+//              32 columns (pairs) per wait, and writes, per pair, 32
+//              consecutive entries of the pair's result row (one aligned
+//              128-byte line), then frees the accumulator.
 // The two accumulators let the epilogue of one task overlap the MMAs of the
 // next.  Groups of higher order go to the CUDA-core kernel.
 constexpr int kTcMaxQ = 10;
@@ -452,7 +454,9 @@ constexpr int kTcKC = 8;           // reduced components per chunk (one MMA K st
 constexpr int kTcStages = 8;
 constexpr int kTcProducers = 64;   // warps 0-1
 constexpr int kTcMmaWarp = 2;
-constexpr int kTcThreads = 224;
+constexpr int kTcEpiWarps = 16;    // warps 3 .. 2 + kTcEpiWarps
+constexpr int kTcThreads = 32 * (3 + kTcEpiWarps);
+constexpr int kTcEpiBatch = 2;     // tensor-memory loads (16 columns each) per wait
 constexpr uint32_t kTcCols = 512;  // two accumulators of kTcPairs columns
 constexpr long long kTcWaitCycles = 4000000000LL;  // about 2 s at 2 GHz
 
@@ -567,7 +571,7 @@ __device__ __forceinline__ int tc_next_task(int t, int ntasks, const int2* __res
     return t;
 }
 
-// Source nodes of a producer thread's rows 8 (rg0 + 2k) + rsub of task t.
+// Source nodes of a producer thread's rows 8 (rg0 + k * producer warps) + rsub of task t.
 template <int RG>
 __device__ __forceinline__ void tc_load_rows(int t, const int2* __restrict__ tasks, const int32_t* __restrict__ gstart,
                                              const int32_t* __restrict__ psrc, int rg0, int rsub, int (&r)[RG]) {
@@ -575,7 +579,7 @@ __device__ __forceinline__ void tc_load_rows(int t, const int2* __restrict__ tas
     const int gs = gstart[tk.x] + tk.y, cnt = min(kTcPairs, gstart[tk.x + 1] - gs);
 #pragma unroll
     for (int k = 0; k < RG; ++k) {
-        const int pr = 8 * (rg0 + 2 * k) + rsub;
+        const int pr = 8 * (rg0 + (kTcProducers / 32) * k) + rsub;
         r[k] = pr < cnt ? psrc[gs + pr] : -1;
     }
 }
@@ -606,7 +610,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
         }
         for (int a = 0; a < 2; ++a) {
             umma::mbar_init(&acc_full[a], 1);
-            umma::mbar_init(&acc_empty[a], 4);  // one arrival per epilogue warp
+            umma::mbar_init(&acc_empty[a], kTcEpiWarps);  // one arrival per epilogue warp
         }
         umma::mbar_fence_init();
     }
@@ -655,7 +659,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
                 for (int k = 0; k < RG; ++k) {
                     const int src = rows[k];
                     const float* gsrc = src >= 0 ? wsp + (size_t)src * 2 * ldk + coff : wsp;
-                    umma::cp16_keep(dst0 + (rg0 + 2 * k) * kTcKC * 8, gsrc, src >= 0, keep);
+                    umma::cp16_keep(dst0 + (rg0 + (kTcProducers / 32) * k) * kTcKC * 8, gsrc, src >= 0, keep);
                 }
                 umma::cp_async_mbar_arrive(&full[st]);
             }
@@ -707,8 +711,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
         __syncwarp();
     } else {
         // ---- epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31
+        // (with more than four epilogue warps, each of a sub-partition's warps
+        // takes its share of the columns), kTcEpiBatch loads per wait
         const int sp = warp & 3;
         const int f = 32 * sp + lane;
+        constexpr int kShares = kTcEpiWarps / 4;
+        const int share = (warp - 3) / 4;
+        constexpr int CB = 16 * kTcEpiBatch;  // columns per wait
         uint32_t tl = 0;
         for (int task = blockIdx.x; task < ntasks && ok; task += gridDim.x) {
             const int2 tk = tasks[task];
@@ -725,13 +734,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
             const uint32_t base = tmem + ((uint32_t)(32 * sp) << 16) + (uint32_t)(acc * kTcPairs);
             const bool tail = sp == 0 && ldo > kTcRows;  // entries beyond the 128 operator rows
 #pragma unroll 1
-            for (int c = 0; c < cnt; c += 16) {
-                float v[16];
-                umma::tmem_ld16(base + (uint32_t)c, v);
+            for (int c = share * CB; c < cnt; c += kShares * CB) {
+                float v[CB];
+#pragma unroll
+                for (int b = 0; b < kTcEpiBatch; ++b) umma::tmem_ld16(base + (uint32_t)(c + 16 * b), v + 16 * b);
                 umma::tmem_ld_wait();
                 // the task's rows are consecutive (group order); streaming stores
 #pragma unroll
-                for (int jj = 0; jj < 16; ++jj) {
+                for (int jj = 0; jj < CB; ++jj) {
                     if (c + jj < cnt) {
                         float* row = out + (size_t)(gs + c + jj) * ldo;
                         if (f < ldo) __stcs(row + f, v[jj]);
@@ -741,7 +751,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
                 }
             }
             umma::fence_before_sync();
-            __syncwarp();  // also: spos is rewritten by the next task
+            __syncwarp();
             if (lane == 0) umma::mbar_arrive(&acc_empty[acc]);
             ++tl;
         }
@@ -816,7 +826,7 @@ bool product_on_cuda_cores() {
 template <typename R, int CPT>
 int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
     const int M = t.num_nodes, nr = (p + 1) * (p + 1), N = 2 * p, nTr = rbase(N + 1);
-    const int ldo = (nr + 3) & ~3;  // result rows of 16-byte multiples
+    const int ldo = (nr + 31) & ~31;  // result rows of whole 128-byte lines
     const bool tc = sizeof(R) == 4 && !product_on_cuda_cores();
     const int cols = tc ? kTcPairs : kTaskCols;
     const int64_t nf = t.nfar;
