@@ -313,8 +313,14 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         FMM_TRY(build_lists(ws, t, tpl, st));
         if (learned && attempt == 0) {
             // FP64 direct sums at the sampled particles (the check of the
-            // result) on a second stream, beside the FP32-bound near field
-            if (!ws.aux) FMM_CUDA_TRY(cudaStreamCreateWithFlags(&ws.aux, cudaStreamNonBlocking));
+            // result) on a second stream of higher priority, so its blocks are
+            // scheduled first and it runs beside the FP32-bound near field
+            // rather than later beside the M2L product
+            if (!ws.aux) {
+                int lo = 0, hi = 0;
+                FMM_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+                FMM_CUDA_TRY(cudaStreamCreateWithPriority(&ws.aux, cudaStreamNonBlocking, hi));
+            }
             int64_t* d_rows = reinterpret_cast<int64_t*>(ws.sel_scratch.as<double>() + (size_t)nt * nf * 2);
             cudaEventRecord(ws.ev[10], st);
             FMM_CUDA_TRY(cudaStreamWaitEvent(ws.aux, ws.ev[10], 0));
