@@ -86,6 +86,21 @@ def workload_config(arm, system="water", n=3 * N_MOL):
     }
 
 
+# DRAM bytes (read + write) per unit of the two dominant kernels, from one ncu
+# capture of each on the 100k water case (profiles/)
+P2P_DRAM_PER_PAIR = 12.84e6 / 415.6e6
+TC_DRAM_PER_PAIR = (493.57e6 + 978.16e6) / 2.026111e6
+
+
+def measured_peaks():
+    """The generated peak figures, if present."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
 class ClockSampler:
     """Samples nvidia-smi clocks and throttle reasons while running."""
 
@@ -403,21 +418,35 @@ def main():
     _lib.check(L.fmm_measure_fma_peak(prec, ctypes.byref(peak)), "fma peak")
     p2p_pairs = stats["p2p_particle_pairs"] - n
     m2l_product_flops = sum(stats["m2l_pairs_q%d" % q] * m2l_product_flops_per_pair(q) for q in range(13))
+    # the FP32 M2L product runs on the tensor cores (tcgen05 kind::tf32) for
+    # orders <= 10, which is every pair of these arms (p = 10)
+    tc_product = prec == 1 and ARMS[args.arm]["p"] <= 10
+    m2l_name = "k_m2l_tc" if tc_product else ("k_m2l_gemm<float>" if prec else "k_m2l_gemm<double>")
     kern = {
         ("k_p2p_f32" if prec else "k_p2p_f64"): (p2p_pairs * pair_flops(2, F_ORDER), phase["t_p2p_kernel"],
                                                  "pair 2*nT(f)*nT(m)+2*C(m+f+4,4)+12 = %d flops" % pair_flops(2, F_ORDER)),
-        ("k_m2l_gemm<float>" if prec else "k_m2l_gemm<double>"): (m2l_product_flops, phase["t_m2l_product"],
-                                                                  "pair of order q: 2*(q+1)^4 flops (reduced basis)"),
+        m2l_name: (m2l_product_flops, phase["t_m2l_product"], "pair of order q: 2*(q+1)^4 flops (reduced basis)"),
     }
     kernels = {k: {"ms": round(v[1], 3), "algorithmic_flops": v[0], "achieved_tflops": v[0] / (v[1] * 1e-3) / 1e12,
                    "frac": v[0] / (v[1] * 1e-3) / 1e12 / peak.value, "convention": v[2]} for k, v in kern.items()
                if v[1] > 0}
+    if tc_product and m2l_name in kernels:
+        # tensor-core view: MMA flops issued (three TF32 products per term, 128
+        # operator rows, K rounded up to 8) against the TF32 rate, half the
+        # measured bf16 burst peak
+        mma = sum(stats["m2l_pairs_q%d" % q] * 3 * 2 * 128 * 8 * (((q + 1) ** 2 + 7) // 8) for q in range(11))
+        tf32_peak = measured_peaks().get("bf16_tflops", 1900.0) / 2
+        kk = kernels[m2l_name]
+        kk["mma_flops_issued"] = mma
+        kk["mma_tflops"] = mma / (kk["ms"] * 1e-3) / 1e12
+        kk["tf32_peak_tflops"] = tf32_peak
+        kk["frac_of_tf32_peak"] = kk["mma_tflops"] / tf32_peak
+        kk["frac"] = kk["achieved_tflops"] / peak.value  # FP32-equivalent work against the FP32 FMA peak
     # DRAM bytes per unit from one ncu capture of each kernel on the 100k case
     # (profiles/), scaled to this launch by its units (pairs): the kernels are
     # compute-bound and their traffic grows in proportion to the pairs
-    per_unit = {"k_p2p_f32": (12.84e6 / 415.6e6, p2p_pairs, "profiles/k_p2p_f32_water100k.md"),
-                "k_m2l_gemm<float>": ((62.88e6 + 947.37e6) / 2.027e6, stats["m2l_pairs"],
-                                      "profiles/k_m2l_gemm_f32_water100k.md")}
+    per_unit = {"k_p2p_f32": (P2P_DRAM_PER_PAIR, p2p_pairs, "profiles/k_p2p_f32_water100k.md"),
+                "k_m2l_tc": (TC_DRAM_PER_PAIR, stats["m2l_pairs"], "profiles/k_m2l_tc_water100k.md")}
     for k, (b, units, src) in per_unit.items():
         if k in kernels:
             kernels[k]["traffic_bytes"] = b * units

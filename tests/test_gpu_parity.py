@@ -205,6 +205,24 @@ def test_damping_aware_acceptance_matches_oracle(damp):
     assert rel_err(G, D, slice(1, 4)) < rel_err(G0, D, slice(1, 4))
 
 
+@pytest.mark.parametrize("one_sided", [False, True])
+def test_mixed_near_field_exclusions(one_sided):
+    """The FP32 near field masks excluded partners by the target's own list,
+    also when exclusions are listed by one partner only (the reference's
+    per-target semantics); both match the FP64 path."""
+    from fmm_gb300 import systems
+    s = systems.water(4000, 70.0, order=2, seed=31)
+    d = s["damping_factors"]
+    E = np.array(s["exclusions"])
+    if one_sided:
+        E[1:600:3, :] = 0  # hydrogens of the first 200 molecules list nothing; their oxygens still do
+    args = (0, s["coordinates"], s["multipoles"], np.asfortranarray(E))
+    F64 = fmm_gb300.field_fmm(*args, 0.5, 64, 8, 1, "AMOEBA", d, options=Options.exact())
+    F32 = fmm_gb300.field_fmm(*args, 0.5, 64, 8, 1, "AMOEBA", d, options=Options.exact(precision="mixed"))
+    assert np.all(np.isfinite(F32))
+    assert rel_err(F32, F64, slice(1, None)) < 5e-6
+
+
 @pytest.mark.parametrize("p", [3, 10, 12])
 def test_m2l_tensor_core_product_matches_cuda_cores(p, monkeypatch):
     """The FP32 M2L product on the tensor cores (operands split into TF32
