@@ -138,7 +138,10 @@ __global__ void __launch_bounds__(128) k_direct_scale(const TreeDev t, const flo
 // Sum over the sources src[0, cnt) of one staged piece of a source leaf
 // (lane group grp of ngr) for the lane's target: compensated FP32 (TwoSum
 // hi + lo), since the per-atom terms are much larger than their neutral
-// total.  k0 is the sorted index of src[0].  CHECK: the piece may hold the
+// total.  The contraction adds each pair into a plain FP32 block sum that
+// is folded into (hi, lo) every four pairs: the block sum's rounding is of
+// the order of a single pair's, and the TwoSum cost is paid once per four
+// pairs.  k0 is the sorted index of src[0].  CHECK: the piece may hold the
 // target itself or one of its excluded partners.
 template <int M, int F, int DAMP, bool CHECK>
 __device__ __forceinline__ void p2p_leaf(const float4* src, int cnt, int k0, int grp, int ngr, int tgt, float xt,
@@ -146,6 +149,10 @@ __device__ __forceinline__ void p2p_leaf(const float4* src, int cnt, int k0, int
                                          float oyl, float ozl, const int32_t* __restrict__ excl, int exw, int64_t n,
                                          int ot, float* hi, float* lo) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
+    float blk[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) blk[f] = 0.0f;
+    int nb = 0;
     for (int k = grp; k < cnt; k += ngr) {
         const float4* r = src + k * NV;
         const float4 a = r[0], b = r[1];
@@ -168,17 +175,25 @@ __device__ __forceinline__ void p2p_leaf(const float4* src, int cnt, int k0, int
         const float dx = ((xt - a.x) + ox) + (oxl - b.x);
         const float dy = ((yt - a.y) + oy) + (oyl - b.y);
         const float dz = ((zt - a.z) + oz) + (ozl - b.z);
-        float c[NF];
+        pair_field_f32acc<M, F>(dx, dy, dz, dt * a.w, DAMP, mc, blk);
+        if (++nb == 4) {
+            nb = 0;
 #pragma unroll
-        for (int f = 0; f < NF; ++f) c[f] = 0.0f;
-        pair_field_f32acc<M, F>(dx, dy, dz, dt * a.w, DAMP, mc, c);
-#pragma unroll
-        for (int f = 0; f < NF; ++f) {
-            const float s = hi[f] + c[f];
-            const float bb = s - hi[f];
-            lo[f] += (hi[f] - (s - bb)) + (c[f] - bb);
-            hi[f] = s;
+            for (int f = 0; f < NF; ++f) {
+                const float s = hi[f] + blk[f];
+                const float bb = s - hi[f];
+                lo[f] += (hi[f] - (s - bb)) + (blk[f] - bb);
+                hi[f] = s;
+                blk[f] = 0.0f;
+            }
         }
+    }
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        const float s = hi[f] + blk[f];
+        const float bb = s - hi[f];
+        lo[f] += (hi[f] - (s - bb)) + (blk[f] - bb);
+        hi[f] = s;
     }
 }
 
