@@ -17,7 +17,10 @@
 // local expansion evaluated by nested Horner schemes in the leaf's length
 // unit (FP32 in the mixed-precision path, where the local expansion's terms
 // decrease with order and carry no cancellation between per-atom terms).
-// P2M, M2M and L2L stay FP64.
+// P2M, M2M and L2L are FP64 in the plain path and double-float (FP32 pipe,
+// exact products by FMA, ~48-bit sums) in the mixed path, M2M and L2L with
+// an FP64 fallback for blocks whose powers or moments leave the range where
+// FP32 exponents suffice.
 #include <algorithm>
 #include <vector>
 
@@ -309,9 +312,34 @@ __device__ __forceinline__ int child_powers(const TreeDev& t, int node, int p, i
     return nch;
 }
 
+// (hi, lo) FP32 pair of an FP64 value; *big set when it is outside the range
+// where double-float products keep their precision.
+__device__ __forceinline__ float2 to_df(double w, int* big) {
+    if (fabs(w) > 1e30) *big = 1;
+    const float hi = (float)w;
+    return make_float2(hi, (float)(w - (double)hi));
+}
+
+// a += x * y in double-float (exact product by FMA, TwoSum accumulation).
+__device__ __forceinline__ void df_mac(float2 x, float2 y, float& h, float& l) {
+    const float pr = x.x * y.x;
+    float er = fmaf(x.x, y.x, -pr);
+    er = fmaf(x.x, y.y, er);
+    er = fmaf(x.y, y.x, er);
+    const float sum = h + pr;
+    const float bb = sum - h;
+    l += ((h - (sum - bb)) + (pr - bb)) + er;
+    h = sum;
+}
+
+// DF: the products and sums in double-float (FP32 pipe; the FP64 pipe is the
+// scarce one) when the block's powers and moments are within range, else
+// FP64.
+template <bool DF>
 __global__ void __launch_bounds__(kXThreads) k_m2m(const TreeDev t, const int32_t* __restrict__ nodes, int p,
                                                    const int* __restrict__ tab, TabView v, double* __restrict__ mom) {
     extern __shared__ __align__(16) double sm_m2m[];
+    __shared__ int big;
     const int nq = v.nq, P1 = p + 1;
     const int node = nodes[blockIdx.x];
     if (t.is_leaf[node]) return;
@@ -325,6 +353,7 @@ __global__ void __launch_bounds__(kXThreads) k_m2m(const TreeDev t, const int32_
     copy_ints(comp, tab + v.comp, nq);
     copy_ints(off, tab + v.m2m_off, nq + 1);
     copy_ints(terms, tab + v.m2m, v.n_m2m);
+    if (threadIdx.x == 0) big = 0;
     __syncthreads();
     // children offsets d = c_child - c_parent
     const int nch = child_powers(t, node, p, nq, comp, ch, e, dp, 1.0);
@@ -333,6 +362,35 @@ __global__ void __launch_bounds__(kXThreads) k_m2m(const TreeDev t, const int32_
         mc[idx] = mom[(size_t)ch[b] * nq + q];
     }
     __syncthreads();
+    if (DF) {
+        // in place: each entry is read and rewritten by the same thread
+        float2* dp2 = reinterpret_cast<float2*>(dp);
+        float2* mc2 = reinterpret_cast<float2*>(mc);
+        for (int idx = threadIdx.x; idx < nch * nq; idx += blockDim.x) {
+            dp2[idx] = to_df(dp[idx], &big);
+            mc2[idx] = to_df(mc[idx], &big);
+        }
+        __syncthreads();
+        if (!big) {
+            for (int tq = threadIdx.x; tq < nq; tq += blockDim.x) {
+                float h = 0.0f, l = 0.0f;
+                for (int j = off[tq]; j < off[tq + 1]; ++j) {
+                    const int u = terms[j] & 0xffff, w = terms[j] >> 16;
+                    for (int b = 0; b < nch; ++b) df_mac(dp2[b * nq + u], mc2[b * nq + w], h, l);
+                }
+                mom[(size_t)node * nq + tq] = (double)h + (double)l;
+            }
+            return;
+        }
+        // out of range: back to FP64 powers and moments
+        __syncthreads();
+        child_powers(t, node, p, nq, comp, ch, e, dp, 1.0);
+        for (int idx = threadIdx.x; idx < nch * nq; idx += blockDim.x) {
+            const int b = idx / nq, q = idx % nq;
+            mc[idx] = mom[(size_t)ch[b] * nq + q];
+        }
+        __syncthreads();
+    }
     for (int tq = threadIdx.x; tq < nq; tq += blockDim.x) {
         double a = 0.0;
         for (int j = off[tq]; j < off[tq + 1]; ++j) {
@@ -344,9 +402,11 @@ __global__ void __launch_bounds__(kXThreads) k_m2m(const TreeDev t, const int32_
 }
 
 // ---------------------------------------------------------------- L2L
+template <bool DF>
 __global__ void __launch_bounds__(kXThreads) k_l2l(const TreeDev t, const int32_t* __restrict__ nodes, int p,
                                                    const int* __restrict__ tab, TabView v, double* __restrict__ loc) {
     extern __shared__ __align__(16) double sm_l2l[];
+    __shared__ int big;
     const int nq = v.nq, P1 = p + 1;
     const int node = nodes[blockIdx.x];
     if (t.is_leaf[node]) return;
@@ -360,10 +420,41 @@ __global__ void __launch_bounds__(kXThreads) k_l2l(const TreeDev t, const int32_
     copy_ints(comp, tab + v.comp, nq);
     copy_ints(off, tab + v.l2l_off, nq + 1);
     copy_ints(terms, tab + v.l2l, v.n_l2l);
+    if (threadIdx.x == 0) big = 0;
     for (int q = threadIdx.x; q < nq; q += blockDim.x) lp[q] = loc[(size_t)node * nq + q];
     __syncthreads();
     const int nch = child_powers(t, node, p, nq, comp, ch, e, dp, 1.0);
     __syncthreads();
+    if (DF) {
+        float2* dp2 = reinterpret_cast<float2*>(dp);
+        float2* lp2 = reinterpret_cast<float2*>(lp);
+        for (int idx = threadIdx.x; idx < nch * nq; idx += blockDim.x) dp2[idx] = to_df(dp[idx], &big);
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) lp2[q] = to_df(lp[q], &big);
+        __syncthreads();
+        if (!big) {
+            for (int tq = threadIdx.x; tq < nq; tq += blockDim.x) {
+                float ah[8], al[8];
+#pragma unroll
+                for (int b = 0; b < 8; ++b) ah[b] = al[b] = 0.0f;
+                for (int j = off[tq]; j < off[tq + 1]; ++j) {
+                    const int u = terms[j] & 0xffff, w = terms[j] >> 16;
+                    const float2 l = lp2[w];
+#pragma unroll
+                    for (int b = 0; b < 8; ++b)
+                        if (b < nch) df_mac(l, dp2[b * nq + u], ah[b], al[b]);
+                }
+#pragma unroll
+                for (int b = 0; b < 8; ++b)
+                    if (b < nch) loc[(size_t)ch[b] * nq + tq] += (double)ah[b] + (double)al[b];
+            }
+            return;
+        }
+        // out of range: back to FP64 powers and locals
+        __syncthreads();
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) lp[q] = loc[(size_t)node * nq + q];
+        child_powers(t, node, p, nq, comp, ch, e, dp, 1.0);
+        __syncthreads();
+    }
     for (int tq = threadIdx.x; tq < nq; tq += blockDim.x) {
         double a[8];
 #pragma unroll
@@ -499,12 +590,16 @@ int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, c
     {
         const size_t sm = sizeof(double) * (16 * (size_t)nq + 8 * 3 * (p + 1)) +
                           sizeof(int) * (2 * (size_t)nq + 1 + v.n_m2m + 9);
-        FMM_TRY(set_smem((const void*)k_m2m, sm));
+        FMM_TRY(set_smem((const void*)k_m2m<false>, sm));
+        FMM_TRY(set_smem((const void*)k_m2m<true>, sm));
         for (int d = t.max_depth - 1; d >= 1; --d) {
             const int lo = t.level_start[d], hi = t.level_start[d + 1];
             if (hi <= lo) continue;
             count_launches(1);
-            k_m2m<<<(unsigned)(hi - lo), kXThreads, sm, st>>>(t, t.level_nodes + lo, p, tab, v, mom);
+            if (df)
+                k_m2m<true><<<(unsigned)(hi - lo), kXThreads, sm, st>>>(t, t.level_nodes + lo, p, tab, v, mom);
+            else
+                k_m2m<false><<<(unsigned)(hi - lo), kXThreads, sm, st>>>(t, t.level_nodes + lo, p, tab, v, mom);
         }
     }
     FMM_CUDA_TRY(cudaGetLastError());
@@ -521,12 +616,16 @@ int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, i
     {
         const size_t sm = sizeof(double) * (9 * (size_t)nq + 8 * 3 * (p + 1)) +
                           sizeof(int) * (2 * (size_t)nq + 1 + v.n_l2l + 9);
-        FMM_TRY(set_smem((const void*)k_l2l, sm));
+        FMM_TRY(set_smem((const void*)k_l2l<false>, sm));
+        FMM_TRY(set_smem((const void*)k_l2l<true>, sm));
         for (int d = 1; d < t.max_depth; ++d) {
             const int lo = t.level_start[d], hi = t.level_start[d + 1];
             if (hi <= lo) continue;
             count_launches(1);
-            k_l2l<<<(unsigned)(hi - lo), kXThreads, sm, st>>>(t, t.level_nodes + lo, p, tab, v, loc);
+            if (fp32)
+                k_l2l<true><<<(unsigned)(hi - lo), kXThreads, sm, st>>>(t, t.level_nodes + lo, p, tab, v, loc);
+            else
+                k_l2l<false><<<(unsigned)(hi - lo), kXThreads, sm, st>>>(t, t.level_nodes + lo, p, tab, v, loc);
         }
     }
     if (t.num_leaves > 0) {
