@@ -285,6 +285,8 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         tpl.sel_lnorm = ws.sel_norms.as<float>();
         tpl.sel_dmin = ws.sel_norms.as<float>() + (size_t)t.num_nodes * (p + 1);
         tpl.sel_P = p;
+        tpl.sel_chi = ws.f32node.as<float4>();  // prepare_f32_records
+        tpl.sel_clo = tpl.sel_chi + t.num_nodes;
         // per-pair error budget from the sampled field scale (FP32 estimate)
         double* d_est = ws.sel_scratch.as<double>() + (size_t)nt * nf;
         const int64_t* d_rows = reinterpret_cast<const int64_t*>(ws.sel_scratch.as<double>() + (size_t)nt * nf * 2);

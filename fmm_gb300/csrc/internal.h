@@ -73,6 +73,8 @@ struct TreeParams {
     int sel_P = 0;                      // order of the stored norms
     float sel_log_budget = 0.0f;        // log10 of the per-pair error budget
     double sel_theta = 0.0;             // loose acceptance test applied before the network
+    const float4* sel_chi = nullptr;    // FP32 node centres (hi, rmax in w) of the learned list build
+    const float4* sel_clo = nullptr;    // and their low parts (half-width in w)
     double root_r = 0.0;                // > 0: root half-width given (batched packing box)
     const int32_t* d_sys = nullptr;     // batched systems: system id of each particle (input order)
 };

@@ -265,4 +265,25 @@ __device__ __forceinline__ void selector_features(const TreeDev& t, const float*
     x[16] = fminf(dmin[i] * dmin[j] * R, 30.0f) * (1.0f / 30.0f);
 }
 
+// The same features from the FP32 node data of the learned list build
+// (centres as double-float pairs, rmax in chi.w, half-width in clo.w).
+__device__ __forceinline__ void selector_features_f32(const float4* __restrict__ chi, const float4* __restrict__ clo,
+                                                      const int32_t* __restrict__ count,
+                                                      const float* __restrict__ lnorm,
+                                                      const float* __restrict__ dmin, int P, int i, int j, float* x) {
+    const float4 ci = chi[i], cj = chi[j], li = clo[i], lj = clo[j];
+    const float dx = (ci.x - cj.x) + (li.x - lj.x), dy = (ci.y - cj.y) + (li.y - lj.y),
+                dz = (ci.z - cj.z) + (li.z - lj.z);
+    const float R = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float lR = log10f(R);
+    const float ri = li.w, rj = lj.w;
+    x[0] = 1.7320508f * (ri + rj) / R;
+    x[1] = log2f(rj / ri);
+    x[2] = log2f((float)count[i]);
+    for (int k = 0; k <= kQmax; ++k)
+        x[3 + k] = (k <= P && k <= kFeatOrders) ? fmaxf(lnorm[(size_t)j * (P + 1) + k] - (float)(k + 2) * lR, -40.0f)
+                                                : -40.0f;
+    x[16] = fminf(dmin[i] * dmin[j] * R, 30.0f) * (1.0f / 30.0f);
+}
+
 }  // namespace fmm

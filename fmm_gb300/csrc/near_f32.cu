@@ -61,14 +61,16 @@ __global__ void k_gather_f32(int64_t n, int dim, const TreeDev t, const double* 
 }
 
 // Node centres as double-float pairs (hi = rounded centre, lo = rounded
-// remainder), so leaf-centre offsets are formed in FP32 without losing bits.
+// remainder), so leaf-centre offsets are formed in FP32 without losing bits;
+// the w components carry rmax (hi) and the half-width (lo) in FP32 for the
+// learned list build.
 __global__ void k_node_centres_f32(int M, const TreeDev t, float4* __restrict__ hi, float4* __restrict__ lo) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= M) return;
     const float hx = (float)t.cx[k], hy = (float)t.cy[k], hz = (float)t.cz[k];
-    hi[k] = make_float4(hx, hy, hz, 0.0f);
+    hi[k] = make_float4(hx, hy, hz, (float)t.rmax[k]);
     lo[k] = make_float4((float)(t.cx[k] - (double)hx), (float)(t.cy[k] - (double)hy), (float)(t.cz[k] - (double)hz),
-                        0.0f);
+                        (float)t.r[k]);
 }
 
 // a - b as an unevaluated pair s + e (Knuth's TwoSum with b negated).

@@ -319,8 +319,9 @@ __device__ __forceinline__ unsigned long long warp_alloc(unsigned long long* ctr
 // or refined into the children of the larger node; entries are appended to
 // the far list, the near list or the next frontier.  Called by every lane of
 // the warp (skip: no candidate).
+template <typename RR>
 __device__ __forceinline__ void emit_pair(bool skip, bool accept, int order, int i, int j, bool li, bool lj,
-                                          bool mixed, double ri, double rj, const TreeDev& t, int2* __restrict__ out,
+                                          bool mixed, RR ri, RR rj, const TreeDev& t, int2* __restrict__ out,
                                           int64_t cap_out, uint64_t* __restrict__ far, int64_t cap_far,
                                           uint64_t* __restrict__ nearp, int64_t cap_near,
                                           unsigned long long* counters, int lane) {
@@ -407,9 +408,10 @@ __global__ void k_list_iter(const int2* __restrict__ in, int nin, int2* __restri
 // budget; otherwise it is refined exactly like a pair the test rejects.
 __global__ void __launch_bounds__(128) k_list_iter_learned(
     const int2* __restrict__ in, int nin, int2* __restrict__ out, int64_t cap_out, uint64_t* __restrict__ far,
-    int64_t cap_far, uint64_t* __restrict__ nearp, int64_t cap_near, const TreeDev t, double theta_loose, double rdamp,
+    int64_t cap_far, uint64_t* __restrict__ nearp, int64_t cap_near, const TreeDev t, float theta_loose, float rdamp,
     int qmax, const float* __restrict__ params, const float* __restrict__ lnorm, const float* __restrict__ dmin,
-    int P, float log_budget, unsigned long long* counters) {
+    int P, float log_budget, const float4* __restrict__ chi, const float4* __restrict__ clo,
+    unsigned long long* counters) {
     extern __shared__ __align__(16) float sm_sel[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float* X = sm_sel + wib * kWarpTcFloats;  // this warp's network scratch
@@ -418,13 +420,18 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     bool skip = q >= nin;
     int i = 0, j = 0;
-    double ri = 0.0, rj = 0.0;
+    float ri = 0.0f, rj = 0.0f;  // FP32 node data throughout: the FP64 pipe is the scarce one
     bool li = false, lj = false, mixed = false, accept = false;
+    float4 ci = make_float4(0.f, 0.f, 0.f, 0.f), cj = ci, oi = ci, oj = ci;
     if (!skip) {
         i = in[q].x;
         j = in[q].y;
-        ri = t.rmax[i];
-        rj = t.rmax[j];
+        ci = chi[i];
+        cj = chi[j];
+        oi = clo[i];
+        oj = clo[j];
+        ri = ci.w;
+        rj = cj.w;
         li = t.is_leaf[i] != 0;
         lj = t.is_leaf[j] != 0;
         // batched systems: no pairs across systems; nodes spanning several
@@ -436,12 +443,13 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
         }
         // loose geometric gate in FP32 (the network decides; no parity with
         // the reference's rule is involved here)
-        const float dx = (float)(t.cx[i] - t.cx[j]), dy = (float)(t.cy[i] - t.cy[j]), dz = (float)(t.cz[i] - t.cz[j]);
+        const float dx = (ci.x - cj.x) + (oi.x - oj.x), dy = (ci.y - cj.y) + (oi.y - oj.y),
+                    dz = (ci.z - cj.z) + (oi.z - oj.z);
         const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-        accept = !skip && !mixed && r * (float)theta_loose > (float)(ri + rj);
-        if (accept && rdamp > 0.0) {
-            const float gap = r - 1.7320508f * (float)(t.r[i] + t.r[j]);
-            accept = gap >= (float)rdamp;
+        accept = !skip && !mixed && r * theta_loose > ri + rj;
+        if (accept && rdamp > 0.0f) {
+            const float gap = r - 1.7320508f * (oi.w + oj.w);
+            accept = gap >= rdamp;
         }
     }
     // the network runs once per warp on the pairs that passed the loose test
@@ -452,7 +460,7 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
         const int slot = __popc(need & ((1u << lane) - 1u));
         if (accept) {
             float x[kMlpIn];
-            selector_features(t, lnorm, dmin, P, i, j, x);
+            selector_features_f32(chi, clo, t.count, lnorm, dmin, P, i, j, x);
             mlp_input(S, x, X + slot * kMlpInP);
         }
         __syncwarp();
@@ -782,8 +790,9 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
                 k_list_iter_learned<<<grid_for(nin, 128), 128, smem, st>>>(
                     fin, (int)nin, fout, cap_front, ws.far_pairs.as<uint64_t>(), cap_far, ws.near_pairs.as<uint64_t>(),
-                    cap_near, t, tp.sel_theta, tp.mac_mode == 1 ? tp.rdamp : 0.0, tp.order, tp.sel_params,
-                    tp.sel_lnorm, tp.sel_dmin, tp.sel_P, tp.sel_log_budget, ctr);
+                    cap_near, t, (float)tp.sel_theta, tp.mac_mode == 1 ? (float)tp.rdamp : 0.0f, tp.order,
+                    tp.sel_params, tp.sel_lnorm, tp.sel_dmin, tp.sel_P, tp.sel_log_budget, tp.sel_chi, tp.sel_clo,
+                    ctr);
             } else
             k_list_iter<<<grid_for(nin, 256), 256, 0, st>>>(fin, (int)nin, fout, cap_front,
                                                              ws.far_pairs.as<uint64_t>(), cap_far,
