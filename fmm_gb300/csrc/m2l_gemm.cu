@@ -75,7 +75,13 @@ __global__ void k_scale_weights(int64_t total, int nr, int ld, const double* __r
 // Group key of every far pair: level difference, expansion order and integer
 // displacement in units of the smaller half-width; pairs off the grid (or
 // with out-of-range fields) get unique keys of their own (code 63 | index).
+// With FP32 node data (chi: centre hi parts; clo: low parts, half-width in
+// w) the displacement is formed from the double-float centres on the FP32
+// pipe; its error (a few 1e-8 relative of the displacement, up to ~1e-4 cell
+// units at the largest encodable displacement) stays far below the 1e-3
+// tolerance of the integer test.  Without them, FP64 with a 1e-6 tolerance.
 __global__ void k_m2l_keys(int64_t nfar, const TreeDev t, const int32_t* __restrict__ tgt, int p,
+                           const float4* __restrict__ chi, const float4* __restrict__ clo,
                            uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= nfar) return;
@@ -83,13 +89,35 @@ __global__ void k_m2l_keys(int64_t nfar, const TreeDev t, const int32_t* __restr
     const int ord = t.far_ord ? min((int)t.far_ord[q], p) : p;
     // half-widths are the root's divided by powers of two: 1/h times an
     // integer multiple of h stays within rounding of that integer
-    const double ihf = 1.0 / fmin(t.r[i], t.r[j]);
-    const double dx = (t.cx[i] - t.cx[j]) * ihf, dy = (t.cy[i] - t.cy[j]) * ihf, dz = (t.cz[i] - t.cz[j]) * ihf;
-    const double rx = rint(dx), ry = rint(dy), rz = rint(dz);
+    float rx, ry, rz, ex, ey, ez, tol;
+    if (chi) {
+        const float4 ci = chi[i], cj = chi[j], li = clo[i], lj = clo[j];
+        const float ihf = 1.0f / fminf(li.w, lj.w);
+        const float dx = ((ci.x - cj.x) + (li.x - lj.x)) * ihf, dy = ((ci.y - cj.y) + (li.y - lj.y)) * ihf,
+                    dz = ((ci.z - cj.z) + (li.z - lj.z)) * ihf;
+        rx = rintf(dx);
+        ry = rintf(dy);
+        rz = rintf(dz);
+        ex = fabsf(dx - rx);
+        ey = fabsf(dy - ry);
+        ez = fabsf(dz - rz);
+        tol = 1e-3f;
+    } else {
+        const double ihf = 1.0 / fmin(t.r[i], t.r[j]);
+        const double dx = (t.cx[i] - t.cx[j]) * ihf, dy = (t.cy[i] - t.cy[j]) * ihf, dz = (t.cz[i] - t.cz[j]) * ihf;
+        const double Rx = rint(dx), Ry = rint(dy), Rz = rint(dz);
+        rx = (float)Rx;
+        ry = (float)Ry;
+        rz = (float)Rz;
+        ex = (float)fabs(dx - Rx);
+        ey = (float)fabs(dy - Ry);
+        ez = (float)fabs(dz - Rz);
+        tol = 1e-6f;
+    }
     const int dl = t.depth[i] - t.depth[j];
-    const double lim = (double)(kDOff - 1);
-    const bool grid = fabs(dx - rx) < 1e-6 && fabs(dy - ry) < 1e-6 && fabs(dz - rz) < 1e-6 && fabs(rx) <= lim &&
-                      fabs(ry) <= lim && fabs(rz) <= lim && dl > -31 && dl < 31;
+    const float lim = (float)(kDOff - 1);
+    const bool grid = ex < tol && ey < tol && ez < tol && fabsf(rx) <= lim && fabsf(ry) <= lim && fabsf(rz) <= lim &&
+                      dl > -31 && dl < 31;
     uint64_t key;
     if (grid)
         key = ((uint64_t)(dl + 31) << 40) | ((uint64_t)ord << 36) | ((uint64_t)((int64_t)rx + kDOff) << 24) |
@@ -852,8 +880,10 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
                                                                            ws.wred.as<double>(), t.r,
                                                                            ws.m2l_wsc.as<R>());
         count_launches(1);
-        k_m2l_keys<<<grid_for(nf, 256), 256, 0, st>>>(nf, t, tgt, p, ws.m2l_keys.as<uint64_t>(),
-                                                       ws.m2l_vals.as<int32_t>());
+        // FP32 node data where the mixed path prepared it
+        const float4* chi = (sizeof(R) == 4 && ws.f32node_ok) ? ws.f32node.as<float4>() : nullptr;
+        k_m2l_keys<<<grid_for(nf, 256), 256, 0, st>>>(nf, t, tgt, p, chi, chi ? chi + M : nullptr,
+                                                       ws.m2l_keys.as<uint64_t>(), ws.m2l_vals.as<int32_t>());
         // sort by key, run-length encode into groups
         int* d_nruns = reinterpret_cast<int*>(ws.counters.as<unsigned long long>() + 14);
         size_t tb1 = 0, tb2 = 0, tb3 = 0;

@@ -376,6 +376,7 @@ int prepare_f32_records(Workspace& ws, const Particles& P, const TreeDev& t, cud
     count_launches(1);
     k_node_centres_f32<<<grid_for(t.num_nodes, 256), 256, 0, st>>>(t.num_nodes, t, chi, chi + t.num_nodes);
     FMM_CUDA_TRY(cudaGetLastError());
+    ws.f32node_ok = true;
     return FMM_OK;
 }
 

@@ -578,6 +578,7 @@ void host_centroid_sequential(const double* X, int64_t n, double c[3]) {
 }
 
 int build_tree(Workspace& ws, const double* d_X, int64_t n, const TreeParams& tp, TreeDev& t, cudaStream_t st) {
+    ws.f32node_ok = false;  // FP32 node data belong to the previous tree
     t.n = n;
     t.ncrit = tp.ncrit;
     FMM_TRY(ws.scalars.ensure(sizeof(double) * (8 + 3 * kLanes)));
