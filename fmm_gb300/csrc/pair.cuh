@@ -76,6 +76,7 @@ struct Real<double> {
 #endif
     }
     __host__ __device__ static __forceinline__ double exp_(double x) { return ::exp(x); }
+    __host__ __device__ static __forceinline__ double expc_(double x) { return ::exp(x); }
     __host__ __device__ static __forceinline__ double erf_(double x) { return ::erf(x); }
     __host__ __device__ static __forceinline__ double sqrt_(double x) { return ::sqrt(x); }
     __host__ __device__ static __forceinline__ double inv_odd(int i) {
@@ -157,6 +158,17 @@ struct Real<float> {
 #endif
     }
     __host__ __device__ static __forceinline__ float exp_(float x) { return ::expf(x); }
+    // e^x for the closed forms of the damped numerators (x <= -3): there it
+    // scales a correction of at most ~0.3 of the numerator's constant term,
+    // so the fast intrinsic's error (~1e-6 relative at |x| ~ 20) stays below
+    // 1e-7 of the numerator
+    __host__ __device__ static __forceinline__ float expc_(float x) {
+#ifdef __CUDA_ARCH__
+        return __expf(x);
+#else
+        return ::expf(x);
+#endif
+    }
     __host__ __device__ static __forceinline__ float erf_(float x) { return ::erff(x); }
     __host__ __device__ static __forceinline__ float sqrt_(float x) { return ::sqrtf(x); }
     __host__ __device__ static __forceinline__ float inv_odd(int i) {
@@ -285,7 +297,7 @@ __host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, 
             }
         }
         if (closed) {
-            const R e = RT::exp_(-x);
+            const R e = RT::expc_(-x);
             const R x2 = x * x;
             R ym1 = (R)1, y0 = -((R)1 + x);  // y_0, y_1 (Yukawa numerators)
             num[0] = (R)1 - e * ((R)1 + (R)0.5 * x);
@@ -328,7 +340,7 @@ __host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, 
             }
         }
         if (closed) {
-            const R e = RT::exp_(-u);
+            const R e = RT::expc_(-u);
 #pragma unroll
             for (int j = 1; j <= N; ++j) {
                 R q = RT::amoebaQ(j, j - 1);
