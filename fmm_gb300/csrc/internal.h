@@ -104,7 +104,7 @@ struct Workspace {
     DevBuf sel_norms, sel_params, sel_scratch;
     // grouped M2L
     DevBuf m2l_tgt, m2l_keys, m2l_keys2, m2l_vals, m2l_vals2, m2l_ukeys, m2l_cnt, m2l_gstart, m2l_tcnt, m2l_toff,
-        m2l_tasks, m2l_T, m2l_gq, m2l_gab, m2l_wsc, m2l_out, m2l_wsplit, m2l_gop, m2l_gopoff;
+        m2l_tasks, m2l_T, m2l_gq, m2l_gab, m2l_wsc, m2l_out, m2l_wsplit, m2l_gop, m2l_gopoff, m2l_rowbase;
     // sorted particle data
     DevBuf sx, sy, sz, smc, sd;
     DevBuf f32buf;   // FP32 particle records of the mixed-precision near field

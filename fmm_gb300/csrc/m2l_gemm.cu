@@ -298,7 +298,7 @@ template <typename R, int RT, int CPT>
 __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, int c_begin, int tcols, int nrq,
                                           int cnt, int gs,
                                           const int32_t* __restrict__ svals, const int32_t* __restrict__ far_src,
-                                          const R* __restrict__ wsc, int ldw, R* __restrict__ out, int ldo) {
+                                          const R* __restrict__ wsc, int ldw, R* __restrict__ gout, int ldo) {
     constexpr int TN = GemmSmem<R, CPT>::TN;
     constexpr int VS = GemmSmem<R, CPT>::VS;
     constexpr int RM = 16 * RT;
@@ -339,7 +339,7 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
 #pragma unroll
         for (int l = 0; l < CPT; ++l) {
             const int c = cb + cg * CPT + l;
-            pos[l] = c < c_end ? gs + c : -1;  // result row: the pair's place in group order
+            pos[l] = c < c_end ? c : -1;  // result row: the pair's place in its group
             wp[l] = pos[l] >= 0 ? reinterpret_cast<const V*>(wsc + (size_t)csrc[c - c_begin] * ldw) : nullptr;
         }
         R acc[RT][CPT];
@@ -369,12 +369,12 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
                     for (int l = 0; l < CPT; ++l) acc[k][l] = fma(gv[k], wv[l][u], acc[k][l]);
             }
         }
-        // full rows of ldo entries (zeros above the pair's order), so the
-        // per-target sum reads them without knowing the order
+        // the group's rows are ldo = (q+1)^2 rounded up to 32 entries each
+        // (zeros above the pair's order, whole 128-byte lines in FP32)
 #pragma unroll
         for (int l = 0; l < CPT; ++l) {
             if (pos[l] >= 0) {
-                R* o = out + (size_t)pos[l] * ldo;
+                R* o = gout + (size_t)pos[l] * ldo;
 #pragma unroll
                 for (int k = 0; k < RT; ++k) {
                     const int f = rg * RT + k;
@@ -389,6 +389,10 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
     }
 }
 
+// Result rows: group g's rows start at rowbase[g] x 32 entries, one row of
+// (q+1)^2 rounded up to 32 entries per pair in group order.
+__host__ __device__ __forceinline__ int row_len(int q) { return ((q + 1) * (q + 1) + 31) & ~31; }
+
 // tcols: pairs per task (at most kTaskCols); tasks of order < qmin are left
 // to the tensor-core kernel.
 template <typename R, int CPT>
@@ -400,7 +404,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restric
                                                            int ldT, const int32_t* __restrict__ svals,
                                                            const int32_t* __restrict__ far_src,
                                                            const R* __restrict__ wsc, R* __restrict__ out,
-                                                           int ldo) {
+                                                           const int32_t* __restrict__ rowbase) {
     extern __shared__ __align__(16) char sm_gemm[];
     const GemmSmem<R, CPT> L(p);
     const int nr = (p + 1) * (p + 1);
@@ -431,8 +435,8 @@ __global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restric
     switch (rt) {
 #define FMM_GEMM_CASE(K)                                                                                     \
     case K:                                                                                                  \
-        gemm_task<R, K, CPT>(L, sm_gemm, task.y, tcols, nrq, cnt, gs, svals, far_src, wsc, wsc_ld<R>(nr), out, \
-                             ldo);                                                                            \
+        gemm_task<R, K, CPT>(L, sm_gemm, task.y, tcols, nrq, cnt, gs, svals, far_src, wsc, wsc_ld<R>(nr),     \
+                             out + (size_t)rowbase[g] * 32, row_len(q));                                      \
         break;
         FMM_GEMM_CASE(1)
         FMM_GEMM_CASE(2)
@@ -520,10 +524,23 @@ __global__ void k_split_weights(int64_t total, int nr, int ldw, int ldk, const f
     }
 }
 
-// Place of every far pair (target order) in group order: inv[svals[k]] = k.
-__global__ void k_inverse_perm(int64_t nf, const int32_t* __restrict__ svals, int32_t* __restrict__ inv) {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k < nf) inv[svals[k]] = (int32_t)k;
+// Rows of each group in units of 32 entries (scanned into rowbase).
+__global__ void k_row_sizes(int ng, const int32_t* __restrict__ gstart, const int32_t* __restrict__ gq,
+                            int32_t* __restrict__ rsz) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g > ng) return;
+    rsz[g] = g < ng ? (gstart[g + 1] - gstart[g]) * (row_len(gq[g]) / 32) : 0;
+}
+
+// Row of every far pair, indexed in target order (svals maps group order to
+// target order), in units of 32 entries.  Warp per group.
+__global__ void k_row_offsets(int ng, const int32_t* __restrict__ gstart, const int32_t* __restrict__ gq,
+                              const int32_t* __restrict__ rowbase, const int32_t* __restrict__ svals,
+                              int32_t* __restrict__ roff) {
+    const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (g >= ng) return;
+    const int lane = threadIdx.x & 31, u = row_len(gq[g]) / 32;
+    for (int k = gstart[g] + lane; k < gstart[g + 1]; k += 32) roff[svals[k]] = rowbase[g] + (k - gstart[g]) * u;
 }
 
 // Source node of every far pair in group order: psrc[k] = far_src[svals[k]].
@@ -619,7 +636,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
                                                          const float* __restrict__ gop,
                                                          const int32_t* __restrict__ psrc,
                                                          const float* __restrict__ wsp, int ldk,
-                                                         float* __restrict__ out, int ldo, int* __restrict__ err) {
+                                                         float* __restrict__ out,
+                                                         const int32_t* __restrict__ rowbase,
+                                                         int* __restrict__ err) {
     extern __shared__ __align__(1024) char sm_tc[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     uint64_t* full = reinterpret_cast<uint64_t*>(sm_tc + TcSmem::off_bar);
@@ -760,22 +779,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
             }
             umma::fence_after_sync();
             const uint32_t base = tmem + ((uint32_t)(32 * sp) << 16) + (uint32_t)(acc * kTcPairs);
-            const bool tail = sp == 0 && ldo > kTcRows;  // entries beyond the 128 operator rows
+            // the group's rows: (q+1)^2 rounded up to 32 entries (at most the
+            // 128 operator rows), from rowbase[g] x 32 in group order
+            const int rl = row_len(q);
+            float* gout = out + ((size_t)rowbase[g] + (size_t)tk.y * (rl / 32)) * 32;
 #pragma unroll 1
             for (int c = share * CB; c < cnt; c += kShares * CB) {
                 float v[CB];
 #pragma unroll
                 for (int b = 0; b < kTcEpiBatch; ++b) umma::tmem_ld16(base + (uint32_t)(c + 16 * b), v + 16 * b);
                 umma::tmem_ld_wait();
-                // the task's rows are consecutive (group order); streaming stores
+                // the task's rows are consecutive; streaming stores of whole lines
+                if (f < rl) {
 #pragma unroll
-                for (int jj = 0; jj < CB; ++jj) {
-                    if (c + jj < cnt) {
-                        float* row = out + (size_t)(gs + c + jj) * ldo;
-                        if (f < ldo) __stcs(row + f, v[jj]);
-                        if (tail)
-                            for (int e = kTcRows + lane; e < ldo; e += 32) __stcs(row + e, 0.0f);
-                    }
+                    for (int jj = 0; jj < CB; ++jj)
+                        if (c + jj < cnt) __stcs(gout + (size_t)(c + jj) * rl + f, v[jj]);
                 }
             }
             umma::fence_before_sync();
@@ -813,12 +831,13 @@ struct Sum<double> {
 };
 
 // Block per target, thread per reduced component: compensated sum of the
-// target's pair rows (stored in group order; inv maps a pair's target-order
-// index to its row; eight loads in flight), back to physical units, into the
+// target's pair rows (stored in group order; roff gives each target-order
+// pair's row in units of 32 entries; a pair of order q contributes its first
+// (q+1)^2 entries; eight loads in flight), back to physical units, into the
 // reduced components of the local expansion.
 template <typename R>
-__global__ void __launch_bounds__(128) k_m2l_sum(const TreeDev t, int p, const R* __restrict__ out, int ldo,
-                                                 const int32_t* __restrict__ inv, double* __restrict__ loc) {
+__global__ void __launch_bounds__(128) k_m2l_sum(const TreeDev t, int p, const R* __restrict__ out,
+                                                 const int32_t* __restrict__ roff, double* __restrict__ loc) {
     const int i = blockIdx.x;
     const int nr = (p + 1) * (p + 1);
     const int q0 = t.far_off[i], q1 = t.far_off[i + 1];
@@ -831,11 +850,17 @@ __global__ void __launch_bounds__(128) k_m2l_sum(const TreeDev t, int p, const R
         for (; q + U <= q1; q += U) {
             R v[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) v[u] = out[(size_t)inv[q + u] * ldo + f];
+            for (int u = 0; u < U; ++u) {
+                const int qq = t.far_ord ? min((int)t.far_ord[q + u], p) : p;
+                v[u] = f < (qq + 1) * (qq + 1) ? out[(size_t)roff[q + u] * 32 + f] : (R)0;
+            }
 #pragma unroll
             for (int u = 0; u < U; ++u) acc.add(v[u]);
         }
-        for (; q < q1; ++q) acc.add(out[(size_t)inv[q] * ldo + f]);
+        for (; q < q1; ++q) {
+            const int qq = t.far_ord ? min((int)t.far_ord[q], p) : p;
+            if (f < (qq + 1) * (qq + 1)) acc.add(out[(size_t)roff[q] * 32 + f]);
+        }
         const int c = qcomp(f);
         const int k = c >> 24;
         double s = ih;
@@ -854,12 +879,10 @@ bool product_on_cuda_cores() {
 template <typename R, int CPT>
 int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
     const int M = t.num_nodes, nr = (p + 1) * (p + 1), N = 2 * p, nTr = rbase(N + 1);
-    const int ldo = (nr + 31) & ~31;  // result rows of whole 128-byte lines
     const bool tc = sizeof(R) == 4 && !product_on_cuda_cores();
     const int cols = tc ? kTcPairs : kTaskCols;
     const int64_t nf = t.nfar;
-    FMM_TRY(ws.m2l_out.ensure(sizeof(R) * (size_t)std::max<int64_t>(1, nf) * ldo));
-    const int32_t* inv = nullptr;  // row of each far pair (target order) in group order
+    const int32_t* roff = nullptr;  // row of each far pair (target order), units of 32 entries
     if (nf > 0) {
         FMM_TRY(ws.m2l_tgt.ensure(sizeof(int32_t) * nf));
         FMM_TRY(ws.m2l_keys.ensure(sizeof(uint64_t) * nf));
@@ -900,12 +923,6 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_CUDA_TRY(cub::DeviceRunLengthEncode::Encode(ws.cub_tmp.p, tb2, ws.m2l_keys2.as<uint64_t>(),
                                                         ws.m2l_ukeys.as<uint64_t>(), ws.m2l_cnt.as<int32_t>(),
                                                         d_nruns, (int)nf, st));
-        // result rows are written in group order; the per-target sum reads
-        // them through the inverse permutation (in the free unsorted-keys buffer)
-        count_launches(1);
-        k_inverse_perm<<<grid_for(nf, 256), 256, 0, st>>>(nf, ws.m2l_vals2.as<int32_t>(),
-                                                          reinterpret_cast<int32_t*>(ws.m2l_keys.p));
-        inv = reinterpret_cast<const int32_t*>(ws.m2l_keys.p);
         int ng = 0;
         FMM_CUDA_TRY(cudaMemcpyAsync(&ng, d_nruns, sizeof(int), cudaMemcpyDeviceToHost, st));
         FMM_CUDA_TRY(cudaStreamSynchronize(st));
@@ -943,9 +960,29 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_TRY(ws.cub_tmp.ensure(tb5));
         FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb5, ws.m2l_tcnt.as<int32_t>(),
                                                    ws.m2l_toff.as<int32_t>(), ng + 1, st));
-        int ntasks = 0;
-        FMM_CUDA_TRY(cudaMemcpyAsync(&ntasks, ws.m2l_toff.as<int32_t>() + ng, sizeof(int), cudaMemcpyDeviceToHost, st));
+        // result rows in group order, (q+1)^2 rounded up to 32 entries per
+        // pair; the per-target sum finds them through roff (in the free
+        // unsorted-keys buffer)
+        FMM_TRY(ws.m2l_rowbase.ensure(sizeof(int32_t) * (ng + 1)));
+        int32_t* rowbase = ws.m2l_rowbase.as<int32_t>();
+        count_launches(1);
+        k_row_sizes<<<grid_for(ng + 1, 256), 256, 0, st>>>(ng, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(),
+                                                            rowbase);
+        size_t tb7 = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tb7, rowbase, rowbase, ng + 1, st);
+        FMM_TRY(ws.cub_tmp.ensure(tb7));
+        FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb7, rowbase, rowbase, ng + 1, st));
+        count_launches(1);
+        k_row_offsets<<<grid_for(ng, 8), 256, 0, st>>>(ng, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(),
+                                                        rowbase, ws.m2l_vals2.as<int32_t>(),
+                                                        reinterpret_cast<int32_t*>(ws.m2l_keys.p));
+        roff = reinterpret_cast<const int32_t*>(ws.m2l_keys.p);
+        int hcnt[2] = {0, 0};  // tasks, rows (units of 32 entries)
+        FMM_CUDA_TRY(cudaMemcpyAsync(&hcnt[0], ws.m2l_toff.as<int32_t>() + ng, sizeof(int), cudaMemcpyDeviceToHost, st));
+        FMM_CUDA_TRY(cudaMemcpyAsync(&hcnt[1], rowbase + ng, sizeof(int), cudaMemcpyDeviceToHost, st));
         FMM_CUDA_TRY(cudaStreamSynchronize(st));
+        const int ntasks = hcnt[0];
+        FMM_TRY(ws.m2l_out.ensure(sizeof(R) * 32 * (size_t)std::max(1, hcnt[1])));
         FMM_TRY(ws.m2l_tasks.ensure(sizeof(int2) * std::max(1, ntasks)));
         count_launches(1);
         k_fill_tasks<<<grid_for(ng, 256), 256, 0, st>>>(ng, cols, ws.m2l_gstart.as<int32_t>(),
@@ -993,7 +1030,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
             k_m2l_tc<<<(unsigned)grid, kTcThreads, TcSmem::bytes, st>>>(
                 ws.m2l_tasks.as<int2>(), ntasks, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(), goff,
                 ws.m2l_gop.as<float>(), ws.m2l_vals.as<int32_t>(), ws.m2l_wsplit.as<float>(), ldk,
-                reinterpret_cast<float*>(ws.m2l_out.p), ldo, d_err);
+                reinterpret_cast<float*>(ws.m2l_out.p), rowbase, d_err);
             if (p > kTcMaxQ) {
                 // groups of order > 10 on the CUDA cores
                 const GemmSmem<float, CPT> L(p);
@@ -1004,7 +1041,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
                     ws.m2l_tasks.as<int2>(), cols, kTcMaxQ + 1, p, ws.m2l_gstart.as<int32_t>(),
                     ws.m2l_gq.as<int32_t>(), ws.m2l_gab.as<float2>(), reinterpret_cast<const float*>(ws.m2l_T.p),
                     ldT, ws.m2l_vals2.as<int32_t>(), t.far_src, reinterpret_cast<const float*>(ws.m2l_wsc.p),
-                    reinterpret_cast<float*>(ws.m2l_out.p), ldo);
+                    reinterpret_cast<float*>(ws.m2l_out.p), rowbase);
             }
             if (ws.product_timed) cudaEventRecord(ws.ev[9], st);
             int herr = 0;
@@ -1023,12 +1060,13 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
             k_m2l_gemm<R, CPT><<<(unsigned)ntasks, kGemmThreads, L.bytes, st>>>(
                 ws.m2l_tasks.as<int2>(), cols, 0, p, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(),
                 ws.m2l_gab.as<float2>(), ws.m2l_T.as<R>(), ldT, ws.m2l_vals2.as<int32_t>(), t.far_src,
-                ws.m2l_wsc.as<R>(), ws.m2l_out.as<R>(), ldo);
+                ws.m2l_wsc.as<R>(), ws.m2l_out.as<R>(), rowbase);
             if (ws.product_timed) cudaEventRecord(ws.ev[9], st);
         }
     }
     count_launches(1);
-    k_m2l_sum<R><<<(unsigned)M, 128, 0, st>>>(t, p, ws.m2l_out.as<R>(), ldo, inv, ws.loc.as<double>());
+    if (nf == 0) FMM_TRY(ws.m2l_out.ensure(sizeof(R) * 32));
+    k_m2l_sum<R><<<(unsigned)M, 128, 0, st>>>(t, p, ws.m2l_out.as<R>(), roff, ws.loc.as<double>());
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
