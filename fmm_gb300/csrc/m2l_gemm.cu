@@ -783,8 +783,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
             // 128 operator rows), from rowbase[g] x 32 in group order
             const int rl = row_len(q);
             float* gout = out + ((size_t)rowbase[g] + (size_t)tk.y * (rl / 32)) * 32;
+            // warps whose 32 rows f lie beyond the row length have nothing to write
 #pragma unroll 1
-            for (int c = share * CB; c < cnt; c += kShares * CB) {
+            for (int c = share * CB; c < cnt && 32 * sp < rl; c += kShares * CB) {
                 float v[CB];
 #pragma unroll
                 for (int b = 0; b < kTcEpiBatch; ++b) umma::tmem_ld16(base + (uint32_t)(c + 16 * b), v + 16 * b);
