@@ -262,6 +262,7 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     }
     TreeDev t;
     const int nf = nT(f);
+    ws.product_err = nullptr;  // set by the tensor-core M2L product, read at the end of the call
     cudaEventRecord(ws.ev[0], st);
     FMM_TRY(build_tree(ws, P.x, P.n, tp, t, st));
     cudaEventRecord(ws.ev[1], st);
@@ -377,8 +378,12 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
                                                                                                     d_hist);
     }
     FMM_CUDA_TRY(cudaMemcpyAsync(hist, d_hist, sizeof(hist), cudaMemcpyDeviceToHost, st));
+    int product_err = 0;
+    if (ws.product_err)
+        FMM_CUDA_TRY(cudaMemcpyAsync(&product_err, ws.product_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     FMM_CUDA_TRY(cudaStreamSynchronize(st));
     FMM_CUDA_TRY(cudaGetLastError());
+    if (product_err) return FMM_ETIMEOUT;  // a bounded wait of the M2L product gave up
     Stats s;
     s.v[0] = t.num_nodes;
     s.v[1] = t.num_leaves;

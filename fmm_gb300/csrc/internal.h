@@ -129,6 +129,7 @@ struct Workspace {
     bool events_ready = false;
     bool product_timed = false;  // ev[8], ev[9] bracket the grouped M2L product kernel of the last call
     bool f32node_ok = false;     // f32node holds the FP32 node data of the current tree
+    int* product_err = nullptr;  // device flag of the tensor-core M2L product, checked at the end of a call
     int64_t m2l_groups = 0;      // displacement groups of the last grouped M2L
     int64_t list_candidates = 0; // cell pairs examined by the last list build
     int64_t list_evals = 0;      // of which evaluated by the selector network

@@ -1008,10 +1008,11 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
             cub::DeviceScan::ExclusiveSum(nullptr, tb6, goff, goff, ng + 1, st);
             FMM_TRY(ws.cub_tmp.ensure(tb6));
             FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb6, goff, goff, ng + 1, st));
-            int64_t gop_total = 0;
-            FMM_CUDA_TRY(cudaMemcpyAsync(&gop_total, goff + ng, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-            FMM_CUDA_TRY(cudaStreamSynchronize(st));
-            FMM_TRY(ws.m2l_gop.ensure(sizeof(float) * (size_t)std::max<int64_t>(1, gop_total)));
+            // room for every group at the largest order of the call (no wait
+            // for the exact total)
+            const int nch_max = (std::min(p, kTcMaxQ) + 1) * (std::min(p, kTcMaxQ) + 1);
+            const size_t gop_max = (size_t)ng * ((nch_max + kTcKC - 1) / kTcKC) * 2 * kTcRows * kTcKC;
+            FMM_TRY(ws.m2l_gop.ensure(sizeof(float) * std::max<size_t>(1, gop_max)));
             count_launches(1);
             k_group_operator<<<(unsigned)ng, 256, 0, st>>>(ldT, reinterpret_cast<const float*>(ws.m2l_T.p),
                                                            ws.m2l_gq.as<int32_t>(), ws.m2l_gab.as<float2>(), goff,
@@ -1022,7 +1023,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
             FMM_CUDA_TRY(cudaGetDevice(&dev));
             FMM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
             const int grid = std::max(1, std::min(ntasks, sms));  // one block per SM (all tensor memory)
-            FMM_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+            if (!ws.product_err) FMM_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));  // first product of the call
             if (ws.events_ready) {
                 cudaEventRecord(ws.ev[8], st);
                 ws.product_timed = true;
@@ -1045,10 +1046,8 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
                     reinterpret_cast<float*>(ws.m2l_out.p), rowbase);
             }
             if (ws.product_timed) cudaEventRecord(ws.ev[9], st);
-            int herr = 0;
-            FMM_CUDA_TRY(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
-            FMM_CUDA_TRY(cudaStreamSynchronize(st));
-            if (herr) return FMM_ETIMEOUT;
+            // the product's error flag is read with the call's final copies
+            ws.product_err = d_err;
         } else {
             const GemmSmem<R, CPT> L(p);
             FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_m2l_gemm<R, CPT>,

@@ -819,21 +819,27 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
         t.nnear = (int64_t)h[2];
         ws.list_candidates = candidates;
         ws.list_evals = (int64_t)h[4];
-        // sort both lists by (target, source) and build CSR offsets
+        // sort both lists by (target, source) and build CSR offsets; the keys
+        // are target << 36 (far, with the order in bits 32-35) or << 32
+        // (near), so only the bits up to the largest node index are sorted
         FMM_TRY(ws.far_sorted.ensure(sizeof(uint64_t) * std::max<int64_t>(1, t.nfar)));
         FMM_TRY(ws.near_sorted.ensure(sizeof(uint64_t) * std::max<int64_t>(1, t.nnear)));
+        int nbits = 1;
+        while (nbits < 31 && (1 << nbits) < M) ++nbits;
+        const int far_bits = std::min(64, 36 + nbits), near_bits = std::min(64, 32 + nbits);
         size_t tb = 0, tb2 = 0;
         cub::DeviceRadixSort::SortKeys(nullptr, tb, ws.far_pairs.as<uint64_t>(), ws.far_sorted.as<uint64_t>(),
-                                       (int)t.nfar, 0, 64, st);
+                                       (int)t.nfar, 0, far_bits, st);
         cub::DeviceRadixSort::SortKeys(nullptr, tb2, ws.near_pairs.as<uint64_t>(), ws.near_sorted.as<uint64_t>(),
-                                       (int)t.nnear, 0, 64, st);
+                                       (int)t.nnear, 0, near_bits, st);
         FMM_TRY(ensure_cub_tmp(ws, std::max(tb, tb2)));
         if (t.nfar > 0)
             FMM_CUDA_TRY(cub::DeviceRadixSort::SortKeys(ws.cub_tmp.p, tb, ws.far_pairs.as<uint64_t>(),
-                                                        ws.far_sorted.as<uint64_t>(), (int)t.nfar, 0, 64, st));
+                                                        ws.far_sorted.as<uint64_t>(), (int)t.nfar, 0, far_bits, st));
         if (t.nnear > 0)
             FMM_CUDA_TRY(cub::DeviceRadixSort::SortKeys(ws.cub_tmp.p, tb2, ws.near_pairs.as<uint64_t>(),
-                                                        ws.near_sorted.as<uint64_t>(), (int)t.nnear, 0, 64, st));
+                                                        ws.near_sorted.as<uint64_t>(), (int)t.nnear, 0, near_bits,
+                                                        st));
         FMM_TRY(ws.far_src.ensure(sizeof(int32_t) * (std::max<int64_t>(1, t.nfar) + (M + 1))));
         FMM_TRY(ws.near_src.ensure(sizeof(int32_t) * (std::max<int64_t>(1, t.nnear) + (M + 1))));
         t.far_src = ws.far_src.as<int32_t>();
