@@ -43,6 +43,11 @@ constexpr int kKeyBits = 46;
 constexpr int64_t kDOff = 1 << 11;       // offset of the 12-bit displacement fields
 constexpr int kTaskCols = 512;           // pairs (columns) per product block
 constexpr int kGemmThreads = 128;        // 16 row groups x 8 column groups
+constexpr int kTcRows = 128;             // tensor-core MMA M: operator rows f per half
+constexpr int kTcPairs = 256;            // tensor-core MMA N: pairs per task
+
+// Operator halves of 128 rows f for order q (two above order 10).
+__host__ __device__ __forceinline__ int tc_halves(int q) { return (q + 1) * (q + 1) > kTcRows ? 2 : 1; }
 
 __global__ void k_far_targets(int M, const int32_t* __restrict__ off, int32_t* __restrict__ tgt) {
     const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -200,19 +205,32 @@ __global__ void __launch_bounds__(128) k_group_tensor(int ngroups, const uint64_
     }
 }
 
-// Tasks of up to `cols` pairs of one group: counts, then (group, first column).
-__global__ void k_task_counts(int ng, int cols, const int32_t* __restrict__ gstart, int32_t* __restrict__ tcnt) {
+// Tasks of up to `cols` pairs of one group: counts, then (group, first
+// column).  cols < 0: tensor-core tasks of kTcPairs pairs and one operator
+// half each, (group, 2 x first column + half).
+__global__ void k_task_counts(int ng, int cols, const int32_t* __restrict__ gq, const int32_t* __restrict__ gstart,
+                              int32_t* __restrict__ tcnt) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g > ng) return;
-    tcnt[g] = g < ng ? (gstart[g + 1] - gstart[g] + cols - 1) / cols : 0;
+    if (g == ng) {
+        tcnt[g] = 0;
+        return;
+    }
+    const int n = gstart[g + 1] - gstart[g];
+    tcnt[g] = cols > 0 ? (n + cols - 1) / cols : (n + kTcPairs - 1) / kTcPairs * tc_halves(gq[g]);
 }
 
-__global__ void k_fill_tasks(int ng, int cols, const int32_t* __restrict__ gstart, const int32_t* __restrict__ toff,
-                             int2* __restrict__ tasks) {
+__global__ void k_fill_tasks(int ng, int cols, const int32_t* __restrict__ gq, const int32_t* __restrict__ gstart,
+                             const int32_t* __restrict__ toff, int2* __restrict__ tasks) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ng) return;
     const int n = toff[g + 1] - toff[g];
-    for (int k = 0; k < n; ++k) tasks[toff[g] + k] = make_int2(g, k * cols);
+    if (cols > 0) {
+        for (int k = 0; k < n; ++k) tasks[toff[g] + k] = make_int2(g, k * cols);
+    } else {
+        const int h = tc_halves(gq[g]);
+        for (int k = 0; k < n; ++k) tasks[toff[g] + k] = make_int2(g, 2 * kTcPairs * (k / h) + k % h);
+    }
 }
 
 // Shared-memory plan of the product kernel (elements of R unless noted).
@@ -456,9 +474,9 @@ __global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restric
 }
 
 // ---------------------------------------------------------------------------
-// Tensor-core product, for groups of order q <= 10 ((q+1)^2 <= 128).  A task
-// is up to 256 pairs of one group: D = G W^T with G the operator (f x s,
-// M = 128 rows f), W the pairs' weights (pairs x s, N = 256) and K = (q+1)^2
+// Tensor-core product.  A task is up to 256 pairs of one group and one half
+// of its operator: D = G W^T with G the operator half (f x s, M = 128 rows
+// f), W the pairs' weights (pairs x s, N = 256) and K = (q+1)^2
 // in chunks of 8 (one MMA K step).  Both operands are split into TF32 parts,
 // x = hi + lo, and D accumulates G_hi W_hi + G_hi W_lo + G_lo W_hi in FP32
 // (the dropped G_lo W_lo and the rounding of the parts leave about 2^-22 of
@@ -478,10 +496,8 @@ __global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restric
 //              consecutive entries of the pair's result row (one aligned
 //              128-byte line), then frees the accumulator.
 // The two accumulators let the epilogue of one task overlap the MMAs of the
-// next.  Groups of higher order go to the CUDA-core kernel.
-constexpr int kTcMaxQ = 10;
-constexpr int kTcRows = 128;       // MMA M: operator rows f
-constexpr int kTcPairs = 256;      // MMA N: pairs per task
+// next.  Orders above 10 ((q+1)^2 > 128 rows f) have two operator halves,
+// each a task of its own over the same pairs.
 constexpr int kTcKC = 8;           // reduced components per chunk (one MMA K step)
 constexpr int kTcStages = 8;
 constexpr int kTcProducers = 64;   // warps 0-1
@@ -550,32 +566,32 @@ __global__ void k_pair_sources(int64_t nf, const int32_t* __restrict__ svals, co
     if (k < nf) psrc[k] = far_src[svals[k]];
 }
 
-// Size in floats of a group's split operator (chunks x (hi + lo) x 128 x KC);
-// zero for the groups the CUDA cores take.
+// Size in floats of a group's split operator (halves x chunks x (hi + lo) x
+// 128 x KC).
 __global__ void k_gop_sizes(int ng, const int32_t* __restrict__ gq, int64_t* __restrict__ sz) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g > ng) return;
-    if (g == ng || gq[g] > kTcMaxQ) {
+    if (g == ng) {
         sz[g] = 0;
         return;
     }
-    const int nrq = (gq[g] + 1) * (gq[g] + 1), nch = (nrq + kTcKC - 1) / kTcKC;
-    sz[g] = (int64_t)nch * 2 * kTcRows * kTcKC;
+    const int q = gq[g], nrq = (q + 1) * (q + 1), nch = (nrq + kTcKC - 1) / kTcKC;
+    sz[g] = (int64_t)tc_halves(q) * nch * 2 * kTcRows * kTcKC;
 }
 
 // Block per group: G_fs = a^(|f|+1) b^|s| T_{f+s}(D_c) split into TF32 parts,
-// written chunk by chunk in the operand layout: [chunk][hi 128 x KC][lo 128 x KC].
+// written half by half and chunk by chunk in the operand layout:
+// [half][chunk][hi 128 x KC][lo 128 x KC] (half h: rows f = 128 h ..).
 __global__ void __launch_bounds__(256) k_group_operator(int ldT, const float* __restrict__ gT,
                                                         const int32_t* __restrict__ gq,
                                                         const float2* __restrict__ gab,
                                                         const int64_t* __restrict__ goff, float* __restrict__ gop) {
-    __shared__ int dec[(kTcMaxQ + 1) * (kTcMaxQ + 1)];
+    __shared__ int dec[(kMaxP + 1) * (kMaxP + 1)];
     __shared__ float apow[32], bpow[32];
-    __shared__ float Tsh[1 + 3 * (2 * kTcMaxQ) * (2 * kTcMaxQ + 1) / 2];
+    __shared__ float Tsh[1 + 3 * (2 * kMaxP) * (2 * kMaxP + 1) / 2];
     const int g = blockIdx.x;
     const int q = gq[g];
-    if (q > kTcMaxQ) return;
-    const int nrq = (q + 1) * (q + 1), nch = (nrq + kTcKC - 1) / kTcKC;
+    const int nrq = (q + 1) * (q + 1), nch = (nrq + kTcKC - 1) / kTcKC, nrow = tc_halves(q) * kTcRows;
     for (int e = threadIdx.x; e < nrq; e += blockDim.x) dec[e] = qcomp(e);
     if (threadIdx.x < 32) {
         const float2 ab = gab[g];
@@ -592,7 +608,7 @@ __global__ void __launch_bounds__(256) k_group_operator(int ldT, const float* __
     __syncthreads();
     float* out = gop + goff[g];
     const int kp = nch * kTcKC;
-    for (int e = threadIdx.x; e < kTcRows * kp; e += blockDim.x) {
+    for (int e = threadIdx.x; e < nrow * kp; e += blockDim.x) {
         const int n = e / kp, s = e - n * kp;
         float v = 0.0f;
         if (n < nrq && s < nrq) {
@@ -603,17 +619,10 @@ __global__ void __launch_bounds__(256) k_group_operator(int ldT, const float* __
         }
         float h, l;
         umma::split_tf32(v, h, l);
-        float* o = out + (size_t)(s / kTcKC) * 2 * kTcRows * kTcKC + tc_off(n, s % kTcKC);
+        float* o = out + ((size_t)(n / kTcRows) * nch + s / kTcKC) * 2 * kTcRows * kTcKC + tc_off(n % kTcRows, s % kTcKC);
         o[0] = h;
         o[kTcRows * kTcKC] = l;
     }
-}
-
-// Next task index >= t of this block's stride that the tensor cores take.
-__device__ __forceinline__ int tc_next_task(int t, int ntasks, const int2* __restrict__ tasks,
-                                            const int32_t* __restrict__ gq) {
-    while (t < ntasks && gq[tasks[t].x] > kTcMaxQ) t += gridDim.x;
-    return t;
 }
 
 // Source nodes of a producer thread's rows 8 (rg0 + k * producer warps) + rsub of task t.
@@ -621,7 +630,7 @@ template <int RG>
 __device__ __forceinline__ void tc_load_rows(int t, const int2* __restrict__ tasks, const int32_t* __restrict__ gstart,
                                              const int32_t* __restrict__ psrc, int rg0, int rsub, int (&r)[RG]) {
     const int2 tk = tasks[t];
-    const int gs = gstart[tk.x] + tk.y, cnt = min(kTcPairs, gstart[tk.x + 1] - gs);
+    const int gs = gstart[tk.x] + (tk.y >> 1), cnt = min(kTcPairs, gstart[tk.x + 1] - gs);
 #pragma unroll
     for (int k = 0; k < RG; ++k) {
         const int pr = 8 * (rg0 + (kTcProducers / 32) * k) + rsub;
@@ -677,15 +686,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
         const int rg0 = pt >> 5;
         const uint64_t keep = umma::l2_evict_last();  // the weights stay in L2 beside the result stream
         uint32_t u = 0;
-        int task = tc_next_task(blockIdx.x, ntasks, tasks, gq);
+        int task = blockIdx.x;
         int rows[RG], nrows[RG];
         if (task < ntasks) tc_load_rows<RG>(task, tasks, gstart, psrc, rg0, rsub, rows);
         while (task < ntasks && ok) {
             const int g = tasks[task].x, q = gq[g];
             const int nch = ((q + 1) * (q + 1) + kTcKC - 1) / kTcKC;
-            const int next = tc_next_task(task + gridDim.x, ntasks, tasks, gq);
+            const int next = task + gridDim.x;
             if (next < ntasks) tc_load_rows<RG>(next, tasks, gstart, psrc, rg0, rsub, nrows);  // in flight
-            const float* G = gop + goff[g];
+            // the task's operator half
+            const float* G = gop + goff[g] + (size_t)(tasks[task].y & 1) * nch * 2 * TcSmem::g_floats;
             for (int ch = 0; ch < nch; ++ch, ++u) {
                 const int st = (int)(u % kTcStages);
                 if (u >= (uint32_t)kTcStages &&
@@ -722,7 +732,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
             constexpr uint32_t LBO = 128, SBO = kTcKC / 4 * 128;
             for (int task = blockIdx.x; task < ntasks && ok; task += gridDim.x) {
                 const int g = tasks[task].x, q = gq[g];
-                if (q > kTcMaxQ) continue;
                 const int nch = ((q + 1) * (q + 1) + kTcKC - 1) / kTcKC;
                 const int acc = (int)(tl & 1);
                 if (tl >= 2 && !umma::mbar_wait(&acc_empty[acc], ((tl >> 1) - 1) & 1, kTcWaitCycles)) {
@@ -769,8 +778,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
         for (int task = blockIdx.x; task < ntasks && ok; task += gridDim.x) {
             const int2 tk = tasks[task];
             const int g = tk.x, q = gq[g];
-            if (q > kTcMaxQ) continue;
-            const int gs = gstart[g] + tk.y;
+            const int f0 = kTcRows * (tk.y & 1), fr = f0 + f;  // the task's operator half; this lane's row
+            const int gs = gstart[g] + (tk.y >> 1);
             const int cnt = min(kTcPairs, gstart[g + 1] - gs);
             const int acc = (int)(tl & 1);
             if (!umma::mbar_wait(&acc_full[acc], (tl >> 1) & 1, kTcWaitCycles)) {
@@ -779,22 +788,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
             }
             umma::fence_after_sync();
             const uint32_t base = tmem + ((uint32_t)(32 * sp) << 16) + (uint32_t)(acc * kTcPairs);
-            // the group's rows: (q+1)^2 rounded up to 32 entries (at most the
-            // 128 operator rows), from rowbase[g] x 32 in group order
+            // the group's rows: (q+1)^2 rounded up to 32 entries, from
+            // rowbase[g] x 32 in group order
             const int rl = row_len(q);
-            float* gout = out + ((size_t)rowbase[g] + (size_t)tk.y * (rl / 32)) * 32;
+            float* gout = out + ((size_t)rowbase[g] + (size_t)(tk.y >> 1) * (rl / 32)) * 32;
             // warps whose 32 rows f lie beyond the row length have nothing to write
 #pragma unroll 1
-            for (int c = share * CB; c < cnt && 32 * sp < rl; c += kShares * CB) {
+            for (int c = share * CB; c < cnt && f0 + 32 * sp < rl; c += kShares * CB) {
                 float v[CB];
 #pragma unroll
                 for (int b = 0; b < kTcEpiBatch; ++b) umma::tmem_ld16(base + (uint32_t)(c + 16 * b), v + 16 * b);
                 umma::tmem_ld_wait();
                 // the task's rows are consecutive; streaming stores of whole lines
-                if (f < rl) {
+                if (fr < rl) {
 #pragma unroll
                     for (int jj = 0; jj < CB; ++jj)
-                        if (c + jj < cnt) __stcs(gout + (size_t)(c + jj) * rl + f, v[jj]);
+                        if (c + jj < cnt) __stcs(gout + (size_t)(c + jj) * rl + fr, v[jj]);
                 }
             }
             umma::fence_before_sync();
@@ -881,7 +890,7 @@ template <typename R, int CPT>
 int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
     const int M = t.num_nodes, nr = (p + 1) * (p + 1), N = 2 * p, nTr = rbase(N + 1);
     const bool tc = sizeof(R) == 4 && !product_on_cuda_cores();
-    const int cols = tc ? kTcPairs : kTaskCols;
+    const int cols = tc ? -1 : kTaskCols;  // -1: tensor-core tasks (256 pairs, one operator half)
     const int64_t nf = t.nfar;
     const int32_t* roff = nullptr;  // row of each far pair (target order), units of 32 entries
     if (nf > 0) {
@@ -950,12 +959,13 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
                 ng, ws.m2l_ukeys.as<uint64_t>(), ws.m2l_gstart.as<int32_t>(), ws.m2l_vals2.as<int32_t>(), tgt, t, p,
                 ldT, ws.m2l_T.as<R>(), ws.m2l_gq.as<int32_t>(), ws.m2l_gab.as<float2>());
         }
-        // tasks: up to kTaskCols pairs of one group each
+        // tasks: up to kTaskCols pairs of one group each (tensor cores: 256
+        // pairs and one operator half)
         FMM_TRY(ws.m2l_tcnt.ensure(sizeof(int32_t) * (ng + 1)));
         FMM_TRY(ws.m2l_toff.ensure(sizeof(int32_t) * (ng + 1)));
         count_launches(1);
-        k_task_counts<<<grid_for(ng + 1, 256), 256, 0, st>>>(ng, cols, ws.m2l_gstart.as<int32_t>(),
-                                                              ws.m2l_tcnt.as<int32_t>());
+        k_task_counts<<<grid_for(ng + 1, 256), 256, 0, st>>>(ng, cols, ws.m2l_gq.as<int32_t>(),
+                                                              ws.m2l_gstart.as<int32_t>(), ws.m2l_tcnt.as<int32_t>());
         size_t tb5 = 0;
         cub::DeviceScan::ExclusiveSum(nullptr, tb5, ws.m2l_tcnt.as<int32_t>(), ws.m2l_toff.as<int32_t>(), ng + 1, st);
         FMM_TRY(ws.cub_tmp.ensure(tb5));
@@ -986,7 +996,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_TRY(ws.m2l_out.ensure(sizeof(R) * 32 * (size_t)std::max(1, hcnt[1])));
         FMM_TRY(ws.m2l_tasks.ensure(sizeof(int2) * std::max(1, ntasks)));
         count_launches(1);
-        k_fill_tasks<<<grid_for(ng, 256), 256, 0, st>>>(ng, cols, ws.m2l_gstart.as<int32_t>(),
+        k_fill_tasks<<<grid_for(ng, 256), 256, 0, st>>>(ng, cols, ws.m2l_gq.as<int32_t>(), ws.m2l_gstart.as<int32_t>(),
                                                         ws.m2l_toff.as<int32_t>(), ws.m2l_tasks.as<int2>());
         int* d_err = reinterpret_cast<int*>(ws.counters.as<unsigned long long>() + 13);
         if (tc) {
@@ -1010,8 +1020,8 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
             FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb6, goff, goff, ng + 1, st));
             // room for every group at the largest order of the call (no wait
             // for the exact total)
-            const int nch_max = (std::min(p, kTcMaxQ) + 1) * (std::min(p, kTcMaxQ) + 1);
-            const size_t gop_max = (size_t)ng * ((nch_max + kTcKC - 1) / kTcKC) * 2 * kTcRows * kTcKC;
+            const int nr_max = (p + 1) * (p + 1);
+            const size_t gop_max = (size_t)ng * tc_halves(p) * ((nr_max + kTcKC - 1) / kTcKC) * 2 * kTcRows * kTcKC;
             FMM_TRY(ws.m2l_gop.ensure(sizeof(float) * std::max<size_t>(1, gop_max)));
             count_launches(1);
             k_group_operator<<<(unsigned)ng, 256, 0, st>>>(ldT, reinterpret_cast<const float*>(ws.m2l_T.p),
@@ -1033,18 +1043,6 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
                 ws.m2l_tasks.as<int2>(), ntasks, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(), goff,
                 ws.m2l_gop.as<float>(), ws.m2l_vals.as<int32_t>(), ws.m2l_wsplit.as<float>(), ldk,
                 reinterpret_cast<float*>(ws.m2l_out.p), rowbase, d_err);
-            if (p > kTcMaxQ) {
-                // groups of order > 10 on the CUDA cores
-                const GemmSmem<float, CPT> L(p);
-                FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_m2l_gemm<float, CPT>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes));
-                count_launches(1);
-                k_m2l_gemm<float, CPT><<<(unsigned)ntasks, kGemmThreads, L.bytes, st>>>(
-                    ws.m2l_tasks.as<int2>(), cols, kTcMaxQ + 1, p, ws.m2l_gstart.as<int32_t>(),
-                    ws.m2l_gq.as<int32_t>(), ws.m2l_gab.as<float2>(), reinterpret_cast<const float*>(ws.m2l_T.p),
-                    ldT, ws.m2l_vals2.as<int32_t>(), t.far_src, reinterpret_cast<const float*>(ws.m2l_wsc.p),
-                    reinterpret_cast<float*>(ws.m2l_out.p), rowbase);
-            }
             if (ws.product_timed) cudaEventRecord(ws.ev[9], st);
             // the product's error flag is read with the call's final copies
             ws.product_err = d_err;

@@ -223,7 +223,7 @@ def test_mixed_near_field_exclusions(one_sided):
     assert rel_err(F32, F64, slice(1, None)) < 5e-6
 
 
-@pytest.mark.parametrize("p", [3, 10, 12])
+@pytest.mark.parametrize("p", [3, 10, 11, 12])
 def test_m2l_tensor_core_product_matches_cuda_cores(p, monkeypatch):
     """The FP32 M2L product on the tensor cores (operands split into TF32
     parts, three products per term, FP32 accumulation in tensor memory) agrees
