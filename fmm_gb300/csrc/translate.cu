@@ -280,37 +280,16 @@ __global__ void __launch_bounds__(kP2mThreads) k_p2m(const TreeDev t, const doub
     }
 }
 
-// ---------------------------------------------------------------- M2M
+// ---------------------------------------------------------------- M2M / L2L
+// Both translations factor over the axes, d^u / u! = (dx^ux/ux!)
+// (dy^uy/uy!) (dz^uz/uz!), so each is three one-dimensional shifts (z, then
+// y, then x) of an expansion held densely in shared memory, index
+// (a (p+1) + b) (p+1) + c for the component (a, b, c): C(p+4,4) terms per
+// shift instead of the C(p+6,6) of the direct sum, and no output of a shift
+// has more than p+1 terms, so the block's outputs finish together.  A block
+// per parent node takes its children one after another.
 constexpr int kXThreads = 256;
-
-// Scaled powers of the offsets of a node's children (into dp[c][u]) and the
-// list of its children; returns the number of children.
-__device__ __forceinline__ int child_powers(const TreeDev& t, int node, int p, int nq, const int* comp, int* ch,
-                                            double* e, double* dp, double sign) {
-    if (threadIdx.x == 0) {
-        int k = 0;
-        for (int o = 0; o < 8; ++o) {
-            const int c = t.child[8 * node + o];
-            if (c >= 0) ch[k++] = c;
-        }
-        ch[8] = k;
-    }
-    __syncthreads();
-    const int nch = ch[8], P1 = p + 1;
-    if (threadIdx.x < 3 * nch) {
-        const int b = threadIdx.x / 3, ax = threadIdx.x % 3, c = ch[b];
-        const double d = ax == 0 ? t.cx[c] - t.cx[node] : (ax == 1 ? t.cy[c] - t.cy[node] : t.cz[c] - t.cz[node]);
-        scaled_powers(sign * d, p, e + (b * 3 + ax) * P1);
-    }
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < nch * nq; idx += blockDim.x) {
-        const int b = idx / nq, u = idx % nq;
-        const int cc = comp[u];
-        const double* eb = e + b * 3 * P1;
-        dp[b * nq + u] = eb[ux_(cc)] * eb[P1 + uy_(cc)] * eb[2 * P1 + uz_(cc)];
-    }
-    return nch;
-}
+constexpr int kXOut = (nT(kMaxP) + kXThreads - 1) / kXThreads;  // outputs per thread
 
 // (hi, lo) FP32 pair of an FP64 value; *big set when it is outside the range
 // where double-float products keep their precision.
@@ -332,144 +311,214 @@ __device__ __forceinline__ void df_mac(float2 x, float2 y, float& h, float& l) {
     h = sum;
 }
 
-// DF: the products and sums in double-float (FP32 pipe; the FP64 pipe is the
-// scarce one) when the block's powers and moments are within range, else
-// FP64.
+// Arithmetic of the shifts: FP64, or double-float pairs on the FP32 pipe.
+template <bool DF>
+struct XOps;
+template <>
+struct XOps<false> {
+    using V = double;
+    struct Acc {
+        double a = 0.0;
+        __device__ __forceinline__ void mac(double x, double y) { a = fma(x, y, a); }
+        __device__ __forceinline__ double val() const { return a; }
+    };
+    static __device__ __forceinline__ double in(double w, int*) { return w; }
+    static __device__ __forceinline__ double out(double v) { return v; }
+};
+template <>
+struct XOps<true> {
+    using V = float2;
+    struct Acc {
+        float h = 0.0f, l = 0.0f;
+        __device__ __forceinline__ void mac(float2 x, float2 y) { df_mac(x, y, h, l); }
+        __device__ __forceinline__ float2 val() const {
+            const float s = h + l;
+            return make_float2(s, l - (s - h));
+        }
+    };
+    static __device__ __forceinline__ float2 in(double w, int* big) { return to_df(w, big); }
+    static __device__ __forceinline__ double out(float2 v) { return (double)v.x + (double)v.y; }
+};
+
+__device__ __forceinline__ int d3(int a, int b, int c, int P1) { return (a * P1 + b) * P1 + c; }
+
+// Children of a node (ch[0..7], count in ch[8]) and the scaled powers
+// d^a / a! of their offsets d = c_child - c_node, e[(k * 3 + axis) * (p+1) + a].
+__device__ __forceinline__ void child_offsets(const TreeDev& t, int node, int p, int* ch, double* e) {
+    if (threadIdx.x == 0) {
+        int k = 0;
+        for (int o = 0; o < 8; ++o) {
+            const int c = t.child[8 * node + o];
+            if (c >= 0) ch[k++] = c;
+        }
+        ch[8] = k;
+    }
+    __syncthreads();
+    const int P1 = p + 1;
+    if (threadIdx.x < 3 * ch[8]) {
+        const int b = threadIdx.x / 3, ax = threadIdx.x % 3, c = ch[b];
+        const double d = ax == 0 ? t.cx[c] - t.cx[node] : (ax == 1 ? t.cy[c] - t.cy[node] : t.cz[c] - t.cz[node]);
+        scaled_powers(d, p, e + (b * 3 + ax) * P1);
+    }
+    __syncthreads();
+}
+
+// M2M of one parent: M'_t = sum_children sum_{u <= t} (d^u/u!) M'_{t-u}(child)
+// as shifts along z (Y from X), y (X from Y) and x (into the accumulators of
+// the thread's outputs).  Writes the result unless *big was raised.
+template <bool DF>
+__device__ __forceinline__ void m2m_node(const TreeDev& t, int node, int p, int nq, const int* comp, const int* ch,
+                                         const double* e, void* buf, int* big, double* __restrict__ mom) {
+    using O = XOps<DF>;
+    using V = typename O::V;
+    const int P1 = p + 1, n3 = P1 * P1 * P1;
+    V* X = reinterpret_cast<V*>(buf);
+    V* Y = X + n3;
+    V* E = Y + n3;  // [8][3][p+1]
+    const int nch = ch[8];
+    for (int k = threadIdx.x; k < nch * 3 * P1; k += blockDim.x) E[k] = O::in(e[k], big);
+    typename O::Acc acc[kXOut];
+    for (int b = 0; b < nch; ++b) {
+        const double* mc = mom + (size_t)ch[b] * nq;
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            const int cc = comp[q];
+            X[d3(cc & 0xff, (cc >> 8) & 0xff, cc >> 16, P1)] = O::in(mc[q], big);
+        }
+        __syncthreads();
+        const V* ex = E + b * 3 * P1;
+        const V* ey = ex + P1;
+        const V* ez = ey + P1;
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            const int cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
+            typename O::Acc s;
+            for (int u = 0; u <= z; ++u) s.mac(ez[u], X[d3(x, y, z - u, P1)]);
+            Y[d3(x, y, z, P1)] = s.val();
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            const int cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
+            typename O::Acc s;
+            for (int u = 0; u <= y; ++u) s.mac(ey[u], Y[d3(x, y - u, z, P1)]);
+            X[d3(x, y, z, P1)] = s.val();
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kXOut; ++r) {
+            const int q = threadIdx.x + kXThreads * r;
+            if (q < nq) {
+                const int cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
+                for (int u = 0; u <= x; ++u) acc[r].mac(ex[u], X[d3(x - u, y, z, P1)]);
+            }
+        }
+        __syncthreads();  // X is the next child's
+    }
+    if (DF && *big) return;
+#pragma unroll
+    for (int r = 0; r < kXOut; ++r) {
+        const int q = threadIdx.x + kXThreads * r;
+        if (q < nq) mom[(size_t)node * nq + q] = O::out(acc[r].val());
+    }
+}
+
+// DF: double-float shifts, FP64 again for the blocks whose powers or moments
+// leave the range where FP32 exponents suffice.
 template <bool DF>
 __global__ void __launch_bounds__(kXThreads) k_m2m(const TreeDev t, const int32_t* __restrict__ nodes, int p,
                                                    const int* __restrict__ tab, TabView v, double* __restrict__ mom) {
     extern __shared__ __align__(16) double sm_m2m[];
-    __shared__ int big;
+    __shared__ int big, ch[9];
     const int nq = v.nq, P1 = p + 1;
     const int node = nodes[blockIdx.x];
     if (t.is_leaf[node]) return;
-    double* dp = sm_m2m;            // [8][nq]
-    double* mc = dp + 8 * nq;       // [8][nq]
-    double* e = mc + 8 * nq;        // [8][3][p+1]
-    int* comp = reinterpret_cast<int*>(e + 8 * 3 * P1);
-    int* off = comp + nq;
-    int* terms = off + nq + 1;
-    int* ch = terms + v.n_m2m;      // [9]
+    double* e = sm_m2m;                                          // [8][3][p+1]
+    int* comp = reinterpret_cast<int*>(e + 8 * 3 * P1);          // [nq]
+    void* buf = e + 8 * 3 * P1 + (nq + 1) / 2;                   // X, Y, E
     copy_ints(comp, tab + v.comp, nq);
-    copy_ints(off, tab + v.m2m_off, nq + 1);
-    copy_ints(terms, tab + v.m2m, v.n_m2m);
     if (threadIdx.x == 0) big = 0;
-    __syncthreads();
-    // children offsets d = c_child - c_parent
-    const int nch = child_powers(t, node, p, nq, comp, ch, e, dp, 1.0);
-    for (int idx = threadIdx.x; idx < nch * nq; idx += blockDim.x) {
-        const int b = idx / nq, q = idx % nq;
-        mc[idx] = mom[(size_t)ch[b] * nq + q];
-    }
-    __syncthreads();
+    child_offsets(t, node, p, ch, e);
+    m2m_node<DF>(t, node, p, nq, comp, ch, e, buf, &big, mom);
     if (DF) {
-        // in place: each entry is read and rewritten by the same thread
-        float2* dp2 = reinterpret_cast<float2*>(dp);
-        float2* mc2 = reinterpret_cast<float2*>(mc);
-        for (int idx = threadIdx.x; idx < nch * nq; idx += blockDim.x) {
-            dp2[idx] = to_df(dp[idx], &big);
-            mc2[idx] = to_df(mc[idx], &big);
-        }
         __syncthreads();
-        if (!big) {
-            for (int tq = threadIdx.x; tq < nq; tq += blockDim.x) {
-                float h = 0.0f, l = 0.0f;
-                for (int j = off[tq]; j < off[tq + 1]; ++j) {
-                    const int u = terms[j] & 0xffff, w = terms[j] >> 16;
-                    for (int b = 0; b < nch; ++b) df_mac(dp2[b * nq + u], mc2[b * nq + w], h, l);
-                }
-                mom[(size_t)node * nq + tq] = (double)h + (double)l;
-            }
-            return;
-        }
-        // out of range: back to FP64 powers and moments
-        __syncthreads();
-        child_powers(t, node, p, nq, comp, ch, e, dp, 1.0);
-        for (int idx = threadIdx.x; idx < nch * nq; idx += blockDim.x) {
-            const int b = idx / nq, q = idx % nq;
-            mc[idx] = mom[(size_t)ch[b] * nq + q];
-        }
-        __syncthreads();
-    }
-    for (int tq = threadIdx.x; tq < nq; tq += blockDim.x) {
-        double a = 0.0;
-        for (int j = off[tq]; j < off[tq + 1]; ++j) {
-            const int u = terms[j] & 0xffff, w = terms[j] >> 16;
-            for (int b = 0; b < nch; ++b) a = fma(dp[b * nq + u], mc[b * nq + w], a);
-        }
-        mom[(size_t)node * nq + tq] = a;
+        if (big) m2m_node<false>(t, node, p, nq, comp, ch, e, buf, &big, mom);
     }
 }
 
-// ---------------------------------------------------------------- L2L
+// L2L of one parent into each child: L_t(child) += sum_u L_{t+u}(parent)
+// d^u/u! (|t + u| <= p) as shifts along z (Y from X, the parent's
+// expansion), y (Z from Y) and x (into the child's expansion).
+template <bool DF>
+__device__ __forceinline__ void l2l_node(int node, int p, int nq, const int* comp, const int* ch, const double* e,
+                                         void* buf, int* big, double* __restrict__ loc) {
+    using O = XOps<DF>;
+    using V = typename O::V;
+    const int P1 = p + 1, n3 = P1 * P1 * P1;
+    V* X = reinterpret_cast<V*>(buf);
+    V* Y = X + n3;
+    V* Z = Y + n3;
+    V* E = Z + n3;  // [8][3][p+1]
+    const int nch = ch[8];
+    for (int k = threadIdx.x; k < nch * 3 * P1; k += blockDim.x) E[k] = O::in(e[k], big);
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        const int cc = comp[q];
+        X[d3(cc & 0xff, (cc >> 8) & 0xff, cc >> 16, P1)] = O::in(loc[(size_t)node * nq + q], big);
+    }
+    __syncthreads();
+    if (DF && *big) return;  // every thread sees the flag after the barrier
+    for (int b = 0; b < nch; ++b) {
+        const V* ex = E + b * 3 * P1;
+        const V* ey = ex + P1;
+        const V* ez = ey + P1;
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            const int cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
+            typename O::Acc s;
+            for (int u = 0; u <= p - x - y - z; ++u) s.mac(ez[u], X[d3(x, y, z + u, P1)]);
+            Y[d3(x, y, z, P1)] = s.val();
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            const int cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
+            typename O::Acc s;
+            for (int u = 0; u <= p - x - y - z; ++u) s.mac(ey[u], Y[d3(x, y + u, z, P1)]);
+            Z[d3(x, y, z, P1)] = s.val();
+        }
+        __syncthreads();
+        double* lc = loc + (size_t)ch[b] * nq;
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            const int cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
+            typename O::Acc s;
+            for (int u = 0; u <= p - x - y - z; ++u) s.mac(ex[u], Z[d3(x + u, y, z, P1)]);
+            lc[q] += O::out(s.val());
+        }
+        __syncthreads();  // Y and Z are the next child's
+    }
+}
+
 template <bool DF>
 __global__ void __launch_bounds__(kXThreads) k_l2l(const TreeDev t, const int32_t* __restrict__ nodes, int p,
                                                    const int* __restrict__ tab, TabView v, double* __restrict__ loc) {
     extern __shared__ __align__(16) double sm_l2l[];
-    __shared__ int big;
+    __shared__ int big, ch[9];
     const int nq = v.nq, P1 = p + 1;
     const int node = nodes[blockIdx.x];
     if (t.is_leaf[node]) return;
-    double* dp = sm_l2l;            // [8][nq]
-    double* lp = dp + 8 * nq;       // [nq]
-    double* e = lp + nq;            // [8][3][p+1]
-    int* comp = reinterpret_cast<int*>(e + 8 * 3 * P1);
-    int* off = comp + nq;
-    int* terms = off + nq + 1;
-    int* ch = terms + v.n_l2l;      // [9]
+    double* e = sm_l2l;                                          // [8][3][p+1]
+    int* comp = reinterpret_cast<int*>(e + 8 * 3 * P1);          // [nq]
+    void* buf = e + 8 * 3 * P1 + (nq + 1) / 2;                   // X, Y, Z, E
     copy_ints(comp, tab + v.comp, nq);
-    copy_ints(off, tab + v.l2l_off, nq + 1);
-    copy_ints(terms, tab + v.l2l, v.n_l2l);
     if (threadIdx.x == 0) big = 0;
-    for (int q = threadIdx.x; q < nq; q += blockDim.x) lp[q] = loc[(size_t)node * nq + q];
-    __syncthreads();
-    const int nch = child_powers(t, node, p, nq, comp, ch, e, dp, 1.0);
-    __syncthreads();
-    if (DF) {
-        float2* dp2 = reinterpret_cast<float2*>(dp);
-        float2* lp2 = reinterpret_cast<float2*>(lp);
-        for (int idx = threadIdx.x; idx < nch * nq; idx += blockDim.x) dp2[idx] = to_df(dp[idx], &big);
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) lp2[q] = to_df(lp[q], &big);
+    child_offsets(t, node, p, ch, e);
+    l2l_node<DF>(node, p, nq, comp, ch, e, buf, &big, loc);
+    if (DF && big) {
         __syncthreads();
-        if (!big) {
-            for (int tq = threadIdx.x; tq < nq; tq += blockDim.x) {
-                float ah[8], al[8];
-#pragma unroll
-                for (int b = 0; b < 8; ++b) ah[b] = al[b] = 0.0f;
-                for (int j = off[tq]; j < off[tq + 1]; ++j) {
-                    const int u = terms[j] & 0xffff, w = terms[j] >> 16;
-                    const float2 l = lp2[w];
-#pragma unroll
-                    for (int b = 0; b < 8; ++b)
-                        if (b < nch) df_mac(l, dp2[b * nq + u], ah[b], al[b]);
-                }
-#pragma unroll
-                for (int b = 0; b < 8; ++b)
-                    if (b < nch) loc[(size_t)ch[b] * nq + tq] += (double)ah[b] + (double)al[b];
-            }
-            return;
-        }
-        // out of range: back to FP64 powers and locals
-        __syncthreads();
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) lp[q] = loc[(size_t)node * nq + q];
-        child_powers(t, node, p, nq, comp, ch, e, dp, 1.0);
-        __syncthreads();
+        l2l_node<false>(node, p, nq, comp, ch, e, buf, &big, loc);
     }
-    for (int tq = threadIdx.x; tq < nq; tq += blockDim.x) {
-        double a[8];
-#pragma unroll
-        for (int b = 0; b < 8; ++b) a[b] = 0.0;
-        for (int j = off[tq]; j < off[tq + 1]; ++j) {
-            const int u = terms[j] & 0xffff, w = terms[j] >> 16;
-            const double l = lp[w];
-#pragma unroll
-            for (int b = 0; b < 8; ++b)
-                if (b < nch) a[b] = fma(l, dp[b * nq + u], a[b]);
-        }
-#pragma unroll
-        for (int b = 0; b < 8; ++b)
-            if (b < nch) loc[(size_t)ch[b] * nq + tq] += a[b];
-    }
+}
+
+// Shared memory of k_m2m / k_l2l: powers, components, dense expansions and
+// the powers in the kernel's arithmetic.
+size_t xlate_smem(int p, int ndense) {
+    const int P1 = p + 1, nq = nT(p);
+    return sizeof(double) * (2 * 8 * 3 * (size_t)P1 + (nq + 1) / 2 + (size_t)ndense * P1 * P1 * P1);
 }
 
 // ---------------------------------------------------------------- L2P
@@ -588,8 +637,7 @@ int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, c
         }
     }
     {
-        const size_t sm = sizeof(double) * (16 * (size_t)nq + 8 * 3 * (p + 1)) +
-                          sizeof(int) * (2 * (size_t)nq + 1 + v.n_m2m + 9);
+        const size_t sm = xlate_smem(p, 2);
         FMM_TRY(set_smem((const void*)k_m2m<false>, sm));
         FMM_TRY(set_smem((const void*)k_m2m<true>, sm));
         for (int d = t.max_depth - 1; d >= 1; --d) {
@@ -614,8 +662,7 @@ int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, i
     const int* tab = ws.xlate.as<int>();
     double* loc = ws.loc.as<double>();
     {
-        const size_t sm = sizeof(double) * (9 * (size_t)nq + 8 * 3 * (p + 1)) +
-                          sizeof(int) * (2 * (size_t)nq + 1 + v.n_l2l + 9);
+        const size_t sm = xlate_smem(p, 3);
         FMM_TRY(set_smem((const void*)k_l2l<false>, sm));
         FMM_TRY(set_smem((const void*)k_l2l<true>, sm));
         for (int d = 1; d < t.max_depth; ++d) {
