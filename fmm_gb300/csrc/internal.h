@@ -119,10 +119,12 @@ struct Workspace {
     // ref-mode closed-form tensor tables
     DevBuf term_off, term_abc, term_c;
     int term_order = -1;
-    // index tables of P2M / M2M / L2L at (xlate_p, xlate_m)
+    // packed components of order <= xlate_p (P2M / M2M / L2L)
     DevBuf xlate;
-    int xlate_p = -1, xlate_m = -1;
-    int xlate_n[3] = {0, 0, 0};
+    int xlate_p = -1;
+    // L2P coefficient table at (l2pt_p, l2pt_f)
+    DevBuf l2pt;
+    int l2pt_p = -1, l2pt_f = -1;
     bool sel_ready = false;  // selector weights loaded
     // timing
     cudaEvent_t ev[16] = {};

@@ -9,19 +9,20 @@
 // (the reference shifts each leaf straight into every ancestor; level by
 // level is the same sum since the shifts compose exactly).
 //
-// The (output, term) index pairs of the convolutions are tabulated once per
-// order on the host and staged in shared memory, so the inner loops are a
-// table load and an FMA.  P2M runs a block per leaf over batches of
-// particles (their scaled powers in shared memory); M2M and L2L a block per
-// parent with all its children at once; L2P a thread per particle with the
-// local expansion evaluated by nested Horner schemes in the leaf's length
-// unit (FP32 in the mixed-precision path, where the local expansion's terms
-// decrease with order and carry no cancellation between per-atom terms).
+// P2M runs a block per leaf with the particles' moments times their scaled
+// powers accumulated per power u in registers; M2M and L2L a block per parent
+// node, each as three one-dimensional shifts of a dense expansion; L2P a work
+// item per (particle, output) with the local expansion evaluated by nested
+// Horner schemes in the leaf's length unit (FP32 in the mixed-precision path,
+// where the local expansion's terms decrease with order and carry no
+// cancellation between per-atom terms), its coefficients staged from a table
+// built once per (p, f).
 // P2M, M2M and L2L are FP64 in the plain path and double-float (FP32 pipe,
 // exact products by FMA, ~48-bit sums) in the mixed path, M2M and L2L with
 // an FP64 fallback for blocks whose powers or moments leave the range where
 // FP32 exponents suffice.
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "internal.h"
@@ -35,89 +36,70 @@ __device__ __forceinline__ int ux_(int c) { return c & 0xff; }
 __device__ __forceinline__ int uy_(int c) { return (c >> 8) & 0xff; }
 __device__ __forceinline__ int uz_(int c) { return (c >> 16) & 0xff; }
 
-// Table layout (int32): comp[nq] | p2m_off[nq+1] | p2m[..] | m2m_off[nq+1] |
-// m2m[..] | l2l_off[nq+1] | l2l[..]; entries pack two packed indices
-// (low 16 bits, high 16 bits).
+// Packed components (x | y << 8 | z << 16) of order <= p in the packed
+// order, uploaded once per order.
 struct TabView {
-    int nq, n_p2m, n_m2m, n_l2l;
-    int comp, p2m_off, p2m, m2m_off, m2m, l2l_off, l2l, total;
+    int nq, comp;
 };
-
-TabView tab_view(int p, int n_p2m, int n_m2m, int n_l2l) {
-    TabView v;
-    v.nq = nT(p);
-    v.n_p2m = n_p2m;
-    v.n_m2m = n_m2m;
-    v.n_l2l = n_l2l;
-    int o = 0;
-    v.comp = o;
-    o += v.nq;
-    v.p2m_off = o;
-    o += v.nq + 1;
-    v.p2m = o;
-    o += n_p2m;
-    v.m2m_off = o;
-    o += v.nq + 1;
-    v.m2m = o;
-    o += n_m2m;
-    v.l2l_off = o;
-    o += v.nq + 1;
-    v.l2l = o;
-    o += n_l2l;
-    v.total = o;
-    return v;
-}
 
 int hidx(int x, int y, int z) { return nT(x + y + z - 1) + ((y + z) * (y + z + 1)) / 2 + z; }
 
-// Builds (once per (p, m)) and uploads the index tables.
-int ensure_tables(Workspace& ws, int p, int m, TabView* out, cudaStream_t st) {
-    if (ws.xlate_p == p && ws.xlate_m == m) {
-        *out = tab_view(p, ws.xlate_n[0], ws.xlate_n[1], ws.xlate_n[2]);
-        return FMM_OK;
-    }
-    const int nq = nT(p), nm = nT(m);
-    std::vector<int> comp(nq), xs(nq), ys(nq), zs(nq);
-    for (int k = 0, q = 0; k <= p; ++k)
+int ensure_tables(Workspace& ws, int p, TabView* out, cudaStream_t st) {
+    out->nq = nT(p);
+    out->comp = 0;
+    if (ws.xlate_p == p) return FMM_OK;
+    std::vector<int> comp;
+    for (int k = 0; k <= p; ++k)
         for (int x = k; x >= 0; --x)
-            for (int y = k - x; y >= 0; --y, ++q) {
-                xs[q] = x;
-                ys[q] = y;
-                zs[q] = k - x - y;
-                comp[q] = pack3(x, y, k - x - y);
-            }
-    std::vector<int> p2m_off(1, 0), p2m, m2m_off(1, 0), m2m, l2l_off(1, 0), l2l;
-    for (int q = 0; q < nq; ++q) {
-        for (int s = 0; s < std::min(nm, nq); ++s)
-            if (xs[s] <= xs[q] && ys[s] <= ys[q] && zs[s] <= zs[q])
-                p2m.push_back(s | (hidx(xs[q] - xs[s], ys[q] - ys[s], zs[q] - zs[s]) << 16));
-        p2m_off.push_back((int)p2m.size());
-        for (int u = 0; u < nq; ++u)
-            if (xs[u] <= xs[q] && ys[u] <= ys[q] && zs[u] <= zs[q])
-                m2m.push_back(u | (hidx(xs[q] - xs[u], ys[q] - ys[u], zs[q] - zs[u]) << 16));
-        m2m_off.push_back((int)m2m.size());
-        const int rem = p - (xs[q] + ys[q] + zs[q]);
-        for (int u = 0; u < nT(rem); ++u) l2l.push_back(u | (hidx(xs[q] + xs[u], ys[q] + ys[u], zs[q] + zs[u]) << 16));
-        l2l_off.push_back((int)l2l.size());
-    }
-    const TabView v = tab_view(p, (int)p2m.size(), (int)m2m.size(), (int)l2l.size());
-    *out = v;
-    std::vector<int> all((size_t)v.total);
-    std::copy(comp.begin(), comp.end(), all.begin() + v.comp);
-    std::copy(p2m_off.begin(), p2m_off.end(), all.begin() + v.p2m_off);
-    std::copy(p2m.begin(), p2m.end(), all.begin() + v.p2m);
-    std::copy(m2m_off.begin(), m2m_off.end(), all.begin() + v.m2m_off);
-    std::copy(m2m.begin(), m2m.end(), all.begin() + v.m2m);
-    std::copy(l2l_off.begin(), l2l_off.end(), all.begin() + v.l2l_off);
-    std::copy(l2l.begin(), l2l.end(), all.begin() + v.l2l);
-    FMM_TRY(ws.xlate.ensure(sizeof(int) * all.size()));
-    FMM_CUDA_TRY(cudaMemcpyAsync(ws.xlate.p, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice, st));
+            for (int y = k - x; y >= 0; --y) comp.push_back(pack3(x, y, k - x - y));
+    FMM_TRY(ws.xlate.ensure(sizeof(int) * comp.size()));
+    FMM_CUDA_TRY(cudaMemcpyAsync(ws.xlate.p, comp.data(), sizeof(int) * comp.size(), cudaMemcpyHostToDevice, st));
     FMM_CUDA_TRY(cudaStreamSynchronize(st));
     ws.xlate_p = p;
-    ws.xlate_m = m;
-    ws.xlate_n[0] = v.n_p2m;
-    ws.xlate_n[1] = v.n_m2m;
-    ws.xlate_n[2] = v.n_l2l;
+    return FMM_OK;
+}
+
+// L2P coefficients of the outputs t (|t| <= f), each in Horner order (ux,
+// uy, uz descending, |u| <= p - |t|): segment starts seg[nT(f)+1], then per
+// coefficient the index of L_{t+u} and its order (w | k << 16), then (from an
+// 8-byte boundary) 1 / (ux! uy! uz!) as FP64.  Once per (p, f).
+struct L2pTab {
+    int nf, ncoef, seg, wk, fac;  // offsets in ints
+};
+
+int ensure_l2p_table(Workspace& ws, int p, int f, L2pTab* out, cudaStream_t st) {
+    const int nf = nT(f);
+    std::vector<int> seg(1, 0), wk;
+    std::vector<double> fac;
+    for (int k = 0, tq = 0; k <= f; ++k)
+        for (int tx = k; tx >= 0; --tx)
+            for (int ty = k - tx; ty >= 0; --ty, ++tq) {
+                const int tz = k - tx - ty, rem = p - k;
+                for (int ux = rem; ux >= 0; --ux)
+                    for (int uy = rem - ux; uy >= 0; --uy)
+                        for (int uz = rem - ux - uy; uz >= 0; --uz) {
+                            wk.push_back(hidx(tx + ux, ty + uy, tz + uz) | ((k + ux + uy + uz) << 16));
+                            fac.push_back(1.0 / (cfact(ux) * cfact(uy) * cfact(uz)));
+                        }
+                seg.push_back((int)wk.size());
+            }
+    L2pTab v;
+    v.nf = nf;
+    v.ncoef = (int)wk.size();
+    v.seg = 0;
+    v.wk = nf + 1;
+    v.fac = (v.wk + v.ncoef + 1) & ~1;
+    *out = v;
+    if (ws.l2pt_p == p && ws.l2pt_f == f) return FMM_OK;
+    std::vector<int> all((size_t)v.fac + 2 * (size_t)v.ncoef, 0);
+    std::copy(seg.begin(), seg.end(), all.begin() + v.seg);
+    std::copy(wk.begin(), wk.end(), all.begin() + v.wk);
+    std::memcpy(all.data() + v.fac, fac.data(), sizeof(double) * fac.size());
+    FMM_TRY(ws.l2pt.ensure(sizeof(int) * all.size()));
+    FMM_CUDA_TRY(cudaMemcpyAsync(ws.l2pt.p, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice, st));
+    FMM_CUDA_TRY(cudaStreamSynchronize(st));
+    ws.l2pt_p = p;
+    ws.l2pt_f = f;
     return FMM_OK;
 }
 
@@ -125,7 +107,7 @@ __device__ __forceinline__ void copy_ints(int* dst, const int* __restrict__ src,
     for (int e = threadIdx.x; e < n; e += blockDim.x) dst[e] = src[e];
 }
 
-// 1/a and 1/a! for a = 0..2 kMaxP (no divisions on the FP64 pipe)
+// 1/a for a = 0..2 kMaxP + 1 (no divisions on the FP64 pipe)
 __constant__ double cInvInt[2 * kMaxP + 2] = {
 #define FMM_X(a) ((a) == 0 ? 0.0 : 1.0 / (a)),
     FMM_X(0) FMM_X(1) FMM_X(2) FMM_X(3) FMM_X(4) FMM_X(5) FMM_X(6) FMM_X(7) FMM_X(8) FMM_X(9) FMM_X(10) FMM_X(11)
@@ -133,24 +115,13 @@ __constant__ double cInvInt[2 * kMaxP + 2] = {
     FMM_X(23) FMM_X(24) FMM_X(25)
 #undef FMM_X
 };
-__constant__ double cInvFact[kMaxP + 1] = {
-#define FMM_F(a) (1.0 / cfact(a)),
-    FMM_F(0) FMM_F(1) FMM_F(2) FMM_F(3) FMM_F(4) FMM_F(5) FMM_F(6) FMM_F(7) FMM_F(8) FMM_F(9) FMM_F(10) FMM_F(11)
-    FMM_F(12)
-#undef FMM_F
-};
-static_assert(kMaxP == 12, "inverse tables cover orders up to 12");
+static_assert(kMaxP == 12, "the inverse table covers orders up to 12");
 
 // e[a] = d^a / a!, a = 0..p
 __device__ __forceinline__ void scaled_powers(double d, int p, double* e) {
     e[0] = 1.0;
     for (int a = 1; a <= p; ++a) e[a] = e[a - 1] * d * cInvInt[a];
 }
-
-// ---------------------------------------------------------------- P2M
-constexpr int kP2mThreads = 128;
-constexpr int kP2mBatch = 8;
-constexpr int kMaxOut = (nT(kMaxP) + kP2mThreads - 1) / kP2mThreads;
 
 // Product of two double-float pairs (hi, lo), renormalised.
 __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
@@ -161,135 +132,6 @@ __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
     const float s = p + e;
     return make_float2(s, e - (s - p));
 }
-
-// DF: accumulate in double-float pairs (FP32 arithmetic, exact products by
-// FMA, ~48-bit sums) instead of FP64; used by the mixed-precision path, where
-// the FP64 pipe is the bottleneck of this kernel.
-template <bool DF>
-__global__ void __launch_bounds__(kP2mThreads) k_p2m(const TreeDev t, const double* __restrict__ sx,
-                                                     const double* __restrict__ sy, const double* __restrict__ sz,
-                                                     const double* __restrict__ smc, int64_t n, int m, int p,
-                                                     const int* __restrict__ tab, TabView v,
-                                                     double* __restrict__ mom) {
-    extern __shared__ __align__(16) double sm_p2m[];
-    const int nq = v.nq, nm = nT(m), P1 = p + 1;
-    double* dp = sm_p2m;                        // [kP2mBatch][nq]  (DF: float2 hi/lo)
-    double* e = dp + kP2mBatch * nq;            // [kP2mBatch][3][p+1]
-    double* ms = e + kP2mBatch * 3 * P1;        // [kP2mBatch][nm]  (DF: float2 hi/lo)
-    int* comp = reinterpret_cast<int*>(ms + kP2mBatch * nm);
-    int* off = comp + nq;
-    int* terms = off + nq + 1;
-    float2* dp2 = reinterpret_cast<float2*>(dp);
-    float2* ms2 = reinterpret_cast<float2*>(ms);
-    copy_ints(comp, tab + v.comp, nq);
-    copy_ints(off, tab + v.p2m_off, nq + 1);
-    copy_ints(terms, tab + v.p2m, v.n_p2m);
-    const int leaf = t.leaves[blockIdx.x];
-    const double cx = t.cx[leaf], cy = t.cy[leaf], cz = t.cz[leaf];
-    const int s0 = t.start[leaf], cnt = t.count[leaf];
-    double acc[kMaxOut];
-    float ah[kMaxOut], al[kMaxOut];
-#pragma unroll
-    for (int r = 0; r < kMaxOut; ++r) {
-        acc[r] = 0.0;
-        ah[r] = al[r] = 0.0f;
-    }
-    __syncthreads();
-    for (int b0 = 0; b0 < cnt; b0 += kP2mBatch) {
-        const int nb = min(kP2mBatch, cnt - b0);
-        if (threadIdx.x < 3 * nb) {
-            const int b = threadIdx.x / 3, ax = threadIdx.x % 3, k = s0 + b0 + b;
-            const double d = ax == 0 ? sx[k] - cx : (ax == 1 ? sy[k] - cy : sz[k] - cz);
-            scaled_powers(d, p, e + (b * 3 + ax) * P1);
-        }
-        for (int idx = threadIdx.x; idx < nb * nm; idx += blockDim.x) {
-            const int b = idx / nm, s = idx % nm;
-            const double c = smc[(size_t)s * n + s0 + b0 + b];
-            const double w = ((order_of(s) + 1) % 2) ? -c : c;  // back to M_s / s!
-            if (DF) {
-                const float hi = (float)w;
-                ms2[b * nm + s] = make_float2(hi, (float)(w - (double)hi));
-            } else {
-                ms[b * nm + s] = w;
-            }
-        }
-        __syncthreads();
-        if (DF) {
-            // scaled powers as double-float pairs, products on the FP32 pipe
-            float2* e2 = reinterpret_cast<float2*>(e);
-            __syncthreads();
-            for (int idx = threadIdx.x; idx < nb * 3 * P1; idx += blockDim.x) {
-                const double w = e[idx];
-                const float hi = (float)w;
-                e2[idx] = make_float2(hi, (float)(w - (double)hi));
-            }
-            __syncthreads();
-            for (int idx = threadIdx.x; idx < nb * nq; idx += blockDim.x) {
-                const int b = idx / nq, u = idx % nq;
-                const int c = comp[u];
-                const float2* eb = e2 + b * 3 * P1;
-                dp2[b * nq + u] = df_mul(df_mul(eb[ux_(c)], eb[P1 + uy_(c)]), eb[2 * P1 + uz_(c)]);
-            }
-        } else {
-            for (int idx = threadIdx.x; idx < nb * nq; idx += blockDim.x) {
-                const int b = idx / nq, u = idx % nq;
-                const int c = comp[u];
-                const double* eb = e + b * 3 * P1;
-                dp[b * nq + u] = eb[ux_(c)] * eb[P1 + uy_(c)] * eb[2 * P1 + uz_(c)];
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < kMaxOut; ++r) {
-            const int tq = threadIdx.x + kP2mThreads * r;
-            if (tq < nq) {
-                if (DF) {
-                    float h = ah[r], l = al[r];
-                    for (int j = off[tq]; j < off[tq + 1]; ++j) {
-                        const int s = terms[j] & 0xffff, u = terms[j] >> 16;
-                        for (int b = 0; b < nb; ++b) {
-                            const float2 d = dp2[b * nq + u], w = ms2[b * nm + s];
-                            const float pr = d.x * w.x;
-                            float er = fmaf(d.x, w.x, -pr);
-                            er = fmaf(d.x, w.y, er);
-                            er = fmaf(d.y, w.x, er);
-                            const float sum = h + pr;
-                            const float bb = sum - h;
-                            l += ((h - (sum - bb)) + (pr - bb)) + er;
-                            h = sum;
-                        }
-                    }
-                    ah[r] = h;
-                    al[r] = l;
-                } else {
-                    double a = acc[r];
-                    for (int j = off[tq]; j < off[tq + 1]; ++j) {
-                        const int s = terms[j] & 0xffff, u = terms[j] >> 16;
-                        for (int b = 0; b < nb; ++b) a = fma(dp[b * nq + u], ms[b * nm + s], a);
-                    }
-                    acc[r] = a;
-                }
-            }
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int r = 0; r < kMaxOut; ++r) {
-        const int tq = threadIdx.x + kP2mThreads * r;
-        if (tq < nq) mom[(size_t)leaf * nq + tq] = DF ? (double)ah[r] + (double)al[r] : acc[r];
-    }
-}
-
-// ---------------------------------------------------------------- M2M / L2L
-// Both translations factor over the axes, d^u / u! = (dx^ux/ux!)
-// (dy^uy/uy!) (dz^uz/uz!), so each is three one-dimensional shifts (z, then
-// y, then x) of an expansion held densely in shared memory, index
-// (a (p+1) + b) (p+1) + c for the component (a, b, c): C(p+4,4) terms per
-// shift instead of the C(p+6,6) of the direct sum, and no output of a shift
-// has more than p+1 terms, so the block's outputs finish together.  A block
-// per parent node takes its children one after another.
-constexpr int kXThreads = 256;
-constexpr int kXOut = (nT(kMaxP) + kXThreads - 1) / kXThreads;  // outputs per thread
 
 // (hi, lo) FP32 pair of an FP64 value; *big set when it is outside the range
 // where double-float products keep their precision.
@@ -320,9 +162,11 @@ struct XOps<false> {
     struct Acc {
         double a = 0.0;
         __device__ __forceinline__ void mac(double x, double y) { a = fma(x, y, a); }
+        __device__ __forceinline__ void add(double x) { a += x; }
         __device__ __forceinline__ double val() const { return a; }
     };
     static __device__ __forceinline__ double in(double w, int*) { return w; }
+    static __device__ __forceinline__ double mul(double x, double y) { return x * y; }
     static __device__ __forceinline__ double out(double v) { return v; }
 };
 template <>
@@ -331,14 +175,137 @@ struct XOps<true> {
     struct Acc {
         float h = 0.0f, l = 0.0f;
         __device__ __forceinline__ void mac(float2 x, float2 y) { df_mac(x, y, h, l); }
+        __device__ __forceinline__ void add(float2 x) {
+            const float sum = h + x.x;
+            const float bb = sum - h;
+            l += ((h - (sum - bb)) + (x.x - bb)) + x.y;
+            h = sum;
+        }
         __device__ __forceinline__ float2 val() const {
             const float s = h + l;
             return make_float2(s, l - (s - h));
         }
     };
     static __device__ __forceinline__ float2 in(double w, int* big) { return to_df(w, big); }
+    static __device__ __forceinline__ float2 mul(float2 x, float2 y) { return df_mul(x, y); }
     static __device__ __forceinline__ double out(float2 v) { return (double)v.x + (double)v.y; }
 };
+
+// ---------------------------------------------------------------- P2M
+// Block per leaf.  With dp_i[u] = d_i^u / u! (d_i = x_i - c_leaf) the leaf's
+// moments are M'_t = sum_{s <= t} A_s[t - s], A_s[u] = sum_i M'_s(i) dp_i[u]
+// (|s| <= m, |u| <= p - |s|): a product of the particles' moments (NM per
+// particle) and powers, accumulated by the thread that owns u in registers
+// (NM independent accumulators per u, the moments read as shared-memory
+// broadcasts, dp_i[u] formed in registers from the particle's powers per
+// axis), then the short sums over s.
+constexpr int kP2mBatch = 16;
+
+__device__ __forceinline__ int pk_index(int x, int y, int z) {
+    const int k = x + y + z, yz = y + z;
+    return k * (k + 1) * (k + 2) / 6 + yz * (yz + 1) / 2 + z;
+}
+
+template <bool DF, int NM, int KS, int NT>
+__global__ void __launch_bounds__(NT) k_p2m(const TreeDev t, const double* __restrict__ sx,
+                                            const double* __restrict__ sy, const double* __restrict__ sz,
+                                            const double* __restrict__ smc, int64_t n, int p,
+                                            const int* __restrict__ tab, TabView v, double* __restrict__ mom) {
+    using O = XOps<DF>;
+    using V = typename O::V;
+    extern __shared__ __align__(16) double sm_p2m[];
+    const int nq = v.nq, P1 = p + 1;
+    V* e = reinterpret_cast<V*>(sm_p2m);    // [kP2mBatch][3][p+1] powers per axis
+    V* ms = e + kP2mBatch * 3 * P1;         // [kP2mBatch][NM] scaled moments
+    V* A = ms + kP2mBatch * NM;             // [nq][NM]
+    int* comp = reinterpret_cast<int*>(A + (size_t)nq * NM);
+    copy_ints(comp, tab + v.comp, nq);
+    const int leaf = t.leaves[blockIdx.x];
+    const double cx = t.cx[leaf], cy = t.cy[leaf], cz = t.cz[leaf];
+    const int s0 = t.start[leaf], cnt = t.count[leaf];
+    int big = 0;
+    __syncthreads();
+    // this thread's u (KS slots) and the moments s that pair with each
+    int ux[KS], uy[KS], uz[KS], ns[KS];
+#pragma unroll
+    for (int r = 0; r < KS; ++r) {
+        const int u = threadIdx.x + NT * r;
+        ns[r] = 0;
+        ux[r] = uy[r] = uz[r] = 0;
+        if (u < nq) {
+            const int c = comp[u];
+            ux[r] = ux_(c);
+            uy[r] = uy_(c);
+            uz[r] = uz_(c);
+            const int rem = p - ux[r] - uy[r] - uz[r];
+            ns[r] = rem >= 2 ? NM : min(NM, nT(rem));
+        }
+    }
+    typename O::Acc acc[KS][NM];
+    for (int b0 = 0; b0 < cnt; b0 += kP2mBatch) {
+        const int nb = min(kP2mBatch, cnt - b0);
+        if (threadIdx.x < 3 * nb) {
+            const int b = threadIdx.x / 3, ax = threadIdx.x % 3, k = s0 + b0 + b;
+            const double d = ax == 0 ? sx[k] - cx : (ax == 1 ? sy[k] - cy : sz[k] - cz);
+            double w = 1.0;
+            V* eb = e + (b * 3 + ax) * P1;
+            eb[0] = O::in(1.0, &big);
+            for (int a = 1; a <= p; ++a) {
+                w *= d * cInvInt[a];
+                eb[a] = O::in(w, &big);
+            }
+        }
+        for (int idx = threadIdx.x; idx < nb * NM; idx += NT) {
+            const int b = idx / NM, s = idx - b * NM;
+            const double c = smc[(size_t)s * n + s0 + b0 + b];
+            ms[idx] = O::in(((order_of(s) + 1) % 2) ? -c : c, &big);  // back to M_s / s!
+        }
+        __syncthreads();
+        for (int b = 0; b < nb; ++b) {
+            const V* eb = e + b * 3 * P1;
+            const V* mb = ms + b * NM;
+#pragma unroll
+            for (int r = 0; r < KS; ++r) {
+                if (ns[r] > 0) {
+                    const V dp = O::mul(O::mul(eb[ux[r]], eb[P1 + uy[r]]), eb[2 * P1 + uz[r]]);
+#pragma unroll
+                    for (int s = 0; s < NM; ++s)
+                        if (s < ns[r]) acc[r][s].mac(dp, mb[s]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < KS; ++r) {
+        const int u = threadIdx.x + NT * r;
+#pragma unroll
+        for (int s = 0; s < NM; ++s)
+            if (s < ns[r]) A[u * NM + s] = acc[r][s].val();
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nq; q += NT) {
+        const int c = comp[q], tx = ux_(c), ty = uy_(c), tz = uz_(c);
+        typename O::Acc sum;
+#pragma unroll
+        for (int s = 0; s < NM; ++s) {
+            const int sc = comp[s], qx = ux_(sc), qy = uy_(sc), qz = uz_(sc);
+            if (qx <= tx && qy <= ty && qz <= tz) sum.add(A[pk_index(tx - qx, ty - qy, tz - qz) * NM + s]);
+        }
+        mom[(size_t)leaf * nq + q] = O::out(sum.val());
+    }
+}
+
+// ---------------------------------------------------------------- M2M / L2L
+// Both translations factor over the axes, d^u / u! = (dx^ux/ux!)
+// (dy^uy/uy!) (dz^uz/uz!), so each is three one-dimensional shifts (z, then
+// y, then x) of an expansion held densely in shared memory, index
+// (a (p+1) + b) (p+1) + c for the component (a, b, c): C(p+4,4) terms per
+// shift instead of the C(p+6,6) of the direct sum, and no output of a shift
+// has more than p+1 terms, so the block's outputs finish together.  A block
+// per parent node takes its children one after another.
+constexpr int kXThreads = 256;
+constexpr int kXOut = (nT(kMaxP) + kXThreads - 1) / kXThreads;  // outputs per thread
 
 __device__ __forceinline__ int d3(int a, int b, int c, int P1) { return (a * P1 + b) * P1 + c; }
 
@@ -522,89 +489,91 @@ size_t xlate_smem(int p, int ndense) {
 }
 
 // ---------------------------------------------------------------- L2P
-// Coefficients of output t (|t| <= f) in Horner order: ux, uy, uz descending,
-// c = L_{t+u} h^|t+u| / u!  (lengths in units of the leaf half-width h).
+// Block per leaf: the leaf's coefficients c = L_{t+u} h^|t+u| / u! (lengths
+// in units of the leaf half-width h) staged from the table, then one work
+// item per (particle, output t): nested Horner schemes over the output's
+// coefficients.
+constexpr int kL2pThreads = 128;
+
 template <typename R>
-__global__ void __launch_bounds__(64) k_l2p(const TreeDev t, const double* __restrict__ sx,
-                                            const double* __restrict__ sy, const double* __restrict__ sz, int64_t n,
-                                            int p, int f, const double* __restrict__ loc, double* __restrict__ fs) {
+__global__ void __launch_bounds__(kL2pThreads) k_l2p(const TreeDev t, const double* __restrict__ sx,
+                                                     const double* __restrict__ sy, const double* __restrict__ sz,
+                                                     int64_t n, int p, int f, const int* __restrict__ tab, L2pTab v,
+                                                     const double* __restrict__ loc, double* __restrict__ fs) {
     extern __shared__ __align__(16) unsigned char sm_l2p_raw[];
     __shared__ double hp[kMaxP + 1];  // h^k
+    __shared__ int seg[nT(2) + 1];
     R* coef = reinterpret_cast<R*>(sm_l2p_raw);
-    const int nq = nT(p), nf = nT(f);
+    const int nq = nT(p), nf = v.nf;
     const int leaf = t.leaves[blockIdx.x];
     const double h = t.r[leaf], ih = 1.0 / h;
     const double* L = loc + (size_t)leaf * nq;
-    if (threadIdx.x == 0) {
-        double v = 1.0;
-        for (int k = 0; k <= p; ++k) {
-            hp[k] = v;
-            v *= h;
-        }
+    if (threadIdx.x <= p) {
+        double w = 1.0;
+        for (int k = 0; k < (int)threadIdx.x; ++k) w *= h;
+        hp[threadIdx.x] = w;
     }
+    if (threadIdx.x <= nf) seg[threadIdx.x] = tab[v.seg + threadIdx.x];
     __syncthreads();
-    // outputs tq of order k_t use nT(p - k_t) coefficients each, stored one
-    // after the other
-    int base = 0;
-    for (int tq = 0; tq < nf; ++tq) {
-        const int kt = order_of(tq);
-        const int tx = comp_x(tq), ty = comp_y(tq), tz = comp_z(tq);
-        const int rem = p - kt;
-        const int cnt = nT(rem);
-        for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-            // e-th entry of the Horner order: decode (ux, uy, uz)
-            int idx = e, ux = rem, uy = 0, uz = 0;
-            for (ux = rem; ux >= 0; --ux) {
-                const int blk = (rem - ux + 1) * (rem - ux + 2) / 2;
-                if (idx < blk) break;
-                idx -= blk;
-            }
-            for (uy = rem - ux; uy >= 0; --uy) {
-                const int blk = rem - ux - uy + 1;
-                if (idx < blk) break;
-                idx -= blk;
-            }
-            uz = rem - ux - uy - idx;
-            const int w = pidx(tx + ux, ty + uy, tz + uz);
-            const double s = hp[kt + ux + uy + uz] * (cInvFact[ux] * cInvFact[uy] * cInvFact[uz]);
-            coef[base + e] = (R)(L[w] * s);
-        }
-        base += cnt;
+    const int* wk = tab + v.wk;
+    const double* fac = reinterpret_cast<const double*>(tab + v.fac);
+    for (int e = threadIdx.x; e < v.ncoef; e += kL2pThreads) {
+        const int w = wk[e];
+        coef[e] = (R)(L[w & 0xffff] * hp[w >> 16] * fac[e]);
     }
     __syncthreads();
     const double cx = t.cx[leaf], cy = t.cy[leaf], cz = t.cz[leaf];
     const int s0 = t.start[leaf], cnt = t.count[leaf];
-    for (int k = s0 + threadIdx.x; k < s0 + cnt; k += blockDim.x) {
+    for (int item = threadIdx.x; item < cnt * nf; item += kL2pThreads) {
+        const int tq = item / cnt, k = s0 + item - tq * cnt;
         const R dx = (R)((sx[k] - cx) * ih), dy = (R)((sy[k] - cy) * ih), dz = (R)((sz[k] - cz) * ih);
+        const int kt = order_of(tq), rem = p - kt;
+        const R* c = coef + seg[tq];
         int b = 0;
-        for (int tq = 0; tq < nf; ++tq) {
-            const int kt = order_of(tq);
-            const int rem = p - kt;
-            R hx = (R)0;
-            for (int ux = rem; ux >= 0; --ux) {
-                R hy = (R)0;
-                for (int uy = rem - ux; uy >= 0; --uy) {
-                    R hz = (R)0;
-                    for (int uz = rem - ux - uy; uz >= 0; --uz) hz = hz * dz + coef[b++];
-                    hy = hy * dy + hz;
-                }
-                hx = hx * dx + hy;
+        R hx = (R)0;
+        for (int ux = rem; ux >= 0; --ux) {
+            R hy = (R)0;
+            for (int uy = rem - ux; uy >= 0; --uy) {
+                R hz = (R)0;
+                for (int uz = rem - ux - uy; uz >= 0; --uz) hz = hz * dz + c[b++];
+                hy = hy * dy + hz;
             }
-            double s = 1.0;
-            for (int a = 0; a < kt; ++a) s *= ih;  // kt <= 2
-            fs[(size_t)tq * n + k] += (double)hx * s;
+            hx = hx * dx + hy;
         }
+        double s = 1.0;
+        for (int a = 0; a < kt; ++a) s *= ih;  // kt <= 2
+        fs[(size_t)tq * n + k] += (double)hx * s;
     }
-}
-
-size_t l2p_coef_count(int p, int f) {
-    size_t c = 0;
-    for (int tq = 0; tq < nT(f); ++tq) c += nT(p - order_of(tq));
-    return c;
 }
 
 int set_smem(const void* fn, size_t bytes) {
     if (bytes > 48 * 1024) FMM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return FMM_OK;
+}
+
+// P2M launch with KS = ceil(nq / NT) output slots per thread.
+template <bool DF, int NM, int NT>
+int launch_p2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, const int* tab, const TabView& v,
+               double* mom, cudaStream_t st) {
+    const size_t sm = sizeof(double) * (kP2mBatch * 3 * (size_t)(p + 1) + kP2mBatch * NM + (size_t)v.nq * NM) +
+                      sizeof(int) * (size_t)v.nq;
+    const int ks = (v.nq + NT - 1) / NT;
+#define FMM_P2M_CASE(KS)                                                                                          \
+    case KS:                                                                                                      \
+        FMM_TRY(set_smem((const void*)k_p2m<DF, NM, KS, NT>, sm));                                                \
+        k_p2m<DF, NM, KS, NT><<<(unsigned)t.num_leaves, NT, sm, st>>>(t, ws.sx.as<double>(), ws.sy.as<double>(),  \
+                                                                      ws.sz.as<double>(), ws.smc.as<double>(), P.n, \
+                                                                      p, tab, v, mom);                            \
+        break;
+    switch (ks) {
+        FMM_P2M_CASE(1)
+        FMM_P2M_CASE(2)
+        FMM_P2M_CASE(3)
+        FMM_P2M_CASE(4)
+        default:
+            return FMM_EINVAL;
+    }
+#undef FMM_P2M_CASE
     return FMM_OK;
 }
 
@@ -614,26 +583,21 @@ int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, c
     const int nq = nT(p);
     const int m = dim_to_order(P.dim);
     TabView v;
-    FMM_TRY(ensure_tables(ws, p, m, &v, st));
+    FMM_TRY(ensure_tables(ws, p, &v, st));
     const int* tab = ws.xlate.as<int>();
     FMM_TRY(ws.mom.ensure(sizeof(double) * (size_t)t.num_nodes * nq));
     double* mom = ws.mom.as<double>();
-    {
+    if (t.num_leaves > 0) {
+        count_launches(1);
         const int nm = nT(m);
-        const size_t sm = sizeof(double) * (kP2mBatch * (size_t)nq + kP2mBatch * 3 * (p + 1) + kP2mBatch * nm) +
-                          sizeof(int) * (2 * (size_t)nq + 1 + v.n_p2m);
-        FMM_TRY(set_smem((const void*)k_p2m<false>, sm));
-        FMM_TRY(set_smem((const void*)k_p2m<true>, sm));
-        if (t.num_leaves > 0) {
-            count_launches(1);
-            if (df)
-                k_p2m<true><<<(unsigned)t.num_leaves, kP2mThreads, sm, st>>>(
-                    t, ws.sx.as<double>(), ws.sy.as<double>(), ws.sz.as<double>(), ws.smc.as<double>(), P.n, m, p,
-                    tab, v, mom);
-            else
-                k_p2m<false><<<(unsigned)t.num_leaves, kP2mThreads, sm, st>>>(
-                    t, ws.sx.as<double>(), ws.sy.as<double>(), ws.sz.as<double>(), ws.smc.as<double>(), P.n, m, p,
-                    tab, v, mom);
+        if (df) {
+            if (nm == 1) FMM_TRY((launch_p2m<true, 1, 128>(ws, P, t, p, tab, v, mom, st)));
+            else if (nm == 4) FMM_TRY((launch_p2m<true, 4, 128>(ws, P, t, p, tab, v, mom, st)));
+            else FMM_TRY((launch_p2m<true, 10, 128>(ws, P, t, p, tab, v, mom, st)));
+        } else {
+            if (nm == 1) FMM_TRY((launch_p2m<false, 1, 256>(ws, P, t, p, tab, v, mom, st)));
+            else if (nm == 4) FMM_TRY((launch_p2m<false, 4, 256>(ws, P, t, p, tab, v, mom, st)));
+            else FMM_TRY((launch_p2m<false, 10, 256>(ws, P, t, p, tab, v, mom, st)));
         }
     }
     {
@@ -658,7 +622,7 @@ int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, i
                    cudaStream_t st) {
     const int nq = nT(p);
     TabView v;
-    FMM_TRY(ensure_tables(ws, p, dim_to_order(P.dim), &v, st));
+    FMM_TRY(ensure_tables(ws, p, &v, st));
     const int* tab = ws.xlate.as<int>();
     double* loc = ws.loc.as<double>();
     {
@@ -676,20 +640,22 @@ int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, i
         }
     }
     if (t.num_leaves > 0) {
-        const size_t ncoef = l2p_coef_count(p, field_order);
+        L2pTab lv;
+        FMM_TRY(ensure_l2p_table(ws, p, field_order, &lv, st));
+        const int* ltab = ws.l2pt.as<int>();
         count_launches(1);
         if (fp32) {
-            const size_t sm = sizeof(float) * ncoef;
+            const size_t sm = sizeof(float) * (size_t)lv.ncoef;
             FMM_TRY(set_smem((const void*)k_l2p<float>, sm));
-            k_l2p<float><<<(unsigned)t.num_leaves, 64, sm, st>>>(t, ws.sx.as<double>(), ws.sy.as<double>(),
-                                                                 ws.sz.as<double>(), P.n, p, field_order, loc,
-                                                                 ws.fsorted.as<double>());
+            k_l2p<float><<<(unsigned)t.num_leaves, kL2pThreads, sm, st>>>(
+                t, ws.sx.as<double>(), ws.sy.as<double>(), ws.sz.as<double>(), P.n, p, field_order, ltab, lv, loc,
+                ws.fsorted.as<double>());
         } else {
-            const size_t sm = sizeof(double) * ncoef;
+            const size_t sm = sizeof(double) * (size_t)lv.ncoef;
             FMM_TRY(set_smem((const void*)k_l2p<double>, sm));
-            k_l2p<double><<<(unsigned)t.num_leaves, 64, sm, st>>>(t, ws.sx.as<double>(), ws.sy.as<double>(),
-                                                                  ws.sz.as<double>(), P.n, p, field_order, loc,
-                                                                  ws.fsorted.as<double>());
+            k_l2p<double><<<(unsigned)t.num_leaves, kL2pThreads, sm, st>>>(
+                t, ws.sx.as<double>(), ws.sy.as<double>(), ws.sz.as<double>(), P.n, p, field_order, ltab, lv, loc,
+                ws.fsorted.as<double>());
         }
     }
     FMM_CUDA_TRY(cudaGetLastError());
