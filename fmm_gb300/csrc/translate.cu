@@ -116,6 +116,13 @@ __constant__ double cInvInt[2 * kMaxP + 2] = {
 #undef FMM_X
 };
 static_assert(kMaxP == 12, "the inverse table covers orders up to 12");
+// 1/a as double-float pairs, a = 0..kMaxP
+__constant__ float2 cInvIntF[kMaxP + 1] = {
+#define FMM_XF(a) {(a) == 0 ? 0.0f : (float)(1.0 / (a)), (a) == 0 ? 0.0f : (float)(1.0 / (a) - (double)(float)(1.0 / (a)))},
+    FMM_XF(0) FMM_XF(1) FMM_XF(2) FMM_XF(3) FMM_XF(4) FMM_XF(5) FMM_XF(6) FMM_XF(7) FMM_XF(8) FMM_XF(9) FMM_XF(10)
+    FMM_XF(11) FMM_XF(12)
+#undef FMM_XF
+};
 
 // e[a] = d^a / a!, a = 0..p
 __device__ __forceinline__ void scaled_powers(double d, int p, double* e) {
@@ -153,6 +160,27 @@ __device__ __forceinline__ void df_mac(float2 x, float2 y, float& h, float& l) {
     h = sum;
 }
 
+// (hi, lo) FP32 pair of an FP64 value from its bit pattern alone (no FP64
+// instruction): hi the value truncated to 24 significant bits, lo the
+// remaining 29 bits rounded to FP32 (zero below 2^-74 in magnitude).  Zero,
+// magnitudes outside the normal FP32 range and non-finite values take the
+// FP64 conversion.
+__device__ __forceinline__ float2 split_bits(double w) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(w);
+    if ((b << 1) == 0ull) return make_float2(0.0f, 0.0f);
+    const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
+    const int e = (int)((hi32 >> 20) & 0x7ffu);
+    if (e < 1023 - 126 || e > 1023 + 127) {
+        const float h = (float)w;
+        return make_float2(h, (float)(w - (double)h));
+    }
+    const unsigned sgn = hi32 & 0x80000000u;
+    const float h = __uint_as_float(sgn | ((unsigned)(e - 1023 + 127) << 23) | ((hi32 & 0xfffffu) << 3) | (lo32 >> 29));
+    const int se = e - 1075 + 127;  // biased FP32 exponent of 2^(e - 1075), the weight of the low bits
+    const float l = se > 0 ? __uint2float_rn(lo32 & 0x1fffffffu) * __uint_as_float((unsigned)se << 23) : 0.0f;
+    return make_float2(h, sgn ? -l : l);
+}
+
 // Arithmetic of the shifts: FP64, or double-float pairs on the FP32 pipe.
 template <bool DF>
 struct XOps;
@@ -167,6 +195,10 @@ struct XOps<false> {
     };
     static __device__ __forceinline__ double in(double w, int*) { return w; }
     static __device__ __forceinline__ double mul(double x, double y) { return x * y; }
+    static __device__ __forceinline__ double split(double w) { return w; }
+    static __device__ __forceinline__ double neg(double x) { return -x; }
+    static __device__ __forceinline__ double one() { return 1.0; }
+    static __device__ __forceinline__ double inv_int(int a) { return cInvInt[a]; }
     static __device__ __forceinline__ double out(double v) { return v; }
 };
 template <>
@@ -188,6 +220,10 @@ struct XOps<true> {
     };
     static __device__ __forceinline__ float2 in(double w, int* big) { return to_df(w, big); }
     static __device__ __forceinline__ float2 mul(float2 x, float2 y) { return df_mul(x, y); }
+    static __device__ __forceinline__ float2 split(double w) { return split_bits(w); }
+    static __device__ __forceinline__ float2 neg(float2 x) { return make_float2(-x.x, -x.y); }
+    static __device__ __forceinline__ float2 one() { return make_float2(1.0f, 0.0f); }
+    static __device__ __forceinline__ float2 inv_int(int a) { return cInvIntF[a]; }
     static __device__ __forceinline__ double out(float2 v) { return (double)v.x + (double)v.y; }
 };
 
@@ -199,7 +235,14 @@ struct XOps<true> {
 // (NM independent accumulators per u, the moments read as shared-memory
 // broadcasts, dp_i[u] formed in registers from the particle's powers per
 // axis), then the short sums over s.
-constexpr int kP2mBatch = 16;
+constexpr int kP2mBatch = 64;
+
+// Shared-memory entries (8 bytes) of the P2M staging area: one batch's
+// powers and moments, or the leaf's A_s[u] at the end.
+__host__ __device__ __forceinline__ int p2m_stage_entries(int p, int nm) {
+    const int a = kP2mBatch * (3 * (p + 1) + nm), b = nT(p) * nm;
+    return a > b ? a : b;
+}
 
 __device__ __forceinline__ int pk_index(int x, int y, int z) {
     const int k = x + y + z, yz = y + z;
@@ -207,23 +250,23 @@ __device__ __forceinline__ int pk_index(int x, int y, int z) {
 }
 
 template <bool DF, int NM, int KS, int NT>
-__global__ void __launch_bounds__(NT) k_p2m(const TreeDev t, const double* __restrict__ sx,
-                                            const double* __restrict__ sy, const double* __restrict__ sz,
-                                            const double* __restrict__ smc, int64_t n, int p,
-                                            const int* __restrict__ tab, TabView v, double* __restrict__ mom) {
+__global__ void __launch_bounds__(NT, 512 / NT) k_p2m(const TreeDev t, const double* __restrict__ sx,
+                                                      const double* __restrict__ sy, const double* __restrict__ sz,
+                                                      const double* __restrict__ smc, int64_t n, int p,
+                                                      const int* __restrict__ tab, TabView v,
+                                                      double* __restrict__ mom) {
     using O = XOps<DF>;
     using V = typename O::V;
+    constexpr int KB = kP2mBatch;
     extern __shared__ __align__(16) double sm_p2m[];
     const int nq = v.nq, P1 = p + 1;
-    V* e = reinterpret_cast<V*>(sm_p2m);    // [kP2mBatch][3][p+1] powers per axis
-    V* ms = e + kP2mBatch * 3 * P1;         // [kP2mBatch][NM] scaled moments
-    V* A = ms + kP2mBatch * NM;             // [nq][NM]
-    int* comp = reinterpret_cast<int*>(A + (size_t)nq * NM);
+    V* stage = reinterpret_cast<V*>(sm_p2m);  // [KB][3][p+1] powers per axis, [KB][NM] moments
+    V* A = stage;                             // [nq][NM], after the last batch
+    int* comp = reinterpret_cast<int*>(stage + p2m_stage_entries(p, NM));
     copy_ints(comp, tab + v.comp, nq);
     const int leaf = t.leaves[blockIdx.x];
     const double cx = t.cx[leaf], cy = t.cy[leaf], cz = t.cz[leaf];
     const int s0 = t.start[leaf], cnt = t.count[leaf];
-    int big = 0;
     __syncthreads();
     // this thread's u (KS slots) and the moments s that pair with each
     int ux[KS], uy[KS], uz[KS], ns[KS];
@@ -242,36 +285,41 @@ __global__ void __launch_bounds__(NT) k_p2m(const TreeDev t, const double* __res
         }
     }
     typename O::Acc acc[KS][NM];
-    for (int b0 = 0; b0 < cnt; b0 += kP2mBatch) {
-        const int nb = min(kP2mBatch, cnt - b0);
-        if (threadIdx.x < 3 * nb) {
-            const int b = threadIdx.x / 3, ax = threadIdx.x % 3, k = s0 + b0 + b;
-            const double d = ax == 0 ? sx[k] - cx : (ax == 1 ? sy[k] - cy : sz[k] - cz);
-            double w = 1.0;
-            V* eb = e + (b * 3 + ax) * P1;
-            eb[0] = O::in(1.0, &big);
+    for (int b0 = 0; b0 < cnt; b0 += KB) {
+        const int nb = min(KB, cnt - b0);
+        // scaled powers d^a / a! per particle axis and the moments M_s / s!
+        // (sign of the potential convention), all of the batch at once
+        for (int k = threadIdx.x; k < 3 * nb; k += NT) {
+            const int b = k / 3, ax = k - 3 * b, i = s0 + b0 + b;
+            const V d = O::split(ax == 0 ? sx[i] - cx : (ax == 1 ? sy[i] - cy : sz[i] - cz));
+            V w = O::one();
+            V* eb = stage + k * P1;
+            eb[0] = w;
             for (int a = 1; a <= p; ++a) {
-                w *= d * cInvInt[a];
-                eb[a] = O::in(w, &big);
+                w = O::mul(O::mul(w, d), O::inv_int(a));
+                eb[a] = w;
             }
         }
+        V* msb = stage + KB * 3 * P1;
         for (int idx = threadIdx.x; idx < nb * NM; idx += NT) {
-            const int b = idx / NM, s = idx - b * NM;
-            const double c = smc[(size_t)s * n + s0 + b0 + b];
-            ms[idx] = O::in(((order_of(s) + 1) % 2) ? -c : c, &big);  // back to M_s / s!
+            const int b = idx / NM, sidx = idx - b * NM;
+            const V w = O::split(smc[(size_t)sidx * n + s0 + b0 + b]);
+            msb[idx] = ((order_of(sidx) + 1) % 2) ? O::neg(w) : w;
         }
         __syncthreads();
         for (int b = 0; b < nb; ++b) {
-            const V* eb = e + b * 3 * P1;
-            const V* mb = ms + b * NM;
+            const V* eb = stage + b * 3 * P1;
+            const V* mb = msb + b * NM;
+            V dp[KS];
 #pragma unroll
-            for (int r = 0; r < KS; ++r) {
-                if (ns[r] > 0) {
-                    const V dp = O::mul(O::mul(eb[ux[r]], eb[P1 + uy[r]]), eb[2 * P1 + uz[r]]);
+            for (int r = 0; r < KS; ++r)
+                dp[r] = O::mul(O::mul(eb[ux[r]], eb[P1 + uy[r]]), eb[2 * P1 + uz[r]]);
 #pragma unroll
-                    for (int s = 0; s < NM; ++s)
-                        if (s < ns[r]) acc[r][s].mac(dp, mb[s]);
-                }
+            for (int sidx = 0; sidx < NM; ++sidx) {
+                const V m = mb[sidx];
+#pragma unroll
+                for (int r = 0; r < KS; ++r)
+                    if (sidx < ns[r]) acc[r][sidx].mac(dp[r], m);
             }
         }
         __syncthreads();
@@ -280,17 +328,17 @@ __global__ void __launch_bounds__(NT) k_p2m(const TreeDev t, const double* __res
     for (int r = 0; r < KS; ++r) {
         const int u = threadIdx.x + NT * r;
 #pragma unroll
-        for (int s = 0; s < NM; ++s)
-            if (s < ns[r]) A[u * NM + s] = acc[r][s].val();
+        for (int sidx = 0; sidx < NM; ++sidx)
+            if (sidx < ns[r]) A[u * NM + sidx] = acc[r][sidx].val();
     }
     __syncthreads();
     for (int q = threadIdx.x; q < nq; q += NT) {
         const int c = comp[q], tx = ux_(c), ty = uy_(c), tz = uz_(c);
         typename O::Acc sum;
 #pragma unroll
-        for (int s = 0; s < NM; ++s) {
-            const int sc = comp[s], qx = ux_(sc), qy = uy_(sc), qz = uz_(sc);
-            if (qx <= tx && qy <= ty && qz <= tz) sum.add(A[pk_index(tx - qx, ty - qy, tz - qz) * NM + s]);
+        for (int sidx = 0; sidx < NM; ++sidx) {
+            const int sc = comp[sidx], qx = ux_(sc), qy = uy_(sc), qz = uz_(sc);
+            if (qx <= tx && qy <= ty && qz <= tz) sum.add(A[pk_index(tx - qx, ty - qy, tz - qz) * NM + sidx]);
         }
         mom[(size_t)leaf * nq + q] = O::out(sum.val());
     }
@@ -555,8 +603,7 @@ int set_smem(const void* fn, size_t bytes) {
 template <bool DF, int NM, int NT>
 int launch_p2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, const int* tab, const TabView& v,
                double* mom, cudaStream_t st) {
-    const size_t sm = sizeof(double) * (kP2mBatch * 3 * (size_t)(p + 1) + kP2mBatch * NM + (size_t)v.nq * NM) +
-                      sizeof(int) * (size_t)v.nq;
+    const size_t sm = sizeof(double) * (size_t)p2m_stage_entries(p, NM) + sizeof(int) * (size_t)v.nq;
     const int ks = (v.nq + NT - 1) / NT;
 #define FMM_P2M_CASE(KS)                                                                                          \
     case KS:                                                                                                      \
