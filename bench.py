@@ -43,11 +43,14 @@ DAMP = "AMOEBA"
 # The reference's own settings (theta 0.5, p 8) give RMS ~2e-4 on this system
 # (the undamped far field and the loose acceptance test); the fixed rule below
 # is the cheapest one measured to reach <= 1e-6 RMS in FP64 and in mixed
-# precision: damping-aware acceptance, theta 0.3, expansion order 10.
+# precision: damping-aware acceptance, theta 0.3, expansion order 10.  The
+# learned selector picks each far pair's order up to p = 12 (higher orders
+# move pairs from the near field to the far field; its fallback is the fixed
+# rule at theta 0.3 and that order).
 ARMS = {
     "fp64": dict(theta=0.3, p=10, precision="fp64", mac_mode="damping", selector="fixed"),
     "mixed": dict(theta=0.3, p=10, precision="mixed", mac_mode="damping", selector="fixed"),
-    "learned": dict(theta=0.3, p=10, precision="mixed", mac_mode="damping", selector="learned"),
+    "learned": dict(theta=0.3, p=12, precision="mixed", mac_mode="damping", selector="learned"),
 }
 REF_SETTINGS = dict(theta=0.5, p=8)  # the reference's rule, used for the CPU baseline
 
@@ -418,9 +421,9 @@ def main():
     _lib.check(L.fmm_measure_fma_peak(prec, ctypes.byref(peak)), "fma peak")
     p2p_pairs = stats["p2p_particle_pairs"] - n
     m2l_product_flops = sum(stats["m2l_pairs_q%d" % q] * m2l_product_flops_per_pair(q) for q in range(13))
-    # the FP32 M2L product runs on the tensor cores (tcgen05 kind::tf32) for
-    # orders <= 10, which is every pair of these arms (p = 10)
-    tc_product = prec == 1 and ARMS[args.arm]["p"] <= 10
+    # the FP32 M2L product runs on the tensor cores (tcgen05 kind::tf32)
+    # unless FMM_GB300_M2L_PRODUCT=cuda moves it to the CUDA cores
+    tc_product = prec == 1 and os.environ.get("FMM_GB300_M2L_PRODUCT") != "cuda"
     m2l_name = "k_m2l_tc" if tc_product else ("k_m2l_gemm<float>" if prec else "k_m2l_gemm<double>")
     kern = {
         ("k_p2p_f32" if prec else "k_p2p_f64"): (p2p_pairs * pair_flops(2, F_ORDER), phase["t_p2p_kernel"],
@@ -432,9 +435,10 @@ def main():
                if v[1] > 0}
     if tc_product and m2l_name in kernels:
         # tensor-core view: MMA flops issued (three TF32 products per term, 128
-        # operator rows, K rounded up to 8) against the TF32 rate, half the
-        # measured bf16 burst peak
-        mma = sum(stats["m2l_pairs_q%d" % q] * 3 * 2 * 128 * 8 * (((q + 1) ** 2 + 7) // 8) for q in range(11))
+        # operator rows per half, two halves above order 10, K rounded up to
+        # 8) against the TF32 rate, half the measured bf16 burst peak
+        mma = sum(stats["m2l_pairs_q%d" % q] * 3 * 2 * 128 * 8 * (((q + 1) ** 2 + 7) // 8) * (2 if q > 10 else 1)
+                  for q in range(13))
         tf32_peak = measured_peaks().get("bf16_tflops", 1900.0) / 2
         kk = kernels[m2l_name]
         kk["mma_flops_issued"] = mma

@@ -63,7 +63,7 @@ def build(verbose=False, force=False):
         for r in results:
             sys.stderr.write(r[1])
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart", "-lpthread"]
         subprocess.check_call(cmd)
         os.replace(LIB + ".tmp", LIB)
     return LIB

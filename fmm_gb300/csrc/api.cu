@@ -6,6 +6,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
+#include <unistd.h>
 #include <vector>
 
 #include "internal.h"
@@ -115,12 +117,46 @@ int check_common(int64_t n, int mdim, int exw, int field_order, int damp, const 
     return FMM_OK;
 }
 
+// Exclusion indices must lie in 0..n (0 = unused slot): a branch-free
+// minimum / maximum over the array (vectorisable), then one comparison.
 int check_exclusions_host(int64_t n, int exw, const int32_t* ex) {
     if (exw > 0 && !ex) return FMM_EINVAL;
-    for (int64_t q = 0; q < n * (int64_t)exw; ++q)
-        if (ex[q] < 0 || ex[q] > n) return FMM_EINVAL;
-    return FMM_OK;
+    const int64_t total = n * (int64_t)exw;
+    int32_t lo = 0, hi = 0;
+    for (int64_t q = 0; q < total; ++q) {
+        lo = std::min(lo, ex[q]);
+        hi = std::max(hi, ex[q]);
+    }
+    return (lo < 0 || (int64_t)hi > n) ? FMM_EINVAL : FMM_OK;
 }
+
+// Populates the pages of a host output buffer from a helper thread while
+// the device works, so that the final device-to-host copy does not take the
+// first-touch faults of freshly allocated memory (each byte is rewritten with
+// its own value).  Joined before the copy, or when leaving the call.
+class OutputPrefault {
+  public:
+    OutputPrefault(void* p, size_t bytes) {
+        if (!p || bytes == 0) return;
+        try {
+            th_ = std::thread([p, bytes] {
+                const long pg = sysconf(_SC_PAGESIZE);
+                const size_t step = pg > 0 ? (size_t)pg : 4096;
+                volatile char* c = static_cast<volatile char*>(p);
+                for (size_t k = 0; k < bytes; k += step) c[k] = c[k];
+                c[bytes - 1] = c[bytes - 1];
+            });
+        } catch (...) {
+        }
+    }
+    void join() {
+        if (th_.joinable()) th_.join();
+    }
+    ~OutputPrefault() { join(); }
+
+  private:
+    std::thread th_;
+};
 
 __global__ void k_check_excl(int64_t total, int64_t n, const int32_t* __restrict__ ex, int* bad) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x)
@@ -489,9 +525,11 @@ int fmm_field_direct(int comm, int64_t n, const double* X, int mdim, const doubl
     const int nf = nT(field_order);
     Particles P;
     FMM_TRY(upload(ws, n, X, mdim, mp, exw, ex, dt != DAMP_NONE ? dampf : nullptr, nf, &P, st));
+    OutputPrefault pf(field, sizeof(double) * (size_t)nf * n);
     P.damp_type = dt;
     Modes md{o.coef_mode, o.excl_mode, o.precision};
     FMM_TRY(launch_direct_f64(ws, P, field_order, md, ws.out_field.as<double>(), st));
+    pf.join();
     FMM_CUDA_TRY(cudaMemcpyAsync(field, ws.out_field.p, sizeof(double) * (size_t)nf * n, cudaMemcpyDeviceToHost, st));
     FMM_CUDA_TRY(cudaStreamSynchronize(st));
     return FMM_OK;
@@ -556,6 +594,7 @@ int fmm_field_fmm(int comm, int64_t n, const double* X, int mdim, const double* 
     const int nf = nT(field_order);
     Particles P;
     FMM_TRY(upload(ws, n, X, mdim, mp, exw, ex, dt != DAMP_NONE ? dampf : nullptr, nf, &P, st));
+    OutputPrefault pf(field, sizeof(double) * (size_t)nf * n);
     P.damp_type = dt;
     TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode, 0.0, p};
     if (o.centroid_mode == 0) {
@@ -563,6 +602,7 @@ int fmm_field_fmm(int comm, int64_t n, const double* X, int mdim, const double* 
         tp.have_host_centroid = 1;
     }
     FMM_TRY(run_fmm(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st));
+    pf.join();
     FMM_CUDA_TRY(cudaMemcpyAsync(field, ws.out_field.p, sizeof(double) * (size_t)nf * n, cudaMemcpyDeviceToHost, st));
     FMM_CUDA_TRY(cudaStreamSynchronize(st));
     return FMM_OK;
