@@ -112,6 +112,7 @@ struct Workspace {
     DevBuf fsorted;
     // expansions
     DevBuf mom, loc, wred;
+    int wred_p = -1;  // order of the reduced weights in wred computed from this call's moments (-1: none)
     // direct sum: scaled multipoles and partial sums
     DevBuf dsmc, partial;
     // second stream (the learned selector's sampled direct sum overlaps the tree phases)

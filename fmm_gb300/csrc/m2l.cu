@@ -299,6 +299,7 @@ int launch_reduce_moments(Workspace& ws, const TreeDev& t, int p, cudaStream_t s
     count_launches(1);
     k_reduce_moments<<<grid_for(M, wpb), 32 * wpb, sm, st>>>(M, p, ws.mom.as<double>(), ws.wred.as<double>());
     FMM_CUDA_TRY(cudaGetLastError());
+    ws.wred_p = p;
     return FMM_OK;
 }
 
@@ -308,7 +309,7 @@ int launch_m2l_reduced(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaSt
     const int M = t.num_nodes, nq = nT(p), nr = (p + 1) * (p + 1);
     FMM_TRY(ws.loc.ensure(sizeof(double) * (size_t)M * nq));
     FMM_TRY(ws.wred.ensure(sizeof(double) * (size_t)M * nr));
-    {
+    if (ws.wred_p != p) {  // not yet reduced from this call's moments
         const int wpb = 4;
         const size_t sm = sizeof(double) * wpb * nq;
         FMM_TRY(set_smem((const void*)k_reduce_moments, sm));

@@ -31,11 +31,16 @@ int num_sms() {
     return sms;
 }
 
+// Contraction coefficients c_s of the multipole components (order <= 2),
+// folded at compile time (no FP64 division per element).
+__constant__ double cSrcCoef[10] = {src_coef(0), src_coef(1), src_coef(2), src_coef(3), src_coef(4),
+                                    src_coef(5), src_coef(6), src_coef(7), src_coef(8), src_coef(9)};
+
 // Multipoles times the contraction coefficient c_s, original particle order.
 __global__ void k_scale_mp(int64_t n, int dim, const double* __restrict__ mp, double* __restrict__ out) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= n) return;
-    for (int c = 0; c < dim; ++c) out[(size_t)c * n + k] = src_coef(c) * mp[(size_t)c * n + k];
+    for (int c = 0; c < dim; ++c) out[(size_t)c * n + k] = cSrcCoef[c] * mp[(size_t)c * n + k];
 }
 
 // Particle data in key-sorted order (coordinates, damping, scaled multipoles).
@@ -50,7 +55,7 @@ __global__ void k_gather(int64_t n, int dim, const uint32_t* __restrict__ perm, 
     sy[k] = X[n + o];
     sz[k] = X[2 * n + o];
     sd[k] = damp ? damp[o] : 0.0;
-    for (int c = 0; c < dim; ++c) smc[(size_t)c * n + k] = src_coef(c) * mp[(size_t)c * n + o];
+    for (int c = 0; c < dim; ++c) smc[(size_t)c * n + k] = cSrcCoef[c] * mp[(size_t)c * n + o];
 }
 
 // P2P: one warp per target leaf.  A leaf's targets are taken 32 at a time;

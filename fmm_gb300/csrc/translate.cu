@@ -634,6 +634,7 @@ int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, c
     const int* tab = ws.xlate.as<int>();
     FMM_TRY(ws.mom.ensure(sizeof(double) * (size_t)t.num_nodes * nq));
     double* mom = ws.mom.as<double>();
+    ws.wred_p = -1;  // new moments: the reduced weights are stale
     if (t.num_leaves > 0) {
         count_launches(1);
         const int nm = nT(m);
