@@ -91,8 +91,8 @@ def workload_config(arm, system="water", n=3 * N_MOL):
 
 # DRAM bytes (read + write) per unit of the two dominant kernels, from one ncu
 # capture of each on the 100k water case (profiles/)
-P2P_DRAM_PER_PAIR = 12.82e6 / 415.53e6
-TC_DRAM_PER_PAIR = (493.49e6 + 730.46e6) / 2.026111e6
+P2P_DRAM_PER_PAIR = 12.81e6 / 412.98e6
+TC_DRAM_PER_PAIR = (571.38e6 + 479.74e6) / 1.084818e6
 
 
 def measured_peaks():
