@@ -310,16 +310,21 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_p2m(const TreeDev t, const dou
         for (int b = 0; b < nb; ++b) {
             const V* eb = stage + b * 3 * P1;
             const V* mb = msb + b * NM;
-            V dp[KS];
+            V m[NM];
 #pragma unroll
-            for (int r = 0; r < KS; ++r)
-                dp[r] = O::mul(O::mul(eb[ux[r]], eb[P1 + uy[r]]), eb[2 * P1 + uz[r]]);
+            for (int sidx = 0; sidx < NM; ++sidx) m[sidx] = mb[sidx];
 #pragma unroll
-            for (int sidx = 0; sidx < NM; ++sidx) {
-                const V m = mb[sidx];
+            for (int r = 0; r < KS; ++r) {
+                if (ns[r] == 0) continue;
+                const V dp = O::mul(O::mul(eb[ux[r]], eb[P1 + uy[r]]), eb[2 * P1 + uz[r]]);
+                if (ns[r] == NM) {  // every moment (all but the top two orders of u)
 #pragma unroll
-                for (int r = 0; r < KS; ++r)
-                    if (sidx < ns[r]) acc[r][sidx].mac(dp[r], m);
+                    for (int sidx = 0; sidx < NM; ++sidx) acc[r][sidx].mac(dp, m[sidx]);
+                } else {
+#pragma unroll
+                    for (int sidx = 0; sidx < NM; ++sidx)
+                        if (sidx < ns[r]) acc[r][sidx].mac(dp, m[sidx]);
+                }
             }
         }
         __syncthreads();
