@@ -36,24 +36,36 @@ __device__ __forceinline__ int ux_(int c) { return c & 0xff; }
 __device__ __forceinline__ int uy_(int c) { return (c >> 8) & 0xff; }
 __device__ __forceinline__ int uz_(int c) { return (c >> 16) & 0xff; }
 
-// Packed components (x | y << 8 | z << 16) of order <= p in the packed
-// order, uploaded once per order.
+// Packed components (x | y << 8 | z << 16) of order <= p: in the packed
+// order, then sorted by z, by y and by x (the orders in which the M2M's
+// three shifts visit their outputs, so that the outputs of a warp have the
+// same number of terms), uploaded once per order.
 struct TabView {
-    int nq, comp;
+    int nq, comp, byz, byy, byx;
 };
 
 int hidx(int x, int y, int z) { return nT(x + y + z - 1) + ((y + z) * (y + z + 1)) / 2 + z; }
 
 int ensure_tables(Workspace& ws, int p, TabView* out, cudaStream_t st) {
-    out->nq = nT(p);
+    const int nq = nT(p);
+    out->nq = nq;
     out->comp = 0;
+    out->byz = nq;
+    out->byy = 2 * nq;
+    out->byx = 3 * nq;
     if (ws.xlate_p == p) return FMM_OK;
     std::vector<int> comp;
     for (int k = 0; k <= p; ++k)
         for (int x = k; x >= 0; --x)
             for (int y = k - x; y >= 0; --y) comp.push_back(pack3(x, y, k - x - y));
-    FMM_TRY(ws.xlate.ensure(sizeof(int) * comp.size()));
-    FMM_CUDA_TRY(cudaMemcpyAsync(ws.xlate.p, comp.data(), sizeof(int) * comp.size(), cudaMemcpyHostToDevice, st));
+    std::vector<int> all(comp);
+    for (int sh : {16, 8, 0}) {  // by z, by y, by x
+        std::vector<int> o(comp);
+        std::stable_sort(o.begin(), o.end(), [sh](int a, int b) { return ((a >> sh) & 0xff) < ((b >> sh) & 0xff); });
+        all.insert(all.end(), o.begin(), o.end());
+    }
+    FMM_TRY(ws.xlate.ensure(sizeof(int) * all.size()));
+    FMM_CUDA_TRY(cudaMemcpyAsync(ws.xlate.p, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice, st));
     FMM_CUDA_TRY(cudaStreamSynchronize(st));
     ws.xlate_p = p;
     return FMM_OK;
@@ -140,14 +152,6 @@ __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
     return make_float2(s, e - (s - p));
 }
 
-// (hi, lo) FP32 pair of an FP64 value; *big set when it is outside the range
-// where double-float products keep their precision.
-__device__ __forceinline__ float2 to_df(double w, int* big) {
-    if (fabs(w) > 1e30) *big = 1;
-    const float hi = (float)w;
-    return make_float2(hi, (float)(w - (double)hi));
-}
-
 // a += x * y in double-float (exact product by FMA, TwoSum accumulation).
 __device__ __forceinline__ void df_mac(float2 x, float2 y, float& h, float& l) {
     const float pr = x.x * y.x;
@@ -179,6 +183,15 @@ __device__ __forceinline__ float2 split_bits(double w) {
     const int se = e - 1075 + 127;  // biased FP32 exponent of 2^(e - 1075), the weight of the low bits
     const float l = se > 0 ? __uint2float_rn(lo32 & 0x1fffffffu) * __uint_as_float((unsigned)se << 23) : 0.0f;
     return make_float2(h, sgn ? -l : l);
+}
+
+// split_bits, and *big set for magnitudes from 2^99 up or non-finite values
+// (outside the range where double-float products keep their precision),
+// on integer instructions.
+__device__ __forceinline__ float2 to_df_bits(double w, int* big) {
+    const int e = (int)(((unsigned long long)__double_as_longlong(w) >> 52) & 0x7ffu);
+    if (e >= 1023 + 99) *big = 1;
+    return split_bits(w);
 }
 
 // Arithmetic of the shifts: FP64, or double-float pairs on the FP32 pipe.
@@ -218,7 +231,7 @@ struct XOps<true> {
             return make_float2(s, l - (s - h));
         }
     };
-    static __device__ __forceinline__ float2 in(double w, int* big) { return to_df(w, big); }
+    static __device__ __forceinline__ float2 in(double w, int* big) { return to_df_bits(w, big); }
     static __device__ __forceinline__ float2 mul(float2 x, float2 y) { return df_mul(x, y); }
     static __device__ __forceinline__ float2 split(double w) { return split_bits(w); }
     static __device__ __forceinline__ float2 neg(float2 x) { return make_float2(-x.x, -x.y); }
@@ -357,7 +370,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_p2m(const TreeDev t, const dou
 // shift instead of the C(p+6,6) of the direct sum, and no output of a shift
 // has more than p+1 terms, so the block's outputs finish together.  A block
 // per parent node takes its children one after another.
-constexpr int kXThreads = 256;
+constexpr int kXThreads = 512;  // one output per thread up to order 12: a shift waits for at most p+1 terms
 constexpr int kXOut = (nT(kMaxP) + kXThreads - 1) / kXThreads;  // outputs per thread
 
 __device__ __forceinline__ int d3(int a, int b, int c, int P1) { return (a * P1 + b) * P1 + c; }
@@ -384,60 +397,64 @@ __device__ __forceinline__ void child_offsets(const TreeDev& t, int node, int p,
 }
 
 // M2M of one parent: M'_t = sum_children sum_{u <= t} (d^u/u!) M'_{t-u}(child)
-// as shifts along z (Y from X), y (X from Y) and x (into the accumulators of
-// the thread's outputs).  Writes the result unless *big was raised.
+// as shifts along z (Y from X), y (X from Y) and x (into the accumulator of
+// the thread's output), each visiting its outputs sorted by the number of
+// terms; the next child's moments are loaded during the current child's
+// shifts.  Writes the result unless *big was raised.
 template <bool DF>
-__device__ __forceinline__ void m2m_node(const TreeDev& t, int node, int p, int nq, const int* comp, const int* ch,
-                                         const double* e, void* buf, int* big, double* __restrict__ mom) {
+__device__ __forceinline__ void m2m_node(int node, int p, int nq, const int* comp, const int* byz, const int* byy,
+                                         const int* byx, const int* ch, const double* e, void* buf, int* big,
+                                         double* __restrict__ mom) {
+    static_assert(kXOut == 1, "one output per thread");
     using O = XOps<DF>;
     using V = typename O::V;
-    const int P1 = p + 1, n3 = P1 * P1 * P1;
+    const int P1 = p + 1, n3 = P1 * P1 * P1, q = threadIdx.x;
     V* X = reinterpret_cast<V*>(buf);
     V* Y = X + n3;
     V* E = Y + n3;  // [8][3][p+1]
     const int nch = ch[8];
     for (int k = threadIdx.x; k < nch * 3 * P1; k += blockDim.x) E[k] = O::in(e[k], big);
-    typename O::Acc acc[kXOut];
+    int cz = 0, cy = 0, cx = 0, xo = 0;
+    if (q < nq) {
+        cz = byz[q];
+        cy = byy[q];
+        cx = byx[q];
+        xo = pk_index(cx & 0xff, (cx >> 8) & 0xff, cx >> 16);
+    }
+    double mnext = (q < nq && nch > 0) ? mom[(size_t)ch[0] * nq + q] : 0.0;
+    typename O::Acc acc;
     for (int b = 0; b < nch; ++b) {
-        const double* mc = mom + (size_t)ch[b] * nq;
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        if (q < nq) {
             const int cc = comp[q];
-            X[d3(cc & 0xff, (cc >> 8) & 0xff, cc >> 16, P1)] = O::in(mc[q], big);
+            X[d3(cc & 0xff, (cc >> 8) & 0xff, cc >> 16, P1)] = O::in(mnext, big);
         }
         __syncthreads();
+        if (b + 1 < nch && q < nq) mnext = mom[(size_t)ch[b + 1] * nq + q];  // in flight during the shifts
         const V* ex = E + b * 3 * P1;
         const V* ey = ex + P1;
         const V* ez = ey + P1;
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-            const int cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
+        if (q < nq) {
+            const int x = cz & 0xff, y = (cz >> 8) & 0xff, z = cz >> 16;
             typename O::Acc s;
             for (int u = 0; u <= z; ++u) s.mac(ez[u], X[d3(x, y, z - u, P1)]);
             Y[d3(x, y, z, P1)] = s.val();
         }
         __syncthreads();
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-            const int cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
+        if (q < nq) {
+            const int x = cy & 0xff, y = (cy >> 8) & 0xff, z = cy >> 16;
             typename O::Acc s;
             for (int u = 0; u <= y; ++u) s.mac(ey[u], Y[d3(x, y - u, z, P1)]);
             X[d3(x, y, z, P1)] = s.val();
         }
         __syncthreads();
-#pragma unroll
-        for (int r = 0; r < kXOut; ++r) {
-            const int q = threadIdx.x + kXThreads * r;
-            if (q < nq) {
-                const int cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
-                for (int u = 0; u <= x; ++u) acc[r].mac(ex[u], X[d3(x - u, y, z, P1)]);
-            }
+        if (q < nq) {
+            const int x = cx & 0xff, y = (cx >> 8) & 0xff, z = cx >> 16;
+            for (int u = 0; u <= x; ++u) acc.mac(ex[u], X[d3(x - u, y, z, P1)]);
         }
         __syncthreads();  // X is the next child's
     }
     if (DF && *big) return;
-#pragma unroll
-    for (int r = 0; r < kXOut; ++r) {
-        const int q = threadIdx.x + kXThreads * r;
-        if (q < nq) mom[(size_t)node * nq + q] = O::out(acc[r].val());
-    }
+    if (q < nq) mom[(size_t)node * nq + xo] = O::out(acc.val());
 }
 
 // DF: double-float shifts, FP64 again for the blocks whose powers or moments
@@ -451,15 +468,15 @@ __global__ void __launch_bounds__(kXThreads) k_m2m(const TreeDev t, const int32_
     const int node = nodes[blockIdx.x];
     if (t.is_leaf[node]) return;
     double* e = sm_m2m;                                          // [8][3][p+1]
-    int* comp = reinterpret_cast<int*>(e + 8 * 3 * P1);          // [nq]
-    void* buf = e + 8 * 3 * P1 + (nq + 1) / 2;                   // X, Y, E
-    copy_ints(comp, tab + v.comp, nq);
+    int* comp = reinterpret_cast<int*>(e + 8 * 3 * P1);          // [4][nq]: packed, by z, by y, by x
+    void* buf = e + 8 * 3 * P1 + (4 * nq + 1) / 2;               // X, Y, E
+    copy_ints(comp, tab + v.comp, 4 * nq);
     if (threadIdx.x == 0) big = 0;
     child_offsets(t, node, p, ch, e);
-    m2m_node<DF>(t, node, p, nq, comp, ch, e, buf, &big, mom);
+    m2m_node<DF>(node, p, nq, comp, comp + nq, comp + 2 * nq, comp + 3 * nq, ch, e, buf, &big, mom);
     if (DF) {
         __syncthreads();
-        if (big) m2m_node<false>(t, node, p, nq, comp, ch, e, buf, &big, mom);
+        if (big) m2m_node<false>(node, p, nq, comp, comp + nq, comp + 2 * nq, comp + 3 * nq, ch, e, buf, &big, mom);
     }
 }
 
@@ -469,6 +486,7 @@ __global__ void __launch_bounds__(kXThreads) k_m2m(const TreeDev t, const int32_
 template <bool DF>
 __device__ __forceinline__ void l2l_node(int node, int p, int nq, const int* comp, const int* ch, const double* e,
                                          void* buf, int* big, double* __restrict__ loc) {
+    static_assert(kXOut == 1, "one output per thread");
     using O = XOps<DF>;
     using V = typename O::V;
     const int P1 = p + 1, n3 = P1 * P1 * P1;
@@ -488,6 +506,9 @@ __device__ __forceinline__ void l2l_node(int node, int p, int nq, const int* com
         const V* ex = E + b * 3 * P1;
         const V* ey = ex + P1;
         const V* ez = ey + P1;
+        // the child's own expansion, in flight during the shifts
+        double* lc = loc + (size_t)ch[b] * nq;
+        const double lprev = threadIdx.x < nq ? lc[threadIdx.x] : 0.0;
         for (int q = threadIdx.x; q < nq; q += blockDim.x) {
             const int cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
             typename O::Acc s;
@@ -502,12 +523,11 @@ __device__ __forceinline__ void l2l_node(int node, int p, int nq, const int* com
             Z[d3(x, y, z, P1)] = s.val();
         }
         __syncthreads();
-        double* lc = loc + (size_t)ch[b] * nq;
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-            const int cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
+        if (threadIdx.x < nq) {  // one output per thread
+            const int q = threadIdx.x, cc = comp[q], x = cc & 0xff, y = (cc >> 8) & 0xff, z = cc >> 16;
             typename O::Acc s;
             for (int u = 0; u <= p - x - y - z; ++u) s.mac(ex[u], Z[d3(x + u, y, z, P1)]);
-            lc[q] += O::out(s.val());
+            lc[q] = lprev + O::out(s.val());
         }
         __syncthreads();  // Y and Z are the next child's
     }
@@ -536,9 +556,9 @@ __global__ void __launch_bounds__(kXThreads) k_l2l(const TreeDev t, const int32_
 
 // Shared memory of k_m2m / k_l2l: powers, components, dense expansions and
 // the powers in the kernel's arithmetic.
-size_t xlate_smem(int p, int ndense) {
+size_t xlate_smem(int p, int ndense, int ncomp) {
     const int P1 = p + 1, nq = nT(p);
-    return sizeof(double) * (2 * 8 * 3 * (size_t)P1 + (nq + 1) / 2 + (size_t)ndense * P1 * P1 * P1);
+    return sizeof(double) * (2 * 8 * 3 * (size_t)P1 + (ncomp * nq + 1) / 2 + (size_t)ndense * P1 * P1 * P1);
 }
 
 // ---------------------------------------------------------------- L2P
@@ -654,7 +674,7 @@ int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, c
         }
     }
     {
-        const size_t sm = xlate_smem(p, 2);
+        const size_t sm = xlate_smem(p, 2, 4);
         FMM_TRY(set_smem((const void*)k_m2m<false>, sm));
         FMM_TRY(set_smem((const void*)k_m2m<true>, sm));
         for (int d = t.max_depth - 1; d >= 1; --d) {
@@ -679,7 +699,7 @@ int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, i
     const int* tab = ws.xlate.as<int>();
     double* loc = ws.loc.as<double>();
     {
-        const size_t sm = xlate_smem(p, 3);
+        const size_t sm = xlate_smem(p, 3, 1);
         FMM_TRY(set_smem((const void*)k_l2l<false>, sm));
         FMM_TRY(set_smem((const void*)k_l2l<true>, sm));
         for (int d = 1; d < t.max_depth; ++d) {
