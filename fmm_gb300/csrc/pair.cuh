@@ -296,7 +296,13 @@ __host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, 
                 }
             }
         }
-        if (closed) {
+        if (closed && sizeof(R) == 8 && x > (R)100) {
+            // FP64, far beyond the damping range: e^{-x} P(x) is below 1e-29
+            // of the undamped value, so the sum rounds to it exactly
+            num[0] = (R)1;
+#pragma unroll
+            for (int j = 1; j <= N; ++j) num[j] = (R)((j % 2 ? -1.0 : 1.0) * dfact_odd(j));
+        } else if (closed) {
             const R e = RT::expc_(-x);
             const R x2 = x * x;
             R ym1 = (R)1, y0 = -((R)1 + x);  // y_0, y_1 (Yukawa numerators)
@@ -339,7 +345,12 @@ __host__ __device__ __forceinline__ void radial_g_ir(int damp, R r2, R ir, R a, 
                 }
             }
         }
-        if (closed) {
+        if (closed && sizeof(R) == 8 && u > (R)80) {
+            // FP64, far beyond the damping range: e^{-u} q(u) is below 1e-25
+            // of the undamped value, so the sum rounds to it exactly
+#pragma unroll
+            for (int j = 1; j <= N; ++j) num[j] = (R)((j % 2 ? -1.0 : 1.0) * dfact_odd(j));
+        } else if (closed) {
             const R e = RT::expc_(-u);
 #pragma unroll
             for (int j = 1; j <= N; ++j) {
