@@ -846,7 +846,7 @@ struct Sum<double> {
 // (q+1)^2 entries; eight loads in flight), back to physical units, into the
 // reduced components of the local expansion.
 template <typename R>
-__global__ void __launch_bounds__(128) k_m2l_sum(const TreeDev t, int p, const R* __restrict__ out,
+__global__ void __launch_bounds__(256) k_m2l_sum(const TreeDev t, int p, const R* __restrict__ out,
                                                  const int32_t* __restrict__ roff, double* __restrict__ loc) {
     const int i = blockIdx.x;
     const int nr = (p + 1) * (p + 1);
@@ -1064,7 +1064,9 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
     }
     count_launches(1);
     if (nf == 0) FMM_TRY(ws.m2l_out.ensure(sizeof(R) * 32));
-    k_m2l_sum<R><<<(unsigned)M, 128, 0, st>>>(t, p, ws.m2l_out.as<R>(), roff, ws.loc.as<double>());
+    // one output per thread: (p+1)^2 rounded up to whole warps (192 at p = 12)
+    k_m2l_sum<R><<<(unsigned)M, (unsigned)std::min(256, (nr + 31) / 32 * 32), 0, st>>>(t, p, ws.m2l_out.as<R>(), roff,
+                                                                                     ws.loc.as<double>());
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
