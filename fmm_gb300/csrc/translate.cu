@@ -166,9 +166,8 @@ __device__ __forceinline__ void df_mac(float2 x, float2 y, float& h, float& l) {
 
 // (hi, lo) FP32 pair of an FP64 value from its bit pattern alone (no FP64
 // instruction): hi the value truncated to 24 significant bits, lo the
-// remaining 29 bits rounded to FP32 (zero below 2^-74 in magnitude).  Zero,
-// magnitudes outside the normal FP32 range and non-finite values take the
-// FP64 conversion.
+// remaining 29 bits rounded to FP32.  Zero, magnitudes outside the normal
+// FP32 range and non-finite values take the FP64 conversion.
 __device__ __forceinline__ float2 split_bits(double w) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(w);
     if ((b << 1) == 0ull) return make_float2(0.0f, 0.0f);
@@ -180,8 +179,12 @@ __device__ __forceinline__ float2 split_bits(double w) {
     }
     const unsigned sgn = hi32 & 0x80000000u;
     const float h = __uint_as_float(sgn | ((unsigned)(e - 1023 + 127) << 23) | ((hi32 & 0xfffffu) << 3) | (lo32 >> 29));
-    const int se = e - 1075 + 127;  // biased FP32 exponent of 2^(e - 1075), the weight of the low bits
-    const float l = se > 0 ? __uint2float_rn(lo32 & 0x1fffffffu) * __uint_as_float((unsigned)se << 23) : 0.0f;
+    // the low 29 bits weigh 2^(e - 1075); below 2^-126 that weight is applied
+    // in two steps (e >= 897 keeps the first step's exponent positive)
+    const int se = e - 1075 + 127;
+    const float r = __uint2float_rn(lo32 & 0x1fffffffu);
+    const float l = se > 0 ? r * __uint_as_float((unsigned)se << 23)
+                           : (r * __uint_as_float((unsigned)(se + 64) << 23)) * 0x1p-64f;
     return make_float2(h, sgn ? -l : l);
 }
 

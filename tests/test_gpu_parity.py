@@ -242,6 +242,21 @@ def test_m2l_tensor_core_product_matches_cuda_cores(p, monkeypatch):
     assert rel_err(Ftc, F64, slice(1, None)) < 5e-6
 
 
+@pytest.mark.parametrize("scale", [1e-24, 1e-9, 1e20])
+def test_mixed_precision_multipole_scale(scale):
+    """The mixed path splits FP64 moments into FP32 pairs from their bit
+    patterns (P2M, M2M, L2L): multipoles far from unit magnitude keep the
+    accuracy of the unit-scale case (the field is linear in them)."""
+    from fmm_gb300 import systems
+    s = systems.water(4000, 70.0, order=2, seed=23)
+    s["multipoles"] = s["multipoles"] * scale
+    d = s["damping_factors"]
+    F64 = fmm_gb300.field_fmm(*_fmm_args(s), 0.4, 64, 10, 1, "AMOEBA", d, options=Options.exact())
+    F32 = fmm_gb300.field_fmm(*_fmm_args(s), 0.4, 64, 10, 1, "AMOEBA", d, options=Options.exact(precision="mixed"))
+    assert np.all(np.isfinite(F32))
+    assert rel_err(F32, F64, slice(1, None)) < 5e-6
+
+
 @pytest.mark.parametrize("damp,mf", [("AMOEBA", (2, 1)), ("", (2, 2)), ("ERF", (1, 1)), ("THOLE", (0, 1))])
 def test_mixed_precision_close_to_fp64(damp, mf):
     """FP32 near field and M2L with FP64 sums: within FP32 accuracy of the FP64
