@@ -175,26 +175,32 @@ __global__ void k_keys(const double* __restrict__ X, int64_t n, const double* __
 // counters: [0] num_nodes, [1] internal nodes created this level, [2] error flag
 __global__ void k_build_level(int d, int p0, int p1, const uint64_t* __restrict__ keys, int ncrit, double* bd,
                               int32_t* bi, int64_t cap, int* counters) {
-    const int b = p0 + blockIdx.x * blockDim.x + threadIdx.x;
+    // eight lanes per node: lane o (1..7) binary-searches the first particle
+    // of octant >= o (the node's keys are sorted), lane 0 writes the children
+    const int sub = threadIdx.x & 7, gbase = threadIdx.x & 24;
+    const unsigned gmask = 0xffu << gbase;
+    const int b = p0 + (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 3);
     if (b >= p1) return;
-    if (bi[5 * cap + b]) return;  // leaf
+    if (bi[5 * cap + b]) return;  // leaf (the node's eight lanes leave together)
     const int s = bi[0 * cap + b];
     const int e = s + bi[1 * cap + b];
     const int shift = 3 * (kMaxDepth - d);
-    int lo[9];
-    lo[0] = s;
-    lo[8] = e;
-    for (int o = 1; o < 8; ++o) {
-        int a = lo[o - 1], h = e;
+    int a = s;
+    if (sub > 0) {
+        int h = e;
         while (a < h) {
             const int mid = (a + h) >> 1;
-            if ((int)((keys[mid] >> shift) & 7ull) < o)
+            if ((int)((keys[mid] >> shift) & 7ull) < sub)
                 a = mid + 1;
             else
                 h = mid;
         }
-        lo[o] = a;
     }
+    int lo[9];
+#pragma unroll
+    for (int o = 0; o < 8; ++o) lo[o] = __shfl_sync(gmask, a, gbase + o);
+    lo[8] = e;
+    if (sub != 0) return;
     int nc = 0, ni = 0;
     for (int o = 0; o < 8; ++o)
         if (lo[o + 1] > lo[o]) {
@@ -638,7 +644,7 @@ int build_tree(Workspace& ws, const double* d_X, int64_t n, const TreeParams& tp
         hc[2] = 0;
         FMM_CUDA_TRY(cudaMemcpyAsync(ctr, hc, sizeof(hc), cudaMemcpyHostToDevice, st));
         count_launches(1);
-        k_build_level<<<grid_for(level_hi - level_lo, 128), 128, 0, st>>>(
+        k_build_level<<<grid_for((int64_t)(level_hi - level_lo) * 8, 128), 128, 0, st>>>(
             d, level_lo, level_hi, skeys, tp.ncrit, ws.node_d.as<double>(), ws.node_i.as<int32_t>(), ws.node_cap, ctr);
         FMM_CUDA_TRY(cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, st));
         FMM_CUDA_TRY(cudaStreamSynchronize(st));
