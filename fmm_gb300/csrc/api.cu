@@ -49,6 +49,8 @@ Workspace::~Workspace() {
     if (events_ready)
         for (auto& e : ev) cudaEventDestroy(e);
     if (aux) cudaStreamDestroy(aux);
+    if (copy) cudaStreamDestroy(copy);
+    if (copy_ev) cudaEventDestroy(copy_ev);
 }
 
 Workspace& thread_workspace() {
@@ -158,6 +160,56 @@ class OutputPrefault {
     std::thread th_;
 };
 
+// Copies the multipoles and exclusions of a host call on the workspace's
+// copy stream from a helper thread, so that the transfer overlaps the tree
+// build; run_fmm joins it (ws.copy_join) and makes its stream wait for the
+// copies before it first reads them.  Without a thread the copies are made
+// here.
+class DeferredInputCopy {
+  public:
+    DeferredInputCopy(Workspace& ws, void* d_mp, const void* mp, size_t mp_bytes, void* d_ex, const void* ex,
+                      size_t ex_bytes)
+        : ws_(ws) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            (!ws.copy && cudaStreamCreateWithFlags(&ws.copy, cudaStreamNonBlocking) != cudaSuccess) ||
+            (!ws.copy_ev && cudaEventCreateWithFlags(&ws.copy_ev, cudaEventDisableTiming) != cudaSuccess)) {
+            status_ = FMM_ECUDA;
+            return;
+        }
+        auto copy = [this, dev, d_mp, mp, mp_bytes, d_ex, ex, ex_bytes] {
+            cudaError_t e = cudaSetDevice(dev);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(d_mp, mp, mp_bytes, cudaMemcpyHostToDevice, ws_.copy);
+            if (e == cudaSuccess && ex_bytes) e = cudaMemcpyAsync(d_ex, ex, ex_bytes, cudaMemcpyHostToDevice, ws_.copy);
+            if (e == cudaSuccess) e = cudaEventRecord(ws_.copy_ev, ws_.copy);
+            status_ = e == cudaSuccess ? FMM_OK : FMM_ECUDA;
+        };
+        started_ = true;
+        try {
+            th_ = std::thread(copy);
+        } catch (...) {
+            copy();
+        }
+        ws_.copy_join = [this] { return join(); };
+    }
+    bool started() const { return started_; }
+    int join() {
+        if (th_.joinable()) th_.join();
+        return status_;
+    }
+    ~DeferredInputCopy() {
+        join();
+        ws_.copy_join = nullptr;
+        if (started_ && status_ == FMM_OK) cudaEventSynchronize(ws_.copy_ev);  // no copy outlives the call
+    }
+
+  private:
+    Workspace& ws_;
+    std::thread th_;
+    int status_ = FMM_OK;
+    bool started_ = false;
+};
+
 __global__ void k_check_excl(int64_t total, int64_t n, const int32_t* __restrict__ ex, int* bad) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x)
         if (ex[q] < 0 || ex[q] > n) atomicExch(bad, 1);
@@ -204,18 +256,22 @@ void ensure_events(Workspace& ws) {
     }
 }
 
-// Copies host inputs into the workspace's device buffers.
+// Copies host inputs into the workspace's device buffers (with defer, the
+// multipoles and exclusions are left to a DeferredInputCopy).
 int upload(Workspace& ws, int64_t n, const double* X, int mdim, const double* mp, int exw, const int32_t* ex,
-           const double* damp, int nf, Particles* P, cudaStream_t st) {
+           const double* damp, int nf, Particles* P, cudaStream_t st, bool defer = false) {
     FMM_TRY(ws.in_coords.ensure(sizeof(double) * 3 * n));
     FMM_TRY(ws.in_mp.ensure(sizeof(double) * (size_t)mdim * n));
     FMM_TRY(ws.in_excl.ensure(sizeof(int32_t) * (size_t)std::max(exw, 1) * n));
     FMM_TRY(ws.in_damp.ensure(sizeof(double) * n));
     FMM_TRY(ws.out_field.ensure(sizeof(double) * (size_t)nf * n));
     FMM_CUDA_TRY(cudaMemcpyAsync(ws.in_coords.p, X, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
-    FMM_CUDA_TRY(cudaMemcpyAsync(ws.in_mp.p, mp, sizeof(double) * (size_t)mdim * n, cudaMemcpyHostToDevice, st));
-    if (exw > 0)
-        FMM_CUDA_TRY(cudaMemcpyAsync(ws.in_excl.p, ex, sizeof(int32_t) * (size_t)exw * n, cudaMemcpyHostToDevice, st));
+    if (!defer) {
+        FMM_CUDA_TRY(cudaMemcpyAsync(ws.in_mp.p, mp, sizeof(double) * (size_t)mdim * n, cudaMemcpyHostToDevice, st));
+        if (exw > 0)
+            FMM_CUDA_TRY(
+                cudaMemcpyAsync(ws.in_excl.p, ex, sizeof(int32_t) * (size_t)exw * n, cudaMemcpyHostToDevice, st));
+    }
     if (damp) FMM_CUDA_TRY(cudaMemcpyAsync(ws.in_damp.p, damp, sizeof(double) * n, cudaMemcpyHostToDevice, st));
     P->n = n;
     P->x = ws.in_coords.as<double>();
@@ -310,6 +366,12 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         FMM_TRY(ws.sel_scratch.ensure(sizeof(double) * (size_t)nt * nf * 2 + sizeof(int64_t) * nt));
         int64_t* d_rows = reinterpret_cast<int64_t*>(ws.sel_scratch.as<double>() + (size_t)nt * nf * 2);
         FMM_CUDA_TRY(cudaMemcpyAsync(d_rows, rows.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, st));
+    }
+    if (ws.copy_join) {  // multipoles and exclusions copied beside the tree build
+        const int cst = ws.copy_join();
+        ws.copy_join = nullptr;
+        FMM_TRY(cst);
+        FMM_CUDA_TRY(cudaStreamWaitEvent(st, ws.copy_ev, 0));
     }
     FMM_TRY(gather_sorted(ws, P, t, st));
     const bool f32_near = md.precision == 1 || md.precision == 2;
@@ -593,7 +655,10 @@ int fmm_field_fmm(int comm, int64_t n, const double* X, int mdim, const double* 
     cudaStream_t st = o.stream;
     const int nf = nT(field_order);
     Particles P;
-    FMM_TRY(upload(ws, n, X, mdim, mp, exw, ex, dt != DAMP_NONE ? dampf : nullptr, nf, &P, st));
+    FMM_TRY(upload(ws, n, X, mdim, mp, exw, ex, dt != DAMP_NONE ? dampf : nullptr, nf, &P, st, true));
+    DeferredInputCopy dc(ws, ws.in_mp.p, mp, sizeof(double) * (size_t)mdim * n, ws.in_excl.p, ex,
+                         exw > 0 ? sizeof(int32_t) * (size_t)exw * n : 0);
+    if (!dc.started()) return FMM_ECUDA;
     OutputPrefault pf(field, sizeof(double) * (size_t)nf * n);
     P.damp_type = dt;
     TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode, 0.0, p};

@@ -1,6 +1,8 @@
 // Internal declarations shared by the translation units of the library.
 #pragma once
 
+#include <functional>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -117,6 +119,12 @@ struct Workspace {
     DevBuf dsmc, partial;
     // second stream (the learned selector's sampled direct sum overlaps the tree phases)
     cudaStream_t aux = nullptr;
+    // host entry points: the multipoles and exclusions are copied on `copy`
+    // by a helper thread while the tree is built; run_fmm waits for
+    // `copy_ev` (after `copy_join`) before it first reads them
+    cudaStream_t copy = nullptr;
+    cudaEvent_t copy_ev = nullptr;
+    std::function<int()> copy_join;
     // ref-mode closed-form tensor tables
     DevBuf term_off, term_abc, term_c;
     int term_order = -1;
