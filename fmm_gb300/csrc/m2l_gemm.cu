@@ -511,9 +511,10 @@ constexpr long long kTcWaitCycles = 4000000000LL;  // about 2 s at 2 GHz
 // Float offset of element (r, k) in a K-major, unswizzled chunk kTcKC wide:
 // core matrices of 8 rows x 4 elements (128 bytes), K-adjacent ones 128 bytes
 // apart (LBO), row groups kTcKC / 4 * 128 bytes apart (SBO).
-__host__ __device__ __forceinline__ int tc_off(int r, int k) {
+__host__ __device__ constexpr int tc_off(int r, int k) {
     return (r >> 3) * (kTcKC * 8) + (k >> 2) * 32 + (r & 7) * 4 + (k & 3);
 }
+static_assert(tc_off(9, 6) == 64 + 32 + 4 + 2, "operand layout: row groups of 8, K groups of 4");
 
 struct TcSmem {
     static constexpr int g_floats = kTcRows * kTcKC;   // one TF32 part of an operator chunk
@@ -607,9 +608,15 @@ __global__ void __launch_bounds__(256) k_group_operator(int ldT, const float* __
     for (int e = threadIdx.x; e < nTq; e += blockDim.x) Tsh[e] = gT[(size_t)g * ldT + e];
     __syncthreads();
     float* out = gop + goff[g];
-    const int kp = nch * kTcKC;
-    for (int e = threadIdx.x; e < nrow * kp; e += blockDim.x) {
-        const int n = e / kp, s = e - n * kp;
+    // consecutive threads write consecutive floats of a (half, chunk) block:
+    // pos inverts tc_off(r, k) = (r/8) 64 + (k/4) 32 + (r%8) 4 + k%4
+    constexpr int BLK = kTcRows * kTcKC;
+    const int nblk = (nrow / kTcRows) * nch;
+    for (int e = threadIdx.x; e < nblk * BLK; e += blockDim.x) {
+        const int blk = e / BLK, pos = e - blk * BLK;
+        const int half = blk / nch, ch = blk - half * nch;
+        const int n = half * kTcRows + (pos >> 6) * 8 + ((pos & 31) >> 2);
+        const int s = ch * kTcKC + ((pos >> 5) & 1) * 4 + (pos & 3);
         float v = 0.0f;
         if (n < nrq && s < nrq) {
             const int cs = dec[s], cf = dec[n];
@@ -619,9 +626,9 @@ __global__ void __launch_bounds__(256) k_group_operator(int ldT, const float* __
         }
         float h, l;
         umma::split_tf32(v, h, l);
-        float* o = out + ((size_t)(n / kTcRows) * nch + s / kTcKC) * 2 * kTcRows * kTcKC + tc_off(n % kTcRows, s % kTcKC);
+        float* o = out + (size_t)blk * 2 * BLK + pos;
         o[0] = h;
-        o[kTcRows * kTcKC] = l;
+        o[BLK] = l;
     }
 }
 
