@@ -59,21 +59,21 @@ __global__ void k_far_targets(int M, const int32_t* __restrict__ off, int32_t* _
 // w'_s = w^_s / h^|s| per node (h the node's half-width).
 // (rows of ld >= nr entries, zero padded)
 template <typename R>
-__global__ void k_scale_weights(int64_t total, int nr, int ld, const double* __restrict__ wred,
-                                const double* __restrict__ h, R* __restrict__ wsc) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t node = e / ld;
-        const int s = (int)(e - node * ld);
-        if (s >= nr) {
-            wsc[e] = (R)0;
-            continue;
-        }
+__global__ void k_scale_weights(int M, int nr, int ld, const double* __restrict__ wred, const double* __restrict__ h,
+                                R* __restrict__ wsc) {
+    // warp per node: lane j holds ih^j (the same sequential product for every
+    // component of order j), components across the lanes
+    const int node = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (node >= M) return;
+    const double ih = 1.0 / h[node];
+    double pw = 1.0;
+    for (int u = 0; u < min(lane, 2 * kMaxP); ++u) pw *= ih;
+    for (int s0 = 0; s0 < ld; s0 += 32) {
+        const int s = s0 + lane;
         int k = 0;
-        while ((k + 1) * (k + 1) <= s) ++k;
-        const double ih = 1.0 / h[node];
-        double sc = 1.0;
-        for (int u = 0; u < k; ++u) sc *= ih;
-        wsc[e] = (R)(wred[node * nr + s] * sc);
+        while ((k + 1) * (k + 1) <= s) ++k;  // order of reduced component s
+        const double sc = __shfl_sync(0xffffffffu, pw, min(k, 31));
+        if (s < ld) wsc[(size_t)node * ld + s] = s < nr ? (R)(wred[(size_t)node * nr + s] * sc) : (R)0;
     }
 }
 
@@ -916,9 +916,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         count_launches(1);
         k_far_targets<<<grid_for(M, 4), 128, 0, st>>>(M, t.far_off, tgt);
         count_launches(1);
-        k_scale_weights<R><<<grid_for((int64_t)M * ldw, 256), 256, 0, st>>>((int64_t)M * ldw, nr, ldw,
-                                                                           ws.wred.as<double>(), t.r,
-                                                                           ws.m2l_wsc.as<R>());
+        k_scale_weights<R><<<grid_for(M, 4), 128, 0, st>>>(M, nr, ldw, ws.wred.as<double>(), t.r, ws.m2l_wsc.as<R>());
         count_launches(1);
         // FP32 node data where the mixed path prepared it
         const float4* chi = (sizeof(R) == 4 && ws.f32node_ok) ? ws.f32node.as<float4>() : nullptr;
