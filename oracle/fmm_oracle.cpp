@@ -7,11 +7,16 @@
 // check and the CPU-baseline leg of the benchmark load it, and only as the
 // checker.  The product library (fmm_gb300) never links or calls it.
 //
-// Parity status: the reference is Fortran and cannot be compiled in the build
-// container (no Fortran compiler), and it ships no tests, golden vectors or
-// fixtures.  This restatement is therefore pinned by analytic identities and
-// by independent high-precision (mpmath) derivatives in tests/, not by
-// reference outputs: "parity unpinned" in the sense of the build rules.
+// Parity status: pinned to the reference's own code.  The reference is
+// Fortran, has no tests or fixtures, and no Fortran compiler exists here; its
+// source statements are instead executed through a mechanical translation
+// (tests/golden/fortran_exec.py) that writes golden fixtures
+// (tests/golden/ref_*.npz).  tests/test_ref_golden.py checks this file against
+// them: the int32 Cnij table and the octree and interaction lists bit for bit,
+// Tn_recursive (orders <= 16), the generated T0..T12 and the damped T0..T6 of
+// all three kinds to 1e-13, and field_direct / field_fmm of five systems
+// (every damping kind, multipole orders 0-2, field orders 1-2, expansion
+// orders 4-8) to 1e-12 relative.
 //
 // Two families of behaviour are selectable per call (OracleOpts):
 //   coef_mode  0 = "ref":   undamped tensors by the reference's closed form
@@ -1094,5 +1099,16 @@ void oracle_tree_get(void* hp, double* center /*3M*/, double* r, double* rmax, i
 }
 
 void oracle_tree_free(void* hp) { delete (TreeHandle*)hp; }
+
+// The Cnij coefficient table for tensors up to order maxo, in the layout of
+// the reference's Cnij(1:2*maxo+3, 0:maxo+1, 0:maxo+1) (column-major;
+// tensors_recursive.F90:64-93): wrap32 = 1 gives the int32 table of the
+// default build, 0 the exact integers.
+void oracle_cnij(int maxo, int wrap32, double* out) {
+    Cnij t = make_cnij(maxo, wrap32 != 0);
+    for (int j = 0; j < t.d1; ++j)
+        for (int i = 0; i < t.d1; ++i)
+            for (int n = 1; n <= t.d0; ++n) out[(size_t)(n - 1) + (size_t)t.d0 * ((size_t)i + (size_t)t.d1 * j)] = t.get(n, i, j);
+}
 
 }  // extern "C"

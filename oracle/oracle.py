@@ -12,7 +12,7 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["field_direct", "field_fmm", "tensors", "radial_g", "tree", "DAMP", "n_components"]
+__all__ = ["field_direct", "field_fmm", "tensors", "radial_g", "tree", "cnij", "DAMP", "n_components"]
 
 DAMP = {"": 0, "AMOEBA": 1, "THOLE": 2, "ERF": 3}
 
@@ -47,6 +47,7 @@ def _load():
         lib.oracle_tree_sizes.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
         lib.oracle_tree_get.argtypes = [ctypes.c_void_p, d, d, d, i32, i32, i32, i32, i32, i32, i32]
         lib.oracle_tree_free.argtypes = [ctypes.c_void_p]
+        lib.oracle_cnij.argtypes = [ctypes.c_int, ctypes.c_int, d]
         _lib = lib
     return _lib
 
@@ -156,3 +157,11 @@ def tree(coordinates, ncrit, theta, centroid="sequential"):
         return out
     finally:
         lib.oracle_tree_free(h)
+
+
+def cnij(maxo, wrap32=True):
+    """The Cnij table Cnij(1:2*maxo+3, 0:maxo+1, 0:maxo+1) of
+    tensors_recursive.F90:64-93, as a Fortran-ordered float64 array."""
+    out = np.zeros((2 * maxo + 3, maxo + 2, maxo + 2), order="F")
+    _load().oracle_cnij(int(maxo), int(bool(wrap32)), _dp(out))
+    return out

@@ -1,0 +1,68 @@
+"""GPU parity against outputs of the reference's own source code.
+
+The fixtures (tests/golden/ref_fields.npz) hold field_direct / field_fmm
+results and octrees computed by executing the reference's Fortran
+statements (see tests/golden/make_ref_golden.py).  The CUDA library in its
+default (reference) mode must reproduce them: relative field error <= 1e-12
+and the octree and interaction lists bit for bit.  Every call goes through
+the C ABI.  The cases include p = 6 and p = 8, where the reference's int32
+Cnij table wraps and its own far field is wrong by 1e-1 to 1e0: the drop-in
+reproduces that result too.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import fmm_gb300
+from helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_fields.npz")
+DAMP_NAMES = {0: "", 1: "AMOEBA", 2: "THOLE", 3: "ERF"}
+CASES = ["water_none", "water_thole", "water_amoeba", "uniform_erf", "uniform_charges"]
+
+
+@pytest.fixture(scope="module")
+def fields():
+    return np.load(GOLD)
+
+
+def _case(fields, name):
+    g = lambda k: fields[name + "_" + k]
+    theta, ncrit, p, f, dcode = g("cfg")
+    damp = DAMP_NAMES[int(dcode)]
+    return dict(X=g("X"), M=g("M"), E=g("E"), d=g("d") if damp else None, theta=float(theta), ncrit=int(ncrit),
+                p=int(p), f=int(f), damp=damp)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_field_direct_matches_reference(fields, name):
+    c = _case(fields, name)
+    G = fmm_gb300.field_direct(0, c["X"], c["M"], c["E"], c["f"], c["damp"], c["d"])
+    cols = slice(1, None) if c["damp"] == "AMOEBA" else slice(None)
+    assert rel_err(G, fields[name + "_direct"], cols) <= 1e-12
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_field_fmm_matches_reference(fields, name):
+    c = _case(fields, name)
+    G = fmm_gb300.field_fmm(0, c["X"], c["M"], c["E"], c["theta"], c["ncrit"], c["p"], c["f"], c["damp"], c["d"])
+    cols = slice(1, None) if c["damp"] == "AMOEBA" else slice(None)
+    assert rel_err(G, fields[name + "_fmm"], cols) <= 1e-12
+
+
+@pytest.mark.parametrize("name", ["water_none", "water_thole"])
+def test_gpu_tree_and_lists_match_reference(fields, name):
+    from test_gpu_parity import _gpu_tree
+    c = _case(fields, name)
+    t = _gpu_tree(c["X"], c["ncrit"], c["theta"], 0)
+    g = lambda k: fields[name + "_tree_" + k]
+    assert np.array_equal(t["center"], g("center"))
+    assert np.array_equal(t["r"], g("r"))
+    assert np.array_equal(t["rmax"], g("rmax"))
+    for k, kk in (("depth", "depth"), ("parent", "parent"), ("is_leaf", "leaf"), ("count", "count")):
+        assert np.array_equal(t[k], g(kk)), k
+    assert np.array_equal(t["far"], g("far"))
+    assert np.array_equal(t["near"], g("near"))
