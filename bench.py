@@ -77,8 +77,9 @@ WORKLOADS = {
 
 def workload_config(arm, system="water", n=3 * N_MOL):
     a = ARMS.get(arm, dict(theta=REF_SETTINGS["theta"], p=REF_SETTINGS["p"]))
+    full = (system == "water" and n == 3 * N_MOL) or (system == "blobs" and n == 2_000_000)
     return {
-        "workload": WORKLOADS[system] if n in (3 * N_MOL, 2_000_000) else WORKLOADS[system] + " (N=%d)" % n,
+        "workload": WORKLOADS[system] if full else WORKLOADS[system] + " (sample of N=%d at the same density)" % n,
         "arm": arm,
         "theta": a["theta"],
         "expansion_order": a["p"],
@@ -175,39 +176,70 @@ def m2l_product_flops_per_pair(q):
     return 2 * (q + 1) ** 4
 
 
-def cpu_sample(n_mol=10_000, threads=None):
-    """Times the oracle (reference semantics) on a sample of the same workload
-    at the same density; returns particles/s and the description."""
+def sample_system(system, n):
+    """A smaller system of the same kind and density as the benchmark's."""
+    from fmm_gb300 import systems
+    if system == "blobs":
+        scale = (n / 2_000_000) ** (1.0 / 3.0)
+        return systems.blobs(n=n, box=600.0 * scale, sigma_range=(5.0 * scale, 30.0 * scale), seed=11)
+    n_mol = n // 3
+    return make_system(seed=11, n_mol=n_mol, box=BOX * (n_mol / N_MOL) ** (1.0 / 3.0))
+
+
+def cpu_sample(n=30_000, threads=None, system="water"):
+    """Times the oracle (the reference's semantics and settings) on a sample of
+    the same kind of system at the same density; returns (particles/s,
+    threads, description).  The rate is that of the sample: FMM work grows
+    about linearly with N, so it is quoted as a rate, not extrapolated."""
     import oracle
-    box = BOX * (n_mol / N_MOL) ** (1.0 / 3.0)
-    s = make_system(seed=11, n_mol=n_mol, box=box)
+    s = sample_system(system, n)
+    n = s["coordinates"].shape[0]
     args = (0, s["coordinates"], s["multipoles"], s["exclusions"])
     nth = threads or os.cpu_count() or 1
     t0 = time.perf_counter()
     oracle.field_fmm(*args, REF_SETTINGS["theta"], NCRIT, REF_SETTINGS["p"], F_ORDER, DAMP, s["damping_factors"],
                      nthreads=nth)
     dt = time.perf_counter() - t0
-    return 3 * n_mol / dt, nth, ("oracle field_fmm with the reference's semantics and settings (int32 Cnij, 1e10 "
-                                 "exclusions, theta 0.5, p 8) on N=%d water-like particles at the benchmark density "
-                                 "(%.1f bohr cube), AMOEBA, f=1, %d OpenMP threads, %.2f s"
-                                 % (3 * n_mol, box, nth, dt))
+    return n / dt, nth, ("C++ restatement of the reference algorithm (oracle/, g++ -O2; the reference is Fortran "
+                         "and has no build here), its semantics and settings (int32 Cnij, 1e10 exclusions, theta "
+                         "0.5, p 8), on a sample of N=%d %s particles at the benchmark density, AMOEBA, f=1, "
+                         "%d thread%s, %.2f s; rate of the sample, not extrapolated to the full N"
+                         % (n, "water-like" if system == "water" else "clustered", nth, "" if nth == 1 else "s", dt))
+
+
+def cpu_baseline_entry(system="water", n=30_000):
+    """All host threads on a 30k sample, plus one serial run (the reference
+    itself is serial) on a 9k sample."""
+    v, nth, desc = cpu_sample(n=n, system=system)
+    v1, _, desc1 = cpu_sample(n=9_000, threads=1, system=system)
+    return {"value": v, "unit": "particles/s", "cores": nth, "kind": "port", "sample": desc,
+            "serial": {"value": v1, "unit": "particles/s", "cores": 1, "sample": desc1}}
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the oracle's restatement of the reference algorithm
+    on the host cores, each step one field_fmm on a bounded sample of the
+    benchmark workload (same kind of system, same density)."""
     if rank != 0:
         return
     vals = []
+    n = 3 * args.ref_sample
     for k in range(args.warmup + args.steps):
-        v, nth, desc = cpu_sample(n_mol=args.ref_sample)
+        v, nth, desc = cpu_sample(n=n, system=args.system)
         if k >= args.warmup:
             vals.append(v)
     value = float(np.mean(vals))
+    v1, _, desc1 = cpu_sample(n=9_000, threads=1, system=args.system)
+    cfg = workload_config("reference-cpu", args.system, n)
+    cfg["sample_of"] = WORKLOADS[args.system]
+    cfg["extrapolated"] = False
     line = {
         "metric": METRIC, "value": value, "unit": "particles/s", "impl": "reference", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * 3 * args.ref_sample / value,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload_config("reference-cpu"),
-        "cpu_baseline": {"value": value, "unit": "particles/s", "cores": nth, "kind": "port", "sample": desc},
+        "config": cfg,
+        "cpu_baseline": {"value": value, "unit": "particles/s", "cores": nth, "kind": "port", "sample": desc,
+                         "serial": {"value": v1, "unit": "particles/s", "cores": 1, "sample": desc1}},
         "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -449,12 +481,13 @@ def main():
     # DRAM bytes per unit from one ncu capture of each kernel on the 100k case
     # (profiles/), scaled to this launch by its units (pairs): the kernels are
     # compute-bound and their traffic grows in proportion to the pairs
-    per_unit = {"k_p2p_f32": (P2P_DRAM_PER_PAIR, p2p_pairs, "profiles/k_p2p_f32_water100k.md"),
-                "k_m2l_tc": (TC_DRAM_PER_PAIR, stats["m2l_pairs"], "profiles/k_m2l_tc_water100k.md")}
-    for k, (b, units, src) in per_unit.items():
+    per_unit = {"k_p2p_f32": (P2P_DRAM_PER_PAIR, p2p_pairs, "near-field pair"),
+                "k_m2l_tc": (TC_DRAM_PER_PAIR, stats["m2l_pairs"], "far pair")}
+    for k, (b, units, unit) in per_unit.items():
         if k in kernels:
             kernels[k]["traffic_bytes"] = b * units
-            kernels[k]["traffic_source"] = src + " (DRAM read+write per unit x units of this launch)"
+            kernels[k]["traffic_source"] = ("DRAM bytes read + written per %s in one ncu capture of this kernel on "
+                                            "the 100k water-like system, times the %ss of this launch" % (unit, unit))
     dom = max(kernels, key=lambda k: kernels[k]["ms"])
     roofline = {"bound": "fp64" if prec == 0 else "fp32", "kernel": dom,
                 "achieved": kernels[dom]["achieved_tflops"], "peak": peak.value, "unit": "TFLOP/s",
@@ -465,37 +498,60 @@ def main():
                 "algorithmic_flops_per_launch": kernels[dom]["algorithmic_flops"],
                 "traffic": kernels[dom].get("traffic_bytes"), "kernels": kernels, "phase_ms": {k: round(v, 3) for k, v in phase.items()}}
 
-    compare = None
-    if args.arm != "fp64" and not args.no_compare:
-        # plain FP64 GPU arm: same workload, fixed rule, FP64 everywhere
-        o64 = arm_options("fp64")
-        o64.stream = stream.cuda_stream
-        step(ARMS["fp64"], o64)
+    def time_arm(settings, o, reps=2):
+        """One untimed and `reps` timed device-resident calls of another arm on
+        the same resident inputs; its accuracy on the same sampled targets."""
+        o.stream = stream.cuda_stream
+        step(settings, o)
         torch.cuda.synchronize()
-        t64 = []
-        for _ in range(2):
+        tt = []
+        for _ in range(reps):
+            flush.fill_(1.0)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            step(ARMS["fp64"], o64)
+            step(settings, o)
             e1.record(stream)
             torch.cuda.synchronize()
-            t64.append(e0.elapsed_time(e1))
-        acc64 = accuracy_of(tF.cpu().numpy().reshape(nf, n).T)
-        v64 = n / (float(np.mean(t64)) * 1e-3)
-        compare = {"arm": "fp64", "value": v64, "unit": "particles/s", "ms_per_step": float(np.mean(t64)),
-                   "accuracy": acc64, "speedup_of_this_arm": value / v64, "settings": ARMS["fp64"]}
+            tt.append(e0.elapsed_time(e1))
+        acc = accuracy_of(tF.cpu().numpy().reshape(nf, n).T)
+        v = n / (float(np.mean(tt)) * 1e-3)
+        return {"value": v, "unit": "particles/s", "ms_per_step": float(np.mean(tt)), "accuracy": acc}
+
+    compare = fixed_mixed = ref_settings = None
+    if args.arm != "fp64" and not args.no_compare:
+        # plain FP64 GPU arm at the same <= 1e-6 accuracy: fixed rule, FP64 everywhere
+        compare = time_arm(ARMS["fp64"], arm_options("fp64"))
+        compare.update({"arm": "fp64", "speedup_of_this_arm": value / compare["value"], "settings": ARMS["fp64"]})
+        if args.arm == "learned":
+            # what the learned selector itself gains: the same mixed-precision
+            # kernels with the fixed acceptance rule at the same accuracy target
+            fixed_mixed = time_arm(ARMS["mixed"], arm_options("mixed"))
+            fixed_mixed.update({"arm": "mixed", "settings": ARMS["mixed"],
+                                "learned_gain": value / fixed_mixed["value"]})
+        # plain FP64 GPU at the reference's own rule and semantics (int32 Cnij,
+        # 1e10 exclusions, theta 0.5, p 8): the same work the CPU arm does
+        from fmm_gb300 import Options
+        rs = dict(theta=REF_SETTINGS["theta"], p=REF_SETTINGS["p"])
+        ref_settings = time_arm(rs, Options())
+        ref_settings.update({"arm": "fp64-reference-settings",
+                             "settings": dict(rs, coef_mode="ref", excl_mode="ref", precision="fp64")})
 
     cpu = None
-    if not args.no_cpu_baseline:
-        v, nth, desc = cpu_sample()
-        cpu = {"value": v, "unit": "particles/s", "cores": nth, "kind": "port", "sample": desc}
+    if not args.no_cpu_baseline and rank == 0:
+        cpu = cpu_baseline_entry(system=args.system)
+        if ref_settings is not None:
+            # same rule, semantics and accuracy on both sides: the GPU's plain
+            # FP64 path against the CPU restatement, both at the reference's settings
+            ref_settings["vs_cpu_all_threads"] = ref_settings["value"] / cpu["value"]
+            ref_settings["vs_cpu_serial"] = ref_settings["value"] / cpu["serial"]["value"]
 
     line = {
         "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.arm == "fp64" else "f32+f64", "data": "synthetic", "config": workload_config(args.arm, args.system, n),
-        "accuracy": accuracy, "e2e": e2e, "roofline": roofline, "plain_fp64": compare, "cpu_baseline": cpu,
+        "accuracy": accuracy, "e2e": e2e, "roofline": roofline, "plain_fp64": compare,
+        "fixed_rule_mixed": fixed_mixed, "plain_fp64_reference_settings": ref_settings, "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
         "tree": {k: stats[k] for k in ("num_nodes", "num_leaves", "max_depth", "m2l_pairs", "m2l_groups",

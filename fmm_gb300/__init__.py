@@ -17,7 +17,7 @@ from . import _lib
 from ._lib import FmmError
 
 __all__ = ["field_direct", "field_fmm", "field_fmm_batched", "field_direct_device", "field_fmm_device", "Options",
-           "last_stats", "n_components", "FmmError", "version", "load_selector"]
+           "last_stats", "n_components", "FmmError", "version", "load_selector", "release_workspace"]
 
 
 def n_components(order):
@@ -234,6 +234,12 @@ def last_stats():
     buf = (ctypes.c_double * len(STAT_NAMES))()
     k = _lib.lib().fmm_last_stats(buf, len(STAT_NAMES))
     return {STAT_NAMES[i]: buf[i] for i in range(k)}
+
+
+def release_workspace():
+    """Frees the device memory the library holds for the calling thread
+    (fmm_release_workspace); the next call allocates again."""
+    _lib.check(_lib.lib().fmm_release_workspace(), "fmm_release_workspace")
 
 
 def version():

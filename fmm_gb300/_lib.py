@@ -48,6 +48,7 @@ EXPORTED = [
     "fmm_field_direct_targets_device",
     "fmm_field_direct_targets_noalloc",
     "fmm_last_stats",
+    "fmm_release_workspace",
     "fmm_debug_tree",
     "fmm_measure_fma_peak",
     "fmm_launch_count",
@@ -100,6 +101,8 @@ def lib():
                                         d, cs, c, d, op]
     L.fmm_field_fmm_batched.restype = c
     L.fmm_last_stats.argtypes = [d, c]
+    L.fmm_release_workspace.argtypes = []
+    L.fmm_release_workspace.restype = c
     L.fmm_measure_fma_peak.argtypes = [c, d]
     L.fmm_launch_count.restype = ctypes.c_int64
     L.fmm_launch_count.argtypes = []

@@ -35,7 +35,7 @@ void DevBuf::release() {
     cap = 0;
 }
 
-Workspace::~Workspace() {
+void Workspace::release_buffers(bool keep_selector) {
     DevBuf* all[] = {&in_coords, &in_mp,     &in_excl,     &in_damp,    &out_field,  &keys_a,     &keys_b,
                      &vals_a,    &vals_b,    &cub_tmp,     &perm,       &pos_of,     &leaf_of,    &node_d,
                      &node_i,    &child,     &level_nodes, &leaves,     &node_key,   &node_val,   &node_key2,
@@ -45,7 +45,14 @@ Workspace::~Workspace() {
                      &term_off,  &term_abc,  &term_c, &f32buf, &wred, &far_ord, &sel_norms, &sel_params, &sel_scratch, &sysbuf,
                      &m2l_tgt, &m2l_keys, &m2l_keys2, &m2l_vals, &m2l_vals2, &m2l_ukeys, &m2l_cnt, &m2l_gstart,
                      &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &m2l_wsplit, &m2l_gop, &m2l_gopoff, &m2l_rowbase, &xlate, &l2pt, &dsmc, &f32node};
-    for (DevBuf* b : all) b->release();
+    for (DevBuf* b : all)
+        if (!(keep_selector && b == &sel_params)) b->release();
+    if (!keep_selector) sel_ready = false;
+    wred_p = term_order = xlate_p = l2pt_p = l2pt_f = -1;
+}
+
+Workspace::~Workspace() {
+    release_buffers(false);
     if (events_ready)
         for (auto& e : ev) cudaEventDestroy(e);
     if (aux) cudaStreamDestroy(aux);
@@ -549,6 +556,13 @@ int fmm_selector_load(const float* params, int64_t count) {
     FMM_CUDA_TRY(cudaDeviceSynchronize());
     ws.sel_ready = true;
     return FMM_OK;
+}
+
+int fmm_release_workspace(void) {
+    Workspace& ws = thread_workspace();
+    // cudaFree waits for the device, so no enqueued work still uses the buffers
+    ws.release_buffers(true);
+    return cudaGetLastError() == cudaSuccess ? FMM_OK : FMM_ECUDA;
 }
 
 int fmm_last_stats(double* out, int len) {

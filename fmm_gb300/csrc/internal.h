@@ -147,6 +147,9 @@ struct Workspace {
     int device = -1;
     int64_t node_cap = 0;
     ~Workspace();
+    // Frees every device buffer (keep_selector: except the loaded selector
+    // network) and forgets the tables cached in them.
+    void release_buffers(bool keep_selector);
 };
 
 Workspace& thread_workspace();

@@ -181,6 +181,21 @@ __global__ void k_excl_static(int64_t n, int64_t ntgt, const int64_t* __restrict
     for (int f = 0; f < NF; ++f) field[(size_t)f * ntgt + ti] += add[f] - sub[f];
 }
 
+// Every exclusion entry of every particle (not only the targets' rows) must be
+// 0 or a 1-based particle index, as the allocating entry points require; a bad
+// entry sets status bit 1 and the call returns FMM_EINVAL.
+__global__ void k_check_excl_static(int64_t n, int exw, const int32_t* __restrict__ excl,
+                                    unsigned long long* status) {
+    const int64_t total = n * (int64_t)exw;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int e = excl[q];
+        if (e < 0 || e > n) {
+            atomicOr(status, 1ull);
+            return;
+        }
+    }
+}
+
 int parse_damp_noalloc(const char* s, int len, int* out) {
     int l = (s && len > 0) ? len : 0;
     while (l > 0 && (s[l - 1] == ' ' || s[l - 1] == '\0')) --l;
@@ -213,7 +228,9 @@ extern "C" int fmm_field_direct_targets_noalloc(int64_t n, const double* d_X, in
     int dt = 0;
     FMM_TRY(parse_damp_noalloc(damp, damp_len, &dt));
     const int m = dim_to_order(mdim);
-    if (n < 1 || m < 0 || exw < 0 || field_order < 0 || ntgt < 1 || !d_targets || !d_X || !d_mp || !d_field)
+    // the same argument checks as the allocating entry points
+    if (n < 1 || n > (int64_t)INT32_MAX - 1 || m < 0 || exw < 0 || field_order < 0 || ntgt < 1 || !d_targets ||
+        !d_X || !d_mp || !d_field)
         return FMM_EINVAL;
     if (m > 2 || field_order > 2) return FMM_ENOTSUP;
     if (dt != DAMP_NONE && !d_damp) return FMM_EINVAL;
@@ -241,6 +258,12 @@ extern "C" int fmm_field_direct_targets_noalloc(int64_t n, const double* d_X, in
     const int64_t chunk = (n + ks - 1) / ks;
     const double* dd = dt != DAMP_NONE ? d_damp : nullptr;
     FMM_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(unsigned long long), st));
+    if (exw > 0) {
+        const int64_t total = n * (int64_t)exw;
+        const unsigned cb = (unsigned)std::min<int64_t>((total + 255) / 256, 4LL * num_sms_noalloc());
+        count_launches(1);
+        k_check_excl_static<<<cb, 256, 0, st>>>(n, exw, d_ex, status);
+    }
     dim3 grid((unsigned)tblocks, (unsigned)ks);
     FMM_MF_SWITCH(m, field_order,
                   (k_direct_static<MM, FF><<<grid, 128, 0, st>>>(n, d_targets, ntgt, d_X, d_mp, dd, dt, chunk,

@@ -18,7 +18,7 @@ module fmm
     implicit none
     private
 
-    public :: field_direct, field_fmm
+    public :: field_direct, field_fmm, release_workspace
 
     integer, parameter :: ip = c_int32_t
     integer, parameter :: rp = c_double
@@ -63,6 +63,10 @@ module fmm
             integer(c_int), value :: is_periodic
             type(c_ptr), value :: box
             type(c_ptr), value :: opts
+        end function
+
+        integer(c_int) function c_release_workspace() bind(C, name="fmm_release_workspace")
+            import :: c_int
         end function
 
         type(c_ptr) function c_strerror(status) bind(C, name="fmm_strerror")
@@ -165,6 +169,15 @@ contains
                          field, dt, dl, dptr, per, bptr, c_null_ptr)
         call report(st, "field_fmm", status)
     end subroutine field_fmm
+
+    ! Frees the device memory the library keeps for this host thread between
+    ! calls (it grows to the largest system seen); call it when the FMM is not
+    ! needed for a while, e.g. at the end of a run.  Not in the reference,
+    ! which frees its tree at the end of every call.
+    subroutine release_workspace(status)
+        integer(ip), intent(out), optional :: status
+        call report(c_release_workspace(), "release_workspace", status)
+    end subroutine release_workspace
 
 end module fmm
 

@@ -137,15 +137,27 @@ int fmm_field_direct_targets_device(int64_t n, const double *d_coordinates, int 
  * call returns FMM_EINVAL without doing any work.  The first call on each
  * device looks up the array's device address (cudaGetSymbolAddress); make that
  * first call before any stream capture.  All calls share the array, so calls
- * whose work overlaps on the GPU (different streams, threads or captured
- * graphs in flight) race and must be serialised by the caller.  The call
- * blocks until its stream has finished (it reads a status word back).
+ * whose work overlaps on the GPU (different streams or threads) race and must
+ * be serialised by the caller.  The call blocks until its stream has finished
+ * (it reads a status word back).  Arguments are validated as by
+ * fmm_field_direct_targets_device: an out-of-range target or an exclusion
+ * entry outside 0..n in any row returns FMM_EINVAL.
  * Supports opts->excl_mode and opts->stream; other options are ignored. */
 #define FMM_NOALLOC_MAX_VALUES 524256
 int fmm_field_direct_targets_noalloc(int64_t n, const double *d_coordinates, int mdim, const double *d_multipoles,
                                      int exw, const int32_t *d_exclusions, int64_t ntgt, const int64_t *d_targets,
                                      int field_order, double *d_field, const char *damp, int damp_len,
                                      const double *d_damping_factors, const fmm_opts *opts);
+
+/* Frees the device memory this library holds for the calling host thread
+ * (no counterpart in the reference, whose module-global tree is freed at the
+ * end of every call by `finalize`, src/fmm.F90:301-309).  The entry points
+ * keep their device buffers between calls, per host thread, growing them to
+ * the largest problem seen (about 9 GB at N = 1M with the learned selector);
+ * a long-running host calls this when it is done with the FMM for a while.
+ * The loaded selector network is kept.  The next call allocates again.
+ * Waits for the device to finish the thread's work first. */
+int fmm_release_workspace(void);
 
 /* Statistics of the last fmm_field_fmm* call on this thread: tree and list
  * sizes and per-phase device times in milliseconds.  `out` receives up to

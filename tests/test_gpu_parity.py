@@ -275,3 +275,15 @@ def test_mixed_precision_close_to_fp64(damp, mf):
     # bound is the FP32 floor of a system of neutral groups of large charges
     # (per-pair rounding ~1e-7, amplified by the cancellation inside groups).
     assert rel_err(F32, F64, slice(1, None)) < 5e-6
+
+
+def test_release_workspace_then_call_again():
+    """fmm_release_workspace frees the thread's device buffers; the next call
+    allocates again and gives the same field."""
+    s = small_system(900, 22.0, seed=7)
+    F1 = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, 5, 1)
+    fmm_gb300.release_workspace()
+    F2 = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, 5, 1)
+    assert rel_err(F2, F1) <= 1e-14
+    fmm_gb300.release_workspace()
+    fmm_gb300.release_workspace()  # releasing an empty workspace is fine
