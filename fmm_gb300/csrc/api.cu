@@ -44,11 +44,13 @@ void Workspace::release_buffers(bool keep_selector) {
                      &sz,        &smc,       &sd,          &fsorted,    &mom,        &loc,        &partial,
                      &term_off,  &term_abc,  &term_c, &f32buf, &wred, &far_ord, &sel_norms, &sel_params, &sel_scratch, &sysbuf,
                      &m2l_tgt, &m2l_keys, &m2l_keys2, &m2l_vals, &m2l_vals2, &m2l_ukeys, &m2l_cnt, &m2l_gstart,
-                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &m2l_wsplit, &m2l_gop, &m2l_gopoff, &m2l_rowbase, &xlate, &l2pt, &dsmc, &f32node};
+                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &m2l_wsplit, &m2l_gop, &m2l_gopoff, &m2l_rowbase, &xlate, &l2pt, &dsmc, &f32node, &lattice};
     for (DevBuf* b : all)
         if (!(keep_selector && b == &sel_params)) b->release();
     if (!keep_selector) sel_ready = false;
     wred_p = term_order = xlate_p = l2pt_p = l2pt_f = -1;
+    node_cap = 0;        // node_d / node_i are gone
+    f32node_ok = false;
 }
 
 Workspace::~Workspace() {
@@ -74,7 +76,7 @@ Workspace& thread_workspace() {
 
 namespace {
 
-constexpr int kNumStats = 16 + kMaxP + 1 + 5;
+constexpr int kNumStats = 16 + kMaxP + 1 + 6;
 struct Stats {
     double v[kNumStats] = {0};
 };
@@ -340,8 +342,52 @@ double sampled_rms(const std::vector<double>& F, const std::vector<double>& R, i
     return std::sqrt(acc / ntgt);
 }
 
+// Periodic boxes (box != null): the 27 images of src/fmm.F90:156-175 in the
+// reference's order (a_x outer, a_z inner), each with its own interaction
+// lists built from (root, root + H a) (fmm.F90:337-343), its near field with
+// the exclusions applied only in the central image (fmm.F90:660-736) and its
+// M2L (fmm.F90:861-878); then the lattice sum beyond the images and the
+// surface term (fmm.F90:884-979), before L2L and L2P.  FP64 and the fixed
+// acceptance rule only.
+int run_periodic(Workspace& ws, const Particles& P, int p, int f, const Modes& md, const TreeParams& tpl, TreeDev& t,
+                 const Box9& box, cudaStream_t st, int* levels) {
+    const int64_t n = P.n;
+    const int nf = nT(f), nq = nT(p);
+    FMM_TRY(ws.fsorted.ensure(sizeof(double) * (size_t)n * nf));
+    FMM_TRY(ws.loc.ensure(sizeof(double) * (size_t)t.num_nodes * nq));
+    FMM_CUDA_TRY(cudaMemsetAsync(ws.fsorted.p, 0, sizeof(double) * (size_t)n * nf, st));
+    FMM_CUDA_TRY(cudaMemsetAsync(ws.loc.p, 0, sizeof(double) * (size_t)t.num_nodes * nq, st));
+    int64_t nfar = 0, nnear = 0, npp = 0;
+    for (int ai = -1; ai <= 1; ++ai)
+        for (int aj = -1; aj <= 1; ++aj)
+            for (int ak = -1; ak <= 1; ++ak) {
+                // displacement = matmul(box_matrix, a) (fmm.F90:355, 662)
+                for (int c = 0; c < 3; ++c)
+                    t.shift[c] = (box.h[c] * ai + box.h[3 + c] * aj) + box.h[6 + c] * ak;
+                t.central = (ai == 0 && aj == 0 && ak == 0) ? 1 : 0;
+                FMM_TRY(build_lists(ws, t, tpl, st));
+                FMM_TRY(launch_p2p_f64(ws, P, t, f, md, st, true));
+                if (t.central) FMM_TRY(launch_excl_correction(ws, P, &t, f, md, ws.fsorted.as<double>(), st));
+                FMM_TRY(launch_m2l_pairwise(ws, t, p, md, true, st));
+                nfar += t.nfar;
+                nnear += t.nnear;
+                npp += t.near_particle_pairs;
+            }
+    t.shift[0] = t.shift[1] = t.shift[2] = 0.0;
+    t.central = 1;
+    int* d_levels = reinterpret_cast<int*>(ws.counters.as<unsigned long long>() + 15);
+    FMM_TRY(launch_periodic_lattice(ws, t, p, f, md, box, ws.fsorted.as<double>(), d_levels, st));
+    FMM_TRY(launch_l2l_l2p(ws, P, t, p, f, false, st));
+    FMM_CUDA_TRY(cudaMemcpyAsync(levels, d_levels, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FMM_CUDA_TRY(cudaStreamSynchronize(st));
+    t.nfar = nfar;
+    t.nnear = nnear;
+    t.near_particle_pairs = npp;
+    return FMM_OK;
+}
+
 int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, int f, const Opts& o,
-            const TreeParams& tp, double* d_field, cudaStream_t st) {
+            const TreeParams& tp, double* d_field, cudaStream_t st, const Box9* box = nullptr) {
     ensure_events(ws);
     ws.product_timed = false;
     ws.m2l_groups = 0;
@@ -417,7 +463,14 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     cudaEventRecord(ws.ev[2], st);
     bool fallback = false;
     double check_rms = -1.0;
-    for (int attempt = 0; attempt < 2; ++attempt) {
+    int lattice_levels = 0;
+    if (box) {
+        FMM_TRY(run_periodic(ws, P, p, f, md, tpl, t, *box, st, &lattice_levels));
+        for (int k = 3; k <= 5; ++k) cudaEventRecord(ws.ev[k], st);
+        cudaEventRecord(ws.ev[7], st);
+        FMM_TRY(scatter_field(ws, t, P.n, nf, d_field, st));
+    }
+    for (int attempt = 0; attempt < 2 && !box; ++attempt) {
         FMM_TRY(build_lists(ws, t, tpl, st));
         if (learned && attempt == 0) {
             // FP64 direct sums at the sampled particles (the check of the
@@ -519,6 +572,7 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     s.v[16 + kMaxP + 3] = (double)ws.m2l_groups;
     s.v[16 + kMaxP + 4] = (double)ws.list_candidates;
     s.v[16 + kMaxP + 5] = (double)ws.list_evals;
+    s.v[16 + kMaxP + 6] = (double)lattice_levels;
     g_stats = s;
     return FMM_OK;
 }
@@ -654,15 +708,20 @@ int fmm_field_fmm(int comm, int64_t n, const double* X, int mdim, const double* 
                   double theta, int ncrit, int p, int field_order, double* field, const char* damp, int damp_len,
                   const double* dampf, int is_periodic, const double* box, const fmm_opts* opts) {
     (void)comm;
-    (void)box;
     int dt = 0;
     FMM_TRY(parse_damp(damp, damp_len, &dt));
     FMM_TRY(check_common(n, mdim, exw, field_order, dt, dampf));
     FMM_TRY(check_exclusions_host(n, exw, ex));
     Opts o;
     FMM_TRY(parse_opts(opts, &o));
-    if (is_periodic) return FMM_ENOTSUP;
     if (ncrit < 1 || p < 0 || !(theta > 0.0)) return FMM_EINVAL;
+    Box9 hbox{};
+    if (is_periodic) {
+        // periodic boxes: FP64, fixed rule; the reference stops when N <= ncrit (fmm.F90:1382)
+        if (!box || n <= ncrit) return FMM_EINVAL;
+        if (o.precision != 0 || o.selector != 0) return FMM_ENOTSUP;
+        for (int k = 0; k < 9; ++k) hbox.h[k] = box[k];
+    }
     if (n <= ncrit) return fmm_field_direct(comm, n, X, mdim, mp, exw, ex, field_order, field, damp, damp_len, dampf, opts);
     if (p > kMaxP) return FMM_ENOTSUP;
     Workspace& ws = thread_workspace();
@@ -680,7 +739,8 @@ int fmm_field_fmm(int comm, int64_t n, const double* X, int mdim, const double* 
         host_centroid_sequential(X, n, tp.host_centroid);
         tp.have_host_centroid = 1;
     }
-    FMM_TRY(run_fmm(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st));
+    FMM_TRY(run_fmm(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st,
+                    is_periodic ? &hbox : nullptr));
     pf.join();
     FMM_CUDA_TRY(cudaMemcpyAsync(field, ws.out_field.p, sizeof(double) * (size_t)nf * n, cudaMemcpyDeviceToHost, st));
     FMM_CUDA_TRY(cudaStreamSynchronize(st));

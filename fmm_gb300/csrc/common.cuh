@@ -60,6 +60,31 @@ inline int dim_to_order(int dim) {
     return -1;
 }
 
+#ifdef __CUDACC__
+// NORM2 of a 3-vector as the scaled sum of squares gfortran expands it to,
+// in a fixed sequence of correctly rounded operations (the reference's tie
+// decisions depend on its last bit, src/fmm.F90:358-364).
+__device__ __forceinline__ double norm2_3(double a0, double a1, double a2) {
+    double scale = 0.0, ssq = 1.0;
+    const double v[3] = {a0, a1, a2};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (v[i] != 0.0) {
+            const double ax = fabs(v[i]);
+            if (scale < ax) {
+                const double t = __ddiv_rn(scale, ax);
+                ssq = __dadd_rn(1.0, __dmul_rn(__dmul_rn(ssq, t), t));
+                scale = ax;
+            } else {
+                const double t = __ddiv_rn(ax, scale);
+                ssq = __dadd_rn(ssq, __dmul_rn(t, t));
+            }
+        }
+    }
+    return __dmul_rn(scale, __dsqrt_rn(ssq));
+}
+#endif
+
 #define FMM_CUDA_TRY(expr)                         \
     do {                                           \
         cudaError_t e_ = (expr);                   \

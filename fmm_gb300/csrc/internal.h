@@ -54,6 +54,15 @@ struct TreeDev {
     int32_t *far_off = nullptr, *far_src = nullptr;
     uint8_t* far_ord = nullptr;  // expansion order of each far pair
     int32_t *near_off = nullptr, *near_src = nullptr;
+    // periodic boxes: the lists in use are those of the image whose source
+    // cells are displaced by `shift`; `central` is 0 for the 26 other images
+    double shift[3] = {0.0, 0.0, 0.0};
+    int central = 1;
+};
+
+// A 3x3 box matrix, column-major (the reference's box_matrix(3,3)).
+struct Box9 {
+    double h[9];
 };
 
 struct Workspace;
@@ -114,6 +123,7 @@ struct Workspace {
     DevBuf fsorted;
     // expansions
     DevBuf mom, loc, wred;
+    DevBuf lattice;  // periodic boxes (level multipoles and contributions), QM/MM classification scratch
     int wred_p = -1;  // order of the reduced weights in wred computed from this call's moments (-1: none)
     // direct sum: scaled multipoles and partial sums
     DevBuf dsmc, partial;
@@ -189,11 +199,21 @@ int launch_direct_scale_f32(Workspace& ws, const Particles& P, const TreeDev& t,
 
 // FMM phases (near.cu / expansions.cu)
 int gather_sorted(Workspace& ws, const Particles& P, const TreeDev& t, cudaStream_t st);
+// image: the lists are a periodic image's (t.shift, t.central) and the near
+// field is added to ws.fsorted instead of written.
 int launch_p2p_f64(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, const Modes& md,
-                   cudaStream_t st);
+                   cudaStream_t st, bool image = false);
 // df: P2M sums in double-float (FP32 pipe) instead of FP64 (mixed path)
 int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, cudaStream_t st, bool df = false);
 int launch_m2l(Workspace& ws, const TreeDev& t, int p, const Modes& md, cudaStream_t st);
+// M2L pair by pair on the CUDA cores (FP64), ref or exact tensors, honouring
+// t.shift; accumulate adds into the local expansions instead of writing them.
+int launch_m2l_pairwise(Workspace& ws, const TreeDev& t, int p, const Modes& md, bool accumulate, cudaStream_t st);
+// Periodic boxes: lattice sum beyond the 27 images into the root's local
+// expansion and the surface (dipole) term into the sorted field d_fs;
+// *d_levels receives the number of lattice levels used.
+int launch_periodic_lattice(Workspace& ws, const TreeDev& t, int p, int f, const Modes& md, const Box9& H,
+                            double* d_fs, int* d_levels, cudaStream_t st);
 int launch_m2l_reduced(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaStream_t st);
 int launch_m2l_grouped(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaStream_t st);
 int launch_reduce_moments(Workspace& ws, const TreeDev& t, int p, cudaStream_t st);

@@ -62,7 +62,10 @@ __global__ void k_gather(int64_t n, int dim, const uint32_t* __restrict__ perm, 
 // when a chunk has g <= 16 targets (g rounded up to a power of two), the warp
 // splits into 32/g groups that walk disjoint subsets of the sources, and the
 // groups are summed with shuffles at the end, so few lanes idle.
-template <int M, int F>
+// IMG: the lists are those of a periodic image (t.shift, t.central): sources
+// sit at x_j + shift, the self pair counts unless the image is the central
+// one, and the result is added to fs (src/fmm.F90:704-736).
+template <int M, int F, bool IMG>
 __global__ void __launch_bounds__(128) k_p2p_f64(const TreeDev t, const double* __restrict__ sx,
                                                  const double* __restrict__ sy, const double* __restrict__ sz,
                                                  const double* __restrict__ sd, const double* __restrict__ smc,
@@ -91,11 +94,15 @@ __global__ void __launch_bounds__(128) k_p2p_f64(const TreeDev t, const double* 
                 const int j = t.near_src[q];
                 const int js = t.start[j], je = js + t.count[j];
                 for (int k = js + grp; k < je; k += ngr) {
-                    if (k == tgt) continue;
+                    if (k == tgt && (!IMG || t.central)) continue;
                     double mc[NM];
 #pragma unroll
                     for (int s = 0; s < NM; ++s) mc[s] = smc[(size_t)s * n + k];
-                    pair_field<M, F, double>(xt - sx[k], yt - sy[k], zt - sz[k], dt * sd[k], damp, mc, acc);
+                    if (IMG)
+                        pair_field<M, F, double>(xt - (sx[k] + t.shift[0]), yt - (sy[k] + t.shift[1]),
+                                                 zt - (sz[k] + t.shift[2]), dt * sd[k], damp, mc, acc);
+                    else
+                        pair_field<M, F, double>(xt - sx[k], yt - sy[k], zt - sz[k], dt * sd[k], damp, mc, acc);
                 }
             }
         }
@@ -105,7 +112,12 @@ __global__ void __launch_bounds__(128) k_p2p_f64(const TreeDev t, const double* 
         }
         if (grp == 0 && valid) {
 #pragma unroll
-            for (int f = 0; f < NF; ++f) fs[(size_t)f * n + tgt] = acc[f];
+            for (int f = 0; f < NF; ++f) {
+                if (IMG)
+                    fs[(size_t)f * n + tgt] += acc[f];
+                else
+                    fs[(size_t)f * n + tgt] = acc[f];
+            }
         }
     }
 }
@@ -355,7 +367,7 @@ int gather_sorted(Workspace& ws, const Particles& P, const TreeDev& t, cudaStrea
 }
 
 int launch_p2p_f64(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, const Modes& md,
-                   cudaStream_t st) {
+                   cudaStream_t st, bool image) {
     (void)md;
     const int m = dim_to_order(P.dim);
     if (!near_orders_supported(m, field_order)) return FMM_ENOTSUP;
@@ -363,11 +375,19 @@ int launch_p2p_f64(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
     const int nf = nT(field_order);
     FMM_TRY(ws.fsorted.ensure(sizeof(double) * (size_t)n * nf));
     const unsigned blocks = grid_for((int64_t)t.num_leaves * 32, 128);
-    FMM_MF_SWITCH(m, field_order,
-                  (k_p2p_f64<MM, FF><<<blocks, 128, 0, st>>>(t, ws.sx.as<double>(), ws.sy.as<double>(),
-                                                              ws.sz.as<double>(), ws.sd.as<double>(),
-                                                              ws.smc.as<double>(), n, P.damp_type,
-                                                              ws.fsorted.as<double>())));
+    if (image) {
+        FMM_MF_SWITCH(m, field_order,
+                      (k_p2p_f64<MM, FF, true><<<blocks, 128, 0, st>>>(t, ws.sx.as<double>(), ws.sy.as<double>(),
+                                                                       ws.sz.as<double>(), ws.sd.as<double>(),
+                                                                       ws.smc.as<double>(), n, P.damp_type,
+                                                                       ws.fsorted.as<double>())));
+    } else {
+        FMM_MF_SWITCH(m, field_order,
+                      (k_p2p_f64<MM, FF, false><<<blocks, 128, 0, st>>>(t, ws.sx.as<double>(), ws.sy.as<double>(),
+                                                                        ws.sz.as<double>(), ws.sd.as<double>(),
+                                                                        ws.smc.as<double>(), n, P.damp_type,
+                                                                        ws.fsorted.as<double>())));
+    }
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }

@@ -41,25 +41,6 @@ namespace {
 
 constexpr int kLanes = 1024;
 
-__device__ __forceinline__ double norm2_3(double a0, double a1, double a2) {
-    double scale = 0.0, ssq = 1.0;
-    const double v[3] = {a0, a1, a2};
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        if (v[i] != 0.0) {
-            const double ax = fabs(v[i]);
-            if (scale < ax) {
-                const double t = __ddiv_rn(scale, ax);
-                ssq = __dadd_rn(1.0, __dmul_rn(__dmul_rn(ssq, t), t));
-                scale = ax;
-            } else {
-                const double t = __ddiv_rn(ax, scale);
-                ssq = __dadd_rn(ssq, __dmul_rn(t, t));
-            }
-        }
-    }
-    return __dmul_rn(scale, __dsqrt_rn(ssq));
-}
 
 // scalars layout: [0..2] centre, [3] r, [4] rmax, [5] max |x - c| (as bits)
 __global__ void k_centroid_lanes(const double* __restrict__ X, int64_t n, double* __restrict__ lanes) {
@@ -382,9 +363,11 @@ __global__ void k_list_iter(const int2* __restrict__ in, int nin, int2* __restri
     if (!skip) {
         i = in[q].x;
         j = in[q].y;
-        const double dx = __dsub_rn(t.cx[i], __dadd_rn(t.cx[j], 0.0));
-        const double dy = __dsub_rn(t.cy[i], __dadd_rn(t.cy[j], 0.0));
-        const double dz = __dsub_rn(t.cz[i], __dadd_rn(t.cz[j], 0.0));
+        // delta = c_i - (c_j + displacement) (fmm.F90:357-358); the
+        // displacement is that of the periodic image (0 without one)
+        const double dx = __dsub_rn(t.cx[i], __dadd_rn(t.cx[j], t.shift[0]));
+        const double dy = __dsub_rn(t.cy[i], __dadd_rn(t.cy[j], t.shift[1]));
+        const double dz = __dsub_rn(t.cz[i], __dadd_rn(t.cz[j], t.shift[2]));
         const double r = norm2_3(dx, dy, dz);
         ri = t.rmax[i];
         rj = t.rmax[j];

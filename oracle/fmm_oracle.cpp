@@ -72,6 +72,12 @@ enum { DAMP_NONE = 0, DAMP_AMOEBA = 1, DAMP_THOLE = 2, DAMP_ERF = 3 };
 enum { OK = 0, E_INVAL = -1, E_NOTSUP = -2, E_DEPTH = -5 };
 
 inline int nT(int k) { return (k + 1) * (k + 2) * (k + 3) / 6; }
+// order of the packed component c (nT(order - 1) <= c < nT(order))
+inline int order_of(int c) {
+    int k = 0;
+    while (nT(k) <= c) ++k;
+    return k;
+}
 
 // Packed alphabetical index, 0-based (fmm.F90:80-89 xyz2idx, which is 1-based).
 inline int pidx(int x, int y, int z) {
@@ -605,16 +611,18 @@ double damping_range(int damp, double a, int nmax, double eps) {
     return last_bad * std::pow(1e8, 1.0 / 4000.0);
 }
 
-// interact_fmm (fmm.F90:352-385), non-periodic.  With rdamp > 0 a pair that
-// passes the reference test is still refused when its closest possible
+// interact_fmm (fmm.F90:352-385): the source cell is displaced by g_disp
+// (the periodic image's displacement, 0 otherwise).  With rdamp > 0 a pair
+// that passes the reference test is still refused when its closest possible
 // particle distance is inside the damping range.
 double g_rdamp = 0.0;
+double g_disp[3] = {0.0, 0.0, 0.0};
 void interact(Tree& t, int i, int j, double theta) {
     const Node& a = t.nd[i];
     const Node& b = t.nd[j];
-    double dx = a.c[0] - (b.c[0] + 0.0);
-    double dy = a.c[1] - (b.c[1] + 0.0);
-    double dz = a.c[2] - (b.c[2] + 0.0);
+    double dx = a.c[0] - (b.c[0] + g_disp[0]);
+    double dy = a.c[1] - (b.c[1] + g_disp[1]);
+    double dz = a.c[2] - (b.c[2] + g_disp[2]);
     double r = norm2_3(dx, dy, dz);
     bool accept = r * theta > a.rmax + b.rmax;
     if (accept && g_rdamp > 0.0) accept = (r - 1.7320508075688772 * (a.r + b.r)) >= g_rdamp;
@@ -631,8 +639,9 @@ void interact(Tree& t, int i, int j, double theta) {
     }
 }
 
-void build_lists(Tree& t, double theta, double rdamp = 0.0) {
+void build_lists(Tree& t, double theta, double rdamp = 0.0, const double* disp = nullptr) {
     g_rdamp = rdamp;
+    for (int c = 0; c < 3; ++c) g_disp[c] = disp ? disp[c] : 0.0;
     size_t M = t.nd.size();
     t.far.assign(M, {});
     t.nearl.assign(M, {});
@@ -716,33 +725,13 @@ void direct_sum(const Problem& P, const Ctx& ctx, double* field, int nthreads) {
     }
 }
 
-int run_fmm(const Problem& P, double theta, int ncrit, int p, const Ctx& ctx0, double* field, int nthreads) {
-    Ctx ctx = ctx0;
-    int64_t n = P.n;
-    int nf = nT(P.pf);
-    int pm = dim_to_order(P.dim);
-    Tree t;
-    int st = build_tree(P.X, n, ncrit, ctx.centroid_mode, t);
-    if (st) return st;
-    double rdamp = 0.0;
-    if (ctx.mac_mode == 1 && P.damp != DAMP_NONE) {
-        double dmin = 1e300;
-        for (int64_t q = 0; q < n; ++q) dmin = std::min(dmin, P.dampf[q]);
-        rdamp = damping_range(P.damp, dmin * dmin, pm + P.pf, 0.1 * ctx.target);
-    }
-    build_lists(t, theta, rdamp);
-    int M = (int)t.nd.size();
-    int ms = nT(p);
-    // leaf id of every particle
-    std::vector<int> leaf_of(n, -1);
-    std::vector<int> term;
-    for (int d = 0; d < M; ++d) {
-        const Node& nd = t.nd[t.dfs[d]];
-        if (!nd.terminal) continue;
-        term.push_back(d);
-        for (int q = 0; q < nd.nleaf; ++q) leaf_of[nd.leaf[q]] = d;
-    }
-    // --- multipole_expansion (fmm.F90:474-546)
+// multipole_expansion (fmm.F90:474-546): P2M of every leaf
+// (shift_multipole_vec, :437-472) and each leaf's moments translated straight
+// into every ancestor (multipole_accumulate, :387-435); raw Cartesian moments,
+// column-major (M, nT(p)).
+std::vector<double> multipole_expansion(const Problem& P, const Tree& t, int p, const std::vector<int>& term) {
+    const int64_t n = P.n;
+    const int M = (int)t.nd.size(), ms = nT(p), pm = dim_to_order(P.dim);
     std::vector<double> cm((size_t)M * ms, 0.0);  // (M, ms) column-major
     for (int d : term) {
         const Node& nd = t.nd[t.dfs[d]];
@@ -808,99 +797,15 @@ int run_fmm(const Problem& P, double theta, int ncrit, int p, const Ctx& ctx0, d
         }
         for (int q = (int)anc.size() - 1; q >= 0; --q) m2m_kernel(d, anc[q]);
     }
-    // --- particle_fields (fmm.F90:623-747)
-    {
-        ctx.ensure_cnij(pm + P.pf);
-#pragma omp parallel num_threads(nthreads)
-        {
-            std::vector<double> x, y, z, a, Mb, Tb, F(nf);
-#pragma omp for schedule(dynamic, 4)
-            for (size_t ti = 0; ti < term.size(); ++ti) {
-                int d = term[ti];
-                const Node& ndi = t.nd[t.dfs[d]];
-                for (int q = 0; q < ndi.nleaf; ++q) {
-                    int64_t i = ndi.leaf[q];
-                    for (int dj : t.nearl[d]) {
-                        const Node& ndj = t.nd[t.dfs[dj]];
-                        int nl = ndj.nleaf;
-                        x.resize(nl);
-                        y.resize(nl);
-                        z.resize(nl);
-                        a.resize(nl);
-                        std::vector<int> src;
-                        src.reserve(nl);
-                        for (int w = 0; w < nl; ++w) {
-                            int64_t j = ndj.leaf[w];
-                            if (ctx.excl_mode == 1 && (j == i || is_excluded(P, i, j))) continue;
-                            size_t s = src.size();
-                            x[s] = P.X[i] - (P.X[j] + 0.0);
-                            y[s] = P.X[n + i] - (P.X[n + j] + 0.0);
-                            z[s] = P.X[2 * n + i] - (P.X[2 * n + j] + 0.0);
-                            if (ctx.excl_mode == 0 && is_excluded(P, i, j)) x[s] = y[s] = z[s] = 1e10;
-                            if (P.damp != DAMP_NONE) a[s] = P.dampf[i] * P.dampf[j];
-                            src.push_back((int)j);
-                        }
-                        int ns = (int)src.size();
-                        Mb.resize((size_t)ns * P.dim);
-                        for (int c = 0; c < P.dim; ++c)
-                            for (int s = 0; s < ns; ++s) Mb[(size_t)c * ns + s] = P.mp[(size_t)c * n + src[s]];
-                        multipole_field(ns, Mb.data(), P.dim, x.data(), y.data(), z.data(), P.pf, P.damp, a.data(), ctx, F.data(), Tb);
-                        for (int c = 0; c < nf; ++c) field[(size_t)c * n + i] = field[(size_t)c * n + i] + F[c];
-                    }
-                    if (ctx.excl_mode == 1) {
-                        // far-field exclusion correction: excluded partners whose
-                        // leaf is not a near leaf were counted through M2L; take
-                        // their undamped pair field out again.
-                        for (int w = 0; w < P.exw; ++w) {
-                            int e = P.ex[(size_t)w * n + i];
-                            if (e == 0 || e - 1 == i) continue;
-                            bool dup = false;
-                            for (int w2 = 0; w2 < w; ++w2)
-                                if (P.ex[(size_t)w2 * n + i] == e) dup = true;
-                            if (dup) continue;
-                            int lj = leaf_of[e - 1];
-                            const auto& nl = t.nearl[d];
-                            if (std::find(nl.begin(), nl.end(), lj) != nl.end()) continue;
-                            int64_t j = e - 1;
-                            double xx = P.X[i] - P.X[j], yy = P.X[n + i] - P.X[n + j], zz = P.X[2 * n + i] - P.X[2 * n + j];
-                            Mb.resize(P.dim);
-                            for (int c = 0; c < P.dim; ++c) Mb[c] = P.mp[(size_t)c * n + j];
-                            multipole_field(1, Mb.data(), P.dim, &xx, &yy, &zz, P.pf, DAMP_NONE, nullptr, ctx, F.data(), Tb);
-                            for (int c = 0; c < nf; ++c) field[(size_t)c * n + i] = field[(size_t)c * n + i] - F[c];
-                        }
-                    }
-                }
-            }
-        }
-    }
-    // --- multipole_to_local (fmm.F90:826-882)
-    std::vector<double> loc((size_t)M * ms, 0.0);
-    {
-        ctx.ensure_cnij(2 * p);
-#pragma omp parallel num_threads(nthreads)
-        {
-            std::vector<double> x, y, z, Mb, Tb, F(ms);
-#pragma omp for schedule(dynamic, 1)
-            for (int d = 0; d < M; ++d) {
-                const auto& fl = t.far[d];
-                int nl = (int)fl.size();
-                const Node& ndi = t.nd[t.dfs[d]];
-                x.resize(nl);
-                y.resize(nl);
-                z.resize(nl);
-                Mb.resize((size_t)nl * ms);
-                for (int q = 0; q < nl; ++q) {
-                    const Node& ndj = t.nd[t.dfs[fl[q]]];
-                    x[q] = ndi.c[0] - (ndj.c[0] + 0.0);
-                    y[q] = ndi.c[1] - (ndj.c[1] + 0.0);
-                    z[q] = ndi.c[2] - (ndj.c[2] + 0.0);
-                    for (int c = 0; c < ms; ++c) Mb[(size_t)c * nl + q] = cm[(size_t)c * M + fl[q]];
-                }
-                multipole_field(nl, Mb.data(), ms, x.data(), y.data(), z.data(), p, DAMP_NONE, nullptr, ctx, F.data(), Tb);
-                for (int c = 0; c < ms; ++c) loc[(size_t)c * M + d] = loc[(size_t)c * M + d] + F[c];
-            }
-        }
-    }
+    return cm;
+}
+
+// local_to_local (fmm.F90:981-1044), depth by depth, then local_to_particle
+// (fmm.F90:1046-1132) into field (n x nT(P.pf), accumulated).
+void local_to_local_and_particle(const Problem& P, const Tree& t, int p, const std::vector<int>& term,
+                                 std::vector<double>& loc, double* field, int nthreads) {
+    const int64_t n = P.n;
+    const int M = (int)t.nd.size();
     // --- local_to_local (fmm.F90:981-1044), depth by depth
     for (int depth = 2; depth <= t.max_depth; ++depth) {
         for (int d = 0; d < M; ++d) {
@@ -956,6 +861,266 @@ int run_fmm(const Problem& P, double theta, int ncrit, int p, const Ctx& ctx0, d
                         }
         }
     }
+}
+
+// NORM2 of a vector with the scaled sum of squares.
+double norm2_n(const double* v, int len) {
+    double scale = 0.0, ssq = 1.0;
+    for (int i = 0; i < len; ++i) {
+        if (v[i] != 0.0) {
+            double ax = std::fabs(v[i]);
+            if (scale < ax) {
+                double t = scale / ax;
+                ssq = 1.0 + (ssq * t) * t;
+                scale = ax;
+            } else {
+                double t = ax / scale;
+                ssq = ssq + t * t;
+            }
+        }
+    }
+    return scale * std::sqrt(ssq);
+}
+
+// displacement = matmul(box, a) for an integer-valued vector a (fmm.F90:355)
+void box_times(const double* box, const double* a, double* out) {
+    for (int i = 0; i < 3; ++i) out[i] = (box[i] * a[0] + box[3 + i] * a[1]) + box[6 + i] * a[2];
+}
+
+// lattice levels used by the last periodic call (diagnostics)
+int g_lattice_levels = 0;
+
+// periodic_sum (fmm.F90:884-952): the lattice beyond the 27 images, in 3x3x3
+// supercells, into the root's local expansion; then dipole_correction
+// (fmm.F90:954-979) on the field.  In exact mode the level's tensors are
+// evaluated at R 2^-k (k ~ level log2 3; scaling by a power of two is exact)
+// with the moments and the result rescaled to match, so orders up to 2p do
+// not underflow at the far levels; ref mode is the reference's arithmetic.
+void periodic_sum_and_surface(const Problem& P, const Tree& t, int p, Ctx& ctx, std::vector<double>& cm,
+                              std::vector<double>& loc, const double* box, double* field) {
+    const int64_t n = P.n;
+    const int M = (int)t.nd.size(), ms = nT(p);
+    const int root = 0;
+    cm[(size_t)0 * M + root] = 0.0;  // the reference forces charge neutrality
+    const int K = 26 * 27;
+    std::vector<double> S(ms), scaled(ms), contrib(ms), Mb((size_t)K * ms), x(K), y(K), z(K), Tb;
+    for (int c = 0; c < ms; ++c) S[c] = scaled[c] = cm[(size_t)c * M + root];
+    ctx.ensure_cnij(2 * p);
+    const bool ref = ctx.coef_mode == 0;
+    g_lattice_levels = 0;
+    for (int level = 1; level <= 50; ++level) {
+        int k = 0;
+        for (int ai = -1; ai <= 1; ++ai)
+            for (int aj = -1; aj <= 1; ++aj)
+                for (int ak = -1; ak <= 1; ++ak) {
+                    if (ai == 0 && aj == 0 && ak == 0) continue;
+                    const double p3 = ipow(3.0, level), p3m = ipow(3.0, level - 1);
+                    const double aijk[3] = {ai * p3, aj * p3, ak * p3};
+                    double da[3], del[3];
+                    box_times(box, aijk, da);
+                    for (int c = 0; c < 3; ++c) del[c] = da[c] / 3.0;
+                    // multipole_accumulate_kernel(d_aijk / 3, S, scaled) (fmm.F90:387-416)
+                    for (int so = 0; so <= p; ++so)
+                        for (int to = so; to <= p; ++to)
+                            for (int sx = so; sx >= 0; --sx)
+                                for (int sy = so; sy >= 0; --sy)
+                                    for (int sz = so; sz >= 0; --sz) {
+                                        if (sx + sy + sz != so) continue;
+                                        int si = pidx(sx, sy, sz);
+                                        for (int tx = to; tx >= sx; --tx)
+                                            for (int ty = to; ty >= sy; --ty)
+                                                for (int tz = to; tz >= sz; --tz) {
+                                                    if (tx + ty + tz != to) continue;
+                                                    int ti = pidx(tx, ty, tz);
+                                                    double symfac = (binom(tx, sx) * binom(ty, sy)) * binom(tz, sz);
+                                                    double mono = (ipow(del[0], tx - sx) * ipow(del[1], ty - sy)) *
+                                                                  ipow(del[2], tz - sz);
+                                                    scaled[ti] = scaled[ti] + (symfac * mono) * S[si];
+                                                }
+                                    }
+                    for (int bi = -1; bi <= 1; ++bi)
+                        for (int bj = -1; bj <= 1; ++bj)
+                            for (int bk = -1; bk <= 1; ++bk) {
+                                const double bijk[3] = {bi * p3m, bj * p3m, bk * p3m};
+                                double db[3];
+                                box_times(box, bijk, db);
+                                x[k] = da[0] + db[0];
+                                y[k] = da[1] + db[1];
+                                z[k] = da[2] + db[2];
+                                ++k;
+                            }
+                }
+        const int ksc = ref ? 0 : (int)std::floor(level * 1.5849625007211563);
+        for (int c = 0; c < ms; ++c)
+            for (int q = 0; q < K; ++q) Mb[(size_t)c * K + q] = std::ldexp(S[c], -ksc * order_of(c));
+        for (int q = 0; q < K; ++q) {
+            x[q] = std::ldexp(x[q], -ksc);
+            y[q] = std::ldexp(y[q], -ksc);
+            z[q] = std::ldexp(z[q], -ksc);
+        }
+        multipole_field(K, Mb.data(), ms, x.data(), y.data(), z.data(), p, DAMP_NONE, nullptr, ctx, contrib.data(), Tb);
+        for (int c = 0; c < ms; ++c) contrib[c] = std::ldexp(contrib[c], -ksc * (order_of(c) + 1));
+        for (int c = 0; c < ms; ++c) loc[(size_t)c * M + root] = loc[(size_t)c * M + root] + contrib[c];
+        S = scaled;
+        g_lattice_levels = level;
+        if (norm2_n(contrib.data() + 1, ms - 1) < 1.0e-8) break;
+    }
+    // --- dipole_correction (fmm.F90:954-979)
+    auto h = [&](int i, int j) { return box[(j - 1) * 3 + (i - 1)]; };
+    const double vol =
+        ref ? h(1, 1) * (h(2, 2) * h(3, 3) - h(2, 3) * h(3, 2)) - h(1, 2) * (h(2, 1) * h(3, 3) - h(2, 3) * h(3, 1)) +
+                  h(1, 3) * (h(1, 2) * h(3, 2) - h(2, 2) * h(3, 1))
+            : h(1, 1) * (h(2, 2) * h(3, 3) - h(2, 3) * h(3, 2)) - h(1, 2) * (h(2, 1) * h(3, 3) - h(2, 3) * h(3, 1)) +
+                  h(1, 3) * (h(2, 1) * h(3, 2) - h(2, 2) * h(3, 1));
+    const double pi = ref ? 3.14159265359 : M_PI;
+    const double dip[3] = {cm[(size_t)1 * M + root], cm[(size_t)2 * M + root], cm[(size_t)3 * M + root]};
+    const double qtr = (cm[(size_t)4 * M + root] + cm[(size_t)7 * M + root]) + cm[(size_t)9 * M + root];
+    for (int64_t i = 0; i < n; ++i) {
+        const double dot = (dip[0] * P.X[i] + dip[1] * P.X[n + i]) + dip[2] * P.X[2 * n + i];
+        field[i] = (field[i] + 4.0 * pi * dot / (3.0 * vol)) + 2.0 * pi * qtr / (3.0 * vol);
+    }
+    if (P.pf >= 1)
+        for (int64_t i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c)
+                field[(size_t)(1 + c) * n + i] = field[(size_t)(1 + c) * n + i] + 4.0 * pi * dip[c] / (3.0 * vol);
+}
+
+int run_fmm(const Problem& P, double theta, int ncrit, int p, const Ctx& ctx0, double* field, int nthreads,
+            const double* box = nullptr) {
+    Ctx ctx = ctx0;
+    int64_t n = P.n;
+    int nf = nT(P.pf);
+    int pm = dim_to_order(P.dim);
+    Tree t;
+    int st = build_tree(P.X, n, ncrit, ctx.centroid_mode, t);
+    if (st) return st;
+    double rdamp = 0.0;
+    if (ctx.mac_mode == 1 && P.damp != DAMP_NONE) {
+        double dmin = 1e300;
+        for (int64_t q = 0; q < n; ++q) dmin = std::min(dmin, P.dampf[q]);
+        rdamp = damping_range(P.damp, dmin * dmin, pm + P.pf, 0.1 * ctx.target);
+    }
+    build_lists(t, theta, rdamp);
+    const int nimg = box ? 27 : 1;
+    int M = (int)t.nd.size();
+    int ms = nT(p);
+    // leaf id of every particle
+    std::vector<int> leaf_of(n, -1);
+    std::vector<int> term;
+    for (int d = 0; d < M; ++d) {
+        const Node& nd = t.nd[t.dfs[d]];
+        if (!nd.terminal) continue;
+        term.push_back(d);
+        for (int q = 0; q < nd.nleaf; ++q) leaf_of[nd.leaf[q]] = d;
+    }
+    std::vector<double> cm = multipole_expansion(P, t, p, term);
+    std::vector<double> loc((size_t)M * ms, 0.0);
+    // periodic boxes: the 27 images (a_x outer, a_z inner; fmm.F90:156-175),
+    // each with its own lists; exclusions only in the central image
+    for (int img = 0; img < nimg; ++img) {
+        double disp[3] = {0.0, 0.0, 0.0};
+        bool central = true;
+        if (box) {
+            const double av[3] = {(double)(img / 9 - 1), (double)((img / 3) % 3 - 1), (double)(img % 3 - 1)};
+            box_times(box, av, disp);
+            central = img == 13;
+            build_lists(t, theta, rdamp, disp);
+        }
+        // --- particle_fields (fmm.F90:623-747)
+        {
+            ctx.ensure_cnij(pm + P.pf);
+    #pragma omp parallel num_threads(nthreads)
+            {
+                std::vector<double> x, y, z, a, Mb, Tb, F(nf);
+    #pragma omp for schedule(dynamic, 4)
+                for (size_t ti = 0; ti < term.size(); ++ti) {
+                    int d = term[ti];
+                    const Node& ndi = t.nd[t.dfs[d]];
+                    for (int q = 0; q < ndi.nleaf; ++q) {
+                        int64_t i = ndi.leaf[q];
+                        for (int dj : t.nearl[d]) {
+                            const Node& ndj = t.nd[t.dfs[dj]];
+                            int nl = ndj.nleaf;
+                            x.resize(nl);
+                            y.resize(nl);
+                            z.resize(nl);
+                            a.resize(nl);
+                            std::vector<int> src;
+                            src.reserve(nl);
+                            for (int w = 0; w < nl; ++w) {
+                                int64_t j = ndj.leaf[w];
+                                if (central && ctx.excl_mode == 1 && (j == i || is_excluded(P, i, j))) continue;
+                                size_t s = src.size();
+                                x[s] = P.X[i] - (P.X[j] + disp[0]);
+                                y[s] = P.X[n + i] - (P.X[n + j] + disp[1]);
+                                z[s] = P.X[2 * n + i] - (P.X[2 * n + j] + disp[2]);
+                                if (central && ctx.excl_mode == 0 && is_excluded(P, i, j)) x[s] = y[s] = z[s] = 1e10;
+                                if (P.damp != DAMP_NONE) a[s] = P.dampf[i] * P.dampf[j];
+                                src.push_back((int)j);
+                            }
+                            int ns = (int)src.size();
+                            Mb.resize((size_t)ns * P.dim);
+                            for (int c = 0; c < P.dim; ++c)
+                                for (int s = 0; s < ns; ++s) Mb[(size_t)c * ns + s] = P.mp[(size_t)c * n + src[s]];
+                            multipole_field(ns, Mb.data(), P.dim, x.data(), y.data(), z.data(), P.pf, P.damp, a.data(), ctx, F.data(), Tb);
+                            for (int c = 0; c < nf; ++c) field[(size_t)c * n + i] = field[(size_t)c * n + i] + F[c];
+                        }
+                        if (central && ctx.excl_mode == 1) {
+                            // far-field exclusion correction: excluded partners whose
+                            // leaf is not a near leaf were counted through M2L; take
+                            // their undamped pair field out again.
+                            for (int w = 0; w < P.exw; ++w) {
+                                int e = P.ex[(size_t)w * n + i];
+                                if (e == 0 || e - 1 == i) continue;
+                                bool dup = false;
+                                for (int w2 = 0; w2 < w; ++w2)
+                                    if (P.ex[(size_t)w2 * n + i] == e) dup = true;
+                                if (dup) continue;
+                                int lj = leaf_of[e - 1];
+                                const auto& nl = t.nearl[d];
+                                if (std::find(nl.begin(), nl.end(), lj) != nl.end()) continue;
+                                int64_t j = e - 1;
+                                double xx = P.X[i] - P.X[j], yy = P.X[n + i] - P.X[n + j], zz = P.X[2 * n + i] - P.X[2 * n + j];
+                                Mb.resize(P.dim);
+                                for (int c = 0; c < P.dim; ++c) Mb[c] = P.mp[(size_t)c * n + j];
+                                multipole_field(1, Mb.data(), P.dim, &xx, &yy, &zz, P.pf, DAMP_NONE, nullptr, ctx, F.data(), Tb);
+                                for (int c = 0; c < nf; ++c) field[(size_t)c * n + i] = field[(size_t)c * n + i] - F[c];
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        // --- multipole_to_local (fmm.F90:826-882)
+        {
+            ctx.ensure_cnij(2 * p);
+    #pragma omp parallel num_threads(nthreads)
+            {
+                std::vector<double> x, y, z, Mb, Tb, F(ms);
+    #pragma omp for schedule(dynamic, 1)
+                for (int d = 0; d < M; ++d) {
+                    const auto& fl = t.far[d];
+                    int nl = (int)fl.size();
+                    const Node& ndi = t.nd[t.dfs[d]];
+                    x.resize(nl);
+                    y.resize(nl);
+                    z.resize(nl);
+                    Mb.resize((size_t)nl * ms);
+                    for (int q = 0; q < nl; ++q) {
+                        const Node& ndj = t.nd[t.dfs[fl[q]]];
+                        x[q] = ndi.c[0] - (ndj.c[0] + disp[0]);
+                        y[q] = ndi.c[1] - (ndj.c[1] + disp[1]);
+                        z[q] = ndi.c[2] - (ndj.c[2] + disp[2]);
+                        for (int c = 0; c < ms; ++c) Mb[(size_t)c * nl + q] = cm[(size_t)c * M + fl[q]];
+                    }
+                    multipole_field(nl, Mb.data(), ms, x.data(), y.data(), z.data(), p, DAMP_NONE, nullptr, ctx, F.data(), Tb);
+                    for (int c = 0; c < ms; ++c) loc[(size_t)c * M + d] = loc[(size_t)c * M + d] + F[c];
+                }
+            }
+        }
+    }
+    if (box) periodic_sum_and_surface(P, t, p, ctx, cm, loc, box, field);
+    local_to_local_and_particle(P, t, p, term, loc, field, nthreads);
     return OK;
 }
 
@@ -1018,19 +1183,27 @@ int oracle_field_direct(int64_t n, const double* coords, int dim, const double* 
     return OK;
 }
 
-int oracle_field_fmm(int64_t n, const double* coords, int dim, const double* mp, int exw, const int32_t* ex,
-                     double theta, int ncrit, int expansion_order, int field_order, double* field, int damp,
-                     const double* dampf, int is_periodic, const OracleOpts* opts) {
+int oracle_field_fmm_box(int64_t n, const double* coords, int dim, const double* mp, int exw, const int32_t* ex,
+                         double theta, int ncrit, int expansion_order, int field_order, double* field, int damp,
+                         const double* dampf, int is_periodic, const double* box, const OracleOpts* opts) {
     int st = parse_common(n, dim, exw, ex, field_order, damp, dampf);
     if (st) return st;
-    if (is_periodic) return E_NOTSUP;
     if (ncrit < 1 || expansion_order < 0 || !(theta > 0.0)) return E_INVAL;
+    if (is_periodic && (!box || n <= ncrit)) return E_INVAL;  // the reference stops (fmm.F90:1382)
     if (n <= ncrit) return oracle_field_direct(n, coords, dim, mp, exw, ex, field_order, field, damp, dampf, opts);
     Ctx ctx = make_ctx(opts);
     ctx.ensure_cnij(std::max(1, dim_to_order(dim) + field_order));
     Problem P{n, coords, dim, mp, exw, ex, field_order, damp, dampf};
     std::memset(field, 0, sizeof(double) * (size_t)n * nT(field_order));
-    return run_fmm(P, theta, ncrit, expansion_order, ctx, field, nthreads_of(opts));
+    return run_fmm(P, theta, ncrit, expansion_order, ctx, field, nthreads_of(opts), is_periodic ? box : nullptr);
+}
+
+int oracle_field_fmm(int64_t n, const double* coords, int dim, const double* mp, int exw, const int32_t* ex,
+                     double theta, int ncrit, int expansion_order, int field_order, double* field, int damp,
+                     const double* dampf, int is_periodic, const OracleOpts* opts) {
+    if (is_periodic) return E_INVAL;  // needs the box: oracle_field_fmm_box
+    return oracle_field_fmm_box(n, coords, dim, mp, exw, ex, theta, ncrit, expansion_order, field_order, field, damp,
+                                dampf, 0, nullptr, opts);
 }
 
 // Tree + lists of the reference construction, for integer comparisons.
@@ -1100,10 +1273,134 @@ void oracle_tree_get(void* hp, double* center /*3M*/, double* r, double* rmax, i
 
 void oracle_tree_free(void* hp) { delete (TreeHandle*)hp; }
 
+// ---------------------------------------------------------------- QM/MM helpers
+// classify_box (fmm.F90:1134-1171): a node with a target within rmax / theta
+// of its centre is refined (a leaf: its particles are used), otherwise its
+// box multipole is used.  type[DFS id]: 0 unused, 1 box, 2 particles.
+void classify(const Tree& t, int b, const double* tc, int64_t ntgt, double theta, std::vector<int>& type) {
+    const Node& nd = t.nd[b];
+    bool too_close = false;
+    for (int64_t i = 0; i < ntgt; ++i) {
+        double r = norm2_3(tc[i] - nd.c[0], tc[ntgt + i] - nd.c[1], tc[2 * ntgt + i] - nd.c[2]);
+        if (r * theta <= nd.rmax) too_close = true;
+    }
+    if (too_close && !nd.terminal) {
+        for (int o = 0; o < 8; ++o)
+            if (nd.child[o] >= 0) classify(t, nd.child[o], tc, ntgt, theta, type);
+    } else if (too_close && nd.terminal) {
+        type[nd.idx] = 2;
+    } else {
+        type[nd.idx] = 1;
+    }
+}
+
+// The outputs of get_boxes / get_multipoles that depend on the tree only
+// (fmm.F90:1173-1233, 1258-1308): near-field particles (1-based, node
+// order, leaf order) and the boxes (centres, 1-based DFS ids).
+void boxes_of(const Tree& t, const std::vector<int>& type, int64_t* sizes, int32_t* idx_near, double* box_c,
+              int32_t* box_idx) {
+    const int M = (int)t.nd.size();
+    int64_t nn = 0, nb = 0;
+    for (int d = 0; d < M; ++d) {
+        const Node& nd = t.nd[t.dfs[d]];
+        if (type[d] == 2) nn += nd.nleaf;
+        if (type[d] == 1) ++nb;
+    }
+    sizes[0] = nn;
+    sizes[1] = nb;
+    int64_t k = 0, b = 0;
+    for (int d = 0; d < M; ++d) {
+        const Node& nd = t.nd[t.dfs[d]];
+        if (type[d] == 2 && idx_near)
+            for (int q = 0; q < nd.nleaf; ++q) idx_near[k++] = (int32_t)(nd.leaf[q] + 1);
+        if (type[d] == 1) {
+            if (box_c)
+                for (int c = 0; c < 3; ++c) box_c[(size_t)c * nb + b] = nd.c[c];
+            if (box_idx) box_idx[b] = d + 1;
+            ++b;
+        }
+    }
+}
+
 // The Cnij coefficient table for tensors up to order maxo, in the layout of
 // the reference's Cnij(1:2*maxo+3, 0:maxo+1, 0:maxo+1) (column-major;
 // tensors_recursive.F90:64-93): wrap32 = 1 gives the int32 table of the
 // default build, 0 the exact integers.
+// get_boxes (fmm.F90:1258-1308).  sizes[0] = near-field particles, sizes[1]
+// = boxes; outputs may be NULL (sizes only).
+int oracle_get_boxes(int64_t n, const double* coords, int64_t ntgt, const double* tgt, double theta, int ncrit,
+                     int64_t* sizes, int32_t* idx_near, double* box_c, int32_t* box_idx) {
+    Tree t;
+    int st = build_tree(coords, n, ncrit, 0, t);
+    if (st) return st;
+    std::vector<int> type(t.nd.size(), 0);
+    classify(t, 0, tgt, ntgt, theta, type);
+    boxes_of(t, type, sizes, idx_near, box_c, box_idx);
+    return OK;
+}
+
+// get_multipoles (fmm.F90:1173-1256): as get_boxes, plus the raw Cartesian
+// multipoles of the boxes for each of ndens multipole sets (box_mp: nbox x
+// nT(p) x ndens, column-major; mp: n x dim x ndens).
+int oracle_get_multipoles(int64_t n, const double* coords, int dim, int ndens, const double* mp, int64_t ntgt,
+                          const double* tgt, double theta, int ncrit, int p, int64_t* sizes, int32_t* idx_near,
+                          double* box_c, double* box_mp) {
+    if (dim_to_order(dim) < 0 || ndens < 1) return E_INVAL;
+    Tree t;
+    int st = build_tree(coords, n, ncrit, 0, t);
+    if (st) return st;
+    std::vector<int> type(t.nd.size(), 0);
+    classify(t, 0, tgt, ntgt, theta, type);
+    boxes_of(t, type, sizes, idx_near, box_c, nullptr);
+    if (!box_mp) return OK;
+    const int M = (int)t.nd.size(), ms = nT(p);
+    const int64_t nb = sizes[1];
+    std::vector<int> term;
+    for (int d = 0; d < M; ++d)
+        if (t.nd[t.dfs[d]].terminal) term.push_back(d);
+    for (int k = 0; k < ndens; ++k) {
+        Problem P{n, coords, dim, mp + (size_t)k * n * dim, 0, nullptr, 0, DAMP_NONE, nullptr};
+        std::vector<double> cm = multipole_expansion(P, t, p, term);
+        int64_t b = 0;
+        for (int d = 0; d < M; ++d) {
+            if (type[d] != 1) continue;
+            for (int c = 0; c < ms; ++c) box_mp[((size_t)k * ms + c) * nb + b] = cm[(size_t)c * M + d];
+            ++b;
+        }
+    }
+    return OK;
+}
+
+// interpolate_electron_fields (fmm.F90:1310-1336): local expansions given at
+// boxes (1-based DFS ids, local: nbox x nT(p) x ndens) carried down the tree
+// (L2L) and evaluated at the particles (L2P); field (n x nT(f) x ndens) is
+// zeroed first (the reference only adds into it).
+int oracle_interpolate_electron_fields(int64_t n, const double* coords, int64_t nbox, int ndens, const double* local,
+                                       const int32_t* box_idx, double theta, int ncrit, int p, int f, double* field) {
+    (void)theta;
+    Tree t;
+    int st = build_tree(coords, n, ncrit, 0, t);
+    if (st) return st;
+    const int M = (int)t.nd.size(), ms = nT(p), nf = nT(f);
+    for (int64_t b = 0; b < nbox; ++b)
+        if (box_idx[b] < 1 || box_idx[b] > M) return E_INVAL;
+    std::vector<int> term;
+    for (int d = 0; d < M; ++d)
+        if (t.nd[t.dfs[d]].terminal) term.push_back(d);
+    std::memset(field, 0, sizeof(double) * (size_t)n * nf * ndens);
+    for (int k = 0; k < ndens; ++k) {
+        std::vector<double> loc((size_t)M * ms, 0.0);
+        for (int64_t b = 0; b < nbox; ++b)
+            for (int c = 0; c < ms; ++c)
+                loc[(size_t)c * M + (box_idx[b] - 1)] = local[((size_t)k * ms + c) * nbox + b];
+        Problem P{n, coords, 1, nullptr, 0, nullptr, f, DAMP_NONE, nullptr};
+        local_to_local_and_particle(P, t, p, term, loc, field + (size_t)k * n * nf, 1);
+    }
+    return OK;
+}
+
+int oracle_last_lattice_levels(void) { return g_lattice_levels; }
+
 void oracle_cnij(int maxo, int wrap32, double* out) {
     Cnij t = make_cnij(maxo, wrap32 != 0);
     for (int j = 0; j < t.d1; ++j)

@@ -12,7 +12,8 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["field_direct", "field_fmm", "tensors", "radial_g", "tree", "cnij", "DAMP", "n_components"]
+__all__ = ["field_direct", "field_fmm", "tensors", "radial_g", "tree", "cnij", "get_boxes", "get_multipoles",
+           "interpolate_electron_fields", "last_lattice_levels", "DAMP", "n_components"]
 
 DAMP = {"": 0, "AMOEBA": 1, "THOLE": 2, "ERF": 3}
 
@@ -39,6 +40,9 @@ def _load():
         lib.oracle_field_fmm.argtypes = [i64, d, ctypes.c_int, d, ctypes.c_int, i32, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_int, d, ctypes.c_int, d, ctypes.c_int,
                                          ctypes.POINTER(_Opts)]
+        lib.oracle_field_fmm_box.argtypes = [i64, d, ctypes.c_int, d, ctypes.c_int, i32, ctypes.c_double,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_int, d, ctypes.c_int, d,
+                                             ctypes.c_int, d, ctypes.POINTER(_Opts)]
         lib.oracle_tensors.argtypes = [ctypes.c_int, i64, d, d, d, ctypes.c_int, d, ctypes.c_int, d]
         lib.oracle_radial_g.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, d]
         lib.oracle_tree_build.restype = ctypes.c_void_p
@@ -48,6 +52,13 @@ def _load():
         lib.oracle_tree_get.argtypes = [ctypes.c_void_p, d, d, d, i32, i32, i32, i32, i32, i32, i32]
         lib.oracle_tree_free.argtypes = [ctypes.c_void_p]
         lib.oracle_cnij.argtypes = [ctypes.c_int, ctypes.c_int, d]
+        lib.oracle_last_lattice_levels.restype = ctypes.c_int
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        lib.oracle_get_boxes.argtypes = [i64, d, i64, d, ctypes.c_double, ctypes.c_int, i64p, i32, d, i32]
+        lib.oracle_get_multipoles.argtypes = [i64, d, ctypes.c_int, ctypes.c_int, d, i64, d, ctypes.c_double,
+                                              ctypes.c_int, ctypes.c_int, i64p, i32, d, d]
+        lib.oracle_interpolate_electron_fields.argtypes = [i64, d, i64, ctypes.c_int, d, i32, ctypes.c_double,
+                                                           ctypes.c_int, ctypes.c_int, ctypes.c_int, d]
         _lib = lib
     return _lib
 
@@ -105,12 +116,22 @@ def field_fmm(comm, coordinates, multipoles, exclusions, theta, ncrit, expansion
     n = X.shape[0]
     F = np.zeros((n, n_components(field_order)), order="F")
     o = _opts(**kw)
-    st = _load().oracle_field_fmm(n, _dp(X), M.shape[1], _dp(M), E.shape[1], _ip(E), float(theta), int(ncrit),
-                                  int(expansion_order), int(field_order), _dp(F), dt, _dp(d), int(bool(is_periodic)),
-                                  ctypes.byref(o))
+    box = None
+    if is_periodic:
+        box = np.asfortranarray(box_matrix, dtype=np.float64)
+    st = _load().oracle_field_fmm_box(n, _dp(X), M.shape[1], _dp(M), E.shape[1], _ip(E), float(theta), int(ncrit),
+                                      int(expansion_order), int(field_order), _dp(F), dt, _dp(d),
+                                      int(bool(is_periodic)), _dp(box) if box is not None else None,
+                                      ctypes.byref(o))
     if st != 0:
         raise RuntimeError("oracle field_fmm failed with status %d" % st)
     return F
+
+
+def last_lattice_levels():
+    """Lattice levels the last periodic field_fmm used (50 = the reference's
+    limit, reached when its convergence test never passes)."""
+    return int(_load().oracle_last_lattice_levels())
 
 
 def tensors(nmax, x, y, z, damp_type="", a=None, coef="ref"):
@@ -165,3 +186,71 @@ def cnij(maxo, wrap32=True):
     out = np.zeros((2 * maxo + 3, maxo + 2, maxo + 2), order="F")
     _load().oracle_cnij(int(maxo), int(bool(wrap32)), _dp(out))
     return out
+
+
+def _i64p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+def get_boxes(coordinates, target_coordinates, theta, ncrit, expansion_order):
+    """get_boxes (src/fmm.F90:1258-1308): (idx_near_field, box_coordinates,
+    box_indices), 1-based indices as in the reference."""
+    X = np.asfortranarray(coordinates, dtype=np.float64)
+    T = np.asfortranarray(target_coordinates, dtype=np.float64)
+    sz = np.zeros(2, dtype=np.int64)
+    lib = _load()
+    st = lib.oracle_get_boxes(X.shape[0], _dp(X), T.shape[0], _dp(T), float(theta), int(ncrit), _i64p(sz), None, None,
+                              None)
+    if st != 0:
+        raise RuntimeError("oracle get_boxes failed with status %d" % st)
+    idx = np.zeros(max(1, sz[0]), dtype=np.int32)
+    bc = np.zeros((max(1, sz[1]), 3), order="F") if not sz[1] else np.zeros((int(sz[1]), 3), order="F")
+    bi = np.zeros(max(1, sz[1]), dtype=np.int32)
+    lib.oracle_get_boxes(X.shape[0], _dp(X), T.shape[0], _dp(T), float(theta), int(ncrit), _i64p(sz), _ip(idx),
+                         _dp(bc), _ip(bi))
+    return idx[:sz[0]], bc[:sz[1]], bi[:sz[1]]
+
+
+def get_multipoles(comm, coordinates, multipoles, target_coordinates, theta, ncrit, expansion_order):
+    """get_multipoles (src/fmm.F90:1173-1256): (idx_near_field,
+    box_coordinates, box_multipoles); multipoles (N, dim, ndens)."""
+    X = np.asfortranarray(coordinates, dtype=np.float64)
+    Mp = np.asfortranarray(multipoles, dtype=np.float64)
+    if Mp.ndim == 2:
+        Mp = Mp.reshape(Mp.shape + (1,), order="F")
+    T = np.asfortranarray(target_coordinates, dtype=np.float64)
+    n, dim, nd = Mp.shape
+    sz = np.zeros(2, dtype=np.int64)
+    lib = _load()
+    args = (n, _dp(X), dim, nd, _dp(Mp), T.shape[0], _dp(T), float(theta), int(ncrit), int(expansion_order))
+    st = lib.oracle_get_multipoles(*args, _i64p(sz), None, None, None)
+    if st != 0:
+        raise RuntimeError("oracle get_multipoles failed with status %d" % st)
+    idx = np.zeros(max(1, sz[0]), dtype=np.int32)
+    nb = max(1, int(sz[1]))
+    bc = np.zeros((nb, 3), order="F")
+    bm = np.zeros((nb, n_components(expansion_order), nd), order="F")
+    if sz[1]:
+        bc = np.zeros((int(sz[1]), 3), order="F")
+        bm = np.zeros((int(sz[1]), n_components(expansion_order), nd), order="F")
+    lib.oracle_get_multipoles(*args, _i64p(sz), _ip(idx), _dp(bc), _dp(bm))
+    return idx[:sz[0]], bc[:sz[1]], bm[:sz[1]]
+
+
+def interpolate_electron_fields(comm, coordinates, local_expansion, box_indices, theta, ncrit, expansion_order,
+                                field_order):
+    """interpolate_electron_fields (src/fmm.F90:1310-1336): the field
+    (N, nT(field_order), ndens) of local expansions given at boxes."""
+    X = np.asfortranarray(coordinates, dtype=np.float64)
+    Lx = np.asfortranarray(local_expansion, dtype=np.float64)
+    if Lx.ndim == 2:
+        Lx = Lx.reshape(Lx.shape + (1,), order="F")
+    bi = np.ascontiguousarray(box_indices, dtype=np.int32)
+    n = X.shape[0]
+    F = np.zeros((n, n_components(field_order), Lx.shape[2]), order="F")
+    st = _load().oracle_interpolate_electron_fields(n, _dp(X), Lx.shape[0], Lx.shape[2], _dp(Lx), _ip(bi),
+                                                     float(theta), int(ncrit), int(expansion_order),
+                                                     int(field_order), _dp(F))
+    if st != 0:
+        raise RuntimeError("oracle interpolate_electron_fields failed with status %d" % st)
+    return F

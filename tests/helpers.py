@@ -29,3 +29,17 @@ def small_system(n=600, box=20.0, order=2, seed=0, damp=""):
         alpha = rng.uniform(1.0, 10.0, n)
         s["damping_factors"] = np.sqrt(0.39) / alpha ** (1.0 / 6.0)
     return s
+
+
+def potential_up_to_constant(F, G):
+    """Potential column of a periodic result against another: the part that
+    varies over the particles (relative to the column's full magnitude) and
+    the relative difference of the constants.  The reference's lattice sum
+    leaves the potential out of its convergence test (src/fmm.F90:950), so
+    the potential carries a constant that, when the sum does not converge, is
+    dominated by rounding; only the varying part is then well-conditioned."""
+    f = np.asarray(F)[:, 0]
+    g = np.asarray(G)[:, 0]
+    var = float(np.linalg.norm((f - f.mean()) - (g - g.mean())) / max(np.linalg.norm(g), 1e-300))
+    const = float(abs(f.mean() - g.mean()) / max(abs(g.mean()), 1e-300))
+    return var, const

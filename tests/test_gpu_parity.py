@@ -179,8 +179,11 @@ def test_invalid_arguments_raise():
     bad[0, 0] = 101
     with pytest.raises(fmm_gb300.FmmError):
         fmm_gb300.field_direct(0, s["coordinates"], s["multipoles"], bad, 1)
+    # periodic boxes need a box matrix and more than ncrit particles
     with pytest.raises(fmm_gb300.FmmError):
-        fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 16, 4, 1, "", None, True, np.eye(3))
+        fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 16, 4, 1, "", None, True, None)
+    with pytest.raises(fmm_gb300.FmmError):
+        fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 400, 4, 1, "", None, True, np.eye(3) * 10.0)
 
 
 @pytest.mark.parametrize("damp", ["AMOEBA", "THOLE", "ERF"])
