@@ -17,7 +17,8 @@ from . import _lib
 from ._lib import FmmError
 
 __all__ = ["field_direct", "field_fmm", "field_fmm_batched", "field_direct_device", "field_fmm_device", "Options",
-           "last_stats", "n_components", "FmmError", "version", "load_selector", "release_workspace"]
+           "last_stats", "n_components", "FmmError", "version", "load_selector", "release_workspace", "get_boxes",
+           "get_multipoles", "interpolate_electron_fields"]
 
 
 def n_components(order):
@@ -226,7 +227,7 @@ def field_fmm_device(coordinates, multipoles, exclusions, theta, ncrit, expansio
 STAT_NAMES = ["num_nodes", "num_leaves", "max_depth", "m2l_pairs", "p2p_leaf_pairs", "p2p_particle_pairs", "t_tree",
               "t_p2m_m2m", "t_lists", "t_p2p", "t_m2l", "t_l2l_l2p", "t_total", "selector_fallback",
               "sampled_rms_err", "m2l_order_mean"] + ["m2l_pairs_q%d" % q for q in range(13)] + \
-             ["t_p2p_kernel", "t_m2l_product", "m2l_groups", "list_candidates", "list_evals"]
+             ["t_p2p_kernel", "t_m2l_product", "m2l_groups", "list_candidates", "list_evals", "lattice_levels"]
 
 
 def last_stats():
@@ -234,6 +235,68 @@ def last_stats():
     buf = (ctypes.c_double * len(STAT_NAMES))()
     k = _lib.lib().fmm_last_stats(buf, len(STAT_NAMES))
     return {STAT_NAMES[i]: buf[i] for i in range(k)}
+
+
+def get_boxes(coordinates, target_coordinates, theta, ncrit, expansion_order, *, options=None):
+    """``fmm::get_boxes`` (src/fmm.F90:1258-1308): returns (idx_near_field,
+    box_coordinates, box_indices), indices 1-based as in the reference."""
+    X = np.asfortranarray(coordinates, dtype=np.float64)
+    T = np.asfortranarray(target_coordinates, dtype=np.float64)
+    L = _lib.lib()
+    sz = np.zeros(2, dtype=np.int64)
+    o = (options or Options()).to_c()
+    args = (X.shape[0], _dptr(X), T.shape[0], _dptr(T), float(theta), int(ncrit), int(expansion_order),
+            sz.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    _lib.check(L.fmm_get_boxes(*args, None, None, None, ctypes.byref(o)), "get_boxes")
+    idx = np.zeros(int(sz[0]), dtype=np.int32)
+    bc = np.zeros((int(sz[1]), 3), order="F")
+    bi = np.zeros(int(sz[1]), dtype=np.int32)
+    _lib.check(L.fmm_get_boxes(*args, idx.ctypes.data, bc.ctypes.data, bi.ctypes.data, ctypes.byref(o)), "get_boxes")
+    return idx, bc, bi
+
+
+def get_multipoles(comm, coordinates, multipoles, target_coordinates, theta, ncrit, expansion_order, *, options=None):
+    """``fmm::get_multipoles`` (src/fmm.F90:1173-1256): returns
+    (idx_near_field, box_coordinates, box_multipoles); multipoles is
+    (N, dim, ndens) (or (N, dim))."""
+    X = np.asfortranarray(coordinates, dtype=np.float64)
+    Mp = np.asfortranarray(multipoles, dtype=np.float64)
+    if Mp.ndim == 2:
+        Mp = Mp.reshape(Mp.shape + (1,), order="F")
+    T = np.asfortranarray(target_coordinates, dtype=np.float64)
+    n, dim, nd = Mp.shape
+    L = _lib.lib()
+    sz = np.zeros(2, dtype=np.int64)
+    o = (options or Options()).to_c()
+    args = (int(comm or 0), n, _dptr(X), dim, nd, _dptr(Mp), T.shape[0], _dptr(T), float(theta), int(ncrit),
+            int(expansion_order), sz.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    _lib.check(L.fmm_get_multipoles(*args, None, None, None, ctypes.byref(o)), "get_multipoles")
+    idx = np.zeros(int(sz[0]), dtype=np.int32)
+    bc = np.zeros((int(sz[1]), 3), order="F")
+    bm = np.zeros((int(sz[1]), n_components(expansion_order), nd), order="F")
+    _lib.check(L.fmm_get_multipoles(*args, idx.ctypes.data, bc.ctypes.data, bm.ctypes.data, ctypes.byref(o)),
+               "get_multipoles")
+    return idx, bc, bm
+
+
+def interpolate_electron_fields(comm, coordinates, local_expansion, box_indices, theta, ncrit, expansion_order,
+                                field_order, *, options=None):
+    """``fmm::interpolate_electron_fields`` (src/fmm.F90:1310-1336): the field
+    (N, nT(field_order), ndens) of local expansions (nbox, nT(p), ndens) given
+    at the 1-based nodes box_indices."""
+    X = np.asfortranarray(coordinates, dtype=np.float64)
+    Lx = np.asfortranarray(local_expansion, dtype=np.float64)
+    if Lx.ndim == 2:
+        Lx = Lx.reshape(Lx.shape + (1,), order="F")
+    bi = np.ascontiguousarray(box_indices, dtype=np.int32)
+    n = X.shape[0]
+    F = np.zeros((n, n_components(field_order), Lx.shape[2]), order="F")
+    o = (options or Options()).to_c()
+    _lib.check(_lib.lib().fmm_interpolate_electron_fields(int(comm or 0), n, _dptr(X), Lx.shape[0], Lx.shape[2],
+                                                          _dptr(Lx), bi.ctypes.data, float(theta), int(ncrit),
+                                                          int(expansion_order), int(field_order), _dptr(F),
+                                                          ctypes.byref(o)), "interpolate_electron_fields")
+    return F
 
 
 def release_workspace():

@@ -49,6 +49,9 @@ EXPORTED = [
     "fmm_field_direct_targets_noalloc",
     "fmm_last_stats",
     "fmm_release_workspace",
+    "fmm_get_boxes",
+    "fmm_get_multipoles",
+    "fmm_interpolate_electron_fields",
     "fmm_debug_tree",
     "fmm_measure_fma_peak",
     "fmm_launch_count",
@@ -102,6 +105,14 @@ def lib():
     L.fmm_field_fmm_batched.restype = c
     L.fmm_last_stats.argtypes = [d, c]
     L.fmm_release_workspace.argtypes = []
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    vp = ctypes.c_void_p
+    L.fmm_get_boxes.argtypes = [i64, d, i64, d, ctypes.c_double, c, c, i64p, vp, vp, vp, op]
+    L.fmm_get_boxes.restype = c
+    L.fmm_get_multipoles.argtypes = [c, i64, d, c, c, d, i64, d, ctypes.c_double, c, c, i64p, vp, vp, vp, op]
+    L.fmm_get_multipoles.restype = c
+    L.fmm_interpolate_electron_fields.argtypes = [c, i64, d, i64, c, d, vp, ctypes.c_double, c, c, c, d, op]
+    L.fmm_interpolate_electron_fields.restype = c
     L.fmm_release_workspace.restype = c
     L.fmm_measure_fma_peak.argtypes = [c, d]
     L.fmm_launch_count.restype = ctypes.c_int64

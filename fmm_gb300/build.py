@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfmm_gb300.so")
-SOURCES = ["api.cu", "tree.cu", "near.cu", "near_f32.cu", "expansions.cu", "translate.cu", "m2l.cu", "m2l_gemm.cu", "diag.cu", "noalloc.cu", "selector.cu"]
+SOURCES = ["api.cu", "tree.cu", "near.cu", "near_f32.cu", "expansions.cu", "translate.cu", "m2l.cu", "m2l_gemm.cu", "diag.cu", "noalloc.cu", "selector.cu", "qmmm.cu"]
 HEADERS = ["common.cuh", "m2l_basis.cuh", "pair.cuh", "dispatch.cuh", "mlp.cuh", "internal.h", "series_tables.h", os.path.join("..", "..", "include", "fmm_gpu.h")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

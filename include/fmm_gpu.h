@@ -79,12 +79,58 @@ int fmm_field_direct(int comm, int64_t n, const double *coordinates, int mdim, c
 
 /* Replaces fmm::field_fmm (src/fmm.F90:1354-1400).  Falls back to the direct
  * sum when n <= ncrit, as the reference does (src/fmm.F90:1381-1383).
- * is_periodic != 0 returns FMM_ENOTSUP; box_matrix (3x3, may be NULL) is
- * otherwise ignored.  Host pointers; blocks until `field` holds the result. */
+ * is_periodic != 0 evaluates the periodic system of box_matrix (3x3,
+ * column-major, the cell vectors as columns) as the reference does: the 27
+ * images of the box with their own interaction lists, near fields (exclusions
+ * only in the central image) and M2L, the lattice sum beyond them (levels of
+ * 3x3x3 supercells until a level's local-expansion norm drops below 1e-8, at
+ * most 50) and the surface (dipole) term (src/fmm.F90:156-175, 337-343,
+ * 623-747, 826-979).  Periodic calls need box_matrix and n > ncrit
+ * (otherwise FMM_EINVAL; the reference stops) and run in FP64 with the fixed
+ * acceptance rule (opts->precision 0, opts->selector 0, else FMM_ENOTSUP).
+ * Host pointers; blocks until `field` holds the result. */
 int fmm_field_fmm(int comm, int64_t n, const double *coordinates, int mdim, const double *multipoles, int exw,
                   const int32_t *exclusions, double theta, int ncrit, int expansion_order, int field_order,
                   double *field, const char *damp, int damp_len, const double *damping_factors, int is_periodic,
                   const double *box_matrix, const fmm_opts *opts);
+
+/* QM/MM helpers.  Replace fmm::get_boxes, fmm::get_multipoles and
+ * fmm::interpolate_electron_fields (src/fmm.F90:1134-1336), which split the
+ * particles into a near field and far-field boxes around a set of QM target
+ * points (classify_box: a node with a target within rmax / theta of its
+ * centre is refined, a leaf that is still that close gives its particles,
+ * any other node its box) and evaluate local expansions given at boxes at the
+ * particles.  The octree is the reference's (same node numbers, 1-based).
+ * Call once with all output pointers NULL to get sizes[0] (near-field
+ * particles) and sizes[1] (boxes), then with outputs of those sizes:
+ *   idx_near_field   sizes[0]                   1-based particle indices,
+ *                                               leaf by leaf in node order,
+ *                                               ascending within a leaf (the
+ *                                               reference uses its insertion
+ *                                               order there)
+ *   box_coordinates  sizes[1] x 3               box centres
+ *   box_indices      sizes[1]                   1-based node numbers
+ *   box_multipoles   sizes[1] x nT(p) x ndens   raw Cartesian moments of the
+ *                                               boxes, one set per density
+ *                                               (multipoles: n x mdim x ndens)
+ * fmm_interpolate_electron_fields takes local expansions local_expansion
+ * (nbox x nT(p) x ndens, the reference's local-expansion convention) at the
+ * 1-based nodes box_indices and writes field (n x nT(field_order) x ndens;
+ * zeroed first, the reference adds into it).  The reference's own helpers stop
+ * in their final clean-up (fmm.F90:301-326 deallocates interaction lists
+ * that they never build); these return their results.  Host pointers;
+ * multipoles of order <= 2. */
+int fmm_get_boxes(int64_t n, const double *coordinates, int64_t ntgt, const double *target_coordinates,
+                  double theta, int ncrit, int expansion_order, int64_t *sizes, int32_t *idx_near_field,
+                  double *box_coordinates, int32_t *box_indices, const fmm_opts *opts);
+int fmm_get_multipoles(int comm, int64_t n, const double *coordinates, int mdim, int ndens, const double *multipoles,
+                       int64_t ntgt, const double *target_coordinates, double theta, int ncrit, int expansion_order,
+                       int64_t *sizes, int32_t *idx_near_field, double *box_coordinates, double *box_multipoles,
+                       const fmm_opts *opts);
+int fmm_interpolate_electron_fields(int comm, int64_t n, const double *coordinates, int64_t nbox, int ndens,
+                                    const double *local_expansion, const int32_t *box_indices, double theta,
+                                    int ncrit, int expansion_order, int field_order, double *field,
+                                    const fmm_opts *opts);
 
 /* Many independent systems in one call (no counterpart in the reference,
  * which handles one system per call).  System k owns particles
@@ -171,8 +217,9 @@ int fmm_release_workspace(void);
  * near-field kernel alone and of the grouped M2L product kernel alone (-1 if
  * that kernel did not run), the number of displacement groups of the grouped
  * M2L, the cell pairs examined by the list build and how many of them the
- * learned selector's network evaluated.  Returns the number written (at most
- * 34). */
+ * learned selector's network evaluated, and the number of lattice levels the
+ * periodic sum used (0 without a periodic box).  Returns the number written
+ * (at most 35). */
 int fmm_last_stats(double *out, int len);
 
 /* Diagnostics (no counterpart in the reference): builds the octree and
@@ -208,7 +255,9 @@ int fmm_selector_param_count(void);
 /* Selector network kernels (training and checks): parameter count, batched
  * forward pass, gradient of the mean squared error, Adam training; and
  * training-data collection for one system (features and log10 errors at
- * orders 2..12 of sampled far pairs).  Host pointers. */
+ * orders 2..12 of sampled far pairs; the octree uses the blocked centroid;
+ * `pairs`, if not NULL, receives each sampled pair's target and source node
+ * ids, depth-first preorder, 2 per pair).  Host pointers. */
 int fmm_mlp_param_count(void);
 int fmm_mlp_forward(const float *params, const float *x, int64_t n, float *y);
 int fmm_mlp_grad(const float *params, const float *x, const float *y, int64_t n, float *grad, float *loss);
@@ -216,7 +265,7 @@ int fmm_mlp_train(float *params, const float *x, const float *y, int64_t n, int 
                   uint64_t seed, float *losses);
 int fmm_selector_collect(int64_t n, const double *coordinates, int mdim, const double *multipoles,
                          const double *damping_factors, int ncrit, double theta, int max_pairs, uint64_t seed,
-                         float *features, float *labels, int *npairs);
+                         float *features, float *labels, int *npairs, int32_t *pairs);
 
 /* Human-readable text for a status code. */
 const char *fmm_strerror(int status);
