@@ -375,8 +375,19 @@ def _ptr(v):
     return FA(np.asarray(v), None, np.asarray(v).dtype.kind == "i")
 
 
+_LENIENT = {"dealloc": False}
+
+
+def set_lenient_dealloc(on):
+    """With on, DEALLOCATE of an unallocated array is skipped instead of
+    stopping the program (to read out what a routine computed before such a
+    DEALLOCATE, e.g. the reference's QM/MM helpers, whose `finalize` frees
+    interaction lists they never built)."""
+    _LENIENT["dealloc"] = bool(on)
+
+
 def _dealloc(v, what):
-    if v is None:
+    if v is None and not _LENIENT["dealloc"]:
         raise FortranStop("Attempt to DEALLOCATE unallocated '%s'" % what)
     return None
 

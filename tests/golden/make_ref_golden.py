@@ -25,7 +25,13 @@ ref_fields.npz
   and for the tree cases the reference's octree and interaction lists
   (``C_tree_*``: per DFS node centre, r, rmax, depth, parent, leaf flag,
   particle count; far and near lists as sorted (target, source) node pairs;
-  node ids are the reference's DFS positions minus one).
+  node ids are the reference's DFS positions minus one); ``C_box`` is the
+  periodic cell of the periodic cases (zero otherwise);
+  ``qmmm_*``: get_boxes, get_multipoles (two multipole sets) and
+  interpolate_electron_fields (two sets of local expansions) on one water
+  system around six target points (src/fmm.F90:1134-1336), read with the
+  DEALLOCATE that stops these helpers at their end skipped; ``qmmm_stops``
+  records those stops.
 
 Run where the reference source is present (the default path below, or
 FMM_REFERENCE_SRC):  python tests/golden/make_ref_golden.py
@@ -148,6 +154,19 @@ CASES = {
     "water_amoeba": ("water", 50, 14.5, 2, "AMOEBA", 0.5, 8, 8, 1, False, 13),
     "uniform_erf": ("uniform", 240, 14.0, 1, "ERF", 0.5, 10, 5, 1, False, 14),
     "uniform_charges": ("uniform", 300, 16.0, 0, "", 0.6, 12, 5, 2, False, 15),
+    # periodic boxes (is_periodic = .true.): particles inside the cell of BOXES[name]
+    "periodic_cubic": ("water", 36, 11.0, 2, "", 0.5, 8, 4, 1, False, 16),
+    "periodic_triclinic_thole": ("water", 30, 10.5, 2, "THOLE", 0.5, 8, 5, 2, False, 17),
+    "periodic_amoeba_p6": ("water", 30, 10.5, 2, "AMOEBA", 0.5, 8, 6, 1, False, 18),
+}
+
+# cell vectors as the columns of box_matrix; the triclinic one has
+# box(1,2) != box(2,1) and box(1,3) box(3,2) != 0, where the reference's
+# volume formula (fmm.F90:963-965) differs from the determinant
+BOXES = {
+    "periodic_cubic": [[11.0, 0.0, 0.0], [0.0, 11.0, 0.0], [0.0, 0.0, 11.0]],
+    "periodic_triclinic_thole": [[10.5, 0.5, 0.3], [1.5, 10.0, 0.4], [0.8, 1.2, 10.2]],
+    "periodic_amoeba_p6": [[10.5, 0.0, 0.0], [0.0, 10.5, 0.0], [0.0, 0.0, 10.5]],
 }
 
 
@@ -163,6 +182,12 @@ def _system(spec):
         s["damping_factors"] = rng.uniform(0.3, 0.8, n) if damp == "ERF" else np.zeros(n)
     if damp == "":
         s["damping_factors"] = np.zeros(s["coordinates"].shape[0])
+    name = [k for k, v in CASES.items() if v == spec][0]
+    if name in BOXES:
+        # fractional coordinates wrapped into [0, 1), then the cell
+        H = np.array(BOXES[name]).T  # columns are the cell vectors
+        u = np.mod(np.linalg.solve(H, np.asarray(s["coordinates"]).T).T, 1.0)
+        s["coordinates"] = np.asfortranarray(u @ H.T)
     return s
 
 
@@ -210,7 +235,12 @@ def field_job(name):
     ns["f_field_direct"](0, X, Mp, E, f, Fd, damp, d)
     ns = tr.new()
     Ff = np.zeros((n, _nT(f)), order="F")
-    if want_tree:
+    periodic = name in BOXES
+    box = np.asfortranarray(np.array(BOXES[name]).T) if periodic else np.zeros((3, 3), order="F")
+    if periodic:
+        ns["f_field_fmm"](0, X, Mp, E, theta, ncrit, p, f, Ff, damp, d, 1, box)
+        tree = None
+    elif want_tree:
         # keep the tree: run the field_fmm steps up to the lists, then the call itself
         ns["f_field_fmm"](0, X, Mp, E, theta, ncrit, p, f, Ff, damp, d, 0, np.zeros((3, 3), order="F"))
         ns2 = tr.new()
@@ -223,6 +253,7 @@ def field_job(name):
         ns["f_field_fmm"](0, X, Mp, E, theta, ncrit, p, f, Ff, damp, d, 0, np.zeros((3, 3), order="F"))
         tree = None
     out = {name + "_X": X, name + "_M": Mp, name + "_E": s["exclusions"].astype(np.int32), name + "_d": d,
+           name + "_box": box,
            name + "_cfg": np.array([theta, ncrit, p, f, DAMP[damp]], dtype=np.float64),
            name + "_direct": Fd, name + "_fmm": Ff}
     if tree:
@@ -232,17 +263,81 @@ def field_job(name):
     return out
 
 
+# ----------------------------------------------------------------------------
+# QM/MM helpers (src/fmm.F90:1134-1336).  As shipped they stop in `finalize`
+# (clean_node deallocates the interaction lists that these helpers never
+# build; gfortran stops at DEALLOCATE of an unallocated array), so their
+# outputs are read with that DEALLOCATE skipped; ``qmmm_stops`` records the
+# stop of the unmodified code.
+
+def _comps(n):
+    return [(kx, ky, k - kx - ky) for k in range(n + 1) for kx in range(k, -1, -1) for ky in range(k - kx, -1, -1)]
+
+
+def qmmm_job(_):
+    fx, tr = _translated()
+    from fmm_gb300 import systems
+    out = {}
+    s = systems.water(90, 15.0, seed=21)
+    X = np.asfortranarray(s["coordinates"])
+    M = np.asfortranarray(s["multipoles"])
+    M3 = np.asfortranarray(np.stack([M, 0.5 * M + 0.01], axis=2))
+    rng = np.random.default_rng(22)
+    T = np.asfortranarray(X[rng.choice(X.shape[0], 6, replace=False)] + rng.normal(0, 0.3, (6, 3)))
+    theta, ncrit, p, f = 0.5, 8, 4, 1
+    stops = []
+    for name in ("get_boxes", "get_multipoles", "interpolate_electron_fields"):
+        try:
+            ns = tr.new()
+            if name == "get_boxes":
+                ns["f_get_boxes"](X, T, theta, ncrit, p, None, None, None)
+            elif name == "get_multipoles":
+                ns["f_get_multipoles"](0, X, M3, T, theta, ncrit, p, None, None, None)
+            else:
+                Fx = np.zeros((X.shape[0], _nT(f), 1), order="F")
+                ns["f_interpolate_electron_fields"](0, X, np.zeros((1, _nT(p), 1), order="F"),
+                                                    np.array([1], dtype=np.int64), theta, ncrit, p, f, Fx)
+        except fx.FortranStop as e:
+            stops.append("%s: %s" % (name, e))
+    fx.set_lenient_dealloc(True)
+    try:
+        ns = tr.new()
+        idx, bc, bi = ns["f_get_boxes"](X, T, theta, ncrit, p, None, None, None)
+        ns = tr.new()
+        idx2, bc2, bm = ns["f_get_multipoles"](0, X, M3, T, theta, ncrit, p, None, None, None)
+        # local expansions at the boxes: random Taylor coefficients that fall
+        # off with the order, different per box and per set
+        nq = _nT(p)
+        nbox = bi.a.shape[0]
+        Lx = np.asfortranarray(rng.normal(0, 1.0, (nbox, nq, 2)) * np.array(
+            [0.1 ** (sum(c)) for c in _comps(p)])[None, :, None])
+        ns = tr.new()
+        F = np.zeros((X.shape[0], _nT(f), 2), order="F")
+        ns["f_interpolate_electron_fields"](0, X, Lx, bi.a.astype(np.int64), theta, ncrit, p, f, F)
+    finally:
+        fx.set_lenient_dealloc(False)
+    out.update(qmmm_X=X, qmmm_M=M3, qmmm_T=T, qmmm_cfg=np.array([theta, ncrit, p, f]),
+               qmmm_idx_near=idx.a.astype(np.int32), qmmm_box_coordinates=bc.a,
+               qmmm_box_indices=bi.a.astype(np.int32), qmmm_idx_near_mp=idx2.a.astype(np.int32),
+               qmmm_box_coordinates_mp=bc2.a, qmmm_box_multipoles=bm.a, qmmm_local=Lx, qmmm_field=F,
+               qmmm_stops=np.array(stops))
+    print("qmmm: %d near particles, %d boxes; unmodified: %s" % (idx.a.shape[0], nbox, stops), flush=True)
+    return out
+
+
 def main():
     if not os.path.isdir(SRC):
         raise SystemExit("reference source not found at %s (set FMM_REFERENCE_SRC)" % SRC)
     ctx = mp.get_context("spawn")
     with ctx.Pool(min(8, len(CASES) + 1)) as pool:
         tj = pool.apply_async(tensors_job, (0,))
+        qj = pool.apply_async(qmmm_job, (0,))
         fj = pool.map_async(field_job, list(CASES))
         tens = tj.get()
         fields = {}
         for part in fj.get():
             fields.update(part)
+        fields.update(qj.get())
     np.savez_compressed(os.path.join(HERE, "ref_tensors.npz"), **tens)
     np.savez_compressed(os.path.join(HERE, "ref_fields.npz"), **fields)
     print("wrote ref_tensors.npz (%d arrays), ref_fields.npz (%d arrays)" % (len(tens), len(fields)))

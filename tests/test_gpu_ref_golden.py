@@ -15,13 +15,14 @@ import numpy as np
 import pytest
 
 import fmm_gb300
-from helpers import rel_err
+from helpers import potential_up_to_constant, rel_err
 
 pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_fields.npz")
 DAMP_NAMES = {0: "", 1: "AMOEBA", 2: "THOLE", 3: "ERF"}
 CASES = ["water_none", "water_thole", "water_amoeba", "uniform_erf", "uniform_charges"]
+PERIODIC = ["periodic_cubic", "periodic_triclinic_thole", "periodic_amoeba_p6"]
 
 
 @pytest.fixture(scope="module")
@@ -33,8 +34,9 @@ def _case(fields, name):
     g = lambda k: fields[name + "_" + k]
     theta, ncrit, p, f, dcode = g("cfg")
     damp = DAMP_NAMES[int(dcode)]
+    box = g("box")
     return dict(X=g("X"), M=g("M"), E=g("E"), d=g("d") if damp else None, theta=float(theta), ncrit=int(ncrit),
-                p=int(p), f=int(f), damp=damp)
+                p=int(p), f=int(f), damp=damp, periodic=bool(np.any(box)), box=box)
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -45,12 +47,22 @@ def test_gpu_field_direct_matches_reference(fields, name):
     assert rel_err(G, fields[name + "_direct"], cols) <= 1e-12
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", CASES + PERIODIC)
 def test_gpu_field_fmm_matches_reference(fields, name):
     c = _case(fields, name)
-    G = fmm_gb300.field_fmm(0, c["X"], c["M"], c["E"], c["theta"], c["ncrit"], c["p"], c["f"], c["damp"], c["d"])
-    cols = slice(1, None) if c["damp"] == "AMOEBA" else slice(None)
-    assert rel_err(G, fields[name + "_fmm"], cols) <= 1e-12
+    G = fmm_gb300.field_fmm(0, c["X"], c["M"], c["E"], c["theta"], c["ncrit"], c["p"], c["f"], c["damp"], c["d"],
+                            c["periodic"], c["box"])
+    ref = fields[name + "_fmm"]
+    assert rel_err(G, ref, slice(1, None)) <= 1e-12
+    if c["periodic"]:
+        # the potential up to a constant; in full where the lattice sum
+        # converged (its constant is otherwise dominated by rounding)
+        var, const = potential_up_to_constant(G, ref)
+        assert var <= 1e-12
+        if fmm_gb300.last_stats()["lattice_levels"] < 50:
+            assert rel_err(G, ref, slice(0, 1)) <= 1e-12
+    elif c["damp"] != "AMOEBA":
+        assert rel_err(G, ref, slice(0, 1)) <= 1e-12
 
 
 @pytest.mark.parametrize("name", ["water_none", "water_thole"])
