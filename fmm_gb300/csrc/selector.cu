@@ -497,7 +497,8 @@ int fmm_selector_param_count(void) { return kMlpParams; }
 // at orders 2..12 of up to max_pairs far pairs sampled uniformly from the
 // far list of the reference acceptance test at `theta`.
 int fmm_selector_collect(int64_t n, const double* X, int mdim, const double* mp, const double* damp, int ncrit,
-                         double theta, int max_pairs, uint64_t seed, float* feats, float* labels, int* npairs_out) {
+                         double theta, int max_pairs, uint64_t seed, float* feats, float* labels, int* npairs_out,
+                         int32_t* pairs_out) {
     if (n < 2 || !X || !mp || ncrit < 1 || !(theta > 0) || max_pairs < 1 || !feats || !labels || !npairs_out)
         return FMM_EINVAL;
     const int m = dim_to_order(mdim);
@@ -538,6 +539,11 @@ int fmm_selector_collect(int64_t n, const double* X, int mdim, const double* mp,
     FMM_TRY(fd.ensure(sizeof(float) * (size_t)np * kMlpIn));
     FMM_TRY(ld.ensure(sizeof(float) * (size_t)np * kMlpOut));
     FMM_CUDA_TRY(cudaMemcpy(sel.p, hp.data(), sizeof(int2) * np, cudaMemcpyHostToDevice));
+    if (pairs_out)
+        for (int q = 0; q < np; ++q) {
+            pairs_out[2 * q] = hp[q].x;
+            pairs_out[2 * q + 1] = hp[q].y;
+        }
     FMM_TRY(selector_pair_data(ws, Pt, t, P, sel.as<int2>(), np, fd.as<float>(), ld.as<float>(), st));
     FMM_CUDA_TRY(cudaMemcpy(feats, fd.p, sizeof(float) * (size_t)np * kMlpIn, cudaMemcpyDeviceToHost));
     FMM_CUDA_TRY(cudaMemcpy(labels, ld.p, sizeof(float) * (size_t)np * kMlpOut, cudaMemcpyDeviceToHost));

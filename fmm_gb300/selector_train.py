@@ -36,7 +36,7 @@ def collect(n_systems, n_mol, thetas, pairs_per_theta, ncrit=64, seed0=1000):
     L.fmm_selector_collect.restype = ctypes.c_int
     L.fmm_selector_collect.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p,
-                                       ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+                                       ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
     box = 270.0 * (n_mol / 333_333) ** (1.0 / 3.0)
     Xs, Ys = [], []
     for k in range(n_systems):
@@ -50,7 +50,7 @@ def collect(n_systems, n_mol, thetas, pairs_per_theta, ncrit=64, seed0=1000):
             npairs = ctypes.c_int(0)
             st = L.fmm_selector_collect(Xc.shape[0], Xc.ctypes.data, Mc.shape[1], Mc.ctypes.data, d.ctypes.data, ncrit,
                                         float(t), pairs_per_theta, seed0 + 7 * k, F.ctypes.data, Y.ctypes.data,
-                                        ctypes.byref(npairs))
+                                        ctypes.byref(npairs), None)
             _lib.check(st, "fmm_selector_collect")
             Xs.append(F[:npairs.value])
             Ys.append(Y[:npairs.value])
