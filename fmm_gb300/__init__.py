@@ -18,7 +18,7 @@ from ._lib import FmmError
 
 __all__ = ["field_direct", "field_fmm", "field_fmm_batched", "field_direct_device", "field_fmm_device", "Options",
            "last_stats", "n_components", "FmmError", "version", "load_selector", "release_workspace", "get_boxes",
-           "get_multipoles", "interpolate_electron_fields"]
+           "get_multipoles", "interpolate_electron_fields", "Plan"]
 
 
 def n_components(order):
@@ -158,6 +158,71 @@ def field_fmm(comm, coordinates, multipoles, exclusions, theta, ncrit, expansion
                                   _dptr(box) if box is not None else None, ctypes.byref(o))
     _lib.check(st, "field_fmm")
     return F
+
+
+class Plan:
+    """Fixed coordinates, many multipole sets (fmm_plan_create / execute).
+
+    The octree, interaction lists and M2L grouping are built once; every
+    ``execute(multipoles)`` replays one captured CUDA graph and returns the
+    field ``field_fmm`` gives for the same inputs.  Arguments as
+    ``field_fmm`` without the multipoles (``dim`` = their column count);
+    fixed acceptance rule only.  ``close()`` (or garbage collection) frees
+    the plan's device memory."""
+
+    def __init__(self, coordinates, dim, exclusions, theta, ncrit, expansion_order, field_order, damp_type="",
+                 damping_factors=None, *, options=None):
+        X, _, E, d = _prep(coordinates, np.zeros(np.shape(coordinates)[0]), exclusions, damping_factors)
+        n = X.shape[0]
+        ds, dl = _damp_bytes(damp_type)
+        o = _options_c(options)
+        h = ctypes.c_void_p(None)
+        L = _lib.lib()
+        st = L.fmm_plan_create(n, _dptr(X), int(dim), E.shape[1], E.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                               float(theta), int(ncrit), int(expansion_order), int(field_order), ds, dl,
+                               _dptr(d) if d is not None else None, ctypes.byref(o), ctypes.byref(h))
+        _lib.check(st, "plan_create")
+        self._h = h
+        self._lib = L
+        self.n, self.dim, self.field_order = n, int(dim), int(field_order)
+
+    @property
+    def kernels(self):
+        """Kernel launches per evaluation (nodes of the captured graph)."""
+        return self._lib.fmm_plan_kernels(self._h)
+
+    def execute(self, multipoles, out=None):
+        M = np.asfortranarray(multipoles, dtype=np.float64)
+        if M.shape != (self.n, self.dim):
+            raise ValueError("multipoles must have shape (%d, %d)" % (self.n, self.dim))
+        F = out if out is not None else np.zeros((self.n, n_components(self.field_order)), order="F")
+        st = self._lib.fmm_plan_execute(self._h, _dptr(M), _dptr(F))
+        _lib.check(st, "plan_execute")
+        return F
+
+    def execute_device(self, multipoles, field):
+        """Device arrays (anything with ``data_ptr()``), column-major."""
+        st = self._lib.fmm_plan_execute_device(self._h, ctypes.c_void_p(int(multipoles.data_ptr())),
+                                               ctypes.c_void_p(int(field.data_ptr())))
+        _lib.check(st, "plan_execute_device")
+        return field
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.fmm_plan_destroy(self._h)
+            self._h = ctypes.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def field_fmm_batched(systems_list, theta, ncrit, expansion_order, field_order, damp_type="", *, options=None):

@@ -62,6 +62,11 @@ EXPORTED = [
     "fmm_mlp_grad",
     "fmm_mlp_train",
     "fmm_selector_collect",
+    "fmm_plan_create",
+    "fmm_plan_execute",
+    "fmm_plan_execute_device",
+    "fmm_plan_kernels",
+    "fmm_plan_destroy",
     "fmm_strerror",
     "fmm_version",
 ]
@@ -114,6 +119,17 @@ def lib():
     L.fmm_interpolate_electron_fields.argtypes = [c, i64, d, i64, c, d, vp, ctypes.c_double, c, c, c, d, op]
     L.fmm_interpolate_electron_fields.restype = c
     L.fmm_release_workspace.restype = c
+    L.fmm_plan_create.argtypes = [i64, d, c, c, i32, ctypes.c_double, c, c, c, cs, c, d, op,
+                                  ctypes.POINTER(ctypes.c_void_p)]
+    L.fmm_plan_create.restype = c
+    L.fmm_plan_execute.argtypes = [ctypes.c_void_p, d, d]
+    L.fmm_plan_execute.restype = c
+    L.fmm_plan_execute_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.fmm_plan_execute_device.restype = c
+    L.fmm_plan_kernels.argtypes = [ctypes.c_void_p]
+    L.fmm_plan_kernels.restype = c
+    L.fmm_plan_destroy.argtypes = [ctypes.c_void_p]
+    L.fmm_plan_destroy.restype = None
     L.fmm_measure_fma_peak.argtypes = [c, d]
     L.fmm_launch_count.restype = ctypes.c_int64
     L.fmm_launch_count.argtypes = []

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <new>
 #include <string>
 #include <thread>
 #include <unistd.h>
@@ -123,7 +124,7 @@ int check_common(int64_t n, int mdim, int exw, int field_order, int damp, const 
     if (n < 1 || n > (int64_t)INT32_MAX - 1) return FMM_EINVAL;
     const int m = dim_to_order(mdim);
     if (m < 0 || exw < 0 || field_order < 0) return FMM_EINVAL;
-    if (m > 2 || field_order > 2) return FMM_ENOTSUP;
+    if (m > 3 || field_order > 3) return FMM_ENOTSUP;
     if (damp != DAMP_NONE && !damping) return FMM_EINVAL;
     return FMM_OK;
 }
@@ -400,6 +401,8 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         md.coef_mode = 1;
     }
     if (learned && (p < 10 || dim_to_order(P.dim) > 2 || f < 1)) return FMM_ENOTSUP;
+    // the FP32 near field and the double-float translations take orders <= 2
+    if (md.precision != 0 && (dim_to_order(P.dim) > 2 || f > 2)) return FMM_ENOTSUP;
     TreeParams tpl = tp;
     if (o.mac_mode == 1 && P.damp_type != DAMP_NONE && P.damp) {
         const double dmin = min_damping_factor(ws, P.damp, P.n, st);
@@ -575,6 +578,148 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     s.v[16 + kMaxP + 6] = (double)lattice_levels;
     g_stats = s;
     return FMM_OK;
+}
+
+// ---------------------------------------------------------------- plans
+// A plan keeps, for fixed coordinates, exclusions, damping factors and
+// settings, the octree, the interaction lists and the M2L grouping in a
+// workspace of its own, and evaluates multipole sets by replaying one CUDA
+// graph of the kernels that read the multipoles (gather, P2M/M2M, near
+// field, exclusion fix-up, M2L, L2L/L2P, scatter): no host synchronisation
+// and no per-kernel launch cost per set.  Polarisation solvers evaluate the
+// field of many induced-dipole sets at fixed coordinates this way.
+struct PlanImpl {
+    Workspace ws;
+    TreeDev t;
+    Particles P{};
+    Modes md{0, 0, 0};
+    int p = 0, f = 0, nf = 0;
+    bool f32_near = false;
+    bool direct = false;  // n <= ncrit: the direct sum, as field_fmm does
+    cudaStream_t st = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;  // kernel nodes of the graph
+    ~PlanImpl() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+// The kernels of one evaluation (multipoles in ws.in_mp, field to
+// ws.out_field), on the plan's structure.
+int plan_numeric(PlanImpl& pl) {
+    Workspace& ws = pl.ws;
+    const Particles& P = pl.P;
+    TreeDev& t = pl.t;
+    cudaStream_t st = pl.st;
+    if (pl.direct) return launch_direct_f64(ws, P, pl.f, pl.md, ws.out_field.as<double>(), st);
+    ws.product_err = nullptr;
+    FMM_TRY(gather_sorted(ws, P, t, st));
+    if (pl.f32_near) FMM_TRY(prepare_f32_records(ws, P, t, st));
+    FMM_TRY(launch_p2m_m2m(ws, P, t, pl.p, st, pl.md.precision != 0));
+    if (pl.f32_near)
+        FMM_TRY(launch_p2p_f32(ws, P, t, pl.f, st));
+    else
+        FMM_TRY(launch_p2p_f64(ws, P, t, pl.f, pl.md, st));
+    FMM_TRY(launch_excl_correction(ws, P, &t, pl.f, pl.md, ws.fsorted.as<double>(), st));
+    FMM_TRY(launch_m2l(ws, t, pl.p, pl.md, st));
+    FMM_TRY(launch_l2l_l2p(ws, P, t, pl.p, pl.f, pl.md.precision == 1 || pl.md.precision == 3, st));
+    FMM_TRY(scatter_field(ws, t, P.n, pl.nf, ws.out_field.as<double>(), st));
+    return FMM_OK;
+}
+
+int count_kernel_nodes(cudaGraph_t g, int* out) {
+    size_t nn = 0;
+    FMM_CUDA_TRY(cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) FMM_CUDA_TRY(cudaGraphGetNodes(g, nodes.data(), &nn));
+    int k = 0;
+    for (size_t i = 0; i < nn; ++i) {
+        cudaGraphNodeType ty;
+        FMM_CUDA_TRY(cudaGraphNodeGetType(nodes[i], &ty));
+        if (ty == cudaGraphNodeTypeKernel) ++k;
+    }
+    *out = k;
+    return FMM_OK;
+}
+
+int plan_build(PlanImpl& pl, int64_t n, const double* X, int mdim, int exw, const int32_t* ex, double theta,
+               int ncrit, int p, int f, int dt, const double* dampf, const Opts& o) {
+    Workspace& ws = pl.ws;
+    FMM_CUDA_TRY(cudaGetDevice(&ws.device));
+    FMM_CUDA_TRY(cudaStreamCreateWithFlags(&pl.st, cudaStreamNonBlocking));
+    cudaStream_t st = pl.st;
+    pl.p = p;
+    pl.f = f;
+    pl.nf = nT(f);
+    pl.md = Modes{o.coef_mode, o.excl_mode, o.precision};
+    if (o.precision != 0) {  // as run_fmm: masked exclusions, exact tensors
+        pl.md.excl_mode = 1;
+        pl.md.coef_mode = 1;
+    }
+    pl.f32_near = o.precision == 1 || o.precision == 2;
+    FMM_TRY(ws.in_coords.ensure(sizeof(double) * 3 * n));
+    FMM_TRY(ws.in_mp.ensure(sizeof(double) * (size_t)mdim * n));
+    FMM_TRY(ws.in_excl.ensure(sizeof(int32_t) * (size_t)std::max(exw, 1) * n));
+    FMM_TRY(ws.in_damp.ensure(sizeof(double) * n));
+    FMM_TRY(ws.out_field.ensure(sizeof(double) * (size_t)pl.nf * n));
+    FMM_CUDA_TRY(cudaMemcpyAsync(ws.in_coords.p, X, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+    FMM_CUDA_TRY(cudaMemsetAsync(ws.in_mp.p, 0, sizeof(double) * (size_t)mdim * n, st));
+    if (exw > 0)
+        FMM_CUDA_TRY(cudaMemcpyAsync(ws.in_excl.p, ex, sizeof(int32_t) * (size_t)exw * n, cudaMemcpyHostToDevice, st));
+    const double* damp = dt != DAMP_NONE ? dampf : nullptr;
+    if (damp) FMM_CUDA_TRY(cudaMemcpyAsync(ws.in_damp.p, damp, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    pl.P = Particles{n, ws.in_coords.as<double>(), mdim, ws.in_mp.as<double>(), exw, ws.in_excl.as<int32_t>(),
+                     damp ? ws.in_damp.as<double>() : nullptr, dt};
+    pl.direct = n <= ncrit;
+    if (!pl.direct) {
+        TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode, 0.0, p};
+        if (o.centroid_mode == 0) {
+            host_centroid_sequential(X, n, tp.host_centroid);
+            tp.have_host_centroid = 1;
+        }
+        if (o.mac_mode == 1 && dt != DAMP_NONE && damp) {
+            const double dmin = min_damping_factor(ws, pl.P.damp, n, st);
+            tp.rdamp = damping_range(dt, dmin * dmin, dim_to_order(mdim) + f, 0.1 * o.target);
+        }
+        FMM_TRY(build_tree(ws, pl.P.x, n, tp, pl.t, st));
+        FMM_TRY(build_lists(ws, pl.t, tp, st));
+    }
+    // one evaluation builds the M2L structure and the cached tables ...
+    FMM_TRY(plan_numeric(pl));
+    FMM_CUDA_TRY(cudaStreamSynchronize(st));
+    // ... then the numeric kernels are captured
+    ws.reuse_structure = true;
+    cudaGraph_t g = nullptr;
+    FMM_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    const int rc = plan_numeric(pl);
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (rc != FMM_OK || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc != FMM_OK ? rc : FMM_ECUDA;
+    }
+    const int kst = count_kernel_nodes(g, &pl.kernels);
+    const cudaError_t ie = cudaGraphInstantiate(&pl.exec, g, 0);
+    cudaGraphDestroy(g);
+    FMM_TRY(kst);
+    if (ie != cudaSuccess) {
+        cudaGetLastError();
+        pl.exec = nullptr;
+        return FMM_ECUDA;
+    }
+    return FMM_OK;
+}
+
+int plan_launch(PlanImpl& pl) {
+    Workspace& ws = pl.ws;
+    FMM_CUDA_TRY(cudaGraphLaunch(pl.exec, pl.st));
+    int err = 0;
+    if (ws.product_err)
+        FMM_CUDA_TRY(cudaMemcpyAsync(&err, ws.product_err, sizeof(int), cudaMemcpyDeviceToHost, pl.st));
+    FMM_CUDA_TRY(cudaStreamSynchronize(pl.st));
+    FMM_CUDA_TRY(cudaGetLastError());
+    return err ? FMM_ETIMEOUT : FMM_OK;
 }
 
 }  // namespace
@@ -830,5 +975,65 @@ int fmm_field_fmm_batched(int nsys, const int64_t* offsets, const double* X, int
     dsys.release();
     return rc;
 }
+
+// Plans (see include/fmm_gpu.h).
+struct fmm_plan {
+    fmm::PlanImpl impl;
+};
+
+int fmm_plan_create(int64_t n, const double* X, int mdim, int exw, const int32_t* ex, double theta, int ncrit, int p,
+                    int field_order, const char* damp, int damp_len, const double* dampf, const fmm_opts* opts,
+                    fmm_plan** plan) {
+    if (!plan) return FMM_EINVAL;
+    *plan = nullptr;
+    int dt = 0;
+    FMM_TRY(parse_damp(damp, damp_len, &dt));
+    FMM_TRY(check_common(n, mdim, exw, field_order, dt, dampf));
+    FMM_TRY(check_exclusions_host(n, exw, ex));
+    Opts o;
+    FMM_TRY(parse_opts(opts, &o));
+    if (!X || ncrit < 1 || p < 0 || !(theta > 0.0)) return FMM_EINVAL;
+    if (p > kMaxP || o.selector != 0) return FMM_ENOTSUP;  // fixed acceptance rule only
+    if (o.precision != 0 && (dim_to_order(mdim) > 2 || field_order > 2)) return FMM_ENOTSUP;
+    fmm_plan* h = new (std::nothrow) fmm_plan;
+    if (!h) return FMM_ENOMEM;
+    const int st = plan_build(h->impl, n, X, mdim, exw, ex, theta, ncrit, p, field_order, dt, dampf, o);
+    if (st != FMM_OK) {
+        delete h;
+        return st;
+    }
+    *plan = h;
+    return FMM_OK;
+}
+
+int fmm_plan_execute(fmm_plan* plan, const double* mp, double* field) {
+    if (!plan || !mp || !field) return FMM_EINVAL;
+    PlanImpl& pl = plan->impl;
+    const Particles& P = pl.P;
+    FMM_CUDA_TRY(cudaMemcpyAsync(pl.ws.in_mp.p, mp, sizeof(double) * (size_t)P.dim * P.n, cudaMemcpyHostToDevice,
+                                 pl.st));
+    FMM_TRY(plan_launch(pl));
+    FMM_CUDA_TRY(cudaMemcpyAsync(field, pl.ws.out_field.p, sizeof(double) * (size_t)pl.nf * P.n,
+                                 cudaMemcpyDeviceToHost, pl.st));
+    FMM_CUDA_TRY(cudaStreamSynchronize(pl.st));
+    return FMM_OK;
+}
+
+int fmm_plan_execute_device(fmm_plan* plan, const double* d_mp, double* d_field) {
+    if (!plan || !d_mp || !d_field) return FMM_EINVAL;
+    PlanImpl& pl = plan->impl;
+    const Particles& P = pl.P;
+    FMM_CUDA_TRY(cudaMemcpyAsync(pl.ws.in_mp.p, d_mp, sizeof(double) * (size_t)P.dim * P.n, cudaMemcpyDeviceToDevice,
+                                 pl.st));
+    FMM_TRY(plan_launch(pl));
+    FMM_CUDA_TRY(cudaMemcpyAsync(d_field, pl.ws.out_field.p, sizeof(double) * (size_t)pl.nf * P.n,
+                                 cudaMemcpyDeviceToDevice, pl.st));
+    FMM_CUDA_TRY(cudaStreamSynchronize(pl.st));
+    return FMM_OK;
+}
+
+int fmm_plan_kernels(const fmm_plan* plan) { return plan ? plan->impl.kernels : -1; }
+
+void fmm_plan_destroy(fmm_plan* plan) { delete plan; }
 
 }  // extern "C"

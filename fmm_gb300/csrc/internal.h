@@ -152,6 +152,10 @@ struct Workspace {
     bool f32node_ok = false;     // f32node holds the FP32 node data of the current tree
     int* product_err = nullptr;  // device flag of the tensor-core M2L product, checked at the end of a call
     int64_t m2l_groups = 0;      // displacement groups of the last grouped M2L
+    // replays (plans): the tree, lists and M2L structure of the previous
+    // evaluation are kept and only the kernels that read multipoles run
+    bool reuse_structure = false;
+    int m2l_ng = 0, m2l_ntasks = 0;  // grouped M2L structure of the last evaluation
     int64_t list_candidates = 0; // cell pairs examined by the last list build
     int64_t list_evals = 0;      // of which evaluated by the selector network
     int device = -1;

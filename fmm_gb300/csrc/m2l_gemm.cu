@@ -899,8 +899,13 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
     const bool tc = sizeof(R) == 4 && !product_on_cuda_cores();
     const int cols = tc ? -1 : kTaskCols;  // -1: tensor-core tasks (256 pairs, one operator half)
     const int64_t nf = t.nfar;
+    const int ldw = wsc_ld<R>(nr);
+    const int ldk = (nr + 15) / 16 * 16;
+    const int ldT = nTr;
     const int32_t* roff = nullptr;  // row of each far pair (target order), units of 32 entries
-    if (nf > 0) {
+    if (nf > 0 && !ws.reuse_structure) {
+        // structure: displacement groups, their tensors and operators, tasks
+        // and result rows (geometry only; kept for replays)
         FMM_TRY(ws.m2l_tgt.ensure(sizeof(int32_t) * nf));
         FMM_TRY(ws.m2l_keys.ensure(sizeof(uint64_t) * nf));
         FMM_TRY(ws.m2l_keys2.ensure(sizeof(uint64_t) * nf));
@@ -909,14 +914,11 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_TRY(ws.m2l_ukeys.ensure(sizeof(uint64_t) * nf));
         FMM_TRY(ws.m2l_cnt.ensure(sizeof(int32_t) * (nf + 1)));
         FMM_TRY(ws.m2l_gstart.ensure(sizeof(int32_t) * (nf + 1)));
-        const int ldw = wsc_ld<R>(nr);
         FMM_TRY(ws.m2l_wsc.ensure(sizeof(R) * (size_t)M * ldw));
         FMM_TRY(ws.counters.ensure(sizeof(unsigned long long) * 32));
         int32_t* tgt = ws.m2l_tgt.as<int32_t>();
         count_launches(1);
         k_far_targets<<<grid_for(M, 4), 128, 0, st>>>(M, t.far_off, tgt);
-        count_launches(1);
-        k_scale_weights<R><<<grid_for(M, 4), 128, 0, st>>>(M, nr, ldw, ws.wred.as<double>(), t.r, ws.m2l_wsc.as<R>());
         count_launches(1);
         // FP32 node data where the mixed path prepared it
         const float4* chi = (sizeof(R) == 4 && ws.f32node_ok) ? ws.f32node.as<float4>() : nullptr;
@@ -949,7 +951,6 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb4, ws.m2l_cnt.as<int32_t>(),
                                                    ws.m2l_gstart.as<int32_t>(), ng + 1, st));
         // per-group tensors
-        const int ldT = nTr;
         FMM_TRY(ws.m2l_T.ensure(sizeof(R) * (size_t)ng * ldT));
         FMM_TRY(ws.m2l_gq.ensure(sizeof(int32_t) * ng));
         FMM_TRY(ws.m2l_gab.ensure(sizeof(float2) * ng));
@@ -992,7 +993,6 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         k_row_offsets<<<grid_for(ng, 8), 256, 0, st>>>(ng, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(),
                                                         rowbase, ws.m2l_vals2.as<int32_t>(),
                                                         reinterpret_cast<int32_t*>(ws.m2l_keys.p));
-        roff = reinterpret_cast<const int32_t*>(ws.m2l_keys.p);
         int hcnt[2] = {0, 0};  // tasks, rows (units of 32 entries)
         FMM_CUDA_TRY(cudaMemcpyAsync(&hcnt[0], ws.m2l_toff.as<int32_t>() + ng, sizeof(int), cudaMemcpyDeviceToHost, st));
         FMM_CUDA_TRY(cudaMemcpyAsync(&hcnt[1], rowbase + ng, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1003,14 +1003,8 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         count_launches(1);
         k_fill_tasks<<<grid_for(ng, 256), 256, 0, st>>>(ng, cols, ws.m2l_gq.as<int32_t>(), ws.m2l_gstart.as<int32_t>(),
                                                         ws.m2l_toff.as<int32_t>(), ws.m2l_tasks.as<int2>());
-        int* d_err = reinterpret_cast<int*>(ws.counters.as<unsigned long long>() + 13);
         if (tc) {
-            // TF32 parts of the weights (per node) and of the operators (per group)
-            const int ldk = (nr + 15) / 16 * 16;
             FMM_TRY(ws.m2l_wsplit.ensure(sizeof(float) * 2 * (size_t)M * ldk));
-            count_launches(1);
-            k_split_weights<<<grid_for((int64_t)M * ldk, 256), 256, 0, st>>>(
-                (int64_t)M * ldk, nr, ldw, ldk, reinterpret_cast<const float*>(ws.m2l_wsc.p), ws.m2l_wsplit.as<float>());
             // source node per sorted pair (into the free unsorted-values buffer)
             count_launches(1);
             k_pair_sources<<<grid_for(nf, 256), 256, 0, st>>>(nf, ws.m2l_vals2.as<int32_t>(), t.far_src,
@@ -1023,8 +1017,8 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
             cub::DeviceScan::ExclusiveSum(nullptr, tb6, goff, goff, ng + 1, st);
             FMM_TRY(ws.cub_tmp.ensure(tb6));
             FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb6, goff, goff, ng + 1, st));
-            // room for every group at the largest order of the call (no wait
-            // for the exact total)
+            // TF32 parts of the operators (per group), room for every group at
+            // the largest order of the call (no wait for the exact total)
             const int nr_max = (p + 1) * (p + 1);
             const size_t gop_max = (size_t)ng * tc_halves(p) * ((nr_max + kTcKC - 1) / kTcKC) * 2 * kTcRows * kTcKC;
             FMM_TRY(ws.m2l_gop.ensure(sizeof(float) * std::max<size_t>(1, gop_max)));
@@ -1032,6 +1026,23 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
             k_group_operator<<<(unsigned)ng, 256, 0, st>>>(ldT, reinterpret_cast<const float*>(ws.m2l_T.p),
                                                            ws.m2l_gq.as<int32_t>(), ws.m2l_gab.as<float2>(), goff,
                                                            ws.m2l_gop.as<float>());
+        }
+        ws.m2l_ng = ng;
+        ws.m2l_ntasks = ntasks;
+    }
+    if (nf > 0) {
+        // numeric: scaled weights, the product, (below) the per-target sums
+        const int ntasks = ws.m2l_ntasks;
+        const int32_t* rowbase = ws.m2l_rowbase.as<int32_t>();
+        roff = reinterpret_cast<const int32_t*>(ws.m2l_keys.p);
+        count_launches(1);
+        k_scale_weights<R><<<grid_for(M, 4), 128, 0, st>>>(M, nr, ldw, ws.wred.as<double>(), t.r, ws.m2l_wsc.as<R>());
+        int* d_err = reinterpret_cast<int*>(ws.counters.as<unsigned long long>() + 13);
+        if (tc) {
+            // TF32 parts of the weights (per node)
+            count_launches(1);
+            k_split_weights<<<grid_for((int64_t)M * ldk, 256), 256, 0, st>>>(
+                (int64_t)M * ldk, nr, ldw, ldk, reinterpret_cast<const float*>(ws.m2l_wsc.p), ws.m2l_wsplit.as<float>());
             FMM_CUDA_TRY(cudaFuncSetAttribute((const void*)k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)TcSmem::bytes));
             int dev = 0, sms = 0;
@@ -1045,9 +1056,9 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
             }
             count_launches(1);
             k_m2l_tc<<<(unsigned)grid, kTcThreads, TcSmem::bytes, st>>>(
-                ws.m2l_tasks.as<int2>(), ntasks, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(), goff,
-                ws.m2l_gop.as<float>(), ws.m2l_vals.as<int32_t>(), ws.m2l_wsplit.as<float>(), ldk,
-                reinterpret_cast<float*>(ws.m2l_out.p), rowbase, d_err);
+                ws.m2l_tasks.as<int2>(), ntasks, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(),
+                ws.m2l_gopoff.as<int64_t>(), ws.m2l_gop.as<float>(), ws.m2l_vals.as<int32_t>(),
+                ws.m2l_wsplit.as<float>(), ldk, reinterpret_cast<float*>(ws.m2l_out.p), rowbase, d_err);
             if (ws.product_timed) cudaEventRecord(ws.ev[9], st);
             // the product's error flag is read with the call's final copies
             ws.product_err = d_err;

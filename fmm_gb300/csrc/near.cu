@@ -31,10 +31,12 @@ int num_sms() {
     return sms;
 }
 
-// Contraction coefficients c_s of the multipole components (order <= 2),
+// Contraction coefficients c_s of the multipole components (order <= 3),
 // folded at compile time (no FP64 division per element).
-__constant__ double cSrcCoef[10] = {src_coef(0), src_coef(1), src_coef(2), src_coef(3), src_coef(4),
-                                    src_coef(5), src_coef(6), src_coef(7), src_coef(8), src_coef(9)};
+__constant__ double cSrcCoef[20] = {src_coef(0),  src_coef(1),  src_coef(2),  src_coef(3),  src_coef(4),
+                                    src_coef(5),  src_coef(6),  src_coef(7),  src_coef(8),  src_coef(9),
+                                    src_coef(10), src_coef(11), src_coef(12), src_coef(13), src_coef(14),
+                                    src_coef(15), src_coef(16), src_coef(17), src_coef(18), src_coef(19)};
 
 // Multipoles times the contraction coefficient c_s, original particle order.
 __global__ void k_scale_mp(int64_t n, int dim, const double* __restrict__ mp, double* __restrict__ out) {
@@ -303,7 +305,7 @@ __global__ void k_scatter(int64_t n, int nf, const uint32_t* __restrict__ perm, 
 
 }  // namespace
 
-bool near_orders_supported(int m, int f) { return m >= 0 && m <= 2 && f >= 0 && f <= 2; }
+bool near_orders_supported(int m, int f) { return m >= 0 && m <= 3 && f >= 0 && f <= 3; }
 
 int launch_direct_f64(Workspace& ws, const Particles& P, int field_order, const Modes& md, double* d_field,
                       cudaStream_t st, int64_t ntgt, const int64_t* d_targets, int split_cap) {
@@ -327,11 +329,11 @@ int launch_direct_f64(Workspace& ws, const Particles& P, int field_order, const 
     FMM_TRY(ws.partial.ensure(sizeof(double) * (size_t)ks * nf * ntgt));
     dim3 grid((unsigned)tblocks, (unsigned)ks);
     if (few) {
-        FMM_MF_SWITCH(m, field_order, (k_direct_few<MM, FF><<<grid, 128, 0, st>>>(n, d_targets, ntgt, P.x, mc, P.damp,
+        FMM_MF_SWITCH_F64(m, field_order, (k_direct_few<MM, FF><<<grid, 128, 0, st>>>(n, d_targets, ntgt, P.x, mc, P.damp,
                                                                                    P.damp_type, chunk,
                                                                                    ws.partial.as<double>())));
     } else {
-        FMM_MF_SWITCH(m, field_order, (k_direct_f64<MM, FF><<<grid, 128, 0, st>>>(n, d_targets, ntgt, P.x, mc,
+        FMM_MF_SWITCH_F64(m, field_order, (k_direct_f64<MM, FF><<<grid, 128, 0, st>>>(n, d_targets, ntgt, P.x, mc,
                                                                                    P.damp, P.damp_type, chunk,
                                                                                    ws.partial.as<double>())));
     }
@@ -339,7 +341,7 @@ int launch_direct_f64(Workspace& ws, const Particles& P, int field_order, const 
     k_direct_reduce<<<grid_for(ntgt, 256), 256, 0, st>>>(ntgt, nf, (int)ks, ws.partial.as<double>(), nullptr, ntgt,
                                                          d_field);
     if (P.exw > 0 || md.excl_mode == 0) {
-        FMM_MF_SWITCH(m, field_order,
+        FMM_MF_SWITCH_F64(m, field_order,
                       (k_excl_fix<MM, FF><<<grid_for(ntgt, 128), 128, 0, st>>>(
                           n, ntgt, d_targets, P.x, mc, P.exw, P.excl, P.damp, P.damp_type, md.excl_mode, nullptr,
                           nullptr, nullptr, nullptr, d_field, ntgt, 0)));
@@ -376,13 +378,13 @@ int launch_p2p_f64(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
     FMM_TRY(ws.fsorted.ensure(sizeof(double) * (size_t)n * nf));
     const unsigned blocks = grid_for((int64_t)t.num_leaves * 32, 128);
     if (image) {
-        FMM_MF_SWITCH(m, field_order,
+        FMM_MF_SWITCH_F64(m, field_order,
                       (k_p2p_f64<MM, FF, true><<<blocks, 128, 0, st>>>(t, ws.sx.as<double>(), ws.sy.as<double>(),
                                                                        ws.sz.as<double>(), ws.sd.as<double>(),
                                                                        ws.smc.as<double>(), n, P.damp_type,
                                                                        ws.fsorted.as<double>())));
     } else {
-        FMM_MF_SWITCH(m, field_order,
+        FMM_MF_SWITCH_F64(m, field_order,
                       (k_p2p_f64<MM, FF, false><<<blocks, 128, 0, st>>>(t, ws.sx.as<double>(), ws.sy.as<double>(),
                                                                         ws.sz.as<double>(), ws.sd.as<double>(),
                                                                         ws.smc.as<double>(), n, P.damp_type,
@@ -397,7 +399,7 @@ int launch_excl_correction(Workspace& ws, const Particles& P, const TreeDev* t, 
     const int m = dim_to_order(P.dim);
     const int64_t n = P.n;
     const double* mc_orig = ws.smc.as<double>() + (size_t)n * P.dim;
-    FMM_MF_SWITCH(m, field_order,
+    FMM_MF_SWITCH_F64(m, field_order,
                   (k_excl_fix<MM, FF><<<grid_for(n, 128), 128, 0, st>>>(
                       n, n, nullptr, P.x, mc_orig, P.exw, P.excl, P.damp, P.damp_type, md.excl_mode, t->pos_of,
                       t->leaf_of, t->near_off, t->near_src, d_field, n,

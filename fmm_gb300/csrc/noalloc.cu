@@ -232,7 +232,7 @@ extern "C" int fmm_field_direct_targets_noalloc(int64_t n, const double* d_X, in
     if (n < 1 || n > (int64_t)INT32_MAX - 1 || m < 0 || exw < 0 || field_order < 0 || ntgt < 1 || !d_targets ||
         !d_X || !d_mp || !d_field)
         return FMM_EINVAL;
-    if (m > 2 || field_order > 2) return FMM_ENOTSUP;
+    if (m > 3 || field_order > 3) return FMM_ENOTSUP;
     if (dt != DAMP_NONE && !d_damp) return FMM_EINVAL;
     if (exw > 0 && !d_ex) return FMM_EINVAL;
     int excl_mode = 0;
@@ -265,13 +265,13 @@ extern "C" int fmm_field_direct_targets_noalloc(int64_t n, const double* d_X, in
         k_check_excl_static<<<cb, 256, 0, st>>>(n, exw, d_ex, status);
     }
     dim3 grid((unsigned)tblocks, (unsigned)ks);
-    FMM_MF_SWITCH(m, field_order,
+    FMM_MF_SWITCH_F64(m, field_order,
                   (k_direct_static<MM, FF><<<grid, 128, 0, st>>>(n, d_targets, ntgt, d_X, d_mp, dd, dt, chunk,
                                                                  partial, status)));
     count_launches(1);
     k_reduce_static<<<grid_for(ntgt, 256), 256, 0, st>>>(ntgt, nf, (int)ks, partial, d_field);
     if (exw > 0 || excl_mode == 0) {
-        FMM_MF_SWITCH(m, field_order,
+        FMM_MF_SWITCH_F64(m, field_order,
                       (k_excl_static<MM, FF><<<grid_for(ntgt, 128), 128, 0, st>>>(
                           n, ntgt, d_targets, d_X, d_mp, exw, d_ex, dd, dt, excl_mode, d_field, status)));
     }

@@ -229,7 +229,7 @@ int fmm_get_multipoles(int comm, int64_t n, const double* X, int mdim, int ndens
         return FMM_EINVAL;
     const int m = dim_to_order(mdim);
     if (m < 0) return FMM_EINVAL;
-    if (m > 2 || p > kMaxP) return FMM_ENOTSUP;
+    if (m > 3 || p > kMaxP) return FMM_ENOTSUP;
     cudaStream_t st;
     FMM_TRY(parse_stream(opts, &st));
     Workspace& ws = thread_workspace();

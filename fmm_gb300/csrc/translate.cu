@@ -578,7 +578,7 @@ __global__ void __launch_bounds__(kL2pThreads) k_l2p(const TreeDev t, const doub
                                                      const double* __restrict__ loc, double* __restrict__ fs) {
     extern __shared__ __align__(16) unsigned char sm_l2p_raw[];
     __shared__ double hp[kMaxP + 1];  // h^k
-    __shared__ int seg[nT(2) + 1];
+    __shared__ int seg[nT(3) + 1];  // field order <= 3
     R* coef = reinterpret_cast<R*>(sm_l2p_raw);
     const int nq = nT(p), nf = v.nf;
     const int leaf = t.leaves[blockIdx.x];
@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(kL2pThreads) k_l2p(const TreeDev t, const doub
             hx = hx * dx + hy;
         }
         double s = 1.0;
-        for (int a = 0; a < kt; ++a) s *= ih;  // kt <= 2
+        for (int a = 0; a < kt; ++a) s *= ih;  // kt <= 3
         fs[(size_t)tq * n + k] += (double)hx * s;
     }
 }
@@ -669,11 +669,14 @@ int launch_p2m_m2m(Workspace& ws, const Particles& P, const TreeDev& t, int p, c
         if (df) {
             if (nm == 1) FMM_TRY((launch_p2m<true, 1, 128>(ws, P, t, p, tab, v, mom, st)));
             else if (nm == 4) FMM_TRY((launch_p2m<true, 4, 128>(ws, P, t, p, tab, v, mom, st)));
-            else FMM_TRY((launch_p2m<true, 10, 128>(ws, P, t, p, tab, v, mom, st)));
+            else if (nm == 10) FMM_TRY((launch_p2m<true, 10, 128>(ws, P, t, p, tab, v, mom, st)));
+            else return FMM_ENOTSUP;  // the double-float path takes multipole orders <= 2
         } else {
             if (nm == 1) FMM_TRY((launch_p2m<false, 1, 256>(ws, P, t, p, tab, v, mom, st)));
             else if (nm == 4) FMM_TRY((launch_p2m<false, 4, 256>(ws, P, t, p, tab, v, mom, st)));
-            else FMM_TRY((launch_p2m<false, 10, 256>(ws, P, t, p, tab, v, mom, st)));
+            else if (nm == 10) FMM_TRY((launch_p2m<false, 10, 256>(ws, P, t, p, tab, v, mom, st)));
+            else if (nm == 20) FMM_TRY((launch_p2m<false, 20, 256>(ws, P, t, p, tab, v, mom, st)));
+            else return FMM_ENOTSUP;
         }
     }
     {

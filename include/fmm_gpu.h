@@ -19,6 +19,10 @@
  *                                         NULL when damp_type is empty
  * field(:,1) is minus the potential, field(:,2:4) the electric field, and
  * the order-k block minus the k-th derivative of the potential.
+ * Orders: multipole order m <= 3 (mdim <= 20) and field order f <= 3 in FP64;
+ * the mixed-precision and learned paths take m <= 2 and f <= 2 (otherwise
+ * FMM_ENOTSUP).  Damped kernels stop at tensor order 6 (m + f <= 6 always
+ * holds here), as the reference's damped tensors do.
  *
  * `damp` is the reference's damp_type: "AMOEBA", "THOLE", "ERF" or "" (any
  * trailing blanks are ignored, as Fortran's trim() does), with length
@@ -119,7 +123,7 @@ int fmm_field_fmm(int comm, int64_t n, const double *coordinates, int mdim, cons
  * zeroed first, the reference adds into it).  The reference's own helpers stop
  * in their final clean-up (fmm.F90:301-326 deallocates interaction lists
  * that they never build); these return their results.  Host pointers;
- * multipoles of order <= 2. */
+ * multipoles of order <= 3. */
 int fmm_get_boxes(int64_t n, const double *coordinates, int64_t ntgt, const double *target_coordinates,
                   double theta, int ncrit, int expansion_order, int64_t *sizes, int32_t *idx_near_field,
                   double *box_coordinates, int32_t *box_indices, const fmm_opts *opts);
@@ -266,6 +270,26 @@ int fmm_mlp_train(float *params, const float *x, const float *y, int64_t n, int 
 int fmm_selector_collect(int64_t n, const double *coordinates, int mdim, const double *multipoles,
                          const double *damping_factors, int ncrit, double theta, int max_pairs, uint64_t seed,
                          float *features, float *labels, int *npairs, int32_t *pairs);
+
+/* Plans (no counterpart in the reference): for fixed coordinates,
+ * exclusions, damping factors and settings, fmm_plan_create builds the octree,
+ * the interaction lists and the M2L grouping once (arguments as
+ * fmm_field_fmm; fixed acceptance rule, opts->selector must be 0; no periodic
+ * boxes) and captures the kernels that read the multipoles into a CUDA graph.
+ * fmm_plan_execute then evaluates the field of one multipole set (n x mdim,
+ * host arrays) by one graph launch, with the results fmm_field_fmm gives for
+ * the same inputs; fmm_plan_execute_device takes device arrays.  A plan owns
+ * its device memory and stream; calls on one plan must not overlap.  Made for
+ * fields of many multipole sets at fixed coordinates (induced dipoles in a
+ * polarisation solver).  fmm_plan_kernels: kernel launches per evaluation. */
+typedef struct fmm_plan fmm_plan;
+int fmm_plan_create(int64_t n, const double *coordinates, int mdim, int exw, const int32_t *exclusions, double theta,
+                    int ncrit, int expansion_order, int field_order, const char *damp, int damp_len,
+                    const double *damping_factors, const fmm_opts *opts, fmm_plan **plan);
+int fmm_plan_execute(fmm_plan *plan, const double *multipoles, double *field);
+int fmm_plan_execute_device(fmm_plan *plan, const double *d_multipoles, double *d_field);
+int fmm_plan_kernels(const fmm_plan *plan);
+void fmm_plan_destroy(fmm_plan *plan);
 
 /* Human-readable text for a status code. */
 const char *fmm_strerror(int status);

@@ -154,6 +154,11 @@ CASES = {
     "water_amoeba": ("water", 50, 14.5, 2, "AMOEBA", 0.5, 8, 8, 1, False, 13),
     "uniform_erf": ("uniform", 240, 14.0, 1, "ERF", 0.5, 10, 5, 1, False, 14),
     "uniform_charges": ("uniform", 300, 16.0, 0, "", 0.6, 12, 5, 2, False, 15),
+    # octupoles (mdim 20) and field order 3: damped tensors up to order 6
+    "uniform_octupole_f3": ("uniform", 120, 12.0, 3, "", 0.5, 10, 5, 3, False, 19),
+    "water_octupole_thole_f3": ("water", 30, 11.0, 3, "THOLE", 0.5, 8, 4, 3, False, 20),
+    "water_amoeba_f3": ("water", 30, 11.0, 2, "AMOEBA", 0.5, 8, 4, 3, False, 21),
+    "uniform_octupole_erf": ("uniform", 90, 11.0, 3, "ERF", 0.5, 10, 4, 1, False, 22),
     # periodic boxes (is_periodic = .true.): particles inside the cell of BOXES[name]
     "periodic_cubic": ("water", 36, 11.0, 2, "", 0.5, 8, 4, 1, False, 16),
     "periodic_triclinic_thole": ("water", 30, 10.5, 2, "THOLE", 0.5, 8, 5, 2, False, 17),

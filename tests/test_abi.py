@@ -63,7 +63,8 @@ def test_host_side_argument_checks(L):
     assert _call_fmm(L, excl=bad) == _lib.FMM_EINVAL
     assert _call_fmm(L, excl=-bad) == _lib.FMM_EINVAL
     assert _call_fmm(L, mdim=7) == _lib.FMM_EINVAL
-    assert _call_fmm(L, mdim=20) == _lib.FMM_ENOTSUP
+    assert _call_fmm(L, mdim=35) == _lib.FMM_ENOTSUP  # multipole order 4
+    assert _call_fmm(L, f=4) == _lib.FMM_ENOTSUP
     assert _call_fmm(L, periodic=1) == _lib.FMM_EINVAL  # periodic without a box matrix
 
 

@@ -24,7 +24,8 @@ def _fmm_args(s):
 
 
 @pytest.mark.parametrize("damp", ["", "THOLE", "AMOEBA", "ERF"])
-@pytest.mark.parametrize("mf", [(0, 0), (0, 1), (1, 1), (2, 1), (2, 2), (1, 2)])
+@pytest.mark.parametrize("mf", [(0, 0), (0, 1), (1, 1), (2, 1), (2, 2), (1, 2), (3, 0), (3, 1), (0, 3), (2, 3),
+                                (3, 3)])
 @pytest.mark.parametrize("excl", ["ref", "mask"])
 def test_direct_matches_oracle(damp, mf, excl):
     m, f = mf
@@ -113,6 +114,36 @@ def test_fmm_ref_mode_matches_oracle_damped(damp, p, f):
     O = oracle.field_fmm(*_fmm_args(s), 0.5, 32, p, f, damp, d)
     cols = slice(1, None) if damp == "AMOEBA" else slice(0, None)
     assert rel_err(G, O, cols) <= TOL
+
+
+@pytest.mark.parametrize("damp", ["", "THOLE", "AMOEBA", "ERF"])
+@pytest.mark.parametrize("mf", [(3, 1), (2, 3), (3, 3)])
+@pytest.mark.parametrize("coef", ["ref", "exact"])
+def test_fmm_higher_orders_match_oracle(damp, mf, coef):
+    """Octupole sources (mdim 20) and field order 3 (damped tensors up to
+    order 6), FP64, both coefficient modes."""
+    m, f = mf
+    s = small_system(1500, 30.0, order=m, seed=31, damp=damp)
+    d = s["damping_factors"] if damp else None
+    if coef == "ref":
+        G = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, 6, f, damp, d)
+        O = oracle.field_fmm(*_fmm_args(s), 0.5, 32, 6, f, damp, d)
+    else:
+        G = fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, 7, f, damp, d, options=Options.exact())
+        O = oracle.field_fmm(*_fmm_args(s), 0.5, 32, 7, f, damp, d, coef_mode="exact", excl_mode="mask",
+                             centroid_mode="blocked")
+    cols = slice(1, None) if damp == "AMOEBA" else slice(0, None)
+    assert np.all(np.isfinite(G[:, cols]))
+    assert rel_err(G, O, cols) <= TOL
+
+
+def test_higher_orders_refused_by_the_mixed_path():
+    s = small_system(600, 20.0, order=3, seed=32)
+    with pytest.raises(fmm_gb300.FmmError):
+        fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, 6, 1, options=Options(precision="mixed"))
+    s = small_system(600, 20.0, order=2, seed=32)
+    with pytest.raises(fmm_gb300.FmmError):
+        fmm_gb300.field_fmm(*_fmm_args(s), 0.5, 32, 6, 3, options=Options(precision="mixed"))
 
 
 @pytest.mark.parametrize("damp", ["", "THOLE"])

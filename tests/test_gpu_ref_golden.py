@@ -21,7 +21,8 @@ pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_fields.npz")
 DAMP_NAMES = {0: "", 1: "AMOEBA", 2: "THOLE", 3: "ERF"}
-CASES = ["water_none", "water_thole", "water_amoeba", "uniform_erf", "uniform_charges"]
+CASES = ["water_none", "water_thole", "water_amoeba", "uniform_erf", "uniform_charges", "uniform_octupole_f3",
+         "water_octupole_thole_f3", "water_amoeba_f3", "uniform_octupole_erf"]
 PERIODIC = ["periodic_cubic", "periodic_triclinic_thole", "periodic_amoeba_p6"]
 
 

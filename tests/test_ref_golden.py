@@ -116,7 +116,8 @@ def _case(fields, name):
                 p=int(p), f=int(f), damp=damp, periodic=bool(np.any(box)), box=box)
 
 
-CASES = ["water_none", "water_thole", "water_amoeba", "uniform_erf", "uniform_charges"]
+CASES = ["water_none", "water_thole", "water_amoeba", "uniform_erf", "uniform_charges", "uniform_octupole_f3",
+         "water_octupole_thole_f3", "water_amoeba_f3", "uniform_octupole_erf"]
 PERIODIC = ["periodic_cubic", "periodic_triclinic_thole", "periodic_amoeba_p6"]
 
 
