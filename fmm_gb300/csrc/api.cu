@@ -351,7 +351,7 @@ double sampled_rms(const std::vector<double>& F, const std::vector<double>& R, i
 // surface term (fmm.F90:884-979), before L2L and L2P.  FP64 and the fixed
 // acceptance rule only.
 int run_periodic(Workspace& ws, const Particles& P, int p, int f, const Modes& md, const TreeParams& tpl, TreeDev& t,
-                 const Box9& box, cudaStream_t st, int* levels) {
+                 const Box9& box, cudaStream_t st, int* levels, unsigned long long* d_hist) {
     const int64_t n = P.n;
     const int nf = nT(f), nq = nT(p);
     FMM_TRY(ws.fsorted.ensure(sizeof(double) * (size_t)n * nf));
@@ -367,6 +367,11 @@ int run_periodic(Workspace& ws, const Particles& P, int p, int f, const Modes& m
                     t.shift[c] = (box.h[c] * ai + box.h[3 + c] * aj) + box.h[6 + c] * ak;
                 t.central = (ai == 0 && aj == 0 && ak == 0) ? 1 : 0;
                 FMM_TRY(build_lists(ws, t, tpl, st));
+                if (t.nfar > 0 && t.far_ord) {  // far pairs per order, summed over the images
+                    count_launches(1);
+                    k_order_hist<<<(unsigned)std::min<int64_t>(1024, (t.nfar + 255) / 256), 256, 0, st>>>(
+                        t.nfar, t.far_ord, d_hist);
+                }
                 FMM_TRY(launch_p2p_f64(ws, P, t, f, md, st, true));
                 if (t.central) FMM_TRY(launch_excl_correction(ws, P, &t, f, md, ws.fsorted.as<double>(), st));
                 FMM_TRY(launch_m2l_pairwise(ws, t, p, md, true, st));
@@ -411,6 +416,11 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     TreeDev t;
     const int nf = nT(f);
     ws.product_err = nullptr;  // set by the tensor-core M2L product, read at the end of the call
+    // device counters: flags and counts of the phases (0..15), far pairs per
+    // expansion order (16..31)
+    FMM_TRY(ws.counters.ensure(sizeof(unsigned long long) * 32));
+    unsigned long long* d_hist = ws.counters.as<unsigned long long>() + 16;
+    FMM_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(unsigned long long) * 16, st));
     cudaEventRecord(ws.ev[0], st);
     FMM_TRY(build_tree(ws, P.x, P.n, tp, t, st));
     cudaEventRecord(ws.ev[1], st);
@@ -468,7 +478,7 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     double check_rms = -1.0;
     int lattice_levels = 0;
     if (box) {
-        FMM_TRY(run_periodic(ws, P, p, f, md, tpl, t, *box, st, &lattice_levels));
+        FMM_TRY(run_periodic(ws, P, p, f, md, tpl, t, *box, st, &lattice_levels, d_hist));
         for (int k = 3; k <= 5; ++k) cudaEventRecord(ws.ev[k], st);
         cudaEventRecord(ws.ev[7], st);
         FMM_TRY(scatter_field(ws, t, P.n, nf, d_field, st));
@@ -530,10 +540,9 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     cudaEventRecord(ws.ev[6], st);
     // far pairs per expansion order (outside the timed phases)
     unsigned long long hist[16] = {0};
-    FMM_TRY(ws.counters.ensure(sizeof(unsigned long long) * 32));
-    unsigned long long* d_hist = ws.counters.as<unsigned long long>() + 16;
-    FMM_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(hist), st));
-    if (t.nfar > 0 && t.far_ord) {
+    // (periodic boxes: summed image by image; t.nfar is then the total over
+    // the images while t.far_ord holds only the last image's pairs)
+    if (!box && t.nfar > 0 && t.far_ord) {
         count_launches(1);
         k_order_hist<<<(unsigned)std::min<int64_t>(1024, (t.nfar + 255) / 256), 256, 0, st>>>(t.nfar, t.far_ord,
                                                                                                     d_hist);

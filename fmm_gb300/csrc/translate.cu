@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_p2m(const TreeDev t, const dou
             uy[r] = uy_(c);
             uz[r] = uz_(c);
             const int rem = p - ux[r] - uy[r] - uz[r];
-            ns[r] = rem >= 2 ? NM : min(NM, nT(rem));
+            ns[r] = min(NM, nT(rem));  // moments of orders <= rem
         }
     }
     typename O::Acc acc[KS][NM];
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_p2m(const TreeDev t, const dou
             for (int r = 0; r < KS; ++r) {
                 if (ns[r] == 0) continue;
                 const V dp = O::mul(O::mul(eb[ux[r]], eb[P1 + uy[r]]), eb[2 * P1 + uz[r]]);
-                if (ns[r] == NM) {  // every moment (all but the top two orders of u)
+                if (ns[r] == NM) {  // every moment (u of order <= p - m)
 #pragma unroll
                     for (int sidx = 0; sidx < NM; ++sidx) acc[r][sidx].mac(dp, m[sidx]);
                 } else {

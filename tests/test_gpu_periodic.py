@@ -48,8 +48,11 @@ def test_periodic_matches_oracle(damp, p, f, cell, mode):
         O = oracle.field_fmm(*args, 0.5, 24, p, f, damp, d, True, box, coef_mode="exact", excl_mode="mask")
     assert np.all(np.isfinite(G))
     assert rel_err(G, O, slice(1, None)) <= 1e-12
-    levels = fmm_gb300.last_stats()["lattice_levels"]
+    st = fmm_gb300.last_stats()
+    levels = st["lattice_levels"]
     assert levels == oracle.last_lattice_levels()
+    # far pairs of all 27 images, counted by expansion order image by image
+    assert sum(st["m2l_pairs_q%d" % q] for q in range(13)) == st["m2l_pairs"] > 0
     var, const = potential_up_to_constant(G, O)
     assert var <= 1e-12
     if levels < 50:
