@@ -18,7 +18,8 @@ from ._lib import FmmError
 
 __all__ = ["field_direct", "field_fmm", "field_fmm_batched", "field_direct_device", "field_fmm_device", "Options",
            "last_stats", "n_components", "FmmError", "version", "load_selector", "release_workspace", "get_boxes",
-           "get_multipoles", "interpolate_electron_fields", "Plan"]
+           "get_multipoles", "interpolate_electron_fields", "Plan",
+           "set_p2p_shape"]
 
 
 def n_components(order):
@@ -41,6 +42,7 @@ class Options:
     selector: str = "fixed"       # "fixed" | "learned"
     target_rel_err: float = 1e-6
     stream: int = 0               # cudaStream_t for the *_device calls
+    autotune: bool = False        # ncrit and near-field launch shape timed per class of calls
 
     @classmethod
     def exact(cls, **kw):
@@ -59,6 +61,7 @@ class Options:
         o.selector = {"fixed": 0, "learned": 1}[self.selector]
         o.target_rel_err = float(self.target_rel_err)
         o.stream = int(self.stream) or None
+        o.autotune = 1 if self.autotune else 0
         return o
 
 
@@ -158,6 +161,12 @@ def field_fmm(comm, coordinates, multipoles, exclusions, theta, ncrit, expansion
                                   _dptr(box) if box is not None else None, ctypes.byref(o))
     _lib.check(st, "field_fmm")
     return F
+
+
+def set_p2p_shape(threads=0, stage=0, queue=0):
+    """Launch shape of the mixed-precision near field for this thread's later
+    calls (fmm_set_p2p_shape); no arguments restores the default."""
+    _lib.check(_lib.lib().fmm_set_p2p_shape(int(threads), int(stage), int(queue)), "set_p2p_shape")
 
 
 class Plan:
@@ -292,7 +301,8 @@ def field_fmm_device(coordinates, multipoles, exclusions, theta, ncrit, expansio
 STAT_NAMES = ["num_nodes", "num_leaves", "max_depth", "m2l_pairs", "p2p_leaf_pairs", "p2p_particle_pairs", "t_tree",
               "t_p2m_m2m", "t_lists", "t_p2p", "t_m2l", "t_l2l_l2p", "t_total", "selector_fallback",
               "sampled_rms_err", "m2l_order_mean"] + ["m2l_pairs_q%d" % q for q in range(13)] + \
-             ["t_p2p_kernel", "t_m2l_product", "m2l_groups", "list_candidates", "list_evals", "lattice_levels"]
+             ["t_p2p_kernel", "t_m2l_product", "m2l_groups", "list_candidates", "list_evals", "lattice_levels",
+              "ncrit_used", "p2p_threads", "p2p_stage", "p2p_queue", "tuned"]
 
 
 def last_stats():

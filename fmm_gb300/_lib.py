@@ -34,7 +34,8 @@ class FmmOpts(ctypes.Structure):
         ("selector", ctypes.c_int),
         ("target_rel_err", ctypes.c_double),
         ("stream", ctypes.c_void_p),
-        ("reserved", ctypes.c_int * 8),
+        ("autotune", ctypes.c_int),
+        ("reserved", ctypes.c_int * 7),
     ]
 
 
@@ -62,6 +63,7 @@ EXPORTED = [
     "fmm_mlp_grad",
     "fmm_mlp_train",
     "fmm_selector_collect",
+    "fmm_set_p2p_shape",
     "fmm_plan_create",
     "fmm_plan_execute",
     "fmm_plan_execute_device",
@@ -119,6 +121,8 @@ def lib():
     L.fmm_interpolate_electron_fields.argtypes = [c, i64, d, i64, c, d, vp, ctypes.c_double, c, c, c, d, op]
     L.fmm_interpolate_electron_fields.restype = c
     L.fmm_release_workspace.restype = c
+    L.fmm_set_p2p_shape.argtypes = [c, c, c]
+    L.fmm_set_p2p_shape.restype = c
     L.fmm_plan_create.argtypes = [i64, d, c, c, i32, ctypes.c_double, c, c, c, cs, c, d, op,
                                   ctypes.POINTER(ctypes.c_void_p)]
     L.fmm_plan_create.restype = c

@@ -5,6 +5,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <thread>
@@ -45,7 +47,7 @@ void Workspace::release_buffers(bool keep_selector) {
                      &sz,        &smc,       &sd,          &fsorted,    &mom,        &loc,        &partial,
                      &term_off,  &term_abc,  &term_c, &f32buf, &wred, &far_ord, &sel_norms, &sel_params, &sel_scratch, &sysbuf,
                      &m2l_tgt, &m2l_keys, &m2l_keys2, &m2l_vals, &m2l_vals2, &m2l_ukeys, &m2l_cnt, &m2l_gstart,
-                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &m2l_wsplit, &m2l_gop, &m2l_gopoff, &m2l_rowbase, &xlate, &l2pt, &dsmc, &f32node, &lattice};
+                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &m2l_wsplit, &m2l_gop, &m2l_gopoff, &m2l_rowbase, &xlate, &l2pt, &dsmc, &f32node, &lattice, &p2p_order};
     for (DevBuf* b : all)
         if (!(keep_selector && b == &sel_params)) b->release();
     if (!keep_selector) sel_ready = false;
@@ -77,7 +79,8 @@ Workspace& thread_workspace() {
 
 namespace {
 
-constexpr int kNumStats = 16 + kMaxP + 1 + 6;
+constexpr int kNumStats = 16 + kMaxP + 1 + 6 + 5;
+constexpr int kTuneStats = 16 + kMaxP + 1 + 6;  // ncrit used, near-field shape (3), tuned by this call
 struct Stats {
     double v[kNumStats] = {0};
 };
@@ -97,7 +100,7 @@ int parse_damp(const char* s, int len, int* out) {
 }
 
 struct Opts {
-    int coef_mode = 0, excl_mode = 0, precision = 0, centroid_mode = 0, mac_mode = 0, selector = 0;
+    int coef_mode = 0, excl_mode = 0, precision = 0, centroid_mode = 0, mac_mode = 0, selector = 0, autotune = 0;
     double target = 1e-6;
     cudaStream_t stream = nullptr;
 };
@@ -107,7 +110,7 @@ int parse_opts(const fmm_opts* o, Opts* out) {
     if (o->version != 0 && o->version != 1) return FMM_EINVAL;
     if (o->coef_mode < 0 || o->coef_mode > 1 || o->excl_mode < 0 || o->excl_mode > 1 || o->precision < 0 ||
         o->precision > 3 || o->centroid_mode < 0 || o->centroid_mode > 1 || o->mac_mode < 0 || o->mac_mode > 1 ||
-        o->selector < 0 || o->selector > 1)
+        o->selector < 0 || o->selector > 1 || o->autotune < 0 || o->autotune > 1)
         return FMM_EINVAL;
     out->coef_mode = o->coef_mode;
     out->excl_mode = o->excl_mode;
@@ -115,6 +118,7 @@ int parse_opts(const fmm_opts* o, Opts* out) {
     out->centroid_mode = o->centroid_mode;
     out->mac_mode = o->mac_mode;
     out->selector = o->selector;
+    out->autotune = o->autotune;
     out->target = o->target_rel_err > 0 ? o->target_rel_err : 1e-6;
     out->stream = (cudaStream_t)o->stream;
     return FMM_OK;
@@ -585,7 +589,150 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     s.v[16 + kMaxP + 4] = (double)ws.list_candidates;
     s.v[16 + kMaxP + 5] = (double)ws.list_evals;
     s.v[16 + kMaxP + 6] = (double)lattice_levels;
+    s.v[kTuneStats + 0] = tp.ncrit;
+    s.v[kTuneStats + 1] = ws.p2p_shape.threads;
+    s.v[kTuneStats + 2] = ws.p2p_shape.stage;
+    s.v[kTuneStats + 3] = ws.p2p_shape.queue;
+    s.v[kTuneStats + 4] = 0.0;
     g_stats = s;
+    return FMM_OK;
+}
+
+// ---------------------------------------------------------------- autotuner
+// For a class of calls (particle count and density in half-octaves, orders,
+// settings) the first call with opts->autotune times candidate values of
+// ncrit with whole evaluations of its own input, then, at the best ncrit,
+// launch shapes of the FP32 near field (threads per block, staging size,
+// per-leaf grid or cost-ordered work queue) by that kernel's own time; the
+// choice is kept for the process and, when the environment variable
+// FMM_GB300_TUNE_CACHE names a file, in that file (one line per class).
+struct TuneCfg {
+    int ncrit = 0;
+    P2pShape shape;
+};
+
+std::mutex g_tune_mu;
+std::map<std::string, TuneCfg> g_tune;
+bool g_tune_loaded = false;
+
+const char* tune_cache_path() {
+    const char* e = std::getenv("FMM_GB300_TUNE_CACHE");
+    return (e && *e) ? e : nullptr;
+}
+
+void tune_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char* path = tune_cache_path();
+    if (!path) return;
+    FILE* fp = std::fopen(path, "r");
+    if (!fp) return;
+    char key[256];
+    TuneCfg c;
+    while (std::fscanf(fp, "%255s %d %d %d %d", key, &c.ncrit, &c.shape.threads, &c.shape.stage, &c.shape.queue) == 5)
+        if (c.ncrit > 0 && c.shape.valid()) g_tune[key] = c;
+    std::fclose(fp);
+}
+
+std::string tune_key(int64_t n, const double* X, int mdim, int f, int p, const Opts& o, int dt, double theta,
+                     bool batched) {
+    double lo[3] = {X[0], X[n], X[2 * n]}, hi[3] = {X[0], X[n], X[2 * n]};
+    for (int d = 0; d < 3; ++d)
+        for (int64_t k = 0; k < n; ++k) {
+            lo[d] = std::min(lo[d], X[d * n + k]);
+            hi[d] = std::max(hi[d], X[d * n + k]);
+        }
+    double vol = 1.0;
+    for (int d = 0; d < 3; ++d) vol *= std::max(hi[d] - lo[d], 1e-3);
+    char b[256];
+    std::snprintf(b, sizeof(b), "n%d:d%d:m%d:f%d:p%d:x%d:s%d:c%d:e%d:a%d:k%d:t%d:b%d",
+                  (int)std::lround(2.0 * std::log2((double)n)), (int)std::lround(2.0 * std::log2((double)n / vol)),
+                  mdim, f, p, o.precision, o.selector, o.coef_mode, o.excl_mode, o.mac_mode, dt,
+                  (int)std::lround(theta * 1000.0), batched ? 1 : 0);
+    return b;
+}
+
+// Runs the call with the tuned configuration of its class (tuning first if
+// the class is new).  tp carries the call's tree parameters; ncrit is
+// replaced by the chosen value, a candidate below ncrit_limit.
+int run_fmm_tuned(Workspace& ws, const Particles& P, double theta, int ncrit, int p, int f, const Opts& o,
+                  TreeParams tp, double* d_field, cudaStream_t st, const std::string& key, int64_t ncrit_limit) {
+    TuneCfg cfg;
+    bool have = false;
+    const P2pShape user_shape = ws.p2p_shape;  // restored after the call
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        tune_load_locked();
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            cfg = it->second;
+            have = true;
+        }
+    }
+    bool tuned_now = false;
+    if (!have) {
+        double best = 1e300;
+        int bestc = ncrit;
+        std::vector<int> cands = {32, 48, 64, 96, 128};
+        if (std::find(cands.begin(), cands.end(), ncrit) == cands.end()) cands.push_back(ncrit);
+        ws.p2p_shape = P2pShape{};
+        for (int c : cands) {
+            if (c >= ncrit_limit) continue;  // batched: every system needs more than ncrit particles
+            tp.ncrit = c;
+            const int rc = run_fmm(ws, P, theta, c, p, f, o, tp, d_field, st);
+            if (rc != FMM_OK) {
+                ws.p2p_shape = user_shape;
+                return rc;
+            }
+            const double t = g_stats.v[12];  // device time of the whole evaluation
+            if (t < best) {
+                best = t;
+                bestc = c;
+            }
+        }
+        cfg.ncrit = bestc;
+        cfg.shape = P2pShape{};
+        const bool f32_near = o.precision == 1 || o.precision == 2 || o.selector == 1;
+        if (f32_near) {
+            const P2pShape shapes[] = {{128, 320, 1}, {256, 320, 1}, {64, 320, 1}, {128, 160, 1},
+                                       {256, 160, 1}, {128, 480, 1}, {128, 320, 0}, {256, 320, 0}};
+            double bt = 1e300;
+            tp.ncrit = bestc;
+            for (const P2pShape& sh : shapes) {
+                ws.p2p_shape = sh;
+                const int rc = run_fmm(ws, P, theta, bestc, p, f, o, tp, d_field, st);
+                if (rc != FMM_OK) {
+                    ws.p2p_shape = user_shape;
+                    return rc;
+                }
+                const double t = g_stats.v[16 + kMaxP + 1];  // near-field kernel
+                if (t > 0 && t < bt) {
+                    bt = t;
+                    cfg.shape = sh;
+                }
+            }
+        }
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[key] = cfg;
+        if (const char* path = tune_cache_path()) {
+            if (FILE* fp = std::fopen(path, "a")) {
+                std::fprintf(fp, "%s %d %d %d %d\n", key.c_str(), cfg.ncrit, cfg.shape.threads, cfg.shape.stage,
+                             cfg.shape.queue);
+                std::fclose(fp);
+            }
+        }
+        tuned_now = true;
+    }
+    ws.p2p_shape = cfg.shape;
+    tp.ncrit = cfg.ncrit;
+    const int rc = run_fmm(ws, P, theta, cfg.ncrit, p, f, o, tp, d_field, st);
+    ws.p2p_shape = user_shape;
+    FMM_TRY(rc);
+    g_stats.v[kTuneStats + 0] = cfg.ncrit;
+    g_stats.v[kTuneStats + 1] = cfg.shape.threads;
+    g_stats.v[kTuneStats + 2] = cfg.shape.stage;
+    g_stats.v[kTuneStats + 3] = cfg.shape.queue;
+    g_stats.v[kTuneStats + 4] = tuned_now ? 1.0 : 0.0;
     return FMM_OK;
 }
 
@@ -845,6 +992,7 @@ int fmm_field_fmm_device(int64_t n, const double* d_X, int mdim, const double* d
     FMM_TRY(check_common(n, mdim, exw, field_order, dt, d_damp));
     Opts o;
     FMM_TRY(parse_opts(opts, &o));
+    if (o.autotune) return FMM_ENOTSUP;  // host entry points only
     if (ncrit < 1 || p < 0 || !(theta > 0.0)) return FMM_EINVAL;
     if (p > kMaxP) return FMM_ENOTSUP;
     Workspace& ws = thread_workspace();
@@ -873,7 +1021,7 @@ int fmm_field_fmm(int comm, int64_t n, const double* X, int mdim, const double* 
     if (is_periodic) {
         // periodic boxes: FP64, fixed rule; the reference stops when N <= ncrit (fmm.F90:1382)
         if (!box || n <= ncrit) return FMM_EINVAL;
-        if (o.precision != 0 || o.selector != 0) return FMM_ENOTSUP;
+        if (o.precision != 0 || o.selector != 0 || o.autotune != 0) return FMM_ENOTSUP;
         for (int k = 0; k < 9; ++k) hbox.h[k] = box[k];
     }
     if (n <= ncrit) return fmm_field_direct(comm, n, X, mdim, mp, exw, ex, field_order, field, damp, damp_len, dampf, opts);
@@ -893,8 +1041,12 @@ int fmm_field_fmm(int comm, int64_t n, const double* X, int mdim, const double* 
         host_centroid_sequential(X, n, tp.host_centroid);
         tp.have_host_centroid = 1;
     }
-    FMM_TRY(run_fmm(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st,
-                    is_periodic ? &hbox : nullptr));
+    if (o.autotune)
+        FMM_TRY(run_fmm_tuned(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st,
+                              tune_key(n, X, mdim, field_order, p, o, dt, theta, false), n));
+    else
+        FMM_TRY(run_fmm(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st,
+                        is_periodic ? &hbox : nullptr));
     pf.join();
     FMM_CUDA_TRY(cudaMemcpyAsync(field, ws.out_field.p, sizeof(double) * (size_t)nf * n, cudaMemcpyDeviceToHost, st));
     FMM_CUDA_TRY(cudaStreamSynchronize(st));
@@ -918,9 +1070,11 @@ int fmm_field_fmm_batched(int nsys, const int64_t* offsets, const double* X, int
     // per system: sizes, exclusion ranges, bounding-box centre and half-extent
     std::vector<double> cen(3 * (size_t)nsys), half((size_t)nsys);
     double hmax = 0.0;
+    int64_t min_size = n;
     for (int k = 0; k < nsys; ++k) {
         const int64_t a = offsets[k], b = offsets[k + 1];
         if (b - a <= ncrit) return FMM_EINVAL;  // every system must need a tree of its own
+        min_size = std::min(min_size, b - a);
         for (int64_t i = a; i < b; ++i)
             for (int w = 0; w < exw; ++w) {
                 const int32_t e = ex[(size_t)w * n + i];
@@ -973,7 +1127,10 @@ int fmm_field_fmm_batched(int nsys, const int64_t* offsets, const double* X, int
     TreeParams tp{ncrit, theta, 1, 1, {0, 0, 0}, o.mac_mode, 0.0, p};
     tp.root_r = 0.5 * G * S;
     tp.d_sys = dsys.as<int32_t>();
-    int rc = run_fmm(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st);
+    int rc = o.autotune ? run_fmm_tuned(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st,
+                                        tune_key(n, Xp.data(), mdim, field_order, p, o, dt, theta, true),
+                                        min_size)
+                        : run_fmm(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st);
     if (rc == FMM_OK) {
         if (cudaMemcpyAsync(field, ws.out_field.p, sizeof(double) * (size_t)nf * n, cudaMemcpyDeviceToHost, st) !=
                 cudaSuccess ||
@@ -983,6 +1140,15 @@ int fmm_field_fmm_batched(int nsys, const int64_t* offsets, const double* X, int
     cudaStreamSynchronize(st);
     dsys.release();
     return rc;
+}
+
+// FP32 near-field launch shape of the calling thread (see include/fmm_gpu.h).
+int fmm_set_p2p_shape(int threads, int stage, int queue) {
+    P2pShape sh{threads, stage, queue};
+    if (threads == 0 && stage == 0 && queue == 0) sh = P2pShape{};
+    if (!sh.valid()) return FMM_EINVAL;
+    thread_workspace().p2p_shape = sh;
+    return FMM_OK;
 }
 
 // Plans (see include/fmm_gpu.h).
@@ -1002,7 +1168,7 @@ int fmm_plan_create(int64_t n, const double* X, int mdim, int exw, const int32_t
     Opts o;
     FMM_TRY(parse_opts(opts, &o));
     if (!X || ncrit < 1 || p < 0 || !(theta > 0.0)) return FMM_EINVAL;
-    if (p > kMaxP || o.selector != 0) return FMM_ENOTSUP;  // fixed acceptance rule only
+    if (p > kMaxP || o.selector != 0 || o.autotune != 0) return FMM_ENOTSUP;  // fixed acceptance rule only
     if (o.precision != 0 && (dim_to_order(mdim) > 2 || field_order > 2)) return FMM_ENOTSUP;
     fmm_plan* h = new (std::nothrow) fmm_plan;
     if (!h) return FMM_ENOMEM;

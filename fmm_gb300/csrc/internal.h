@@ -102,6 +102,13 @@ double min_damping_factor(Workspace& ws, const double* d_damp, int64_t n, cudaSt
 // Host-side sequential centroid (the reference's SUM order).
 void host_centroid_sequential(const double* coords, int64_t n, double c[3]);
 
+struct P2pShape {
+    int threads = 128;
+    int stage = 320;
+    int queue = 1;
+    bool valid() const;
+};
+
 struct Workspace {
     // inputs on device (host entry points copy here)
     DevBuf in_coords, in_mp, in_excl, in_damp, out_field;
@@ -155,6 +162,8 @@ struct Workspace {
     // replays (plans): the tree, lists and M2L structure of the previous
     // evaluation are kept and only the kernels that read multipoles run
     bool reuse_structure = false;
+    P2pShape p2p_shape;  // FP32 near-field launch shape
+    DevBuf p2p_order;    // target leaves by decreasing pair work (queue mode), and scratch
     int m2l_ng = 0, m2l_ntasks = 0;  // grouped M2L structure of the last evaluation
     int64_t list_candidates = 0; // cell pairs examined by the last list build
     int64_t list_evals = 0;      // of which evaluated by the selector network
@@ -228,6 +237,10 @@ int selector_pair_data(Workspace& ws, const Particles& Pt, const TreeDev& t, int
 int selector_unpack_far(Workspace& ws, const TreeDev& t, int2* d_out, cudaStream_t st);
 int launch_l2l_l2p(Workspace& ws, const Particles& P, const TreeDev& t, int p, int field_order, bool fp32,
                    cudaStream_t st);
+// Launch shape of the FP32 near field (Workspace::p2p_shape; the autotuner
+// sets it): threads per block (64, 128, 256), float4s per staging buffer
+// (two per warp), and whether warps take target leaves from a queue ordered
+// by decreasing pair work (persistent grid) instead of one leaf each.
 int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, cudaStream_t st);
 int launch_excl_correction(Workspace& ws, const Particles& P, const TreeDev* t, int field_order, const Modes& md,
                            double* d_field_sorted_or_orig, cudaStream_t st);

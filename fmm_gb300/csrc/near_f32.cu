@@ -12,6 +12,8 @@
 // accumulators.  Excluded partners and the self pair are masked in the loop.
 #include <algorithm>
 
+#include <cub/cub.cuh>
+
 #include "dispatch.cuh"
 #include "internal.h"
 #include "pair.cuh"
@@ -200,9 +202,10 @@ __device__ __forceinline__ void p2p_leaf(const float4* src, int cnt, int k0, int
 }
 
 // Source records are staged per warp in shared memory, double-buffered:
-// while one piece (a source leaf, or kStage / NV of its particles when it is
-// larger) is evaluated, the next is copied with cp.async.
-constexpr int kStage = 320;  // float4s per staging buffer
+// while one piece (a source leaf, or `stage` / NV of its particles when it
+// is larger) is evaluated, the next is copied with cp.async.  The staging
+// size (float4s per buffer) is a launch parameter (dynamic shared memory).
+constexpr int kStage = 320;  // default float4s per staging buffer
 
 __device__ __forceinline__ void cp_async16(float4* smem, const float4* gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -218,19 +221,34 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // of the warp's targets run without the exclusion test.
 // DAMP is the damping kind as a template parameter: one specialised kernel
 // per kind keeps the pair loop free of kind dispatch and its code small.
+// Work: with `next` null, warp w takes leaf t.leaves[w]; otherwise the warps
+// stay resident and take leaves order[0], order[1], ... (the target leaves
+// by decreasing pair count) from the counter `next`, so the largest leaves
+// start first and the last wave is made of the smallest.
 template <int M, int F, int DAMP>
-__global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* __restrict__ rec,
-                                                 const float4* __restrict__ chi, const float4* __restrict__ clo,
-                                                 const int32_t* __restrict__ excl, int exw, int64_t n,
-                                                 double* __restrict__ fs) {
+__global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float4* __restrict__ rec,
+                                                    const float4* __restrict__ chi, const float4* __restrict__ clo,
+                                                    const int32_t* __restrict__ excl, int exw, int64_t n,
+                                                    double* __restrict__ fs, int stage,
+                                                    const int32_t* __restrict__ order, unsigned* __restrict__ next) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
-    constexpr int CAP = kStage / NV;  // particles per staged piece
-    __shared__ float4 sbuf[4][2][kStage];
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    extern __shared__ __align__(16) float4 sbuf_p2p[];
+    const int cap = stage / NV;  // particles per staged piece
     const int lane = threadIdx.x & 31;
-    if (w >= t.num_leaves) return;
-    float4(*buf)[kStage] = sbuf[threadIdx.x >> 5];
-    const int leaf = t.leaves[w];
+    float4* const bufs = sbuf_p2p + (size_t)(threadIdx.x >> 5) * 2 * stage;
+    const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (int round = 0;; ++round) {
+    int item;
+    if (next) {
+        unsigned v = 0;
+        if (lane == 0) v = atomicAdd(next, 1u);
+        item = (int)__shfl_sync(0xffffffffu, v, 0);
+    } else {
+        if (round > 0) break;
+        item = w0;
+    }
+    if (item >= t.num_leaves) break;
+    const int leaf = order ? order[item] : t.leaves[item];
     const int s0 = t.start[leaf], cnt = t.count[leaf];
     const int q0 = t.near_off[leaf], q1 = t.near_off[leaf + 1];
     const float4 ca = chi[leaf], cal = clo[leaf];
@@ -263,14 +281,14 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
             j = t.near_src[q];
             js = t.start[j];
             jc = t.count[j];
-            const int pc = min(CAP, jc);
-            for (int i = lane; i < pc * NV; i += 32) cp_async16(&buf[0][i], rec + (size_t)js * NV + i);
+            const int pc = min(cap, jc);
+            for (int i = lane; i < pc * NV; i += 32) cp_async16(&bufs[i], rec + (size_t)js * NV + i);
         }
         cp_async_commit();
         int slot = 0;
         while (q < q1) {
             // stage the next piece
-            int nq = q, noff = off + CAP, nj = j, njs = js, njc = jc;
+            int nq = q, noff = off + cap, nj = j, njs = js, njc = jc;
             if (noff >= jc) {
                 nq = q + 1;
                 noff = 0;
@@ -281,9 +299,10 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
                 }
             }
             if (nq < q1) {
-                const int npc = min(CAP, njc - noff);
+                const int npc = min(cap, njc - noff);
                 const float4* gsrc = rec + (size_t)(njs + noff) * NV;
-                for (int i = lane; i < npc * NV; i += 32) cp_async16(&buf[slot ^ 1][i], gsrc + i);
+                float4* dst = bufs + (slot ^ 1) * stage;
+                for (int i = lane; i < npc * NV; i += 32) cp_async16(&dst[i], gsrc + i);
             }
             cp_async_commit();
             cp_async_wait_prev();
@@ -299,15 +318,16 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
                 bool need = (j == leaf) || exw > kExwRegs;
 #pragma unroll
                 for (int e = 0; e < kExwRegs; ++e) need |= (exl[e] == j);
-                const int pc = min(CAP, jc - off);
+                const int pc = min(cap, jc - off);
+                const float4* cur = bufs + slot * stage;
                 float hi[NF], lo[NF];
 #pragma unroll
                 for (int f = 0; f < NF; ++f) hi[f] = lo[f] = 0.0f;
                 if (__any_sync(__activemask(), need))
-                    p2p_leaf<M, F, DAMP, true>(buf[slot], pc, js + off, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy,
+                    p2p_leaf<M, F, DAMP, true>(cur, pc, js + off, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy,
                                                oz, oxl, oyl, ozl, excl, exw, n, ot, hi, lo);
                 else
-                    p2p_leaf<M, F, DAMP, false>(buf[slot], pc, js + off, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox,
+                    p2p_leaf<M, F, DAMP, false>(cur, pc, js + off, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox,
                                                 oy, oz, oxl, oyl, ozl, excl, exw, n, ot, hi, lo);
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
@@ -328,6 +348,7 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
             slot ^= 1;
         }
         cp_async_wait_all();
+        __syncwarp();
         double acc[NF];
 #pragma unroll
         for (int f = 0; f < NF; ++f) acc[f] = (double)AH[f] + (double)AL[f];
@@ -340,25 +361,81 @@ __global__ void __launch_bounds__(128) k_p2p_f32(const TreeDev t, const float4* 
             for (int f = 0; f < NF; ++f) fs[(size_t)f * n + tgt] = acc[f];
         }
     }
+    }
+}
+
+// Pair work of each target leaf (its particles times the particles of its
+// near list) for the work queue's order.
+__global__ void k_leaf_cost(const TreeDev t, uint32_t* __restrict__ cost, int32_t* __restrict__ ids) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= t.num_leaves) return;
+    const int leaf = t.leaves[w];
+    uint32_t s = 0;
+    for (int q = t.near_off[leaf] + lane; q < t.near_off[leaf + 1]; q += 32) s += (uint32_t)t.count[t.near_src[q]];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        const uint64_t c = (uint64_t)t.count[leaf] * s;
+        cost[w] = c > 0xffffffffull ? 0xffffffffu : (uint32_t)c;
+        ids[w] = leaf;
+    }
 }
 
 template <int M, int F>
-void launch_p2p_kind(unsigned blocks, cudaStream_t st, const TreeDev& t, const float4* rec, const float4* chi,
-                     const float4* clo, const int32_t* excl, int exw, int64_t n, int damp, double* fs) {
+void launch_p2p_kind(unsigned blocks, int threads, size_t smem, int stage, const int32_t* order, unsigned* next,
+                     cudaStream_t st, const TreeDev& t, const float4* rec, const float4* chi, const float4* clo,
+                     const int32_t* excl, int exw, int64_t n, int damp, double* fs) {
     switch (damp) {
         case DAMP_AMOEBA:
-            k_p2p_f32<M, F, DAMP_AMOEBA><<<blocks, 128, 0, st>>>(t, rec, chi, clo, excl, exw, n, fs);
+            k_p2p_f32<M, F, DAMP_AMOEBA><<<blocks, threads, smem, st>>>(t, rec, chi, clo, excl, exw, n, fs, stage,
+                                                                          order, next);
             break;
         case DAMP_THOLE:
-            k_p2p_f32<M, F, DAMP_THOLE><<<blocks, 128, 0, st>>>(t, rec, chi, clo, excl, exw, n, fs);
+            k_p2p_f32<M, F, DAMP_THOLE><<<blocks, threads, smem, st>>>(t, rec, chi, clo, excl, exw, n, fs, stage,
+                                                                         order, next);
             break;
         case DAMP_ERF:
-            k_p2p_f32<M, F, DAMP_ERF><<<blocks, 128, 0, st>>>(t, rec, chi, clo, excl, exw, n, fs);
+            k_p2p_f32<M, F, DAMP_ERF><<<blocks, threads, smem, st>>>(t, rec, chi, clo, excl, exw, n, fs, stage, order,
+                                                                       next);
             break;
         default:
-            k_p2p_f32<M, F, DAMP_NONE><<<blocks, 128, 0, st>>>(t, rec, chi, clo, excl, exw, n, fs);
+            k_p2p_f32<M, F, DAMP_NONE><<<blocks, threads, smem, st>>>(t, rec, chi, clo, excl, exw, n, fs, stage, order,
+                                                                        next);
             break;
     }
+}
+
+template <int M, int F>
+int set_p2p_smem(size_t smem) {
+    const void* fns[4] = {(const void*)k_p2p_f32<M, F, DAMP_NONE>, (const void*)k_p2p_f32<M, F, DAMP_AMOEBA>,
+                          (const void*)k_p2p_f32<M, F, DAMP_THOLE>, (const void*)k_p2p_f32<M, F, DAMP_ERF>};
+    for (const void* fn : fns)
+        FMM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return FMM_OK;
+}
+
+template <int M, int F>
+int p2p_blocks_per_sm(int damp, int threads, size_t smem) {
+    int nb = 0;
+    const void* fn = damp == DAMP_AMOEBA  ? (const void*)k_p2p_f32<M, F, DAMP_AMOEBA>
+                     : damp == DAMP_THOLE ? (const void*)k_p2p_f32<M, F, DAMP_THOLE>
+                     : damp == DAMP_ERF   ? (const void*)k_p2p_f32<M, F, DAMP_ERF>
+                                          : (const void*)k_p2p_f32<M, F, DAMP_NONE>;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return std::max(1, nb);
+}
+
+int num_sms_f32() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
 }
 
 }  // namespace
@@ -397,6 +474,11 @@ int launch_direct_scale_f32(Workspace& ws, const Particles& P, const TreeDev& t,
     return FMM_OK;
 }
 
+bool P2pShape::valid() const {
+    return (threads == 64 || threads == 128 || threads == 256) && stage >= 64 && stage <= 1024 && stage % 16 == 0 &&
+           (queue == 0 || queue == 1);
+}
+
 int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, cudaStream_t st) {
     const int m = dim_to_order(P.dim);
     const int64_t n = P.n;
@@ -405,9 +487,43 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
     const float4* chi = ws.f32node.as<float4>();
     const float4* clo = chi + t.num_nodes;
     FMM_TRY(ws.fsorted.ensure(sizeof(double) * (size_t)n * nf));
-    const unsigned blocks = grid_for((int64_t)t.num_leaves * 32, 128);
-    FMM_MF_SWITCH(m, field_order, (launch_p2p_kind<MM, FF>(blocks, st, t, rec, chi, clo, P.excl, P.exw, n,
-                                                           P.damp_type, ws.fsorted.as<double>())));
+    const P2pShape sh = ws.p2p_shape.valid() ? ws.p2p_shape : P2pShape{};
+    const size_t smem = sizeof(float4) * 2 * (size_t)sh.stage * (sh.threads / 32);
+    if (rec_vec(P.dim) > sh.stage) return FMM_EINVAL;
+    const int32_t* order = nullptr;
+    unsigned* next = nullptr;
+    unsigned blocks = grid_for((int64_t)t.num_leaves * 32, sh.threads);
+    if (sh.queue && t.num_leaves > 0) {
+        // target leaves by decreasing pair work (structure: kept for replays)
+        FMM_TRY(ws.counters.ensure(sizeof(unsigned long long) * 32));
+        next = reinterpret_cast<unsigned*>(ws.counters.as<unsigned long long>() + 11);
+        if (!ws.reuse_structure) {
+            const int L = t.num_leaves;
+            FMM_TRY(ws.p2p_order.ensure(sizeof(int32_t) * 2 * (size_t)L + sizeof(uint32_t) * 2 * (size_t)L));
+            int32_t* ids = ws.p2p_order.as<int32_t>() + L;
+            uint32_t* cost = reinterpret_cast<uint32_t*>(ws.p2p_order.as<int32_t>() + 2 * (size_t)L);
+            uint32_t* cost2 = cost + L;
+            count_launches(1);
+            k_leaf_cost<<<grid_for((int64_t)L * 32, 128), 128, 0, st>>>(t, cost, ids);
+            size_t tb = 0;
+            cub::DeviceRadixSort::SortPairsDescending(nullptr, tb, cost, cost2, ids, ws.p2p_order.as<int32_t>(), L, 0,
+                                                      32, st);
+            FMM_TRY(ws.cub_tmp.ensure(tb));
+            FMM_CUDA_TRY(cub::DeviceRadixSort::SortPairsDescending(ws.cub_tmp.p, tb, cost, cost2, ids,
+                                                                   ws.p2p_order.as<int32_t>(), L, 0, 32, st));
+        }
+        order = ws.p2p_order.as<int32_t>();
+        FMM_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(unsigned), st));
+        int bps = 1;
+        FMM_MF_SWITCH(m, field_order, (bps = p2p_blocks_per_sm<MM, FF>(P.damp_type, sh.threads, smem)));
+        blocks = (unsigned)std::min<int64_t>(blocks, (int64_t)bps * num_sms_f32());
+    }
+    if (smem > 48 * 1024) {
+        FMM_MF_SWITCH(m, field_order, FMM_TRY((set_p2p_smem<MM, FF>(smem))));
+    }
+    FMM_MF_SWITCH(m, field_order,
+                  (launch_p2p_kind<MM, FF>(blocks, sh.threads, smem, sh.stage, order, next, st, t, rec, chi, clo,
+                                           P.excl, P.exw, n, P.damp_type, ws.fsorted.as<double>())));
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }

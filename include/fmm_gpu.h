@@ -72,7 +72,13 @@ typedef struct fmm_opts {
     int selector;       /* 0 fixed expansion order; 1 learned per-pair order (MLP)           */
     double target_rel_err; /* error target for mac_mode 1 / selector 1 (default 1e-6)       */
     void *stream;       /* cudaStream_t for the *_device entry points (NULL = legacy stream) */
-    int reserved[8];
+    int autotune;       /* 1: ncrit and the FP32 near field's launch shape chosen by timing
+                           candidates on the first call of each class of calls (size,
+                           density, orders, settings; host entry points fmm_field_fmm and
+                           fmm_field_fmm_batched, not periodic); the choice is kept for
+                           the process and in the file $FMM_GB300_TUNE_CACHE if set.  The
+                           ncrit argument is then only a candidate.                       */
+    int reserved[7];
 } fmm_opts;
 
 /* Replaces fmm::field_direct (src/fmm.F90:1338-1352); O(N^2) direct sum.
@@ -222,8 +228,10 @@ int fmm_release_workspace(void);
  * that kernel did not run), the number of displacement groups of the grouped
  * M2L, the cell pairs examined by the list build and how many of them the
  * learned selector's network evaluated, and the number of lattice levels the
- * periodic sum used (0 without a periodic box).  Returns the number written
- * (at most 35). */
+ * periodic sum used (0 without a periodic box); then the ncrit the call used,
+ * the FP32 near field's launch shape (threads per block, staging float4s,
+ * work queue 0/1) and 1 if this call ran the autotuner.  Returns the number
+ * written (at most 40). */
 int fmm_last_stats(double *out, int len);
 
 /* Diagnostics (no counterpart in the reference): builds the octree and
@@ -270,6 +278,16 @@ int fmm_mlp_train(float *params, const float *x, const float *y, int64_t n, int 
 int fmm_selector_collect(int64_t n, const double *coordinates, int mdim, const double *multipoles,
                          const double *damping_factors, int ncrit, double theta, int max_pairs, uint64_t seed,
                          float *features, float *labels, int *npairs, int32_t *pairs);
+
+/* Launch shape of the mixed-precision near field for the calling thread's
+ * later calls (no counterpart in the reference): threads per block (64, 128
+ * or 256), float4s per staging buffer (64..1024, a multiple of 16; two
+ * buffers per warp) and queue = 1 for resident warps that take target leaves
+ * in order of decreasing pair work, 0 for one warp per leaf.  (0, 0, 0)
+ * restores the default (128, 320, 1).  Results do not depend on threads or
+ * queue; the staging size changes the grouping of the compensated sums.  An
+ * autotuned call uses its class's shape and leaves this one in place. */
+int fmm_set_p2p_shape(int threads, int stage, int queue);
 
 /* Plans (no counterpart in the reference): for fixed coordinates,
  * exclusions, damping factors and settings, fmm_plan_create builds the octree,
