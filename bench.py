@@ -245,45 +245,176 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def run_batched(args):
-    """512 independent systems (N log-uniform in [1k, 64k], uniform at density
-    0.1 per bohr^3, erf damping, multipoles order 1, theta 0.5, p 6, f 1)
-    through fmm_gb300.field_fmm_batched: host arrays in, host field out, so
-    the time includes the host<->device copies.  Accuracy on 8 of the systems
-    against their FP64 direct sums."""
+def sampled_reference(s, tgt, damp):
+    """FP64 GPU direct sum at the particles tgt (device targets call)."""
+    import ctypes
+    import torch
+    import fmm_gb300
+    from fmm_gb300 import Options, _lib
+    L = _lib.lib()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n = s["coordinates"].shape[0]
+    dim = s["multipoles"].shape[1]
+    E = np.asarray(s["exclusions"]).reshape(n, -1)
+    col = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).T).reshape(-1)).to(dev)
+    tX, tM, tE = col(s["coordinates"]), col(s["multipoles"]), col(E.astype(np.int32))
+    tD = torch.from_numpy(np.ascontiguousarray(s["damping_factors"], dtype=np.float64)).to(dev)
+    tT = torch.from_numpy(np.asarray(tgt, dtype=np.int64)).to(dev)
+    nf = n_t(F_ORDER)
+    tR = torch.empty(len(tgt) * nf, dtype=torch.float64, device=dev)
+    o = Options(excl_mode="mask").to_c()
+    st = L.fmm_field_direct_targets_device(n, ctypes.c_void_p(tX.data_ptr()), dim, ctypes.c_void_p(tM.data_ptr()),
+                                           E.shape[1], ctypes.c_void_p(tE.data_ptr()), len(tgt),
+                                           ctypes.c_void_p(tT.data_ptr()), F_ORDER, ctypes.c_void_p(tR.data_ptr()),
+                                           damp.encode(), len(damp), ctypes.c_void_p(tD.data_ptr()), ctypes.byref(o))
+    _lib.check(st, "direct on sampled targets")
+    torch.cuda.synchronize()
+    return tR.cpu().numpy().reshape(nf, -1).T
+
+
+def rel_errors(Fgot, Fref):
+    d = np.linalg.norm(Fgot[:, 1:] - Fref[:, 1:], axis=1)
+    g = np.linalg.norm(Fref[:, 1:], axis=1)
+    per = d / g
+    return {"rms_rel_err": float(np.sqrt(np.mean(per ** 2))), "max_rel_err": float(per.max()),
+            "targets": int(len(per))}
+
+
+def timed_host(call, steps, warmup=1):
+    for _ in range(warmup):
+        call()
+    tt = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        out = call()
+        tt.append(time.perf_counter() - t0)
+    return out, float(np.mean(tt))
+
+
+def fma_peak(prec):
+    import ctypes
+    from fmm_gb300 import _lib
+    peak = ctypes.c_double(0)
+    _lib.check(_lib.lib().fmm_measure_fma_peak(prec, ctypes.byref(peak)), "fma peak")
+    return peak.value
+
+
+def batched_measure(steps=2, warmup=1, cpu=True):
+    """Configuration of 512 independent systems (N log-uniform in [1k, 64k],
+    uniform at density 0.1 per bohr^3, erf damping, multipoles order 1,
+    theta 0.5, p 6, f 1) in one call: fixed settings (ncrit 64, default
+    near-field shape), autotuned (ncrit and shape chosen on the first call),
+    and a plan (the same packing replayed as one CUDA graph).  Host arrays in
+    and out, copies timed.  Accuracy on 8 systems against their FP64 direct
+    sums; the CPU baseline times the oracle (reference semantics and rule) on
+    8 of the smaller systems."""
     import fmm_gb300
     from fmm_gb300 import Options, systems
     sl = systems.batched_uniform(n_systems=512, seed=3)
-    n = sum(s["coordinates"].shape[0] for s in sl)
+    sizes = np.array([s["coordinates"].shape[0] for s in sl])
+    n = int(sizes.sum())
     rng = np.random.default_rng(5)
     check = sorted(rng.choice(len(sl), size=8, replace=False).tolist())
     refs = {k: fmm_gb300.field_direct(0, sl[k]["coordinates"], sl[k]["multipoles"], sl[k]["exclusions"], 1, "ERF",
                                       sl[k]["damping_factors"], options=Options(excl_mode="mask")) for k in check}
-    out = {}
-    for name, opt in (("mixed", Options.exact(precision="mixed")), ("fp64", Options.exact())):
-        for _ in range(args.warmup):
-            F = fmm_gb300.field_fmm_batched(sl, 0.5, NCRIT, 6, 1, "ERF", options=opt)
-        times = []
-        for _ in range(args.steps):
+
+    def acc(F):
+        return rel_errors(np.concatenate([F[k] for k in check]), np.concatenate([refs[k] for k in check]))
+
+    arms = {}
+    for name, opt in (("fixed", Options.exact(precision="mixed")),
+                      ("autotuned", Options.exact(precision="mixed", autotune=True))):
+        t0 = time.perf_counter()
+        fmm_gb300.field_fmm_batched(sl, 0.5, NCRIT, 6, 1, "ERF", options=opt)
+        first = time.perf_counter() - t0
+        F, t = timed_host(lambda: fmm_gb300.field_fmm_batched(sl, 0.5, NCRIT, 6, 1, "ERF", options=opt), steps,
+                          warmup=0)
+        st = fmm_gb300.last_stats()
+        arms[name] = {"value": n / t, "ms_per_step": 1e3 * t, "first_call_s": first, "accuracy": acc(F),
+                      "ncrit": int(st["ncrit_used"]), "near_field_shape": [int(st["p2p_threads"]),
+                                                                            int(st["p2p_stage"]),
+                                                                            int(st["p2p_queue"])],
+                      "t_p2p_kernel_ms": st["t_p2p_kernel"], "p2p_particle_pairs": st["p2p_particle_pairs"],
+                      "t_total_device_ms": st["t_total"]}
+    t0 = time.perf_counter()
+    plan = fmm_gb300.Plan.batched(sl, 4, 0.5, NCRIT, 6, 1, "ERF", options=Options.exact(precision="mixed"))
+    create = time.perf_counter() - t0
+    mps = [s["multipoles"] for s in sl]
+    F, t = timed_host(lambda: plan.execute_systems(mps), steps, warmup=warmup)
+    arms["plan_graph"] = {"value": n / t, "ms_per_step": 1e3 * t, "create_s": create, "accuracy": acc(F),
+                          "kernels_per_replay": plan.kernels}
+    plan.close()
+    best = max(("fixed", "autotuned"), key=lambda k: arms[k]["value"])
+    a = arms["autotuned"]
+    peak = fma_peak(1)
+    flops = (a["p2p_particle_pairs"] - n) * pair_flops(1, 1)
+    roof = {"bound": "fp32", "kernel": "k_p2p_f32", "achieved": flops / (a["t_p2p_kernel_ms"] * 1e-3) / 1e12,
+            "peak": peak, "unit": "TFLOP/s",
+            "peak_source": "measured live by fmm_measure_fma_peak (register FMA loop on all SMs)"}
+    roof["frac"] = roof["achieved"] / peak
+    out = {"metric": "field_fmm_batched particles/s, 512 systems", "value": arms["autotuned"]["value"],
+           "unit": "particles/s", "n_particles": n, "arms": arms, "tuned_over_fixed": a["value"] / arms["fixed"]["value"],
+           "best_arm": best, "roofline": roof,
+           "e2e": {"value": arms["autotuned"]["value"], "unit": "particles/s", "h2d_bytes_per_step": 8 * (3 + 4 + 1) * n
+                   + 4 * n, "d2h_bytes_per_step": 8 * 4 * n},
+           "config": {"workload": "512 systems, N log-uniform in [1k, 64k] (%d total), density 0.1 per bohr^3, erf "
+                                  "damping U(0.3,0.8), multipoles order 1, theta 0.5, p 6, f 1, mixed precision; host "
+                                  "arrays, copies timed" % n}}
+    if cpu:
+        import oracle
+        small = [k for k in np.argsort(sizes)[: len(sl) // 2][::32]][:8]
+        nn, tt = 0, 0.0
+        for k in small:
+            s = sl[k]
             t0 = time.perf_counter()
-            F = fmm_gb300.field_fmm_batched(sl, 0.5, NCRIT, 6, 1, "ERF", options=opt)
-            times.append(time.perf_counter() - t0)
-        errs = []
-        for k in check:
-            d = np.linalg.norm(F[k][:, 1:] - refs[k][:, 1:], axis=1)
-            g = np.linalg.norm(refs[k][:, 1:], axis=1)
-            errs.append(d / g)
-        e = np.concatenate(errs)
-        out[name] = {"value": n / float(np.mean(times)), "ms_per_step": 1e3 * float(np.mean(times)),
-                     "rms_rel_err": float(np.sqrt(np.mean(e ** 2))), "max_rel_err": float(e.max())}
-    line = {"metric": "field_fmm_batched particles/s, 512 systems", "value": out["mixed"]["value"],
-            "unit": "particles/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": out["mixed"]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": "512 systems, N log-uniform in [1k, 64k] (%d total), density 0.1, erf U(0.3,0.8), "
-                                   "multipoles order 1, theta 0.5, p 6, f 1, ncrit 64; host arrays (copies timed)" % n},
-            "arms": out}
-    print(json.dumps(line), flush=True)
+            oracle.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"], 0.5, NCRIT, 6, 1, "ERF",
+                             s["damping_factors"], nthreads=os.cpu_count() or 1)
+            tt += time.perf_counter() - t0
+            nn += s["coordinates"].shape[0]
+        out["cpu_baseline"] = {"value": nn / tt, "unit": "particles/s", "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": "oracle (reference semantics, theta 0.5, p 6) on %d of the systems "
+                                         "(%d particles), one call each, all host threads" % (len(small), nn)}
+    return out
+
+
+def blobs_measure(steps=2):
+    """The learned selector's workload: N = 2M clustered particles (AMOEBA,
+    multipoles order 2, f 1, target 1e-6): learned + mixed against the fixed
+    rule in mixed precision at the same target (damping MAC, theta 0.3,
+    p 10) and the fixed order 8 / theta 0.5 rule, host calls, accuracy on
+    4096 sampled particles against the FP64 direct sum."""
+    import fmm_gb300
+    from fmm_gb300 import Options, systems
+    s = systems.blobs(n=2_000_000, seed=0)
+    n = s["coordinates"].shape[0]
+    rng = np.random.default_rng(9)
+    tgt = np.sort(rng.choice(n, size=4096, replace=False))
+    ref = sampled_reference(s, tgt, DAMP)
+    args = (0, s["coordinates"], s["multipoles"], s["exclusions"])
+    arms = {}
+    for name, theta, p, opt in (
+            ("learned", 0.3, 12, Options.exact(precision="mixed", mac_mode="damping", selector="learned")),
+            ("fixed_mixed_theta0.3_p10", 0.3, 10, Options.exact(precision="mixed", mac_mode="damping")),
+            ("fixed_mixed_theta0.5_p8", 0.5, 8, Options.exact(precision="mixed"))):
+        F, t = timed_host(lambda: fmm_gb300.field_fmm(*args, theta, NCRIT, p, F_ORDER, DAMP, s["damping_factors"],
+                                                      options=opt), steps)
+        st = fmm_gb300.last_stats()
+        arms[name] = {"value": n / t, "ms_per_step": 1e3 * t, "accuracy": rel_errors(F[tgt], ref),
+                      "selector_fallback": int(st["selector_fallback"]), "t_total_device_ms": st["t_total"]}
+    return {"workload": WORKLOADS["blobs"], "n_particles": n, "arms": arms,
+            "learned_over_fixed_same_target": arms["learned"]["value"] / arms["fixed_mixed_theta0.3_p10"]["value"]}
+
+
+def run_batched(args):
+    """--batched: the 512-system configuration as its own JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    with ClockSampler(0) as clk:
+        out = batched_measure(steps=args.steps, warmup=args.warmup, cpu=not args.no_cpu_baseline)
+    out.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": out["arms"]["autotuned"]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "clocks": clk.summary()})
+    print(json.dumps(out), flush=True)
 
 
 def main():
@@ -537,6 +668,53 @@ def main():
         ref_settings.update({"arm": "fp64-reference-settings",
                              "settings": dict(rs, coef_mode="ref", excl_mode="ref", precision="fp64")})
 
+    extras = {}
+    if args.system == "water" and args.arm == "learned" and not args.no_compare and world == 1:
+        # the autotuner on this workload (host calls; the first call tunes)
+        ta = Options.exact(precision="mixed", mac_mode="damping", selector="learned", autotune=True)
+        t0 = time.perf_counter()
+        fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"], arm["theta"], NCRIT, arm["p"],
+                            F_ORDER, DAMP, s["damping_factors"], options=ta)
+        first = time.perf_counter() - t0
+        Ft, tt_ = timed_host(lambda: fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"],
+                                                         arm["theta"], NCRIT, arm["p"], F_ORDER, DAMP,
+                                                         s["damping_factors"], options=ta), args.steps, warmup=0)
+        stt = fmm_gb300.last_stats()
+        extras["autotuned"] = {"e2e_value": n / tt_, "unit": "particles/s", "first_call_s": first,
+                               "gain_over_untuned_e2e": (n / tt_) / e2e["value"], "accuracy": accuracy_of(Ft),
+                               "ncrit": int(stt["ncrit_used"]),
+                               "near_field_shape": [int(stt["p2p_threads"]), int(stt["p2p_stage"]),
+                                                    int(stt["p2p_queue"])], "t_total_device_ms": stt["t_total"]}
+        # plans: the fixed rule replayed as one CUDA graph per multipole set,
+        # device-resident (as the fixed_rule_mixed arm) and through host arrays
+        fa = ARMS["mixed"]
+        fo = arm_options("mixed")
+        plan = fmm_gb300.Plan(s["coordinates"], 10, s["exclusions"], fa["theta"], NCRIT, fa["p"], F_ORDER, DAMP,
+                              s["damping_factors"], options=fo)
+        Mv = Shape(tM, n, 10)
+        plan.execute_device(Mv, tF)
+        torch.cuda.synchronize()
+        pt = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            plan.execute_device(Mv, tF)
+            pt.append(time.perf_counter() - t0)
+        acc_p = accuracy_of(tF.cpu().numpy().reshape(nf, n).T)
+        Fp, tp_ = timed_host(lambda: plan.execute(s["multipoles"]), args.steps)
+        _, tf_ = timed_host(lambda: fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"],
+                                                        fa["theta"], NCRIT, fa["p"], F_ORDER, DAMP,
+                                                        s["damping_factors"], options=fo), args.steps)
+        dev_v = n / float(np.mean(pt))
+        extras["plan_replay"] = {"settings": fa, "value": dev_v, "unit": "particles/s",
+                                 "gain_over_field_fmm_device": dev_v / fixed_mixed["value"] if fixed_mixed else None,
+                                 "e2e_value": n / tp_, "field_fmm_e2e_value": n / tf_, "e2e_gain": tf_ / tp_,
+                                 "kernels_per_replay": plan.kernels, "accuracy": acc_p}
+        plan.close()
+        extras["batched_512"] = batched_measure(steps=2, warmup=1, cpu=not args.no_cpu_baseline)
+        extras["blobs_2m"] = blobs_measure(steps=2)
+
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline_entry(system=args.system)
@@ -554,6 +732,7 @@ def main():
         "fixed_rule_mixed": fixed_mixed, "plain_fp64_reference_settings": ref_settings, "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
+        "other_workloads": extras or None,
         "tree": {k: stats[k] for k in ("num_nodes", "num_leaves", "max_depth", "m2l_pairs", "m2l_groups",
                                        "m2l_order_mean", "p2p_leaf_pairs", "p2p_particle_pairs", "list_candidates",
                                        "list_evals")},

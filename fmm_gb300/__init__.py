@@ -195,6 +195,47 @@ class Plan:
         self._lib = L
         self.n, self.dim, self.field_order = n, int(dim), int(field_order)
 
+    @classmethod
+    def batched(cls, systems_list, dim, theta, ncrit, expansion_order, field_order, damp_type="", *, options=None):
+        """A plan over independent systems packed as ``field_fmm_batched``
+        packs them (dicts with coordinates, exclusions, damping_factors);
+        ``execute_systems`` takes and returns per-system arrays."""
+        sizes = [np.asarray(s["coordinates"]).shape[0] for s in systems_list]
+        offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        n = int(offsets[-1])
+        X = np.asfortranarray(np.concatenate([np.asarray(s["coordinates"], dtype=np.float64) for s in systems_list]))
+        width = max(np.asarray(s["exclusions"]).reshape(sizes[k], -1).shape[1] for k, s in enumerate(systems_list))
+        E = np.zeros((n, width), dtype=np.int32, order="F")
+        for k, s in enumerate(systems_list):
+            e = np.asarray(s["exclusions"], dtype=np.int32).reshape(sizes[k], -1)
+            E[offsets[k]:offsets[k + 1], :e.shape[1]] = e
+        d = None
+        if damp_type:
+            d = np.ascontiguousarray(np.concatenate([np.asarray(s["damping_factors"], dtype=np.float64)
+                                                     for s in systems_list]))
+        ds, dl = _damp_bytes(damp_type)
+        o = _options_c(options)
+        h = ctypes.c_void_p(None)
+        L = _lib.lib()
+        st = L.fmm_plan_create_batched(len(systems_list), offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                       _dptr(X), int(dim), E.shape[1], E.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                       float(theta), int(ncrit), int(expansion_order), int(field_order), ds, dl,
+                                       _dptr(d) if d is not None else None, ctypes.byref(o), ctypes.byref(h))
+        _lib.check(st, "plan_create_batched")
+        obj = cls.__new__(cls)
+        obj._h, obj._lib = h, L
+        obj.n, obj.dim, obj.field_order = n, int(dim), int(field_order)
+        obj.offsets = offsets
+        return obj
+
+    def execute_systems(self, multipoles_list):
+        """Per-system multipoles in, per-system fields out (batched plans)."""
+        M = np.asfortranarray(np.concatenate([np.asarray(m, dtype=np.float64).reshape(-1, self.dim)
+                                              for m in multipoles_list]))
+        F = self.execute(M)
+        o = self.offsets
+        return [F[o[k]:o[k + 1]] for k in range(len(o) - 1)]
+
     @property
     def kernels(self):
         """Kernel launches per evaluation (nodes of the captured graph)."""

@@ -65,6 +65,7 @@ EXPORTED = [
     "fmm_selector_collect",
     "fmm_set_p2p_shape",
     "fmm_plan_create",
+    "fmm_plan_create_batched",
     "fmm_plan_execute",
     "fmm_plan_execute_device",
     "fmm_plan_kernels",
@@ -126,6 +127,9 @@ def lib():
     L.fmm_plan_create.argtypes = [i64, d, c, c, i32, ctypes.c_double, c, c, c, cs, c, d, op,
                                   ctypes.POINTER(ctypes.c_void_p)]
     L.fmm_plan_create.restype = c
+    L.fmm_plan_create_batched.argtypes = [c, ctypes.POINTER(ctypes.c_int64), d, c, c, i32, ctypes.c_double, c, c, c,
+                                          cs, c, d, op, ctypes.POINTER(ctypes.c_void_p)]
+    L.fmm_plan_create_batched.restype = c
     L.fmm_plan_execute.argtypes = [ctypes.c_void_p, d, d]
     L.fmm_plan_execute.restype = c
     L.fmm_plan_execute_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]

@@ -598,6 +598,68 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     return FMM_OK;
 }
 
+// ---------------------------------------------------------------- batched packing
+// Independent systems packed into one box: a G^3 grid (G a power of two) of
+// cells of side S, one system centred in each, so that cell boundaries are
+// octree node boundaries; exclusions become global indices.  Every system
+// must hold more than ncrit particles (a tree of its own).
+struct Packed {
+    std::vector<double> Xp;
+    std::vector<int32_t> exg, sys;
+    double root_r = 0.0;
+    int64_t min_size = 0;
+};
+
+int pack_systems(int nsys, const int64_t* offsets, const double* X, int exw, const int32_t* ex, int ncrit,
+                 Packed* out) {
+    const int64_t n = offsets[nsys];
+    std::vector<double> cen(3 * (size_t)nsys);
+    double hmax = 0.0;
+    int64_t min_size = n;
+    for (int k = 0; k < nsys; ++k) {
+        const int64_t a = offsets[k], b = offsets[k + 1];
+        if (b - a <= ncrit) return FMM_EINVAL;  // every system must need a tree of its own
+        min_size = std::min(min_size, b - a);
+        for (int64_t i = a; i < b; ++i)
+            for (int w = 0; w < exw; ++w) {
+                const int32_t e = ex[(size_t)w * n + i];
+                if (e < 0 || e > b - a) return FMM_EINVAL;
+            }
+        double h = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            double lo = X[d * n + a], hi = lo;
+            for (int64_t i = a; i < b; ++i) {
+                lo = std::min(lo, X[d * n + i]);
+                hi = std::max(hi, X[d * n + i]);
+            }
+            cen[3 * (size_t)k + d] = 0.5 * (lo + hi);
+            h = std::max(h, 0.5 * (hi - lo));
+        }
+        hmax = std::max(hmax, h);
+    }
+    int G = 1;
+    while ((int64_t)G * G * G < nsys) G *= 2;
+    const double S = 2.0 * hmax * 1.05 + 1e-6;
+    out->Xp.assign((size_t)3 * n, 0.0);
+    out->exg.assign((size_t)std::max(exw, 0) * n, 0);
+    out->sys.assign((size_t)n, 0);
+    for (int k = 0; k < nsys; ++k) {
+        const int ix = k % G, iy = (k / G) % G, iz = k / (G * G);
+        const double cc[3] = {(ix - 0.5 * (G - 1)) * S, (iy - 0.5 * (G - 1)) * S, (iz - 0.5 * (G - 1)) * S};
+        for (int64_t i = offsets[k]; i < offsets[k + 1]; ++i) {
+            for (int d = 0; d < 3; ++d) out->Xp[d * n + i] = (X[d * n + i] - cen[3 * (size_t)k + d]) + cc[d];
+            out->sys[i] = k;
+            for (int w = 0; w < exw; ++w) {
+                const int32_t e = ex[(size_t)w * n + i];
+                out->exg[(size_t)w * n + i] = e == 0 ? 0 : (int32_t)(e + offsets[k]);
+            }
+        }
+    }
+    out->root_r = 0.5 * G * S;
+    out->min_size = min_size;
+    return FMM_OK;
+}
+
 // ---------------------------------------------------------------- autotuner
 // For a class of calls (particle count and density in half-octaves, orders,
 // settings) the first call with opts->autotune times candidate values of
@@ -634,16 +696,23 @@ void tune_load_locked() {
     std::fclose(fp);
 }
 
+// The density is that of the bounding box of (at most 16384) evenly strided
+// particles, or of the packing box of batched systems (half-width root_r).
 std::string tune_key(int64_t n, const double* X, int mdim, int f, int p, const Opts& o, int dt, double theta,
-                     bool batched) {
-    double lo[3] = {X[0], X[n], X[2 * n]}, hi[3] = {X[0], X[n], X[2 * n]};
-    for (int d = 0; d < 3; ++d)
-        for (int64_t k = 0; k < n; ++k) {
-            lo[d] = std::min(lo[d], X[d * n + k]);
-            hi[d] = std::max(hi[d], X[d * n + k]);
-        }
+                     bool batched, double root_r = 0.0) {
     double vol = 1.0;
-    for (int d = 0; d < 3; ++d) vol *= std::max(hi[d] - lo[d], 1e-3);
+    if (root_r > 0.0) {
+        vol = 8.0 * root_r * root_r * root_r;
+    } else {
+        const int64_t step = std::max<int64_t>(1, n / 16384);
+        double lo[3] = {X[0], X[n], X[2 * n]}, hi[3] = {X[0], X[n], X[2 * n]};
+        for (int d = 0; d < 3; ++d)
+            for (int64_t k = 0; k < n; k += step) {
+                lo[d] = std::min(lo[d], X[d * n + k]);
+                hi[d] = std::max(hi[d], X[d * n + k]);
+            }
+        for (int d = 0; d < 3; ++d) vol *= std::max(hi[d] - lo[d], 1e-3);
+    }
     char b[256];
     std::snprintf(b, sizeof(b), "n%d:d%d:m%d:f%d:p%d:x%d:s%d:c%d:e%d:a%d:k%d:t%d:b%d",
                   (int)std::lround(2.0 * std::log2((double)n)), (int)std::lround(2.0 * std::log2((double)n / vol)),
@@ -746,6 +815,7 @@ int run_fmm_tuned(Workspace& ws, const Particles& P, double theta, int ncrit, in
 // field of many induced-dipole sets at fixed coordinates this way.
 struct PlanImpl {
     Workspace ws;
+    DevBuf sys;  // packed systems: system id per particle
     TreeDev t;
     Particles P{};
     Modes md{0, 0, 0};
@@ -800,7 +870,8 @@ int count_kernel_nodes(cudaGraph_t g, int* out) {
 }
 
 int plan_build(PlanImpl& pl, int64_t n, const double* X, int mdim, int exw, const int32_t* ex, double theta,
-               int ncrit, int p, int f, int dt, const double* dampf, const Opts& o) {
+               int ncrit, int p, int f, int dt, const double* dampf, const Opts& o, const int32_t* sys = nullptr,
+               double root_r = 0.0) {
     Workspace& ws = pl.ws;
     FMM_CUDA_TRY(cudaGetDevice(&ws.device));
     FMM_CUDA_TRY(cudaStreamCreateWithFlags(&pl.st, cudaStreamNonBlocking));
@@ -830,7 +901,14 @@ int plan_build(PlanImpl& pl, int64_t n, const double* X, int mdim, int exw, cons
     pl.direct = n <= ncrit;
     if (!pl.direct) {
         TreeParams tp{ncrit, theta, o.centroid_mode, 0, {0, 0, 0}, o.mac_mode, 0.0, p};
-        if (o.centroid_mode == 0) {
+        if (sys) {  // packed systems (as fmm_field_fmm_batched): root given, system-aware lists
+            FMM_TRY(pl.sys.ensure(sizeof(int32_t) * (size_t)n));
+            FMM_CUDA_TRY(cudaMemcpyAsync(pl.sys.p, sys, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+            tp.centroid_mode = 1;
+            tp.have_host_centroid = 1;
+            tp.root_r = root_r;
+            tp.d_sys = pl.sys.as<int32_t>();
+        } else if (o.centroid_mode == 0) {
             host_centroid_sequential(X, n, tp.host_centroid);
             tp.have_host_centroid = 1;
         }
@@ -1067,51 +1145,12 @@ int fmm_field_fmm_batched(int nsys, const int64_t* offsets, const double* X, int
     if (ncrit < 1 || p < 0 || !(theta > 0.0)) return FMM_EINVAL;
     if (p > kMaxP) return FMM_ENOTSUP;
     if (exw > 0 && !ex) return FMM_EINVAL;
-    // per system: sizes, exclusion ranges, bounding-box centre and half-extent
-    std::vector<double> cen(3 * (size_t)nsys), half((size_t)nsys);
-    double hmax = 0.0;
-    int64_t min_size = n;
-    for (int k = 0; k < nsys; ++k) {
-        const int64_t a = offsets[k], b = offsets[k + 1];
-        if (b - a <= ncrit) return FMM_EINVAL;  // every system must need a tree of its own
-        min_size = std::min(min_size, b - a);
-        for (int64_t i = a; i < b; ++i)
-            for (int w = 0; w < exw; ++w) {
-                const int32_t e = ex[(size_t)w * n + i];
-                if (e < 0 || e > b - a) return FMM_EINVAL;
-            }
-        double h = 0.0;
-        for (int d = 0; d < 3; ++d) {
-            double lo = X[d * n + a], hi = lo;
-            for (int64_t i = a; i < b; ++i) {
-                lo = std::min(lo, X[d * n + i]);
-                hi = std::max(hi, X[d * n + i]);
-            }
-            cen[3 * (size_t)k + d] = 0.5 * (lo + hi);
-            h = std::max(h, 0.5 * (hi - lo));
-        }
-        half[k] = h;
-        hmax = std::max(hmax, h);
-    }
-    // packing: a G^3 grid (G a power of two) of cells of side S, one system
-    // centred in each; cell boundaries are octree node boundaries
-    int G = 1;
-    while ((int64_t)G * G * G < nsys) G *= 2;
-    const double S = 2.0 * hmax * 1.05 + 1e-6;
-    std::vector<double> Xp((size_t)3 * n);
-    std::vector<int32_t> exg((size_t)std::max(exw, 0) * n), sys((size_t)n);
-    for (int k = 0; k < nsys; ++k) {
-        const int ix = k % G, iy = (k / G) % G, iz = k / (G * G);
-        const double cc[3] = {(ix - 0.5 * (G - 1)) * S, (iy - 0.5 * (G - 1)) * S, (iz - 0.5 * (G - 1)) * S};
-        for (int64_t i = offsets[k]; i < offsets[k + 1]; ++i) {
-            for (int d = 0; d < 3; ++d) Xp[d * n + i] = (X[d * n + i] - cen[3 * (size_t)k + d]) + cc[d];
-            sys[i] = k;
-            for (int w = 0; w < exw; ++w) {
-                const int32_t e = ex[(size_t)w * n + i];
-                exg[(size_t)w * n + i] = e == 0 ? 0 : (int32_t)(e + offsets[k]);
-            }
-        }
-    }
+    Packed pk;
+    FMM_TRY(pack_systems(nsys, offsets, X, exw, ex, ncrit, &pk));
+    const std::vector<double>& Xp = pk.Xp;
+    const std::vector<int32_t>& exg = pk.exg;
+    const std::vector<int32_t>& sys = pk.sys;
+    const int64_t min_size = pk.min_size;
     Workspace& ws = thread_workspace();
     cudaStream_t st = o.stream;
     const int nf = nT(field_order);
@@ -1125,10 +1164,10 @@ int fmm_field_fmm_batched(int nsys, const int64_t* offsets, const double* X, int
     FMM_TRY(dsys.ensure(sizeof(int32_t) * (size_t)n));
     FMM_CUDA_TRY(cudaMemcpyAsync(dsys.p, sys.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
     TreeParams tp{ncrit, theta, 1, 1, {0, 0, 0}, o.mac_mode, 0.0, p};
-    tp.root_r = 0.5 * G * S;
+    tp.root_r = pk.root_r;
     tp.d_sys = dsys.as<int32_t>();
     int rc = o.autotune ? run_fmm_tuned(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st,
-                                        tune_key(n, Xp.data(), mdim, field_order, p, o, dt, theta, true),
+                                        tune_key(n, Xp.data(), mdim, field_order, p, o, dt, theta, true, pk.root_r),
                                         min_size)
                         : run_fmm(ws, P, theta, ncrit, p, field_order, o, tp, ws.out_field.as<double>(), st);
     if (rc == FMM_OK) {
@@ -1173,6 +1212,36 @@ int fmm_plan_create(int64_t n, const double* X, int mdim, int exw, const int32_t
     fmm_plan* h = new (std::nothrow) fmm_plan;
     if (!h) return FMM_ENOMEM;
     const int st = plan_build(h->impl, n, X, mdim, exw, ex, theta, ncrit, p, field_order, dt, dampf, o);
+    if (st != FMM_OK) {
+        delete h;
+        return st;
+    }
+    *plan = h;
+    return FMM_OK;
+}
+
+int fmm_plan_create_batched(int nsys, const int64_t* offsets, const double* X, int mdim, int exw, const int32_t* ex,
+                            double theta, int ncrit, int p, int field_order, const char* damp, int damp_len,
+                            const double* dampf, const fmm_opts* opts, fmm_plan** plan) {
+    if (!plan) return FMM_EINVAL;
+    *plan = nullptr;
+    if (nsys < 1 || !offsets || offsets[0] != 0 || !X) return FMM_EINVAL;
+    const int64_t n = offsets[nsys];
+    int dt = 0;
+    FMM_TRY(parse_damp(damp, damp_len, &dt));
+    FMM_TRY(check_common(n, mdim, exw, field_order, dt, dampf));
+    Opts o;
+    FMM_TRY(parse_opts(opts, &o));
+    if (ncrit < 1 || p < 0 || !(theta > 0.0)) return FMM_EINVAL;
+    if (exw > 0 && !ex) return FMM_EINVAL;
+    if (p > kMaxP || o.selector != 0 || o.autotune != 0) return FMM_ENOTSUP;
+    if (o.precision != 0 && (dim_to_order(mdim) > 2 || field_order > 2)) return FMM_ENOTSUP;
+    Packed pk;
+    FMM_TRY(pack_systems(nsys, offsets, X, exw, ex, ncrit, &pk));
+    fmm_plan* h = new (std::nothrow) fmm_plan;
+    if (!h) return FMM_ENOMEM;
+    const int st = plan_build(h->impl, n, pk.Xp.data(), mdim, exw, pk.exg.data(), theta, ncrit, p, field_order, dt,
+                              dampf, o, pk.sys.data(), pk.root_r);
     if (st != FMM_OK) {
         delete h;
         return st;

@@ -304,6 +304,13 @@ typedef struct fmm_plan fmm_plan;
 int fmm_plan_create(int64_t n, const double *coordinates, int mdim, int exw, const int32_t *exclusions, double theta,
                     int ncrit, int expansion_order, int field_order, const char *damp, int damp_len,
                     const double *damping_factors, const fmm_opts *opts, fmm_plan **plan);
+/* The same for independent systems packed as fmm_field_fmm_batched packs
+ * them (arguments as that call without the multipoles); execute then takes
+ * and returns the concatenated arrays of all systems. */
+int fmm_plan_create_batched(int nsys, const int64_t *offsets, const double *coordinates, int mdim, int exw,
+                            const int32_t *exclusions, double theta, int ncrit, int expansion_order, int field_order,
+                            const char *damp, int damp_len, const double *damping_factors, const fmm_opts *opts,
+                            fmm_plan **plan);
 int fmm_plan_execute(fmm_plan *plan, const double *multipoles, double *field);
 int fmm_plan_execute_device(fmm_plan *plan, const double *d_multipoles, double *d_field);
 int fmm_plan_kernels(const fmm_plan *plan);

@@ -91,3 +91,15 @@ def test_plan_argument_checks():
     with fmm_gb300.Plan(X, 10, E, 0.5, 32, 6, 1) as plan:
         with pytest.raises(ValueError):
             plan.execute(np.zeros((X.shape[0], 4)))
+
+
+@pytest.mark.parametrize("opt", [Options.exact(), Options.exact(precision="mixed")])
+def test_batched_plan_matches_batched_call(opt):
+    sl = systems.batched_uniform(n_systems=9, nmin=400, nmax=4000, density=0.1, order=1, seed=8)
+    Fb = fmm_gb300.field_fmm_batched(sl, 0.5, 32, 6, 1, "ERF", options=opt)
+    with fmm_gb300.Plan.batched(sl, 4, 0.5, 32, 6, 1, "ERF", options=opt) as plan:
+        Fp = plan.execute_systems([s["multipoles"] for s in sl])
+        Fp2 = plan.execute_systems([2.0 * np.asarray(s["multipoles"]) for s in sl])
+    for a, b, c in zip(Fb, Fp, Fp2):
+        assert rel_err(b, a) <= 1e-13
+        assert rel_err(c, 2.0 * a) <= 1e-12
