@@ -676,12 +676,24 @@ def main():
         fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"], arm["theta"], NCRIT, arm["p"],
                             F_ORDER, DAMP, s["damping_factors"], options=ta)
         first = time.perf_counter() - t0
-        Ft, tt_ = timed_host(lambda: fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"],
-                                                         arm["theta"], NCRIT, arm["p"], F_ORDER, DAMP,
-                                                         s["damping_factors"], options=ta), args.steps, warmup=0)
-        stt = fmm_gb300.last_stats()
+        # tuned and untuned host calls interleaved, so that both see the same
+        # state of the host and the GPU
+        tt_l, tu_l = [], []
+        for _ in range(args.steps):
+            Ft, t1_ = timed_host(lambda: fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"],
+                                                             arm["theta"], NCRIT, arm["p"], F_ORDER, DAMP,
+                                                             s["damping_factors"], options=ta), 1, warmup=0)
+            stt = fmm_gb300.last_stats()
+            _, t2_ = timed_host(lambda: fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"],
+                                                            arm["theta"], NCRIT, arm["p"], F_ORDER, DAMP,
+                                                            s["damping_factors"], options=arm_options(args.arm)), 1,
+                                warmup=0)
+            tt_l.append(t1_)
+            tu_l.append(t2_)
+        tt_, tu_ = float(np.mean(tt_l)), float(np.mean(tu_l))
         extras["autotuned"] = {"e2e_value": n / tt_, "unit": "particles/s", "first_call_s": first,
-                               "gain_over_untuned_e2e": (n / tt_) / e2e["value"], "accuracy": accuracy_of(Ft),
+                               "untuned_e2e_value": n / tu_, "gain_over_untuned_e2e": tu_ / tt_,
+                               "accuracy": accuracy_of(Ft),
                                "ncrit": int(stt["ncrit_used"]),
                                "near_field_shape": [int(stt["p2p_threads"]), int(stt["p2p_stage"]),
                                                     int(stt["p2p_queue"])], "t_total_device_ms": stt["t_total"]}

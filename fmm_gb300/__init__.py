@@ -68,7 +68,7 @@ class Options:
 import os
 import threading
 
-SELECTOR_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "selector_v1.bin")
+SELECTOR_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "selector_v2.bin")
 _sel_local = threading.local()
 
 

@@ -47,7 +47,7 @@ void Workspace::release_buffers(bool keep_selector) {
                      &sz,        &smc,       &sd,          &fsorted,    &mom,        &loc,        &partial,
                      &term_off,  &term_abc,  &term_c, &f32buf, &wred, &far_ord, &sel_norms, &sel_params, &sel_scratch, &sysbuf,
                      &m2l_tgt, &m2l_keys, &m2l_keys2, &m2l_vals, &m2l_vals2, &m2l_ukeys, &m2l_cnt, &m2l_gstart,
-                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &m2l_wsplit, &m2l_gop, &m2l_gopoff, &m2l_rowbase, &xlate, &l2pt, &dsmc, &f32node, &lattice, &p2p_order};
+                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &m2l_wsplit, &m2l_gop, &m2l_gopoff, &m2l_rowbase, &xlate, &l2pt, &dsmc, &f32node, &lattice, &p2p_order, &sel_budget};
     for (DevBuf* b : all)
         if (!(keep_selector && b == &sel_params)) b->release();
     if (!keep_selector) sel_ready = false;
@@ -330,6 +330,19 @@ double sel_theta_loose() {
     return v;
 }
 constexpr double kSelPairsPerTarget = 150.0;
+constexpr double kSelMargin = 0.6;  // default log10 margin of the per-pair budget
+
+// log10 margin between a pair's predicted error and its budget:
+// FMM_GB300_SEL_MARGIN overrides the default (tuning; values outside [0, 3]
+// are ignored).
+double sel_margin() {
+    static const double v = [] {
+        const char* e = std::getenv("FMM_GB300_SEL_MARGIN");
+        const double x = e ? std::atof(e) : -1.0;
+        return (x >= 0.0 && x <= 3.0) ? x : kSelMargin;
+    }();
+    return v;
+}
 
 // Relative RMS error (field columns of order >= 1) of F against R, both
 // (ntgt x nf) column-major on the host.
@@ -456,25 +469,14 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         tpl.sel_P = p;
         tpl.sel_chi = ws.f32node.as<float4>();  // prepare_f32_records
         tpl.sel_clo = tpl.sel_chi + t.num_nodes;
-        // per-pair error budget from the sampled field scale (FP32 estimate)
-        double* d_est = ws.sel_scratch.as<double>() + (size_t)nt * nf;
-        const int64_t* d_rows = reinterpret_cast<const int64_t*>(ws.sel_scratch.as<double>() + (size_t)nt * nf * 2);
-        FMM_TRY(launch_direct_scale_f32(ws, P, t, f, d_est, st, nt, d_rows));
-        std::vector<double> est((size_t)nt * nf);
-        FMM_CUDA_TRY(cudaMemcpyAsync(est.data(), d_est, sizeof(double) * nt * nf, cudaMemcpyDeviceToHost, st));
-        FMM_CUDA_TRY(cudaStreamSynchronize(st));
-        std::vector<double> mag(nt);
-        for (int k = 0; k < nt; ++k) {
-            double g = 0.0;
-            for (int c = 1; c < 4; ++c) g += est[(size_t)c * nt + k] * est[(size_t)c * nt + k];
-            mag[k] = std::sqrt(g);
-        }
-        std::sort(mag.begin(), mag.end());
-        const double scale = 0.5 * mag[nt / 2];
-        // truncation budget: what the FP32 near field leaves of the target
+        // per-pair error budgets by target node: the truncation share of the
+        // target error times half the node's typical local field (geometric
+        // mean over its particles), spread over the far pairs a particle sees
         const double floor_fp32 = md.precision == 0 ? 0.0 : 9e-7;
         const double trunc = std::sqrt(std::max(o.target * o.target - floor_fp32 * floor_fp32, 0.04 * o.target * o.target));
-        tpl.sel_log_budget = (float)(std::log10(trunc * scale / std::sqrt(kSelPairsPerTarget)) - 0.3);
+        const float base = (float)(std::log10(trunc / std::sqrt(kSelPairsPerTarget)) - sel_margin());
+        FMM_TRY(selector_node_budgets(ws, P, t, base, st));
+        tpl.sel_budget = ws.sel_budget.as<float>();
         tpl.sel_theta = sel_theta_loose();
     }
     cudaEventRecord(ws.ev[2], st);

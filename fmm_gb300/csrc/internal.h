@@ -82,7 +82,7 @@ struct TreeParams {
     const float* sel_lnorm = nullptr;   // per node log10 norms of reduced weights by order
     const float* sel_dmin = nullptr;    // per node smallest damping factor
     int sel_P = 0;                      // order of the stored norms
-    float sel_log_budget = 0.0f;        // log10 of the per-pair error budget
+    const float* sel_budget = nullptr;  // per target node: log10 of the per-pair error budget
     double sel_theta = 0.0;             // loose acceptance test applied before the network
     const float4* sel_chi = nullptr;    // FP32 node centres (hi, rmax in w) of the learned list build
     const float4* sel_clo = nullptr;    // and their low parts (half-width in w)
@@ -102,6 +102,15 @@ double min_damping_factor(Workspace& ws, const double* d_damp, int64_t n, cudaSt
 // Host-side sequential centroid (the reference's SUM order).
 void host_centroid_sequential(const double* coords, int64_t n, double c[3]);
 
+// A batch of consecutive displacement groups of the grouped M2L whose
+// operators are held at once: groups [g0, g1), their tasks [t0, t1), and the
+// offset of their first operator.
+struct M2lBatch {
+    int g0, g1;
+    int64_t gop_base;
+    int t0, t1;
+};
+
 struct P2pShape {
     int threads = 128;
     int stage = 320;
@@ -120,6 +129,7 @@ struct Workspace {
     DevBuf front_a, front_b, far_pairs, near_pairs, far_sorted, near_sorted;
     DevBuf node_dfs, far_src, near_src, far_ord, sysbuf;
     DevBuf sel_norms, sel_params, sel_scratch;
+    DevBuf sel_budget;  // per node: log10 error budget of far pairs with that target, then its field scale
     // grouped M2L
     DevBuf m2l_tgt, m2l_keys, m2l_keys2, m2l_vals, m2l_vals2, m2l_ukeys, m2l_cnt, m2l_gstart, m2l_tcnt, m2l_toff,
         m2l_tasks, m2l_T, m2l_gq, m2l_gab, m2l_wsc, m2l_out, m2l_wsplit, m2l_gop, m2l_gopoff, m2l_rowbase;
@@ -165,6 +175,8 @@ struct Workspace {
     P2pShape p2p_shape;  // FP32 near-field launch shape
     DevBuf p2p_order;    // target leaves by decreasing pair work (queue mode), and scratch
     int m2l_ng = 0, m2l_ntasks = 0;  // grouped M2L structure of the last evaluation
+    bool m2l_pairwise = false;       // the last structure chose the per-pair M2L kernel
+    std::vector<M2lBatch> m2l_batches;  // operator batches of the last structure
     int64_t list_candidates = 0; // cell pairs examined by the last list build
     int64_t list_evals = 0;      // of which evaluated by the selector network
     int device = -1;
@@ -232,6 +244,10 @@ int launch_m2l_grouped(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaSt
 int launch_reduce_moments(Workspace& ws, const TreeDev& t, int p, cudaStream_t st);
 // selector.cu
 int selector_node_norms(Workspace& ws, const TreeDev& t, int P, const double* d_sorted_damp, cudaStream_t st);
+// Local field scale per leaf (near_f32.cu; after prepare_f32_records) and the
+// per-node error budgets built from it (selector.cu).
+int launch_leaf_field_scale(Workspace& ws, const Particles& P, const TreeDev& t, float* d_scale, cudaStream_t st);
+int selector_node_budgets(Workspace& ws, const Particles& P, const TreeDev& t, float base, cudaStream_t st);
 int selector_pair_data(Workspace& ws, const Particles& Pt, const TreeDev& t, int P, const int2* d_pairs, int npairs,
                        float* d_feats, float* d_labels, cudaStream_t st);
 int selector_unpack_far(Workspace& ws, const TreeDev& t, int2* d_out, cudaStream_t st);

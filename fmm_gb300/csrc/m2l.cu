@@ -316,7 +316,9 @@ int launch_m2l_reduced(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaSt
         count_launches(1);
         k_reduce_moments<<<grid_for(M, wpb), 32 * wpb, sm, st>>>(M, p, ws.mom.as<double>(), ws.wred.as<double>());
     }
-    const int gst = launch_m2l_grouped(ws, t, p, fp32, st);
+    // (replays keep the choice between grouped products and the per-pair
+    // kernel made when the structure was built)
+    const int gst = (ws.reuse_structure && ws.m2l_pairwise) ? FMM_ENOTSUP : launch_m2l_grouped(ws, t, p, fp32, st);
     if (gst == FMM_ENOTSUP) {
         // FP64 operator too large for shared memory: per-pair kernel
         if (fp32)

@@ -85,7 +85,7 @@ __global__ void k_scale_weights(int M, int nr, int ld, const double* __restrict_
 // pipe; its error (a few 1e-8 relative of the displacement, up to ~1e-4 cell
 // units at the largest encodable displacement) stays far below the 1e-3
 // tolerance of the integer test.  Without them, FP64 with a 1e-6 tolerance.
-__global__ void k_m2l_keys(int64_t nfar, const TreeDev t, const int32_t* __restrict__ tgt, int p,
+__global__ void k_m2l_keys(int64_t nfar, const TreeDev t, const int32_t* __restrict__ tgt, int p, int oclass,
                            const float4* __restrict__ chi, const float4* __restrict__ clo,
                            uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -120,12 +120,13 @@ __global__ void k_m2l_keys(int64_t nfar, const TreeDev t, const int32_t* __restr
         tol = 1e-6f;
     }
     const int dl = t.depth[i] - t.depth[j];
+    const int oc = (ord + oclass - 1) / oclass;  // order class: the group takes its pairs' highest order
     const float lim = (float)(kDOff - 1);
     const bool grid = ex < tol && ey < tol && ez < tol && fabsf(rx) <= lim && fabsf(ry) <= lim && fabsf(rz) <= lim &&
                       dl > -31 && dl < 31;
     uint64_t key;
     if (grid)
-        key = ((uint64_t)(dl + 31) << 40) | ((uint64_t)ord << 36) | ((uint64_t)((int64_t)rx + kDOff) << 24) |
+        key = ((uint64_t)(dl + 31) << 40) | ((uint64_t)oc << 36) | ((uint64_t)((int64_t)rx + kDOff) << 24) |
               ((uint64_t)((int64_t)ry + kDOff) << 12) | (uint64_t)((int64_t)rz + kDOff);
     else
         key = ((uint64_t)kFallback << 40) | (uint64_t)q;
@@ -157,8 +158,11 @@ __global__ void __launch_bounds__(128) k_group_tensor(int ngroups, const uint64_
     const uint64_t key = ukeys[g];
     const int pos0 = svals[gstart[g]];
     const int i = tgt[pos0], j = t.far_src[pos0];
-    const int q = (int)(key >> 40) == kFallback ? (t.far_ord ? min((int)t.far_ord[pos0], p) : p)
-                                                 : (int)((key >> 36) & 15);
+    // the group's order: the highest of its pairs' orders
+    int q = 0;
+    for (int k = gstart[g] + lane; k < gstart[g + 1]; k += 32)
+        q = max(q, t.far_ord ? min((int)t.far_ord[svals[k]], p) : p);
+    for (int off = 16; off > 0; off >>= 1) q = max(q, __shfl_xor_sync(0xffffffffu, q, off));
     const double hi = t.r[i], hj = t.r[j], hc = fmax(hi, hj);
     const double X = (t.cx[i] - t.cx[j]) / hc, Y = (t.cy[i] - t.cy[j]) / hc, Z = (t.cz[i] - t.cz[j]) / hc;
     const int Nq = 2 * q;
@@ -586,11 +590,12 @@ __global__ void k_gop_sizes(int ng, const int32_t* __restrict__ gq, int64_t* __r
 __global__ void __launch_bounds__(256) k_group_operator(int ldT, const float* __restrict__ gT,
                                                         const int32_t* __restrict__ gq,
                                                         const float2* __restrict__ gab,
-                                                        const int64_t* __restrict__ goff, float* __restrict__ gop) {
+                                                        const int64_t* __restrict__ goff, int g0, int64_t gop_base,
+                                                        float* __restrict__ gop) {
     __shared__ int dec[(kMaxP + 1) * (kMaxP + 1)];
     __shared__ float apow[32], bpow[32];
     __shared__ float Tsh[1 + 3 * (2 * kMaxP) * (2 * kMaxP + 1) / 2];
-    const int g = blockIdx.x;
+    const int g = g0 + blockIdx.x;
     const int q = gq[g];
     const int nrq = (q + 1) * (q + 1), nch = (nrq + kTcKC - 1) / kTcKC, nrow = tc_halves(q) * kTcRows;
     for (int e = threadIdx.x; e < nrq; e += blockDim.x) dec[e] = qcomp(e);
@@ -607,7 +612,7 @@ __global__ void __launch_bounds__(256) k_group_operator(int ldT, const float* __
     const int nTq = rbase(2 * q + 1);
     for (int e = threadIdx.x; e < nTq; e += blockDim.x) Tsh[e] = gT[(size_t)g * ldT + e];
     __syncthreads();
-    float* out = gop + goff[g];
+    float* out = gop + (goff[g] - gop_base);
     // consecutive threads write consecutive floats of a (half, chunk) block:
     // pos inverts tc_off(r, k) = (r/8) 64 + (k/4) 32 + (r%8) 4 + k%4
     constexpr int BLK = kTcRows * kTcKC;
@@ -648,7 +653,7 @@ __device__ __forceinline__ void tc_load_rows(int t, const int2* __restrict__ tas
 __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict__ tasks, int ntasks,
                                                          const int32_t* __restrict__ gstart,
                                                          const int32_t* __restrict__ gq,
-                                                         const int64_t* __restrict__ goff,
+                                                         const int64_t* __restrict__ goff, int64_t gop_base,
                                                          const float* __restrict__ gop,
                                                          const int32_t* __restrict__ psrc,
                                                          const float* __restrict__ wsp, int ldk,
@@ -702,7 +707,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
             const int next = task + gridDim.x;
             if (next < ntasks) tc_load_rows<RG>(next, tasks, gstart, psrc, rg0, rsub, nrows);  // in flight
             // the task's operator half
-            const float* G = gop + goff[g] + (size_t)(tasks[task].y & 1) * nch * 2 * TcSmem::g_floats;
+            const float* G = gop + (goff[g] - gop_base) + (size_t)(tasks[task].y & 1) * nch * 2 * TcSmem::g_floats;
             for (int ch = 0; ch < nch; ++ch, ++u) {
                 const int st = (int)(u % kTcStages);
                 if (u >= (uint32_t)kTcStages &&
@@ -893,6 +898,14 @@ bool product_on_cuda_cores() {
     return e && std::strcmp(e, "cuda") == 0;
 }
 
+// Orders share a displacement group in classes of kOrderClass consecutive
+// orders; the group takes its pairs' highest order (fewer operators for the
+// learned selector's mixed orders).
+constexpr int kOrderClass = 2;
+
+constexpr double kMinGroupPairs = 16.0;    // mean far pairs per displacement group for the grouped products
+constexpr double kOperatorBytes = 16e9;  // TF32 operator parts of one batch of groups
+
 template <typename R, int CPT>
 int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
     const int M = t.num_nodes, nr = (p + 1) * (p + 1), N = 2 * p, nTr = rbase(N + 1);
@@ -906,6 +919,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
     if (nf > 0 && !ws.reuse_structure) {
         // structure: displacement groups, their tensors and operators, tasks
         // and result rows (geometry only; kept for replays)
+        ws.m2l_pairwise = false;
         FMM_TRY(ws.m2l_tgt.ensure(sizeof(int32_t) * nf));
         FMM_TRY(ws.m2l_keys.ensure(sizeof(uint64_t) * nf));
         FMM_TRY(ws.m2l_keys2.ensure(sizeof(uint64_t) * nf));
@@ -922,7 +936,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         count_launches(1);
         // FP32 node data where the mixed path prepared it
         const float4* chi = (sizeof(R) == 4 && ws.f32node_ok) ? ws.f32node.as<float4>() : nullptr;
-        k_m2l_keys<<<grid_for(nf, 256), 256, 0, st>>>(nf, t, tgt, p, chi, chi ? chi + M : nullptr,
+        k_m2l_keys<<<grid_for(nf, 256), 256, 0, st>>>(nf, t, tgt, p, kOrderClass, chi, chi ? chi + M : nullptr,
                                                        ws.m2l_keys.as<uint64_t>(), ws.m2l_vals.as<int32_t>());
         // sort by key, run-length encode into groups
         int* d_nruns = reinterpret_cast<int*>(ws.counters.as<unsigned long long>() + 14);
@@ -944,6 +958,13 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_CUDA_TRY(cudaMemcpyAsync(&ng, d_nruns, sizeof(int), cudaMemcpyDeviceToHost, st));
         FMM_CUDA_TRY(cudaStreamSynchronize(st));
         ws.m2l_groups = ng;
+        // displacement groups of a few pairs each (irregular trees, mixed
+        // orders) leave the products' columns empty and multiply the
+        // per-group operators: the per-pair kernel is then the faster one
+        if ((double)nf < kMinGroupPairs * (double)ng) {
+            ws.m2l_pairwise = true;
+            return FMM_ENOTSUP;
+        }
         FMM_CUDA_TRY(cudaMemsetAsync(ws.m2l_cnt.as<int32_t>() + ng, 0, sizeof(int32_t), st));
         size_t tb4 = 0;
         cub::DeviceScan::ExclusiveSum(nullptr, tb4, ws.m2l_cnt.as<int32_t>(), ws.m2l_gstart.as<int32_t>(), ng + 1, st);
@@ -1017,15 +1038,33 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
             cub::DeviceScan::ExclusiveSum(nullptr, tb6, goff, goff, ng + 1, st);
             FMM_TRY(ws.cub_tmp.ensure(tb6));
             FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb6, goff, goff, ng + 1, st));
-            // TF32 parts of the operators (per group), room for every group at
-            // the largest order of the call (no wait for the exact total)
-            const int nr_max = (p + 1) * (p + 1);
-            const size_t gop_max = (size_t)ng * tc_halves(p) * ((nr_max + kTcKC - 1) / kTcKC) * 2 * kTcRows * kTcKC;
-            FMM_TRY(ws.m2l_gop.ensure(sizeof(float) * std::max<size_t>(1, gop_max)));
-            count_launches(1);
-            k_group_operator<<<(unsigned)ng, 256, 0, st>>>(ldT, reinterpret_cast<const float*>(ws.m2l_T.p),
-                                                           ws.m2l_gq.as<int32_t>(), ws.m2l_gab.as<float2>(), goff,
-                                                           ws.m2l_gop.as<float>());
+            // TF32 parts of the operators (per group, at each group's order),
+            // in batches of consecutive groups of at most kOperatorBytes: one
+            // batch is built here once; several are built, each before the
+            // product over its tasks, at every evaluation
+            std::vector<int64_t> hgoff((size_t)ng + 1);
+            std::vector<int32_t> htoff((size_t)ng + 1);
+            FMM_CUDA_TRY(cudaMemcpyAsync(hgoff.data(), goff, sizeof(int64_t) * (ng + 1), cudaMemcpyDeviceToHost, st));
+            FMM_CUDA_TRY(cudaMemcpyAsync(htoff.data(), ws.m2l_toff.as<int32_t>(), sizeof(int32_t) * (ng + 1),
+                                         cudaMemcpyDeviceToHost, st));
+            FMM_CUDA_TRY(cudaStreamSynchronize(st));
+            const int64_t cap = (int64_t)(kOperatorBytes / sizeof(float));
+            ws.m2l_batches.clear();
+            int64_t biggest = 0;
+            for (int g0 = 0; g0 < ng;) {
+                int g1 = g0 + 1;
+                while (g1 < ng && hgoff[g1 + 1] - hgoff[g0] <= cap) ++g1;
+                ws.m2l_batches.push_back({g0, g1, hgoff[g0], htoff[g0], htoff[g1]});
+                biggest = std::max(biggest, hgoff[g1] - hgoff[g0]);
+                g0 = g1;
+            }
+            FMM_TRY(ws.m2l_gop.ensure(sizeof(float) * std::max<int64_t>(1, biggest)));
+            if (ws.m2l_batches.size() == 1) {
+                count_launches(1);
+                k_group_operator<<<(unsigned)ng, 256, 0, st>>>(ldT, reinterpret_cast<const float*>(ws.m2l_T.p),
+                                                               ws.m2l_gq.as<int32_t>(), ws.m2l_gab.as<float2>(), goff,
+                                                               0, 0, ws.m2l_gop.as<float>());
+            }
         }
         ws.m2l_ng = ng;
         ws.m2l_ntasks = ntasks;
@@ -1048,17 +1087,29 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
             int dev = 0, sms = 0;
             FMM_CUDA_TRY(cudaGetDevice(&dev));
             FMM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-            const int grid = std::max(1, std::min(ntasks, sms));  // one block per SM (all tensor memory)
             if (!ws.product_err) FMM_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));  // first product of the call
             if (ws.events_ready) {
                 cudaEventRecord(ws.ev[8], st);
                 ws.product_timed = true;
             }
-            count_launches(1);
-            k_m2l_tc<<<(unsigned)grid, kTcThreads, TcSmem::bytes, st>>>(
-                ws.m2l_tasks.as<int2>(), ntasks, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(),
-                ws.m2l_gopoff.as<int64_t>(), ws.m2l_gop.as<float>(), ws.m2l_vals.as<int32_t>(),
-                ws.m2l_wsplit.as<float>(), ldk, reinterpret_cast<float*>(ws.m2l_out.p), rowbase, d_err);
+            const bool many = ws.m2l_batches.size() > 1;
+            for (const M2lBatch& b : ws.m2l_batches) {
+                if (many) {
+                    count_launches(1);
+                    k_group_operator<<<(unsigned)(b.g1 - b.g0), 256, 0, st>>>(
+                        ldT, reinterpret_cast<const float*>(ws.m2l_T.p), ws.m2l_gq.as<int32_t>(),
+                        ws.m2l_gab.as<float2>(), ws.m2l_gopoff.as<int64_t>(), b.g0, b.gop_base, ws.m2l_gop.as<float>());
+                }
+                const int nt = b.t1 - b.t0;
+                if (nt <= 0) continue;
+                const int grid = std::max(1, std::min(nt, sms));  // one block per SM (all tensor memory)
+                count_launches(1);
+                k_m2l_tc<<<(unsigned)grid, kTcThreads, TcSmem::bytes, st>>>(
+                    ws.m2l_tasks.as<int2>() + b.t0, nt, ws.m2l_gstart.as<int32_t>(), ws.m2l_gq.as<int32_t>(),
+                    ws.m2l_gopoff.as<int64_t>(), many ? b.gop_base : 0, ws.m2l_gop.as<float>(),
+                    ws.m2l_vals.as<int32_t>(), ws.m2l_wsplit.as<float>(), ldk, reinterpret_cast<float*>(ws.m2l_out.p),
+                    rowbase, d_err);
+            }
             if (ws.product_timed) cudaEventRecord(ws.ev[9], st);
             // the product's error flag is read with the call's final copies
             ws.product_err = d_err;

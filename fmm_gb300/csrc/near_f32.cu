@@ -364,6 +364,84 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
     }
 }
 
+// Local field scale of each leaf for the learned selector's error budgets:
+// the field (order-1 components, FP32, damped as the call) at up to
+// kScaleSamples particles of the leaf from every particle of its smallest
+// ancestor holding at least kScaleNeighbours particles (a subtree is one
+// contiguous range of the sorted particles; at most kScaleWindow of them
+// around the leaf), excluded partners and the
+// particle itself skipped; the leaf's values are the mean and the minimum
+// of log10 of the magnitudes found (-30 for a zero field), at scale[leaf]
+// and scale[num_nodes + leaf].  The field at a particle is
+// dominated by its nearest neighbours, which lie in that range except near
+// the range's faces; the estimate sets how much absolute error each far pair
+// may carry at the leaf.
+constexpr int kScaleSamples = 4;
+constexpr int kScaleNeighbours = 256;
+constexpr int kScaleWindow = 1024;
+
+template <int M>
+__global__ void __launch_bounds__(128) k_leaf_field_scale(const TreeDev t, const float4* __restrict__ rec,
+                                                          const float4* __restrict__ chi, int damp, int exw,
+                                                          const int32_t* __restrict__ excl, int64_t n,
+                                                          float* __restrict__ scale) {
+    constexpr int NM = nT(M), NV = rec_vec(NM);
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= t.num_leaves) return;
+    const int leaf = t.leaves[w];
+    const int s0 = t.start[leaf], cnt = t.count[leaf];
+    int anc = leaf;
+    while (t.count[anc] < kScaleNeighbours && t.parent[anc] >= 0) anc = t.parent[anc];
+    // at most kScaleWindow particles of that range, centred on the leaf's
+    // (Morton order keeps them near it)
+    int a0 = t.start[anc], a1 = a0 + t.count[anc];
+    if (a1 - a0 > kScaleWindow) {
+        a0 = max(a0, min(s0 + cnt / 2 - kScaleWindow / 2, a1 - kScaleWindow));
+        a1 = a0 + kScaleWindow;
+    }
+    const int ns = min(kScaleSamples, cnt);
+    float lsum = 0.0f, lmin = 30.0f;
+    for (int sidx = 0; sidx < ns; ++sidx) {
+        const int k = s0 + (int)((int64_t)sidx * cnt / ns);
+        const float4 ta = rec[(size_t)k * NV], tb = rec[(size_t)k * NV + 1];
+        const float4 ca = chi[leaf];
+        const float tx = ta.x + ca.x, ty = ta.y + ca.y, tz = ta.z + ca.z;
+        const int ot = __float_as_int(tb.w) - 1;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int q = a0 + lane; q < a1; q += 32) {
+            if (q == k) continue;
+            const float4* r = rec + (size_t)q * NV;
+            const float4 sa = r[0], sb = r[1];
+            const int o = __float_as_int(sb.w);
+            bool ex = false;
+            for (int e = 0; e < exw; ++e) ex |= (excl[(size_t)e * n + ot] == o);
+            if (ex) continue;
+            const float4 cb = chi[t.leaf_of[q]];
+            float mc[4 * (NV - 2)];
+#pragma unroll
+            for (int v = 0; v < NV - 2; ++v) {
+                const float4 wv = r[2 + v];
+                mc[4 * v] = wv.x;
+                mc[4 * v + 1] = wv.y;
+                mc[4 * v + 2] = wv.z;
+                mc[4 * v + 3] = wv.w;
+            }
+            pair_field<M, 1, float>(tx - (sa.x + cb.x), ty - (sa.y + cb.y), tz - (sa.z + cb.z), ta.w * sa.w, damp,
+                                    mc, acc);
+        }
+#pragma unroll
+        for (int c = 1; c < 4; ++c)
+            for (int off = 16; off > 0; off >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], off);
+        const float l = log10f(fmaxf(sqrtf(acc[1] * acc[1] + acc[2] * acc[2] + acc[3] * acc[3]), 1e-30f));
+        lsum += l;
+        lmin = fminf(lmin, l);
+    }
+    if (lane == 0) {
+        scale[leaf] = ns > 0 ? lsum / (float)ns : -30.0f;
+        scale[t.num_nodes + leaf] = ns > 0 ? lmin : -30.0f;
+    }
+}
+
 // Pair work of each target leaf (its particles times the particles of its
 // near list) for the work queue's order.
 __global__ void k_leaf_cost(const TreeDev t, uint32_t* __restrict__ cost, int32_t* __restrict__ ids) {
@@ -470,6 +548,29 @@ int launch_direct_scale_f32(Workspace& ws, const Particles& P, const TreeDev& t,
     FMM_MF_SWITCH(m, field_order,
                   (k_direct_scale<MM, FF><<<grid, 128, 0, st>>>(t, ws.f32buf.as<float4>(), chi, d_targets, ntgt, P.n,
                                                                  P.damp_type, P.exw, P.excl, chunk, d_out)));
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
+int launch_leaf_field_scale(Workspace& ws, const Particles& P, const TreeDev& t, float* d_scale, cudaStream_t st) {
+    const int m = dim_to_order(P.dim);
+    const float4* rec = ws.f32buf.as<float4>();  // prepare_f32_records
+    const float4* chi = ws.f32node.as<float4>();
+    const unsigned blocks = grid_for((int64_t)t.num_leaves * 32, 128);
+    switch (m) {
+        case 0:
+            k_leaf_field_scale<0><<<blocks, 128, 0, st>>>(t, rec, chi, P.damp_type, P.exw, P.excl, P.n, d_scale);
+            break;
+        case 1:
+            k_leaf_field_scale<1><<<blocks, 128, 0, st>>>(t, rec, chi, P.damp_type, P.exw, P.excl, P.n, d_scale);
+            break;
+        case 2:
+            k_leaf_field_scale<2><<<blocks, 128, 0, st>>>(t, rec, chi, P.damp_type, P.exw, P.excl, P.n, d_scale);
+            break;
+        default:
+            return FMM_ENOTSUP;
+    }
+    count_launches(1);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }

@@ -76,7 +76,50 @@ __global__ void k_dmin_up(int M, const TreeDev t, float* __restrict__ dmin) {
     for (int a = t.parent[node]; a >= 0; a = t.parent[a]) atomicMin(reinterpret_cast<int*>(dmin + a), v);
 }
 
+// Order-preserving map of floats to ints (for atomicMin on any sign).
+__device__ __forceinline__ int ordered_int(float f) {
+    const int b = __float_as_int(f);
+    return b >= 0 ? b : b ^ 0x7fffffff;
+}
+__device__ __forceinline__ float ordered_float(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+// Per node: the smallest of its leaves' scales (each leaf's mean log10 local
+// field over its sample particles), by atomicMin into every ancestor.
+__global__ void k_scale_up(int M, const TreeDev t, const float* __restrict__ lmean, int* __restrict__ mn) {
+    const int node = blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= M || !t.is_leaf[node]) return;
+    const int m = ordered_int(lmean[node]);
+    for (int a = node; a >= 0; a = t.parent[a]) atomicMin(mn + a, m);
+}
+
+// log10 error budget of a far pair with the node as target: base + the
+// node's scale.  A node's particles differ in field strength; the weakest
+// leaf of a node (the tail of a cluster, a particle far from its
+// neighbours) sets how much absolute error that node's far pairs may carry.
+__global__ void k_node_budget(int M, float base, const int* __restrict__ mn, float* __restrict__ budget) {
+    const int node = blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= M) return;
+    budget[node] = base + ordered_float(mn[node]);
+}
+
 }  // namespace
+
+// Per-node log10 error budgets of the learned selector (see k_node_budget):
+// leaf field scales from the FP32 records, minimum over each subtree.
+int selector_node_budgets(Workspace& ws, const Particles& P, const TreeDev& t, float base, cudaStream_t st) {
+    const int M = t.num_nodes;
+    FMM_TRY(ws.sel_budget.ensure(sizeof(float) * 4 * (size_t)M));
+    float* lscale = ws.sel_budget.as<float>() + M;  // leaf means, then leaf minima
+    int* mn = reinterpret_cast<int*>(lscale + 2 * (size_t)M);
+    FMM_CUDA_TRY(cudaMemsetAsync(mn, 0x7f, sizeof(int) * (size_t)M, st));
+    FMM_TRY(launch_leaf_field_scale(ws, P, t, lscale, st));
+    count_launches(1);
+    k_scale_up<<<grid_for(M, 128), 128, 0, st>>>(M, t, lscale, mn);
+    count_launches(1);
+    k_node_budget<<<grid_for(M, 256), 256, 0, st>>>(M, base, mn, ws.sel_budget.as<float>());
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
 
 namespace {
 

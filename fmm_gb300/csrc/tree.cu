@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
     const int2* __restrict__ in, int nin, int2* __restrict__ out, int64_t cap_out, uint64_t* __restrict__ far,
     int64_t cap_far, uint64_t* __restrict__ nearp, int64_t cap_near, const TreeDev t, float theta_loose, float rdamp,
     int qmax, const float* __restrict__ params, const float* __restrict__ lnorm, const float* __restrict__ dmin,
-    int P, float log_budget, const float4* __restrict__ chi, const float4* __restrict__ clo,
+    int P, const float* __restrict__ log_budget, const float4* __restrict__ chi, const float4* __restrict__ clo,
     unsigned long long* counters) {
     extern __shared__ __align__(16) float sm_sel[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -455,8 +455,9 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
         __syncwarp();
         warp_mlp_tc(params, X, Y, __popc(need), lane);
         if (accept) {
+            const float b = log_budget[i];  // the target node's budget
             for (int o = kQmin; o <= qmax; ++o)
-                if (Y[slot * kMlpOutP + (o - kQmin)] <= log_budget) {
+                if (Y[slot * kMlpOutP + (o - kQmin)] <= b) {
                     order = o;
                     break;
                 }
@@ -781,7 +782,7 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
                 k_list_iter_learned<<<grid_for(nin, 128), 128, smem, st>>>(
                     fin, (int)nin, fout, cap_front, ws.far_pairs.as<uint64_t>(), cap_far, ws.near_pairs.as<uint64_t>(),
                     cap_near, t, (float)tp.sel_theta, tp.mac_mode == 1 ? (float)tp.rdamp : 0.0f, tp.order,
-                    tp.sel_params, tp.sel_lnorm, tp.sel_dmin, tp.sel_P, tp.sel_log_budget, tp.sel_chi, tp.sel_clo,
+                    tp.sel_params, tp.sel_lnorm, tp.sel_dmin, tp.sel_P, tp.sel_budget, tp.sel_chi, tp.sel_clo,
                     ctr);
             } else
             k_list_iter<<<grid_for(nin, 256), 256, 0, st>>>(fin, (int)nin, fout, cap_front,

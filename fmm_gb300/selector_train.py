@@ -1,9 +1,12 @@
 """Trains the expansion-order selector on the GPU.
 
-    python -m fmm_gb300.selector_train [--systems 50] [--n-mol 33334] [--out fmm_gb300/data/selector_v1]
+    python -m fmm_gb300.selector_train [--systems 50] [--blob-systems 25] [--n-mol 33334]
+                                       [--out fmm_gb300/data/selector_v2]
 
 For each of `systems` seeded water-like systems (N = 3 x n_mol particles at
-the density of the 1M benchmark system, AMOEBA damping factors) far pairs are
+the density of the 1M benchmark system, AMOEBA damping factors) and
+`blob_systems` clustered ones (Gaussian blobs as the 2M clustered benchmark
+system, scaled to the same N at its density) far pairs are
 sampled from the far lists of the reference acceptance test at several theta
 values, and the library measures each pair's M2L + L2P field error at
 expansion orders 2..12 against the FP64 direct sum over the source cell
@@ -28,19 +31,30 @@ if ROOT not in sys.path:
 from fmm_gb300 import _lib, systems  # noqa: E402
 
 IN, OUT = 17, 11
-DEFAULT_OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "selector_v1")
+DEFAULT_OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "selector_v2")
 
 
-def collect(n_systems, n_mol, thetas, pairs_per_theta, ncrit=64, seed0=1000):
+def make_training_system(kind, n_mol, seed):
+    """water: water-like triplets at the density of the 1M benchmark system;
+    blobs: the clustered benchmark system's kind (64 Gaussian blobs) scaled to
+    3 n_mol particles at its density."""
+    if kind == "water":
+        box = 270.0 * (n_mol / 333_333) ** (1.0 / 3.0)
+        return systems.water(n_mol, box, seed=seed)
+    n = 3 * n_mol
+    sc = (n / 2_000_000) ** (1.0 / 3.0)
+    return systems.blobs(n=n, box=600.0 * sc, sigma_range=(5.0 * sc, 30.0 * sc), seed=seed)
+
+
+def collect(n_systems, n_mol, thetas, pairs_per_theta, ncrit=64, seed0=1000, kind="water"):
     L = _lib.lib()
     L.fmm_selector_collect.restype = ctypes.c_int
     L.fmm_selector_collect.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
-    box = 270.0 * (n_mol / 333_333) ** (1.0 / 3.0)
     Xs, Ys = [], []
     for k in range(n_systems):
-        s = systems.water(n_mol, box, seed=seed0 + k)
+        s = make_training_system(kind, n_mol, seed0 + k)
         Xc = np.asfortranarray(s["coordinates"])
         Mc = np.asfortranarray(s["multipoles"])
         d = np.ascontiguousarray(s["damping_factors"])
@@ -96,6 +110,7 @@ def train(X, Y, epochs=40, batch=256, lr=2e-3, seed=0):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--systems", type=int, default=50)
+    ap.add_argument("--blob-systems", type=int, default=25)
     ap.add_argument("--n-mol", type=int, default=33_334)
     ap.add_argument("--pairs", type=int, default=1500, help="sampled far pairs per system and theta")
     ap.add_argument("--epochs", type=int, default=60)
@@ -104,6 +119,9 @@ def main():
     thetas = (0.25, 0.35, 0.5, 0.7)
     t0 = time.time()
     X, Y = collect(args.systems, args.n_mol, thetas, args.pairs)
+    if args.blob_systems > 0:
+        Xb, Yb = collect(args.blob_systems, args.n_mol, thetas, args.pairs, seed0=2000, kind="blobs")
+        X, Y = np.concatenate([X, Xb]), np.concatenate([Y, Yb])
     t1 = time.time()
     rng = np.random.default_rng(0)
     perm = rng.permutation(X.shape[0])
@@ -127,7 +145,8 @@ def main():
         "outputs": "log10 RMS field error of the pair's M2L+L2P contribution at expansion orders 2..12",
         "features": ["rho=sqrt3(r_i+r_j)/R", "log2(r_j/r_i)", "log2(count_i)"] +
                     ["log10(|w^(%d)_j|/R^%d)" % (k, k + 2) for k in range(13)] + ["min(dmin_i dmin_j R,30)/30"],
-        "training": {"systems": args.systems, "particles_per_system": 3 * args.n_mol, "thetas": thetas,
+        "training": {"systems": args.systems, "blob_systems": args.blob_systems,
+                     "particles_per_system": 3 * args.n_mol, "thetas": thetas,
                      "pairs_per_system_theta": args.pairs, "samples": int(X.shape[0]), "epochs": args.epochs,
                      "train_loss_last": float(losses[-1]), "collect_s": round(t1 - t0, 1),
                      "train_s": round(t2 - t1, 1)},

@@ -82,3 +82,22 @@ def test_underestimating_network_falls_back(water, tmp_path):
     assert st["selector_fallback"] == 1
     assert st["m2l_order_mean"] == 10.0
     assert _rms(F, D) <= 1e-6
+
+
+def test_learned_on_clustered_particles_meets_target():
+    """Heterogeneous density (Gaussian blobs, the clustered benchmark system's
+    kind at 120k particles): whichever path the call takes (the learned lists
+    with per-node error budgets from the local field, or the fixed rule after
+    a failed sampled check), the result meets the target at 256 sampled
+    particles."""
+    import bench
+    sc = (120_000 / 2_000_000) ** (1.0 / 3.0)
+    for seed in (5, 7):
+        s = systems.blobs(n=120_000, box=600.0 * sc, sigma_range=(5.0 * sc, 30.0 * sc), seed=seed)
+        opt = Options.exact(precision="mixed", mac_mode="damping", selector="learned")
+        F = fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"], 0.3, 64, 12, 1, "AMOEBA",
+                                s["damping_factors"], options=opt)
+        rng = np.random.default_rng(1)
+        rows = np.sort(rng.choice(F.shape[0], 256, replace=False))
+        ref = bench.sampled_reference(s, rows, "AMOEBA")
+        assert bench.rel_errors(F[rows], ref)["rms_rel_err"] <= 1e-6
