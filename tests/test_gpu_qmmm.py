@@ -81,3 +81,14 @@ def test_gpu_qmmm_helpers_match_oracle_larger(ntgt, theta, p):
     F = fmm_gb300.interpolate_electron_fields(0, X, Lx, bi, theta, 32, p, 2)
     O = oracle.interpolate_electron_fields(0, X, Lx, bi, theta, 32, p, 2)
     assert np.linalg.norm(F - O) <= 1e-12 * np.linalg.norm(O)
+
+
+def test_octree_module_exposes_the_helpers(fx):
+    import octree
+    th, nc, p, f = fx["qmmm_cfg"]
+    a = octree.fmm.get_boxes(fx["qmmm_X"], fx["qmmm_T"], th, int(nc), int(p))
+    b = fmm_gb300.get_boxes(fx["qmmm_X"], fx["qmmm_T"], th, int(nc), int(p))
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+    F = octree.fmm.interpolate_electron_fields(0, fx["qmmm_X"], fx["qmmm_local"], fx["qmmm_box_indices"], th,
+                                               int(nc), int(p), int(f))
+    assert np.linalg.norm(F - fx["qmmm_field"]) <= 1e-12 * np.linalg.norm(fx["qmmm_field"])
