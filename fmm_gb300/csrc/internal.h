@@ -115,6 +115,7 @@ struct P2pShape {
     int threads = 128;
     int stage = 320;
     int queue = 1;
+    int pack = 1;  // sources two at a time in packed FP32 (Blackwell f32x2 instructions)
     bool valid() const;
 };
 
@@ -174,6 +175,8 @@ struct Workspace {
     bool reuse_structure = false;
     P2pShape p2p_shape;  // FP32 near-field launch shape
     DevBuf p2p_order;    // target leaves by decreasing pair work (queue mode), and scratch
+    DevBuf p2p_pad;      // packed near field: padded leaf starts (node-indexed), odd-leaf flags and their scan
+    DevBuf f32x2;        // packed near field: interleaved source records of padded leaves
     int m2l_ng = 0, m2l_ntasks = 0;  // grouped M2L structure of the last evaluation
     bool m2l_pairwise = false;       // the last structure chose the per-pair M2L kernel
     std::vector<M2lBatch> m2l_batches;  // operator batches of the last structure

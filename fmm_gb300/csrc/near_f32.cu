@@ -11,12 +11,14 @@
 // compensated FP32 (TwoSum hi + lo) and the per-leaf sums are added into FP64
 // accumulators.  Excluded partners and the self pair are masked in the loop.
 #include <algorithm>
+#include <cstdlib>
 
 #include <cub/cub.cuh>
 
 #include "dispatch.cuh"
 #include "internal.h"
 #include "pair.cuh"
+#include "pair_x2.cuh"
 
 namespace fmm {
 
@@ -60,6 +62,43 @@ __global__ void k_gather_f32(int64_t n, int dim, const TreeDev t, const double* 
         }
         r[v] = make_float4(m[0], m[1], m[2], m[3]);
     }
+}
+
+// Source records of the packed near field: the sorted particles of each leaf
+// from an even slot ps[leaf] on, an odd leaf padded by one empty particle
+// (zero multipoles, 1000 bohr from its leaf centre, damping factor 1: its
+// pair terms are exactly zero); slots 2b and 2b + 1 form block b, stored
+// element by element interleaved (float 2e + h of the block is element e of
+// the record of slot 2b + h), so one 16-byte shared-memory load gives two
+// elements of both particles as two packed pairs.
+__global__ void k_gather_x2(int64_t n, int nv, const TreeDev t, const int32_t* __restrict__ ps,
+                            const float4* __restrict__ rec, float* __restrict__ x2) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int leaf = t.leaf_of[k];
+    const int within = (int)(k - t.start[leaf]), cnt = t.count[leaf];
+    const int64_t slot = (int64_t)ps[leaf] + within;
+    const float* s = reinterpret_cast<const float*>(rec + (size_t)k * nv);
+    float* d = x2 + (size_t)(slot >> 1) * 8 * nv + (slot & 1);
+    for (int e = 0; e < 4 * nv; ++e) d[2 * e] = s[e];
+    if (within == cnt - 1 && (cnt & 1)) {
+        float* dd = d + 1;  // slot + 1: the odd half of the same block
+        for (int e = 0; e < 4 * nv; ++e) dd[2 * e] = 0.0f;
+        dd[0] = 1000.0f;  // x
+        dd[2 * 3] = 1.0f; // damping factor
+    }
+}
+
+__global__ void k_leaf_odd(const TreeDev t, int32_t* __restrict__ odd) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w < t.num_leaves) odd[w] = t.count[t.leaves[w]] & 1;
+}
+
+// Leaves are in DFS order, i.e. by increasing start: the padded start of a
+// leaf is its start plus the odd leaves before it.
+__global__ void k_leaf_pstart(const TreeDev t, const int32_t* __restrict__ pre, int32_t* __restrict__ ps) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w < t.num_leaves) ps[t.leaves[w]] = t.start[t.leaves[w]] + pre[w];
 }
 
 // Node centres as double-float pairs (hi = rounded centre, lo = rounded
@@ -201,6 +240,80 @@ __device__ __forceinline__ void p2p_leaf(const float4* src, int cnt, int k0, int
     }
 }
 
+// p2p_leaf on the packed records (k_gather_x2): blocks b = grp, grp + ngr,
+// ... of the staged piece, each the lane's target against two sources in
+// packed arithmetic.  Each half keeps its own compensated sum (H, L) over all
+// pieces of the target chunk, fed from a plain block sum B folded every four
+// blocks (four pairs per fold per half, as in the scalar loop).  The target
+// position enters as xo = x_t + (c_A - c_B)_hi per piece and the low parts as
+// oxl, so R = (xo - x_s) + (oxl - x_s,lo).  k0 is the sorted index of slot 0.
+template <int M, int F, int DAMP, bool CHECK>
+__device__ __forceinline__ void p2p_leaf_x2(const float4* src, int nblk, int k0, int grp, int ngr, int tgt, f2 xo,
+                                            f2 yo, f2 zo, f2 dt, f2 oxl, f2 oyl, f2 ozl,
+                                            const int32_t* __restrict__ excl, int exw, int64_t n, int ot, f2* H,
+                                            f2* L) {
+    constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM), NE = 4 * (NV - 2);
+    f2 B[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) B[f] = bc2(0.0f);
+    int nb = 0;
+    for (int b = grp; b < nblk; b += ngr) {
+        const ulonglong2* r = reinterpret_cast<const ulonglong2*>(src + (size_t)b * 2 * NV);
+        // element pairs: (x, y), (z, d), (x_lo, y_lo), (z_lo, index), multipoles
+        const ulonglong2 v0 = r[0], v1 = r[1], v2 = r[2], v3 = r[3];
+        f2 mc[NE];
+#pragma unroll
+        for (int v = 0; v < NE / 2; ++v) {
+            const ulonglong2 w = r[4 + v];
+            mc[2 * v].v = w.x;
+            mc[2 * v + 1].v = w.y;
+        }
+        f2 dx = (xo - f2{v0.x}) + (oxl - f2{v2.x});
+        const f2 dy = (yo - f2{v0.y}) + (oyl - f2{v2.y});
+        const f2 dz = (zo - f2{v1.x}) + (ozl - f2{v3.x});
+        const f2 a = dt * f2{v1.y};
+        if (CHECK) {
+            float o0, o1;
+            sp2(f2{v3.y}, o0, o1);
+            const int k = k0 + 2 * b;
+            bool s0 = k == tgt, s1 = k + 1 == tgt;
+            for (int e = 0; e < exw; ++e) {
+                const int x = excl[(size_t)e * n + ot];
+                s0 |= x == __float_as_int(o0);
+                s1 |= x == __float_as_int(o1);
+            }
+            if (s0 || s1) {
+                // a skipped half gets zero multipoles at a finite distance
+                const f2 keep = mk2(s0 ? 0.0f : 1.0f, s1 ? 0.0f : 1.0f);
+#pragma unroll
+                for (int e = 0; e < NE; ++e) mc[e] = mc[e] * keep;
+                float d0, d1;
+                sp2(dx, d0, d1);
+                dx = mk2(s0 ? 1000.0f : d0, s1 ? 1000.0f : d1);
+            }
+        }
+        pair_field_x2<M, F>(dx, dy, dz, a, DAMP, mc, B);
+        if (++nb == 4) {
+            nb = 0;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                const f2 s = H[f] + B[f];
+                const f2 bb = s - H[f];
+                L[f] += (H[f] - (s - bb)) + (B[f] - bb);
+                H[f] = s;
+                B[f] = bc2(0.0f);
+            }
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        const f2 s = H[f] + B[f];
+        const f2 bb = s - H[f];
+        L[f] += (H[f] - (s - bb)) + (B[f] - bb);
+        H[f] = s;
+    }
+}
+
 // Source records are staged per warp in shared memory, double-buffered:
 // while one piece (a source leaf, or `stage` / NV of its particles when it
 // is larger) is evaluated, the next is copied with cp.async.  The staging
@@ -225,15 +338,19 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // stay resident and take leaves order[0], order[1], ... (the target leaves
 // by decreasing pair count) from the counter `next`, so the largest leaves
 // start first and the last wave is made of the smallest.
-template <int M, int F, int DAMP>
+// X2: sources from the packed records `srec` (k_gather_x2, padded leaf starts
+// sstart) evaluated two at a time; otherwise srec = rec, sstart = t.start.
+template <int M, int F, int DAMP, bool X2>
 __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float4* __restrict__ rec,
+                                                    const float4* __restrict__ srec,
+                                                    const int32_t* __restrict__ sstart,
                                                     const float4* __restrict__ chi, const float4* __restrict__ clo,
                                                     const int32_t* __restrict__ excl, int exw, int64_t n,
                                                     double* __restrict__ fs, int stage,
                                                     const int32_t* __restrict__ order, unsigned* __restrict__ next) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
     extern __shared__ __align__(16) float4 sbuf_p2p[];
-    const int cap = stage / NV;  // particles per staged piece
+    const int cap = X2 ? (stage / NV) & ~1 : stage / NV;  // particles (slots) per staged piece
     const int lane = threadIdx.x & 31;
     float4* const bufs = sbuf_p2p + (size_t)(threadIdx.x >> 5) * 2 * stage;
     const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -272,17 +389,22 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
         // per-target sums over all source leaves as double-float pairs (FP32
         // arithmetic; the FP64 pipe is the scarce one)
         float AH[NF], AL[NF];
+        f2 XH[NF], XL[NF];  // packed kernel: one compensated sum per half
 #pragma unroll
-        for (int f = 0; f < NF; ++f) AH[f] = AL[f] = 0.0f;
+        for (int f = 0; f < NF; ++f) {
+            AH[f] = AL[f] = 0.0f;
+            XH[f] = XL[f] = bc2(0.0f);
+        }
         // current piece (q, off) of source leaf j = [js, js + jc); the first
         // one is staged before the loop
         int q = q0, off = 0, j = 0, js = 0, jc = 0;
         if (q < q1) {
             j = t.near_src[q];
-            js = t.start[j];
+            js = sstart[j];
             jc = t.count[j];
+            if (X2) jc += jc & 1;  // padded to whole blocks
             const int pc = min(cap, jc);
-            for (int i = lane; i < pc * NV; i += 32) cp_async16(&bufs[i], rec + (size_t)js * NV + i);
+            for (int i = lane; i < pc * NV; i += 32) cp_async16(&bufs[i], srec + (size_t)js * NV + i);
         }
         cp_async_commit();
         int slot = 0;
@@ -294,13 +416,14 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
                 noff = 0;
                 if (nq < q1) {
                     nj = t.near_src[nq];
-                    njs = t.start[nj];
+                    njs = sstart[nj];
                     njc = t.count[nj];
+                    if (X2) njc += njc & 1;
                 }
             }
             if (nq < q1) {
                 const int npc = min(cap, njc - noff);
-                const float4* gsrc = rec + (size_t)(njs + noff) * NV;
+                const float4* gsrc = srec + (size_t)(njs + noff) * NV;
                 float4* dst = bufs + (slot ^ 1) * stage;
                 for (int i = lane; i < npc * NV; i += 32) cp_async16(&dst[i], gsrc + i);
             }
@@ -320,23 +443,35 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
                 for (int e = 0; e < kExwRegs; ++e) need |= (exl[e] == j);
                 const int pc = min(cap, jc - off);
                 const float4* cur = bufs + slot * stage;
-                float hi[NF], lo[NF];
+                const int k0 = (X2 ? t.start[j] : js) + off;  // sorted index of the piece's first slot
+                if constexpr (X2) {
+                    const f2 xo = bc2(ta.x + ox), yo = bc2(ta.y + oy), zo = bc2(ta.z + oz), dt = bc2(ta.w);
+                    const f2 oxl2 = bc2(oxl), oyl2 = bc2(oyl), ozl2 = bc2(ozl);
+                    if (__any_sync(__activemask(), need))
+                        p2p_leaf_x2<M, F, DAMP, true>(cur, pc >> 1, k0, grp, ngr, tgt, xo, yo, zo, dt, oxl2, oyl2,
+                                                      ozl2, excl, exw, n, ot, XH, XL);
+                    else
+                        p2p_leaf_x2<M, F, DAMP, false>(cur, pc >> 1, k0, grp, ngr, tgt, xo, yo, zo, dt, oxl2, oyl2,
+                                                       ozl2, excl, exw, n, ot, XH, XL);
+                } else {
+                    float hi[NF], lo[NF];
 #pragma unroll
-                for (int f = 0; f < NF; ++f) hi[f] = lo[f] = 0.0f;
-                if (__any_sync(__activemask(), need))
-                    p2p_leaf<M, F, DAMP, true>(cur, pc, js + off, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy,
-                                               oz, oxl, oyl, ozl, excl, exw, n, ot, hi, lo);
-                else
-                    p2p_leaf<M, F, DAMP, false>(cur, pc, js + off, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox,
-                                                oy, oz, oxl, oyl, ozl, excl, exw, n, ot, hi, lo);
+                    for (int f = 0; f < NF; ++f) hi[f] = lo[f] = 0.0f;
+                    if (__any_sync(__activemask(), need))
+                        p2p_leaf<M, F, DAMP, true>(cur, pc, k0, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy, oz,
+                                                   oxl, oyl, ozl, excl, exw, n, ot, hi, lo);
+                    else
+                        p2p_leaf<M, F, DAMP, false>(cur, pc, k0, grp, ngr, tgt, ta.x, ta.y, ta.z, ta.w, ox, oy, oz,
+                                                    oxl, oyl, ozl, excl, exw, n, ot, hi, lo);
 #pragma unroll
-                for (int f = 0; f < NF; ++f) {
-                    // (AH, AL) += (hi, lo)
-                    const float sum = AH[f] + hi[f];
-                    const float bb = sum - AH[f];
-                    const float err = (AH[f] - (sum - bb)) + (hi[f] - bb);
-                    AH[f] = sum;
-                    AL[f] += err + lo[f];
+                    for (int f = 0; f < NF; ++f) {
+                        // (AH, AL) += (hi, lo)
+                        const float sum = AH[f] + hi[f];
+                        const float bb = sum - AH[f];
+                        const float err = (AH[f] - (sum - bb)) + (hi[f] - bb);
+                        AH[f] = sum;
+                        AL[f] += err + lo[f];
+                    }
                 }
             }
             __syncwarp();
@@ -351,7 +486,16 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
         __syncwarp();
         double acc[NF];
 #pragma unroll
-        for (int f = 0; f < NF; ++f) acc[f] = (double)AH[f] + (double)AL[f];
+        for (int f = 0; f < NF; ++f) {
+            if constexpr (X2) {
+                float h0, h1, l0, l1;
+                sp2(XH[f], h0, h1);
+                sp2(XL[f], l0, l1);
+                acc[f] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
+            } else {
+                acc[f] = (double)AH[f] + (double)AL[f];
+            }
+        }
         for (int o = g; o < 32; o <<= 1) {
 #pragma unroll
             for (int f = 0; f < NF; ++f) acc[f] += __shfl_xor_sync(0xffffffffu, acc[f], o);
@@ -458,46 +602,60 @@ __global__ void k_leaf_cost(const TreeDev t, uint32_t* __restrict__ cost, int32_
     }
 }
 
-template <int M, int F>
+template <int M, int F, bool X2>
 void launch_p2p_kind(unsigned blocks, int threads, size_t smem, int stage, const int32_t* order, unsigned* next,
-                     cudaStream_t st, const TreeDev& t, const float4* rec, const float4* chi, const float4* clo,
-                     const int32_t* excl, int exw, int64_t n, int damp, double* fs) {
+                     cudaStream_t st, const TreeDev& t, const float4* rec, const float4* srec, const int32_t* sstart,
+                     const float4* chi, const float4* clo, const int32_t* excl, int exw, int64_t n, int damp,
+                     double* fs) {
+    if constexpr (X2 && F > 1) {
+        return;  // not instantiated: the packed kernel is used for field orders 0 and 1
+    } else {
     switch (damp) {
         case DAMP_AMOEBA:
-            k_p2p_f32<M, F, DAMP_AMOEBA><<<blocks, threads, smem, st>>>(t, rec, chi, clo, excl, exw, n, fs, stage,
-                                                                          order, next);
+            k_p2p_f32<M, F, DAMP_AMOEBA, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw,
+                                                                              n, fs, stage, order, next);
             break;
         case DAMP_THOLE:
-            k_p2p_f32<M, F, DAMP_THOLE><<<blocks, threads, smem, st>>>(t, rec, chi, clo, excl, exw, n, fs, stage,
-                                                                         order, next);
+            k_p2p_f32<M, F, DAMP_THOLE, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw,
+                                                                             n, fs, stage, order, next);
             break;
         case DAMP_ERF:
-            k_p2p_f32<M, F, DAMP_ERF><<<blocks, threads, smem, st>>>(t, rec, chi, clo, excl, exw, n, fs, stage, order,
-                                                                       next);
+            k_p2p_f32<M, F, DAMP_ERF, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw, n,
+                                                                           fs, stage, order, next);
             break;
         default:
-            k_p2p_f32<M, F, DAMP_NONE><<<blocks, threads, smem, st>>>(t, rec, chi, clo, excl, exw, n, fs, stage, order,
-                                                                        next);
+            k_p2p_f32<M, F, DAMP_NONE, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw,
+                                                                            n, fs, stage, order, next);
             break;
     }
+    }
+}
+
+template <int M, int F, bool X2>
+const void* p2p_kernel(int damp) {
+    if constexpr (X2 && F > 1) return nullptr;
+    else
+    return damp == DAMP_AMOEBA  ? (const void*)k_p2p_f32<M, F, DAMP_AMOEBA, X2>
+           : damp == DAMP_THOLE ? (const void*)k_p2p_f32<M, F, DAMP_THOLE, X2>
+           : damp == DAMP_ERF   ? (const void*)k_p2p_f32<M, F, DAMP_ERF, X2>
+                                : (const void*)k_p2p_f32<M, F, DAMP_NONE, X2>;
 }
 
 template <int M, int F>
 int set_p2p_smem(size_t smem) {
-    const void* fns[4] = {(const void*)k_p2p_f32<M, F, DAMP_NONE>, (const void*)k_p2p_f32<M, F, DAMP_AMOEBA>,
-                          (const void*)k_p2p_f32<M, F, DAMP_THOLE>, (const void*)k_p2p_f32<M, F, DAMP_ERF>};
+    const void* fns[8] = {p2p_kernel<M, F, false>(DAMP_NONE), p2p_kernel<M, F, false>(DAMP_AMOEBA),
+                          p2p_kernel<M, F, false>(DAMP_THOLE), p2p_kernel<M, F, false>(DAMP_ERF),
+                          p2p_kernel<M, F, true>(DAMP_NONE),  p2p_kernel<M, F, true>(DAMP_AMOEBA),
+                          p2p_kernel<M, F, true>(DAMP_THOLE),  p2p_kernel<M, F, true>(DAMP_ERF)};
     for (const void* fn : fns)
-        FMM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (fn) FMM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return FMM_OK;
 }
 
 template <int M, int F>
-int p2p_blocks_per_sm(int damp, int threads, size_t smem) {
+int p2p_blocks_per_sm(int damp, bool x2, int threads, size_t smem) {
     int nb = 0;
-    const void* fn = damp == DAMP_AMOEBA  ? (const void*)k_p2p_f32<M, F, DAMP_AMOEBA>
-                     : damp == DAMP_THOLE ? (const void*)k_p2p_f32<M, F, DAMP_THOLE>
-                     : damp == DAMP_ERF   ? (const void*)k_p2p_f32<M, F, DAMP_ERF>
-                                          : (const void*)k_p2p_f32<M, F, DAMP_NONE>;
+    const void* fn = x2 ? p2p_kernel<M, F, true>(damp) : p2p_kernel<M, F, false>(damp);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess) {
         cudaGetLastError();
         return 1;
@@ -577,7 +735,7 @@ int launch_leaf_field_scale(Workspace& ws, const Particles& P, const TreeDev& t,
 
 bool P2pShape::valid() const {
     return (threads == 64 || threads == 128 || threads == 256) && stage >= 64 && stage <= 1024 && stage % 16 == 0 &&
-           (queue == 0 || queue == 1);
+           (queue == 0 || queue == 1) && (pack == 0 || pack == 1);
 }
 
 int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, cudaStream_t st) {
@@ -591,6 +749,35 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
     const P2pShape sh = ws.p2p_shape.valid() ? ws.p2p_shape : P2pShape{};
     const size_t smem = sizeof(float4) * 2 * (size_t)sh.stage * (sh.threads / 32);
     if (rec_vec(P.dim) > sh.stage) return FMM_EINVAL;
+    // packed kernel: sources two at a time from the padded, interleaved
+    // records, for field orders 0 and 1 (at order 2 the packed registers do
+    // not fit); FMM_GB300_P2P_PACKED=0 selects the one-source kernel
+    const char* pe = std::getenv("FMM_GB300_P2P_PACKED");
+    const bool x2 = sh.pack && !(pe && pe[0] == '0') && field_order <= 1 && t.num_leaves > 0 &&
+                    n + (int64_t)t.num_leaves < (int64_t)INT32_MAX;
+    if (x2) {
+        const int nv = rec_vec(P.dim);
+        const int L = t.num_leaves;
+        FMM_TRY(ws.f32x2.ensure(sizeof(float4) * (size_t)(n + L + 1) * nv));
+        if (!ws.reuse_structure) {
+            // padded leaf starts (structure: kept for replays)
+            FMM_TRY(ws.p2p_pad.ensure(sizeof(int32_t) * ((size_t)t.num_nodes + 2 * (size_t)L)));
+            int32_t* ps = ws.p2p_pad.as<int32_t>();
+            int32_t* odd = ps + t.num_nodes;
+            int32_t* pre = odd + L;
+            count_launches(1);
+            k_leaf_odd<<<grid_for(L, 256), 256, 0, st>>>(t, odd);
+            size_t tb = 0;
+            cub::DeviceScan::ExclusiveSum(nullptr, tb, odd, pre, L, st);
+            FMM_TRY(ws.cub_tmp.ensure(tb));
+            FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb, odd, pre, L, st));
+            count_launches(1);
+            k_leaf_pstart<<<grid_for(L, 256), 256, 0, st>>>(t, pre, ps);
+        }
+        count_launches(1);
+        k_gather_x2<<<grid_for(n, 256), 256, 0, st>>>(n, nv, t, ws.p2p_pad.as<int32_t>(), rec,
+                                                       reinterpret_cast<float*>(ws.f32x2.as<float4>()));
+    }
     const int32_t* order = nullptr;
     unsigned* next = nullptr;
     unsigned blocks = grid_for((int64_t)t.num_leaves * 32, sh.threads);
@@ -616,15 +803,23 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
         order = ws.p2p_order.as<int32_t>();
         FMM_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(unsigned), st));
         int bps = 1;
-        FMM_MF_SWITCH(m, field_order, (bps = p2p_blocks_per_sm<MM, FF>(P.damp_type, sh.threads, smem)));
+        FMM_MF_SWITCH(m, field_order, (bps = p2p_blocks_per_sm<MM, FF>(P.damp_type, x2, sh.threads, smem)));
         blocks = (unsigned)std::min<int64_t>(blocks, (int64_t)bps * num_sms_f32());
     }
     if (smem > 48 * 1024) {
         FMM_MF_SWITCH(m, field_order, FMM_TRY((set_p2p_smem<MM, FF>(smem))));
     }
-    FMM_MF_SWITCH(m, field_order,
-                  (launch_p2p_kind<MM, FF>(blocks, sh.threads, smem, sh.stage, order, next, st, t, rec, chi, clo,
-                                           P.excl, P.exw, n, P.damp_type, ws.fsorted.as<double>())));
+    if (x2) {
+        FMM_MF_SWITCH(m, field_order,
+                      (launch_p2p_kind<MM, FF, true>(blocks, sh.threads, smem, sh.stage, order, next, st, t, rec,
+                                                     ws.f32x2.as<float4>(), ws.p2p_pad.as<int32_t>(), chi, clo,
+                                                     P.excl, P.exw, n, P.damp_type, ws.fsorted.as<double>())));
+    } else {
+        FMM_MF_SWITCH(m, field_order,
+                      (launch_p2p_kind<MM, FF, false>(blocks, sh.threads, smem, sh.stage, order, next, st, t, rec, rec,
+                                                      t.start, chi, clo, P.excl, P.exw, n, P.damp_type,
+                                                      ws.fsorted.as<double>())));
+    }
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }

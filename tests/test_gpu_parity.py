@@ -311,6 +311,39 @@ def test_mixed_precision_close_to_fp64(damp, mf):
     assert rel_err(F32, F64, slice(1, None)) < 5e-6
 
 
+@pytest.mark.parametrize("damp,mf", [("AMOEBA", (2, 1)), ("THOLE", (2, 1)), ("ERF", (1, 1)), ("", (2, 1)),
+                                     ("AMOEBA", (0, 1)), ("THOLE", (1, 0))])
+@pytest.mark.parametrize("one_sided", [False, True])
+def test_packed_near_field_matches_one_source_kernel(damp, mf, one_sided, monkeypatch):
+    """The packed near field (two sources per thread in f32x2 arithmetic, odd
+    leaves padded with an empty particle, skipped halves zeroed) agrees with
+    the one-source FP32 kernel to FP32 rounding, and both with the FP64 path;
+    exclusions listed by one partner only included."""
+    from fmm_gb300 import systems
+    m, f = mf
+    s = systems.water(3001, 70.0, order=m, seed=41)
+    if damp == "ERF":
+        s["damping_factors"] = np.random.default_rng(42).uniform(0.3, 0.8, 9003)
+    d = s["damping_factors"] if damp else None
+    E = np.array(s["exclusions"])
+    if one_sided:
+        E[1:900:3, :] = 0
+    args = (0, s["coordinates"], s["multipoles"], np.asfortranarray(E))
+    mixed = Options.exact(precision="mixed")
+    F64 = fmm_gb300.field_fmm(*args, 0.5, 64, 8, f, damp, d, options=Options.exact())
+    Fx2 = fmm_gb300.field_fmm(*args, 0.5, 64, 8, f, damp, d, options=mixed)
+    monkeypatch.setenv("FMM_GB300_P2P_PACKED", "0")
+    F1 = fmm_gb300.field_fmm(*args, 0.5, 64, 8, f, damp, d, options=mixed)
+    assert np.all(np.isfinite(Fx2))
+    if f > 0:
+        assert rel_err(Fx2, F1, slice(1, None)) < 1e-6
+        assert rel_err(Fx2, F64, slice(1, None)) < 5e-6
+    else:
+        # the potential of neutral groups: a sum with heavy cancellation
+        assert rel_err(Fx2, F1) < 1e-5
+        assert rel_err(Fx2, F64) < 5e-5
+
+
 def test_release_workspace_then_call_again():
     """fmm_release_workspace frees the thread's device buffers; the next call
     allocates again and gives the same field."""
