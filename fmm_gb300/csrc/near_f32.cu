@@ -28,6 +28,13 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 
 constexpr int kExwRegs = 8;  // exclusion entries held in registers per target
 
+// Sub-chunks of a target leaf's last rem < 32 particles (index rem): the
+// count that minimises the lane-steps of a piece of source blocks for leaves
+// of about 30 particles (c sub-chunks of ceil(rem / c) targets run
+// floor(32 / ceil(rem / c)) lane groups each).
+__constant__ int kSubChunks[32] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 2, 1, 1, 1,
+                                   1, 3, 3, 2, 2, 3, 3, 3, 3, 1, 1, 1, 1, 1, 1, 1};
+
 // Per sorted particle, one record of float4s: (x, y, z, d), (x_lo, y_lo, z_lo,
 // original index + 1 as int bits), then the FP32 scaled multipoles padded to
 // a multiple of 4 (for quadrupoles the first pad slot holds the trace of the
@@ -71,7 +78,10 @@ __global__ void k_gather_f32(int64_t n, int dim, const TreeDev t, const double* 
 // element by element interleaved (float 2e + h of the block is element e of
 // the record of slot 2b + h), so one 16-byte shared-memory load gives two
 // elements of both particles as two packed pairs.
-__global__ void k_gather_x2(int64_t n, int nv, const TreeDev t, const int32_t* __restrict__ ps,
+// With q1 (quadrupole sources, field order 1: contract_q1_x2) the
+// off-diagonal second moments xy, xz, yz (record elements 13, 14, 16) are
+// stored halved, an exact scaling.
+__global__ void k_gather_x2(int64_t n, int nv, bool q1, const TreeDev t, const int32_t* __restrict__ ps,
                             const float4* __restrict__ rec, float* __restrict__ x2) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -81,6 +91,11 @@ __global__ void k_gather_x2(int64_t n, int nv, const TreeDev t, const int32_t* _
     const float* s = reinterpret_cast<const float*>(rec + (size_t)k * nv);
     float* d = x2 + (size_t)(slot >> 1) * 8 * nv + (slot & 1);
     for (int e = 0; e < 4 * nv; ++e) d[2 * e] = s[e];
+    if (q1) {
+        d[2 * 13] = 0.5f * s[13];
+        d[2 * 14] = 0.5f * s[14];
+        d[2 * 16] = 0.5f * s[16];
+    }
     if (within == cnt - 1 && (cnt & 1)) {
         float* dd = d + 1;  // slot + 1: the odd half of the same block
         for (int e = 0; e < 4 * nv; ++e) dd[2 * e] = 0.0f;
@@ -369,13 +384,18 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
     const int s0 = t.start[leaf], cnt = t.count[leaf];
     const int q0 = t.near_off[leaf], q1 = t.near_off[leaf + 1];
     const float4 ca = chi[leaf], cal = clo[leaf];
-    for (int chunk = 0; chunk < cnt; chunk += 32) {
-        const int nt = min(32, cnt - chunk);
-        int g = 1;
-        while (g < nt) g <<= 1;
+    // chunks of 32 targets, then the remaining rem < 32 in cs sub-chunks of
+    // gs targets; a chunk of g targets runs ngr = 32 / g lane groups of g
+    // lanes (any g), each taking every ngr-th block of each staged piece
+    const int full = cnt >> 5, rem = cnt & 31;
+    const int cs = rem ? kSubChunks[rem] : 0, gs = rem ? (rem + cs - 1) / cs : 1;
+    for (int ci = 0; ci < full + cs; ++ci) {
+        const int chunk = ci < full ? 32 * ci : 32 * full + (ci - full) * gs;
+        const int g = ci < full ? 32 : gs;
+        const int nt = min(g, cnt - chunk);
         const int ngr = 32 / g;
-        const int tl = lane & (g - 1), grp = lane / g;
-        const bool valid = tl < nt;
+        const int tl = lane % g, grp = lane / g;
+        const bool valid = tl < nt && grp < ngr;
         const int tgt = s0 + chunk + (valid ? tl : 0);
         const float4 ta = rec[(size_t)tgt * NV], tb = rec[(size_t)tgt * NV + 1];
         const int ot = __float_as_int(tb.w) - 1;
@@ -496,9 +516,20 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
                 acc[f] = (double)AH[f] + (double)AL[f];
             }
         }
-        for (int o = g; o < 32; o <<= 1) {
+        if ((g & (g - 1)) == 0) {
+            for (int o = g; o < 32; o <<= 1) {
 #pragma unroll
-            for (int f = 0; f < NF; ++f) acc[f] += __shfl_xor_sync(0xffffffffu, acc[f], o);
+                for (int f = 0; f < NF; ++f) acc[f] += __shfl_xor_sync(0xffffffffu, acc[f], o);
+            }
+        } else {
+            // group 0 adds groups 1 .. ngr - 1 (lanes tl + k g)
+            double part[NF];
+#pragma unroll
+            for (int f = 0; f < NF; ++f) part[f] = acc[f];
+            for (int k = 1; k < ngr; ++k) {
+#pragma unroll
+                for (int f = 0; f < NF; ++f) acc[f] += __shfl_sync(0xffffffffu, part[f], (tl + k * g) & 31);
+            }
         }
         if (grp == 0 && valid) {
 #pragma unroll
@@ -775,7 +806,8 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
             k_leaf_pstart<<<grid_for(L, 256), 256, 0, st>>>(t, pre, ps);
         }
         count_launches(1);
-        k_gather_x2<<<grid_for(n, 256), 256, 0, st>>>(n, nv, t, ws.p2p_pad.as<int32_t>(), rec,
+        k_gather_x2<<<grid_for(n, 256), 256, 0, st>>>(n, nv, P.dim == 10 && field_order == 1, t,
+                                                       ws.p2p_pad.as<int32_t>(), rec,
                                                        reinterpret_cast<float*>(ws.f32x2.as<float4>()));
     }
     const int32_t* order = nullptr;

@@ -135,21 +135,24 @@ __device__ __forceinline__ void radial_g_x2(int damp, f2 r2, f2 ir, f2 a, f2 eps
     for (int j = 0; j <= N; ++j) g[j] = mk2(gh[0][j], gh[1][j]);
 }
 
-// contract_q1 (quadrupole sources, field order 1) on two pairs.
+// contract_q1 (quadrupole sources, field order 1) on two pairs, with the
+// off-diagonal second moments Mc_xy, Mc_xz, Mc_yz supplied halved: then
+// w = grad q / 2 = (Mc_xx X + Mc_xy/2 Y + Mc_xz/2 Z, ...), q = R . w, and the
+// gradient term v g_2 of contract_q1 is w (2 g_2).
 __device__ __forceinline__ void contract_q1_x2(f2 X, f2 Y, f2 Z, const f2* g, const f2* Mc, int damp, f2* acc) {
-    const f2 X2 = X + X, Y2 = Y + Y, Z2 = Z + Z;
-    const f2 vx = fma2(Mc[4], X2, fma2(Mc[5], Y, Mc[6] * Z));
-    const f2 vy = fma2(Mc[5], X, fma2(Mc[7], Y2, Mc[8] * Z));
-    const f2 vz = fma2(Mc[6], X, fma2(Mc[8], Y, Mc[9] * Z2));
-    const f2 q = bc2(0.5f) * fma2(X, vx, fma2(Y, vy, Z * vz));
+    const f2 wx = fma2(Mc[4], X, fma2(Mc[5], Y, Mc[6] * Z));
+    const f2 wy = fma2(Mc[5], X, fma2(Mc[7], Y, Mc[8] * Z));
+    const f2 wz = fma2(Mc[6], X, fma2(Mc[8], Y, Mc[9] * Z));
+    const f2 q = fma2(X, wx, fma2(Y, wy, Z * wz));
     const f2 dtr = fma2(Mc[1], X, fma2(Mc[2], Y, fma2(Mc[3], Z, Mc[10])));
     const f2 sc = fma2(Mc[0], g[1], fma2(dtr, g[2], q * g[3]));
+    const f2 g2d = g[2] + g[2];
     f2 a0 = fma2(dtr, g[1], q * g[2]);
     if (damp != DAMP_AMOEBA) a0 = fma2(Mc[0], g[0], a0);
     acc[0] += a0;
-    acc[1] += fma2(X, sc, fma2(Mc[1], g[1], vx * g[2]));
-    acc[2] += fma2(Y, sc, fma2(Mc[2], g[1], vy * g[2]));
-    acc[3] += fma2(Z, sc, fma2(Mc[3], g[1], vz * g[2]));
+    acc[1] += fma2(X, sc, fma2(Mc[1], g[1], wx * g2d));
+    acc[2] += fma2(Y, sc, fma2(Mc[2], g[1], wy * g2d));
+    acc[3] += fma2(Z, sc, fma2(Mc[3], g[1], wz * g2d));
 }
 
 // Cartesian derivative tensor of all orders <= N (md_tensor) on two pairs.
