@@ -391,8 +391,8 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
                     for (int l = 0; l < CPT; ++l) acc[k][l] = fma(gv[k], wv[l][u], acc[k][l]);
             }
         }
-        // the group's rows are ldo = (q+1)^2 rounded up to 32 entries each
-        // (zeros above the pair's order, whole 128-byte lines in FP32)
+        // the group's rows are ldo = (q+1)^2 rounded up to kRowUnit entries
+        // each (zeros above the pair's order)
 #pragma unroll
         for (int l = 0; l < CPT; ++l) {
             if (pos[l] >= 0) {
@@ -411,9 +411,13 @@ __device__ __forceinline__ void gemm_task(const GemmSmem<R, CPT>& L, char* sm, i
     }
 }
 
-// Result rows: group g's rows start at rowbase[g] x 32 entries, one row of
-// (q+1)^2 rounded up to 32 entries per pair in group order.
-__host__ __device__ __forceinline__ int row_len(int q) { return ((q + 1) * (q + 1) + 31) & ~31; }
+// Result rows: group g's rows start at rowbase[g] x kRowUnit entries, one
+// row of (q+1)^2 rounded up to kRowUnit entries (32 bytes in FP32, one DRAM
+// sector) per pair in group order.
+constexpr int kRowUnit = 8;
+__host__ __device__ __forceinline__ int row_len(int q) {
+    return ((q + 1) * (q + 1) + kRowUnit - 1) / kRowUnit * kRowUnit;
+}
 
 // tcols: pairs per task (at most kTaskCols); tasks of order < qmin are left
 // to the tensor-core kernel.
@@ -458,7 +462,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_m2l_gemm(const int2* __restric
 #define FMM_GEMM_CASE(K)                                                                                     \
     case K:                                                                                                  \
         gemm_task<R, K, CPT>(L, sm_gemm, task.y, tcols, nrq, cnt, gs, svals, far_src, wsc, wsc_ld<R>(nr),     \
-                             out + (size_t)rowbase[g] * 32, row_len(q));                                      \
+                             out + (size_t)rowbase[g] * kRowUnit, row_len(q));                                      \
         break;
         FMM_GEMM_CASE(1)
         FMM_GEMM_CASE(2)
@@ -545,22 +549,22 @@ __global__ void k_split_weights(int64_t total, int nr, int ldw, int ldk, const f
     }
 }
 
-// Rows of each group in units of 32 entries (scanned into rowbase).
+// Rows of each group in units of kRowUnit entries (scanned into rowbase).
 __global__ void k_row_sizes(int ng, const int32_t* __restrict__ gstart, const int32_t* __restrict__ gq,
                             int32_t* __restrict__ rsz) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g > ng) return;
-    rsz[g] = g < ng ? (gstart[g + 1] - gstart[g]) * (row_len(gq[g]) / 32) : 0;
+    rsz[g] = g < ng ? (gstart[g + 1] - gstart[g]) * (row_len(gq[g]) / kRowUnit) : 0;
 }
 
 // Row of every far pair, indexed in target order (svals maps group order to
-// target order), in units of 32 entries.  Warp per group.
+// target order), in units of kRowUnit entries.  Warp per group.
 __global__ void k_row_offsets(int ng, const int32_t* __restrict__ gstart, const int32_t* __restrict__ gq,
                               const int32_t* __restrict__ rowbase, const int32_t* __restrict__ svals,
                               int32_t* __restrict__ roff) {
     const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (g >= ng) return;
-    const int lane = threadIdx.x & 31, u = row_len(gq[g]) / 32;
+    const int lane = threadIdx.x & 31, u = row_len(gq[g]) / kRowUnit;
     for (int k = gstart[g] + lane; k < gstart[g + 1]; k += 32) roff[svals[k]] = rowbase[g] + (k - gstart[g]) * u;
 }
 
@@ -800,10 +804,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_m2l_tc(const int2* __restrict
             }
             umma::fence_after_sync();
             const uint32_t base = tmem + ((uint32_t)(32 * sp) << 16) + (uint32_t)(acc * kTcPairs);
-            // the group's rows: (q+1)^2 rounded up to 32 entries, from
-            // rowbase[g] x 32 in group order
+            // the group's rows: (q+1)^2 rounded up to kRowUnit entries, from
+            // rowbase[g] x kRowUnit in group order
             const int rl = row_len(q);
-            float* gout = out + ((size_t)rowbase[g] + (size_t)(tk.y >> 1) * (rl / 32)) * 32;
+            float* gout = out + ((size_t)rowbase[g] + (size_t)(tk.y >> 1) * (rl / kRowUnit)) * kRowUnit;
             // warps whose 32 rows f lie beyond the row length have nothing to write
 #pragma unroll 1
             for (int c = share * CB; c < cnt && f0 + 32 * sp < rl; c += kShares * CB) {
@@ -854,7 +858,7 @@ struct Sum<double> {
 
 // Block per target, thread per reduced component: compensated sum of the
 // target's pair rows (stored in group order; roff gives each target-order
-// pair's row in units of 32 entries; a pair of order q contributes its first
+// pair's row in units of kRowUnit entries; a pair of order q contributes its first
 // (q+1)^2 entries; eight loads in flight), back to physical units, into the
 // reduced components of the local expansion.
 template <typename R>
@@ -874,14 +878,14 @@ __global__ void __launch_bounds__(256) k_m2l_sum(const TreeDev t, int p, const R
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int qq = t.far_ord ? min((int)t.far_ord[q + u], p) : p;
-                v[u] = f < (qq + 1) * (qq + 1) ? out[(size_t)roff[q + u] * 32 + f] : (R)0;
+                v[u] = f < (qq + 1) * (qq + 1) ? out[(size_t)roff[q + u] * kRowUnit + f] : (R)0;
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) acc.add(v[u]);
         }
         for (; q < q1; ++q) {
             const int qq = t.far_ord ? min((int)t.far_ord[q], p) : p;
-            if (f < (qq + 1) * (qq + 1)) acc.add(out[(size_t)roff[q] * 32 + f]);
+            if (f < (qq + 1) * (qq + 1)) acc.add(out[(size_t)roff[q] * kRowUnit + f]);
         }
         const int c = qcomp(f);
         const int k = c >> 24;
@@ -998,7 +1002,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_TRY(ws.cub_tmp.ensure(tb5));
         FMM_CUDA_TRY(cub::DeviceScan::ExclusiveSum(ws.cub_tmp.p, tb5, ws.m2l_tcnt.as<int32_t>(),
                                                    ws.m2l_toff.as<int32_t>(), ng + 1, st));
-        // result rows in group order, (q+1)^2 rounded up to 32 entries per
+        // result rows in group order, (q+1)^2 rounded up to kRowUnit entries per
         // pair; the per-target sum finds them through roff (in the free
         // unsorted-keys buffer)
         FMM_TRY(ws.m2l_rowbase.ensure(sizeof(int32_t) * (ng + 1)));
@@ -1019,7 +1023,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         FMM_CUDA_TRY(cudaMemcpyAsync(&hcnt[1], rowbase + ng, sizeof(int), cudaMemcpyDeviceToHost, st));
         FMM_CUDA_TRY(cudaStreamSynchronize(st));
         const int ntasks = hcnt[0];
-        FMM_TRY(ws.m2l_out.ensure(sizeof(R) * 32 * (size_t)std::max(1, hcnt[1])));
+        FMM_TRY(ws.m2l_out.ensure(sizeof(R) * kRowUnit * (size_t)std::max(1, hcnt[1])));
         FMM_TRY(ws.m2l_tasks.ensure(sizeof(int2) * std::max(1, ntasks)));
         count_launches(1);
         k_fill_tasks<<<grid_for(ng, 256), 256, 0, st>>>(ng, cols, ws.m2l_gq.as<int32_t>(), ws.m2l_gstart.as<int32_t>(),
@@ -1130,7 +1134,7 @@ int grouped(Workspace& ws, const TreeDev& t, int p, cudaStream_t st) {
         }
     }
     count_launches(1);
-    if (nf == 0) FMM_TRY(ws.m2l_out.ensure(sizeof(R) * 32));
+    if (nf == 0) FMM_TRY(ws.m2l_out.ensure(sizeof(R) * kRowUnit));
     // one output per thread: (p+1)^2 rounded up to whole warps (192 at p = 12)
     k_m2l_sum<R><<<(unsigned)M, (unsigned)std::min(256, (nr + 31) / 32 * 32), 0, st>>>(t, p, ws.m2l_out.as<R>(), roff,
                                                                                      ws.loc.as<double>());
