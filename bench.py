@@ -92,7 +92,7 @@ def workload_config(arm, system="water", n=3 * N_MOL):
 
 # DRAM bytes (read + write) per unit of the two dominant kernels, from one ncu
 # capture of each on the 100k water case (profiles/)
-P2P_DRAM_PER_PAIR = 12.81e6 / 412.98e6
+P2P_DRAM_PER_PAIR = (21.25e6 + 0.13e6) / 413.08e6
 TC_DRAM_PER_PAIR = (571.38e6 + 479.74e6) / 1.084818e6
 
 
