@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "pair_x2.cuh"
 
 namespace fmm {
 
@@ -256,8 +257,24 @@ constexpr int kP2mBatch = 64;
 // Shared-memory entries (8 bytes) of the P2M staging area: one batch's
 // powers and moments, or the leaf's A_s[u] at the end.
 __host__ __device__ __forceinline__ int p2m_stage_entries(int p, int nm) {
-    const int a = kP2mBatch * (3 * (p + 1) + nm), b = nT(p) * nm;
+    const int a = kP2mBatch * (3 * (p + 1) + nm + 1), b = nT(p) * nm;
     return a > b ? a : b;
+}
+
+// Two double-float multiply-adds at once in packed FP32 (f32x2): the
+// accumulators (h, l) of moments s and s' as packed pairs H, L, the product
+// x * (y_s, y_s'), with x = (xh, xl) broadcast (nxh = -xh) and y given as
+// packed hi and lo parts.  Each half is df_mac's exact sequence (the
+// product's rounding error by FMA, TwoSum into h), written with -pr.
+__device__ __forceinline__ void df_mac_x2(f2 xh, f2 nxh, f2 xl, f2 yh, f2 yl, f2& H, f2& L) {
+    const f2 npr = nxh * yh;
+    f2 er = fma2(xh, yh, npr);
+    er = fma2(xh, yl, er);
+    er = fma2(xl, yh, er);
+    const f2 sum = H - npr;
+    const f2 bb = sum - H;
+    L = L + (((H - (sum - bb)) - (npr + bb)) + er);
+    H = sum;
 }
 
 __device__ __forceinline__ int pk_index(int x, int y, int z) {
@@ -300,7 +317,15 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_p2m(const TreeDev t, const dou
             ns[r] = min(NM, nT(rem));  // moments of orders <= rem
         }
     }
-    typename O::Acc acc[KS][NM];
+    typename O::Acc acc[KS][DF ? 1 : NM];
+    // double-float path: the accumulators of moments (2k, 2k + 1) as packed pairs
+    f2 PH[KS][DF ? (NM + 1) / 2 : 1], PL[KS][DF ? (NM + 1) / 2 : 1];
+    if constexpr (DF) {
+#pragma unroll
+        for (int r = 0; r < KS; ++r)
+#pragma unroll
+            for (int k = 0; k < (NM + 1) / 2; ++k) PH[r][k] = PL[r][k] = bc2(0.0f);
+    }
     for (int b0 = 0; b0 < cnt; b0 += KB) {
         const int nb = min(KB, cnt - b0);
         // scaled powers d^a / a! per particle axis and the moments M_s / s!
@@ -317,12 +342,57 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_p2m(const TreeDev t, const dou
             }
         }
         V* msb = stage + KB * 3 * P1;
-        for (int idx = threadIdx.x; idx < nb * NM; idx += NT) {
-            const int b = idx / NM, sidx = idx - b * NM;
-            const V w = O::split(smc[(size_t)sidx * n + s0 + b0 + b]);
-            msb[idx] = ((order_of(sidx) + 1) % 2) ? O::neg(w) : w;
+        if constexpr (DF) {
+            // moments in pairs (s, s + 1) as float4 (hi_s, hi_s+1, lo_s, lo_s+1)
+            // (16-byte aligned: KB * 3 * P1 8-byte entries is even)
+            constexpr int NMP = (NM + 1) / 2;
+            float* mf = reinterpret_cast<float*>(msb);
+            for (int idx = threadIdx.x; idx < nb * 2 * NMP; idx += NT) {
+                const int b = idx / (2 * NMP), sidx = idx - b * (2 * NMP);
+                V w = sidx < NM ? O::split(smc[(size_t)sidx * n + s0 + b0 + b]) : O::split(0.0);
+                if (sidx < NM && ((order_of(sidx) + 1) % 2)) w = O::neg(w);
+                float* e = mf + ((size_t)b * NMP + (sidx >> 1)) * 4 + (sidx & 1);
+                e[0] = w.x;
+                e[2] = w.y;
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < nb * NM; idx += NT) {
+                const int b = idx / NM, sidx = idx - b * NM;
+                const V w = O::split(smc[(size_t)sidx * n + s0 + b0 + b]);
+                msb[idx] = ((order_of(sidx) + 1) % 2) ? O::neg(w) : w;
+            }
         }
         __syncthreads();
+        if constexpr (DF) {
+            constexpr int NMP = (NM + 1) / 2;
+            const float4* mq = reinterpret_cast<const float4*>(msb);
+            for (int b = 0; b < nb; ++b) {
+                const V* eb = stage + b * 3 * P1;
+                f2 mh[NMP], ml[NMP];
+#pragma unroll
+                for (int k = 0; k < NMP; ++k) {
+                    const float4 w = mq[(size_t)b * NMP + k];
+                    mh[k] = mk2(w.x, w.y);
+                    ml[k] = mk2(w.z, w.w);
+                }
+#pragma unroll
+                for (int r = 0; r < KS; ++r) {
+                    if (ns[r] == 0) continue;
+                    const V dp = O::mul(O::mul(eb[ux[r]], eb[P1 + uy[r]]), eb[2 * P1 + uz[r]]);
+                    const f2 xh = bc2(dp.x), nxh = bc2(-dp.x), xl = bc2(dp.y);
+                    if (ns[r] == NM) {  // every moment (u of order <= p - m)
+#pragma unroll
+                        for (int k = 0; k < NMP; ++k) df_mac_x2(xh, nxh, xl, mh[k], ml[k], PH[r][k], PL[r][k]);
+                    } else {
+                        // pairs holding a moment below ns (the other half of
+                        // the last pair feeds an accumulator that is not read)
+#pragma unroll
+                        for (int k = 0; k < NMP; ++k)
+                            if (2 * k < ns[r]) df_mac_x2(xh, nxh, xl, mh[k], ml[k], PH[r][k], PL[r][k]);
+                    }
+                }
+            }
+        } else
         for (int b = 0; b < nb; ++b) {
             const V* eb = stage + b * 3 * P1;
             const V* mb = msb + b * NM;
@@ -349,8 +419,20 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_p2m(const TreeDev t, const dou
     for (int r = 0; r < KS; ++r) {
         const int u = threadIdx.x + NT * r;
 #pragma unroll
-        for (int sidx = 0; sidx < NM; ++sidx)
-            if (sidx < ns[r]) A[u * NM + sidx] = acc[r][sidx].val();
+        for (int sidx = 0; sidx < NM; ++sidx) {
+            if (sidx >= ns[r]) continue;
+            if constexpr (DF) {
+                float h0, h1, l0, l1;
+                sp2(PH[r][sidx >> 1], h0, h1);
+                sp2(PL[r][sidx >> 1], l0, l1);
+                typename O::Acc a;
+                a.h = (sidx & 1) ? h1 : h0;
+                a.l = (sidx & 1) ? l1 : l0;
+                A[u * NM + sidx] = a.val();
+            } else {
+                A[u * NM + sidx] = acc[r][sidx].val();
+            }
+        }
     }
     __syncthreads();
     for (int q = threadIdx.x; q < nq; q += NT) {
