@@ -91,7 +91,7 @@ def workload_config(arm, system="water", n=3 * N_MOL):
 
 
 # DRAM bytes (read + write) per unit of the two dominant kernels, from one ncu
-# capture of each on the 100k water case (profiles/)
+# capture of each on the 100k water case
 P2P_DRAM_PER_PAIR = (21.25e6 + 0.13e6) / 413.08e6
 TC_DRAM_PER_PAIR = (571.38e6 + 479.74e6) / 1.084818e6
 
@@ -609,8 +609,8 @@ def main():
         kk["tf32_peak_tflops"] = tf32_peak
         kk["frac_of_tf32_peak"] = kk["mma_tflops"] / tf32_peak
         kk["frac"] = kk["achieved_tflops"] / peak.value  # FP32-equivalent work against the FP32 FMA peak
-    # DRAM bytes per unit from one ncu capture of each kernel on the 100k case
-    # (profiles/), scaled to this launch by its units (pairs): the kernels are
+    # DRAM bytes per unit from one ncu capture of each kernel on the 100k case,
+    # scaled to this launch by its units (pairs): the kernels are
     # compute-bound and their traffic grows in proportion to the pairs
     per_unit = {"k_p2p_f32": (P2P_DRAM_PER_PAIR, p2p_pairs, "near-field pair"),
                 "k_m2l_tc": (TC_DRAM_PER_PAIR, stats["m2l_pairs"], "far pair")}
@@ -747,7 +747,7 @@ def main():
         "other_workloads": extras or None,
         "tree": {k: stats[k] for k in ("num_nodes", "num_leaves", "max_depth", "m2l_pairs", "m2l_groups",
                                        "m2l_order_mean", "p2p_leaf_pairs", "p2p_particle_pairs", "list_candidates",
-                                       "list_evals")},
+                                       "list_evals", "corr_leaf_pairs")},
     }
     print(json.dumps(line), flush=True)
     if dist:

@@ -47,7 +47,7 @@ void Workspace::release_buffers(bool keep_selector) {
                      &sz,        &smc,       &sd,          &fsorted,    &mom,        &loc,        &partial,
                      &term_off,  &term_abc,  &term_c, &f32buf, &wred, &far_ord, &sel_norms, &sel_params, &sel_scratch, &sysbuf,
                      &m2l_tgt, &m2l_keys, &m2l_keys2, &m2l_vals, &m2l_vals2, &m2l_ukeys, &m2l_cnt, &m2l_gstart,
-                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &m2l_wsplit, &m2l_gop, &m2l_gopoff, &m2l_rowbase, &xlate, &l2pt, &dsmc, &f32node, &lattice, &p2p_order, &p2p_pad, &f32x2, &sel_budget};
+                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &m2l_wsplit, &m2l_gop, &m2l_gopoff, &m2l_rowbase, &xlate, &l2pt, &dsmc, &f32node, &lattice, &p2p_order, &p2p_pad, &f32x2, &sel_budget, &corr_pairs, &corr_sorted, &corr_src};
     for (DevBuf* b : all)
         if (!(keep_selector && b == &sel_params)) b->release();
     if (!keep_selector) sel_ready = false;
@@ -79,7 +79,7 @@ Workspace& thread_workspace() {
 
 namespace {
 
-constexpr int kNumStats = 16 + kMaxP + 1 + 6 + 5;
+constexpr int kNumStats = 16 + kMaxP + 1 + 6 + 5 + 1;
 constexpr int kTuneStats = 16 + kMaxP + 1 + 6;  // ncrit used, near-field shape (3), tuned by this call
 struct Stats {
     double v[kNumStats] = {0};
@@ -429,6 +429,18 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     if (o.mac_mode == 1 && P.damp_type != DAMP_NONE && P.damp) {
         const double dmin = min_damping_factor(ws, P.damp, P.n, st);
         tpl.rdamp = damping_range(P.damp_type, dmin * dmin, dim_to_order(P.dim) + f, 0.1 * o.target);
+        // learned lists with the packed FP32 near field, AMOEBA: leaf pairs
+        // inside the damping range may be far pairs, their particle pairs
+        // inside the range corrected in the near field (FMM_GB300_DAMP_CORR=0:
+        // demote them)
+        const char* ce = std::getenv("FMM_GB300_DAMP_CORR");
+        if (learned && (md.precision == 1 || md.precision == 2) && tpl.rdamp > 0.0 && P.damp_type == DAMP_AMOEBA &&
+            p2p_packed_enabled(ws.p2p_shape.valid() ? ws.p2p_shape : P2pShape{}, f, P.damp_type) && !(ce && ce[0] == '0')) {
+            tpl.corr_mode = 1;
+            // AMOEBA depends on a r only: the range at a = 1 is the cutoff of a r
+            const double xc = damping_range(P.damp_type, 1.0, dim_to_order(P.dim) + f, 0.1 * o.target);
+            ws.corr_xcut2 = (float)(xc * xc);
+        }
     }
     TreeDev t;
     const int nf = nT(f);
@@ -596,6 +608,7 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     s.v[kTuneStats + 2] = ws.p2p_shape.stage;
     s.v[kTuneStats + 3] = ws.p2p_shape.queue;
     s.v[kTuneStats + 4] = 0.0;
+    s.v[kTuneStats + 5] = (double)t.ncorr;
     g_stats = s;
     return FMM_OK;
 }

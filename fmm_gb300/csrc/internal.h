@@ -54,6 +54,10 @@ struct TreeDev {
     int32_t *far_off = nullptr, *far_src = nullptr;
     uint8_t* far_ord = nullptr;  // expansion order of each far pair
     int32_t *near_off = nullptr, *near_src = nullptr;
+    // damping-correction list (corr_mode): far leaf pairs inside the damping
+    // range, CSR by target leaf like the near list
+    int64_t ncorr = 0;
+    int32_t *corr_off = nullptr, *corr_src = nullptr;
     // periodic boxes: the lists in use are those of the image whose source
     // cells are displaced by `shift`; `central` is 0 for the 26 other images
     double shift[3] = {0.0, 0.0, 0.0};
@@ -87,6 +91,8 @@ struct TreeParams {
     const float4* sel_chi = nullptr;    // FP32 node centres (hi, rmax in w) of the learned list build
     const float4* sel_clo = nullptr;    // and their low parts (half-width in w)
     double root_r = 0.0;                // > 0: root half-width given (batched packing box)
+    int corr_mode = 0;                  // learned lists: leaf pairs inside the damping range may be far
+                                        // (listed in the damping-correction list)
     const int32_t* d_sys = nullptr;     // batched systems: system id of each particle (input order)
 };
 
@@ -118,6 +124,9 @@ struct P2pShape {
     int pack = 1;  // sources two at a time in packed FP32 (Blackwell f32x2 instructions)
     bool valid() const;
 };
+// Whether the FP32 near field runs the packed kernel for this shape, field
+// order and damping kind.
+bool p2p_packed_enabled(const P2pShape& sh, int field_order, int damp);
 
 struct Workspace {
     // inputs on device (host entry points copy here)
@@ -127,7 +136,7 @@ struct Workspace {
     DevBuf perm, pos_of, leaf_of;
     DevBuf node_d, node_i, child, level_nodes, leaves, node_key, node_val, node_key2, node_val2;
     DevBuf counters, scalars;
-    DevBuf front_a, front_b, far_pairs, near_pairs, far_sorted, near_sorted;
+    DevBuf front_a, front_b, far_pairs, near_pairs, far_sorted, near_sorted, corr_pairs, corr_sorted, corr_src;
     DevBuf node_dfs, far_src, near_src, far_ord, sysbuf;
     DevBuf sel_norms, sel_params, sel_scratch;
     DevBuf sel_budget;  // per node: log10 error budget of far pairs with that target, then its field scale
@@ -175,6 +184,7 @@ struct Workspace {
     bool reuse_structure = false;
     P2pShape p2p_shape;  // FP32 near-field launch shape
     DevBuf p2p_order;    // target leaves by decreasing pair work (queue mode), and scratch
+    float corr_xcut2 = 0.0f;  // damping correction: (a r)^2 beyond which a pair needs none
     DevBuf p2p_pad;      // packed near field: padded leaf starts (node-indexed), odd-leaf flags and their scan
     DevBuf f32x2;        // packed near field: interleaved source records of padded leaves
     int m2l_ng = 0, m2l_ntasks = 0;  // grouped M2L structure of the last evaluation

@@ -262,11 +262,15 @@ __device__ __forceinline__ void p2p_leaf(const float4* src, int cnt, int k0, int
 // blocks (four pairs per fold per half, as in the scalar loop).  The target
 // position enters as xo = x_t + (c_A - c_B)_hi per piece and the low parts as
 // oxl, so R = (xo - x_s) + (oxl - x_s,lo).  k0 is the sorted index of slot 0.
-template <int M, int F, int DAMP, bool CHECK>
+// CORR (a piece of a far leaf inside the damping range): only the damping
+// correction (damped minus undamped kernel) of the pairs with (a r)^2 below
+// xcut2, beyond which the damped kernel equals the undamped one to the
+// requested accuracy; a block is skipped when no lane has such a pair.
+template <int M, int F, int DAMP, bool CHECK, bool CORR = false>
 __device__ __forceinline__ void p2p_leaf_x2(const float4* src, int nblk, int k0, int grp, int ngr, int tgt, f2 xo,
                                             f2 yo, f2 zo, f2 dt, f2 oxl, f2 oyl, f2 ozl,
                                             const int32_t* __restrict__ excl, int exw, int64_t n, int ot, f2* H,
-                                            f2* L) {
+                                            f2* L, float xcut2 = 0.0f) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM), NE = 4 * (NV - 2);
     f2 B[NF];
 #pragma unroll
@@ -275,7 +279,16 @@ __device__ __forceinline__ void p2p_leaf_x2(const float4* src, int nblk, int k0,
     for (int b = grp; b < nblk; b += ngr) {
         const ulonglong2* r = reinterpret_cast<const ulonglong2*>(src + (size_t)b * 2 * NV);
         // element pairs: (x, y), (z, d), (x_lo, y_lo), (z_lo, index), multipoles
-        const ulonglong2 v0 = r[0], v1 = r[1], v2 = r[2], v3 = r[3];
+        const ulonglong2 v0 = r[0], v1 = r[1];
+        if constexpr (CORR) {
+            const f2 cx = xo - f2{v0.x}, cy = yo - f2{v0.y}, cz = zo - f2{v1.x};
+            const f2 aa = dt * f2{v1.y};
+            const f2 tt = (aa * aa) * fma2(cx, cx, fma2(cy, cy, cz * cz));
+            float t0, t1;
+            sp2(tt, t0, t1);
+            if (!__any_sync(__activemask(), t0 < xcut2 || t1 < xcut2)) continue;
+        }
+        const ulonglong2 v2 = r[2], v3 = r[3];
         f2 mc[NE];
 #pragma unroll
         for (int v = 0; v < NE / 2; ++v) {
@@ -307,7 +320,7 @@ __device__ __forceinline__ void p2p_leaf_x2(const float4* src, int nblk, int k0,
                 dx = mk2(s0 ? 1000.0f : d0, s1 ? 1000.0f : d1);
             }
         }
-        pair_field_x2<M, F>(dx, dy, dz, a, DAMP, mc, B);
+        pair_field_x2<M, F, CORR>(dx, dy, dz, a, DAMP, mc, B);
         if (++nb == 4) {
             nb = 0;
 #pragma unroll
@@ -362,8 +375,12 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
                                                     const float4* __restrict__ chi, const float4* __restrict__ clo,
                                                     const int32_t* __restrict__ excl, int exw, int64_t n,
                                                     double* __restrict__ fs, int stage,
-                                                    const int32_t* __restrict__ order, unsigned* __restrict__ next) {
+                                                    const int32_t* __restrict__ order, unsigned* __restrict__ next,
+                                                    float xcut2) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
+    // the damping-correction list is walked after the near list (packed
+    // kernel, AMOEBA)
+    constexpr bool kCorr = X2 && DAMP == DAMP_AMOEBA;
     extern __shared__ __align__(16) float4 sbuf_p2p[];
     const int cap = X2 ? (stage / NV) & ~1 : stage / NV;  // particles (slots) per staged piece
     const int lane = threadIdx.x & 31;
@@ -382,7 +399,11 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
     if (item >= t.num_leaves) break;
     const int leaf = order ? order[item] : t.leaves[item];
     const int s0 = t.start[leaf], cnt = t.count[leaf];
-    const int q0 = t.near_off[leaf], q1 = t.near_off[leaf + 1];
+    const int q0 = t.near_off[leaf], nn = t.near_off[leaf + 1] - q0;
+    const int c0 = (kCorr && t.corr_off) ? t.corr_off[leaf] : 0;
+    const int q1 = nn + ((kCorr && t.corr_off) ? t.corr_off[leaf + 1] - c0 : 0);
+    // source leaf of list entry q: near entries [0, nn), then correction entries
+    auto src_of = [&](int q) { return q < nn ? t.near_src[q0 + q] : t.corr_src[c0 + q - nn]; };
     const float4 ca = chi[leaf], cal = clo[leaf];
     // chunks of 32 targets, then the remaining rem < 32 in cs sub-chunks of
     // gs targets; a chunk of g targets runs ngr = 32 / g lane groups of g
@@ -417,9 +438,9 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
         }
         // current piece (q, off) of source leaf j = [js, js + jc); the first
         // one is staged before the loop
-        int q = q0, off = 0, j = 0, js = 0, jc = 0;
+        int q = 0, off = 0, j = 0, js = 0, jc = 0;
         if (q < q1) {
-            j = t.near_src[q];
+            j = src_of(q);
             js = sstart[j];
             jc = t.count[j];
             if (X2) jc += jc & 1;  // padded to whole blocks
@@ -435,7 +456,7 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
                 nq = q + 1;
                 noff = 0;
                 if (nq < q1) {
-                    nj = t.near_src[nq];
+                    nj = src_of(nq);
                     njs = sstart[nj];
                     njc = t.count[nj];
                     if (X2) njc += njc & 1;
@@ -467,7 +488,18 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
                 if constexpr (X2) {
                     const f2 xo = bc2(ta.x + ox), yo = bc2(ta.y + oy), zo = bc2(ta.z + oz), dt = bc2(ta.w);
                     const f2 oxl2 = bc2(oxl), oyl2 = bc2(oyl), ozl2 = bc2(ozl);
-                    if (__any_sync(__activemask(), need))
+                    const bool anyneed = __any_sync(__activemask(), need);
+                    if (kCorr && q >= nn) {
+                        if constexpr (kCorr) {
+                            if (anyneed)
+                                p2p_leaf_x2<M, F, DAMP, true, true>(cur, pc >> 1, k0, grp, ngr, tgt, xo, yo, zo, dt,
+                                                                    oxl2, oyl2, ozl2, excl, exw, n, ot, XH, XL, xcut2);
+                            else
+                                p2p_leaf_x2<M, F, DAMP, false, true>(cur, pc >> 1, k0, grp, ngr, tgt, xo, yo, zo, dt,
+                                                                     oxl2, oyl2, ozl2, excl, exw, n, ot, XH, XL,
+                                                                     xcut2);
+                        }
+                    } else if (anyneed)
                         p2p_leaf_x2<M, F, DAMP, true>(cur, pc >> 1, k0, grp, ngr, tgt, xo, yo, zo, dt, oxl2, oyl2,
                                                       ozl2, excl, exw, n, ot, XH, XL);
                     else
@@ -625,6 +657,13 @@ __global__ void k_leaf_cost(const TreeDev t, uint32_t* __restrict__ cost, int32_
     const int leaf = t.leaves[w];
     uint32_t s = 0;
     for (int q = t.near_off[leaf] + lane; q < t.near_off[leaf + 1]; q += 32) s += (uint32_t)t.count[t.near_src[q]];
+    if (t.corr_off) {
+        // damping-correction pieces: mostly the cheap range test, about a
+        // quarter of a near pair each
+        uint32_t c = 0;
+        for (int q = t.corr_off[leaf] + lane; q < t.corr_off[leaf + 1]; q += 32) c += (uint32_t)t.count[t.corr_src[q]];
+        s += c / 4;
+    }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (lane == 0) {
         const uint64_t c = (uint64_t)t.count[leaf] * s;
@@ -637,26 +676,26 @@ template <int M, int F, bool X2>
 void launch_p2p_kind(unsigned blocks, int threads, size_t smem, int stage, const int32_t* order, unsigned* next,
                      cudaStream_t st, const TreeDev& t, const float4* rec, const float4* srec, const int32_t* sstart,
                      const float4* chi, const float4* clo, const int32_t* excl, int exw, int64_t n, int damp,
-                     double* fs) {
+                     double* fs, float xcut2) {
     if constexpr (X2 && F > 1) {
         return;  // not instantiated: the packed kernel is used for field orders 0 and 1
     } else {
     switch (damp) {
         case DAMP_AMOEBA:
             k_p2p_f32<M, F, DAMP_AMOEBA, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw,
-                                                                              n, fs, stage, order, next);
+                                                                              n, fs, stage, order, next, xcut2);
             break;
         case DAMP_THOLE:
             k_p2p_f32<M, F, DAMP_THOLE, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw,
-                                                                             n, fs, stage, order, next);
+                                                                             n, fs, stage, order, next, xcut2);
             break;
         case DAMP_ERF:
             k_p2p_f32<M, F, DAMP_ERF, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw, n,
-                                                                           fs, stage, order, next);
+                                                                           fs, stage, order, next, xcut2);
             break;
         default:
             k_p2p_f32<M, F, DAMP_NONE, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw,
-                                                                            n, fs, stage, order, next);
+                                                                            n, fs, stage, order, next, xcut2);
             break;
     }
     }
@@ -764,6 +803,11 @@ int launch_leaf_field_scale(Workspace& ws, const Particles& P, const TreeDev& t,
     return FMM_OK;
 }
 
+bool p2p_packed_enabled(const P2pShape& sh, int field_order, int damp) {
+    const char* pe = std::getenv("FMM_GB300_P2P_PACKED");
+    return sh.pack && !(pe && pe[0] == '0') && field_order <= 1 && damp != DAMP_ERF;
+}
+
 bool P2pShape::valid() const {
     return (threads == 64 || threads == 128 || threads == 256) && stage >= 64 && stage <= 1024 && stage % 16 == 0 &&
            (queue == 0 || queue == 1) && (pack == 0 || pack == 1);
@@ -782,10 +826,13 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
     if (rec_vec(P.dim) > sh.stage) return FMM_EINVAL;
     // packed kernel: sources two at a time from the padded, interleaved
     // records, for field orders 0 and 1 (at order 2 the packed registers do
-    // not fit); FMM_GB300_P2P_PACKED=0 selects the one-source kernel
-    const char* pe = std::getenv("FMM_GB300_P2P_PACKED");
-    const bool x2 = sh.pack && !(pe && pe[0] == '0') && field_order <= 1 && t.num_leaves > 0 &&
+    // not fit) and all kernels but erf (whose Boys series, at a r^2 < 6 for
+    // much of an erf near field, runs per half: measured slower than the
+    // one-source kernel); FMM_GB300_P2P_PACKED=0 selects the one-source kernel
+    const bool x2 = p2p_packed_enabled(sh, field_order, P.damp_type) && t.num_leaves > 0 &&
                     n + (int64_t)t.num_leaves < (int64_t)INT32_MAX;
+    // a damping-correction list is walked by the packed kernel only
+    if (t.ncorr > 0 && !(x2 && P.damp_type == DAMP_AMOEBA)) return FMM_ENOTSUP;
     if (x2) {
         const int nv = rec_vec(P.dim);
         const int L = t.num_leaves;
@@ -845,12 +892,13 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
         FMM_MF_SWITCH(m, field_order,
                       (launch_p2p_kind<MM, FF, true>(blocks, sh.threads, smem, sh.stage, order, next, st, t, rec,
                                                      ws.f32x2.as<float4>(), ws.p2p_pad.as<int32_t>(), chi, clo,
-                                                     P.excl, P.exw, n, P.damp_type, ws.fsorted.as<double>())));
+                                                     P.excl, P.exw, n, P.damp_type, ws.fsorted.as<double>(),
+                                                     ws.corr_xcut2)));
     } else {
         FMM_MF_SWITCH(m, field_order,
                       (launch_p2p_kind<MM, FF, false>(blocks, sh.threads, smem, sh.stage, order, next, st, t, rec, rec,
                                                       t.start, chi, clo, P.excl, P.exw, n, P.damp_type,
-                                                      ws.fsorted.as<double>())));
+                                                      ws.fsorted.as<double>(), 0.0f)));
     }
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;

@@ -64,7 +64,10 @@ __device__ __forceinline__ f2& operator+=(f2& a, f2 b) { return a = a + b; }
 // per half).  Both halves beyond the interval tables (the common case in the
 // near field) take the packed closed forms; otherwise each half runs the
 // scalar routine.
-template <int N>
+// CORR: the damped kernel's difference from the undamped one (g_damped -
+// g_undamped, AMOEBA only): the closed form keeps just its exponential part,
+// so the difference carries no cancellation.
+template <int N, bool CORR = false>
 __device__ __forceinline__ void radial_g_x2(int damp, f2 r2, f2 ir, f2 a, f2 eps, f2* g) {
     const f2 ir2 = ir * ir;
     f2 num[N + 1];
@@ -80,13 +83,13 @@ __device__ __forceinline__ void radial_g_x2(int damp, f2 r2, f2 ir, f2 a, f2 eps
         packed = !(u0 < Real<float>::kAmoebaHi) && !(u1 < Real<float>::kAmoebaHi);
         if (packed) {
             const f2 e = mk2(Real<float>::expc_(-u0), Real<float>::expc_(-u1));
-            num[0] = bc2(0.0f);
+            num[0] = bc2(CORR ? -1.0f : 0.0f);
 #pragma unroll
             for (int j = 1; j <= N; ++j) {
                 f2 q = bc2(Real<float>::amoebaQ(j, j - 1));
 #pragma unroll
                 for (int d = j - 2; d >= 0; --d) q = fma2(q, u, bc2(Real<float>::amoebaQ(j, d)));
-                num[j] = fma2(e, q, bc2((float)((j % 2 ? -1.0 : 1.0) * dfact_odd(j))));
+                num[j] = CORR ? e * q : fma2(e, q, bc2((float)((j % 2 ? -1.0 : 1.0) * dfact_odd(j))));
             }
         }
     } else if (damp == DAMP_THOLE) {
@@ -130,7 +133,16 @@ __device__ __forceinline__ void radial_g_x2(int damp, f2 r2, f2 ir, f2 a, f2 eps
     sp2(a, ah[0], ah[1]);
     sp2(eps, eh[0], eh[1]);
 #pragma unroll 1
-    for (int h = 0; h < 2; ++h) radial_g_ir<N, float>(damp, r2h[h], irh[h], ah[h], gh[h], eh[h]);
+    for (int h = 0; h < 2; ++h) {
+        radial_g_ir<N, float>(damp, r2h[h], irh[h], ah[h], gh[h], eh[h]);
+        if (CORR) {
+            // inside the tables the difference is of the order of the terms
+            float gu[N + 1];
+            radial_g_ir<N, float>(DAMP_NONE, r2h[h], irh[h], ah[h], gu, eh[h]);
+#pragma unroll
+            for (int j = 0; j <= N; ++j) gh[h][j] -= gu[j];
+        }
+    }
 #pragma unroll
     for (int j = 0; j <= N; ++j) g[j] = mk2(gh[0][j], gh[1][j]);
 }
@@ -213,7 +225,9 @@ __device__ __forceinline__ void contract_x2(const f2* T, const f2* Mc, f2* acc) 
 // pair_field_f32acc on two pairs: compensated r^2 (FMA-captured product
 // errors, TwoSum of the squares), one Newton step for 1/r on the compensated
 // r^2, radial functions with the 1/r correction, contraction.
-template <int M, int F>
+// CORR: the damping correction of a pair (AMOEBA): the field of the damped
+// kernel minus that of the undamped one, potential term included.
+template <int M, int F, bool CORR = false>
 __device__ __forceinline__ void pair_field_x2(f2 dx, f2 dy, f2 dz, f2 a, int damp, const f2* Mc, f2* acc) {
     constexpr int N = M + F;
     const f2 px = dx * dx, py = dy * dy, pz = dz * dz;
@@ -238,9 +252,9 @@ __device__ __forceinline__ void pair_field_x2(f2 dx, f2 dy, f2 dz, f2 a, int dam
     const f2 ir = y0 + c;
     const f2 ir_lo = c - (ir - y0);
     f2 g[N + 1];
-    radial_g_x2<N>(damp, r2, ir, a, ir_lo * (r2 * ir), g);
+    radial_g_x2<N, CORR>(damp, r2, ir, a, ir_lo * (r2 * ir), g);
     if constexpr (M == 2 && F == 1) {
-        contract_q1_x2(dx, dy, dz, g, Mc, damp, acc);
+        contract_q1_x2(dx, dy, dz, g, Mc, CORR ? (int)DAMP_NONE : damp, acc);
     } else {
         f2 T[nT(N)];
         md_tensor_x2<N>(dx, dy, dz, g, T);

@@ -306,15 +306,19 @@ __device__ __forceinline__ unsigned long long warp_alloc(unsigned long long* ctr
 // or refined into the children of the larger node; entries are appended to
 // the far list, the near list or the next frontier.  Called by every lane of
 // the warp (skip: no candidate).
+// With corr (two leaves inside the damping range, accepted as far), the pair
+// is also appended to the damping-correction list corrp (counter 5).
 template <typename RR>
 __device__ __forceinline__ void emit_pair(bool skip, bool accept, int order, int i, int j, bool li, bool lj,
                                           bool mixed, RR ri, RR rj, const TreeDev& t, int2* __restrict__ out,
                                           int64_t cap_out, uint64_t* __restrict__ far, int64_t cap_far,
                                           uint64_t* __restrict__ nearp, int64_t cap_near,
-                                          unsigned long long* counters, int lane) {
+                                          unsigned long long* counters, int lane, bool corr = false,
+                                          uint64_t* __restrict__ corrp = nullptr, int64_t cap_corr = 0) {
     const bool isfar = !skip && accept;
     const bool isnear = !skip && !accept && li && lj && !mixed;
     const bool refine = !skip && !accept && !isnear;
+    const bool iscorr = isfar && corr;
     int c[8], nc = 0;
     bool descend_i = false;
     if (refine) {
@@ -329,6 +333,13 @@ __device__ __forceinline__ void emit_pair(bool skip, bool accept, int order, int
     const unsigned long long kf = warp_alloc(&counters[1], isfar ? 1u : 0u, lane);
     const unsigned long long kn = warp_alloc(&counters[2], isnear ? 1u : 0u, lane);
     const unsigned long long kr = warp_alloc(&counters[0], (unsigned)nc, lane);
+    const unsigned long long kc = warp_alloc(&counters[5], iscorr ? 1u : 0u, lane);
+    if (iscorr) {
+        if (kc < (unsigned long long)cap_corr)
+            corrp[kc] = ((uint64_t)(uint32_t)i << 32) | (uint32_t)j;
+        else
+            counters[3] = 1;
+    }
     if (isfar) {
         if (kf < (unsigned long long)cap_far)
             far[kf] = ((uint64_t)(uint32_t)i << 36) | ((uint64_t)(order & 15) << 32) | (uint32_t)j;
@@ -395,12 +406,18 @@ __global__ void k_list_iter(const int2* __restrict__ in, int nin, int2* __restri
 // (theta_loose) and the damping-range test is accepted at the lowest order q
 // (2..qmax) whose predicted log10 truncation error is within the per-pair
 // budget; otherwise it is refined exactly like a pair the test rejects.
+// corr_mode: two leaves that pass the geometric test but lie inside the
+// damping range go to the network as well, as undamped pairs (the damping
+// feature at its far value: the M2L carries the undamped kernel); accepted,
+// they are far pairs whose particle pairs inside the range are corrected by
+// the near-field kernel (the difference of the damped and undamped
+// kernels), and listed in corrp.
 __global__ void __launch_bounds__(128) k_list_iter_learned(
     const int2* __restrict__ in, int nin, int2* __restrict__ out, int64_t cap_out, uint64_t* __restrict__ far,
     int64_t cap_far, uint64_t* __restrict__ nearp, int64_t cap_near, const TreeDev t, float theta_loose, float rdamp,
     int qmax, const float* __restrict__ params, const float* __restrict__ lnorm, const float* __restrict__ dmin,
     int P, const float* __restrict__ log_budget, const float4* __restrict__ chi, const float4* __restrict__ clo,
-    unsigned long long* counters) {
+    unsigned long long* counters, int corr_mode, uint64_t* __restrict__ corrp, int64_t cap_corr) {
     extern __shared__ __align__(16) float sm_sel[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float* X = sm_sel + wib * kWarpTcFloats;  // this warp's network scratch
@@ -410,7 +427,7 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
     bool skip = q >= nin;
     int i = 0, j = 0;
     float ri = 0.0f, rj = 0.0f;  // FP32 node data throughout: the FP64 pipe is the scarce one
-    bool li = false, lj = false, mixed = false, accept = false;
+    bool li = false, lj = false, mixed = false, accept = false, corr = false;
     float4 ci = make_float4(0.f, 0.f, 0.f, 0.f), cj = ci, oi = ci, oj = ci;
     if (!skip) {
         i = in[q].x;
@@ -438,7 +455,12 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
         accept = !skip && !mixed && r * theta_loose > ri + rj;
         if (accept && rdamp > 0.0f) {
             const float gap = r - 1.7320508f * (oi.w + oj.w);
-            accept = gap >= rdamp;
+            if (gap < rdamp) {
+                if (corr_mode && li && lj)
+                    corr = true;
+                else
+                    accept = false;
+            }
         }
     }
     // the network runs once per warp on the pairs that passed the loose test
@@ -450,6 +472,7 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
         if (accept) {
             float x[kMlpIn];
             selector_features_f32(chi, clo, t.count, lnorm, dmin, P, i, j, x);
+            if (corr) x[16] = 1.0f;  // the M2L carries the undamped kernel; the damping is corrected pairwise
             mlp_input(S, x, X + slot * kMlpInP);
         }
         __syncwarp();
@@ -465,7 +488,7 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
         }
     }
     emit_pair(skip, accept, order, i, j, li, lj, mixed, ri, rj, t, out, cap_out, far, cap_far, nearp, cap_near,
-              counters, lane);
+              counters, lane, corr, corrp, cap_corr);
 }
 
 __global__ void k_split_pairs(int64_t m, const uint64_t* __restrict__ sorted, int32_t* __restrict__ src,
@@ -756,15 +779,19 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
     int64_t cap_near = std::max<int64_t>(
         {4096, (int64_t)(0.4 * per * t.num_leaves), (int64_t)(ws.near_pairs.cap / sizeof(uint64_t))});
     int64_t cap_front = std::max<int64_t>({4096, cap_far, (int64_t)(ws.front_a.cap / sizeof(int2))});
+    const bool corr = tp.sel_params && tp.corr_mode && tp.mac_mode == 1 && tp.rdamp > 0.0;
+    int64_t cap_corr = corr ? std::max<int64_t>({4096, cap_near, (int64_t)(ws.corr_pairs.cap / sizeof(uint64_t))}) : 0;
     unsigned long long* ctr = ws.counters.as<unsigned long long>();
     for (int attempt = 0; attempt < 8; ++attempt) {
         FMM_TRY(ws.front_a.ensure(sizeof(int2) * cap_front));
         FMM_TRY(ws.front_b.ensure(sizeof(int2) * cap_front));
         FMM_TRY(ws.far_pairs.ensure(sizeof(uint64_t) * cap_far));
         FMM_TRY(ws.near_pairs.ensure(sizeof(uint64_t) * cap_near));
+        if (corr) FMM_TRY(ws.corr_pairs.ensure(sizeof(uint64_t) * cap_corr));
         const int2 root = make_int2(0, 0);
         FMM_CUDA_TRY(cudaMemcpyAsync(ws.front_a.p, &root, sizeof(int2), cudaMemcpyHostToDevice, st));
-        unsigned long long h[5] = {0, 0, 0, 0, 0};  // frontier, far, near, overflow flag, network evaluations
+        // frontier, far, near, overflow flag, network evaluations, correction pairs
+        unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
         FMM_CUDA_TRY(cudaMemcpyAsync(ctr, h, sizeof(h), cudaMemcpyHostToDevice, st));
         int64_t nin = 1;
         int64_t candidates = 0;
@@ -783,7 +810,7 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
                     fin, (int)nin, fout, cap_front, ws.far_pairs.as<uint64_t>(), cap_far, ws.near_pairs.as<uint64_t>(),
                     cap_near, t, (float)tp.sel_theta, tp.mac_mode == 1 ? (float)tp.rdamp : 0.0f, tp.order,
                     tp.sel_params, tp.sel_lnorm, tp.sel_dmin, tp.sel_P, tp.sel_budget, tp.sel_chi, tp.sel_clo,
-                    ctr);
+                    ctr, corr ? 1 : 0, corr ? ws.corr_pairs.as<uint64_t>() : nullptr, cap_corr);
             } else
             k_list_iter<<<grid_for(nin, 256), 256, 0, st>>>(fin, (int)nin, fout, cap_front,
                                                              ws.far_pairs.as<uint64_t>(), cap_far,
@@ -802,11 +829,13 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
             if ((int64_t)h[0] > cap_front) cap_front = 2 * (int64_t)h[0];
             if ((int64_t)h[1] > cap_far) cap_far = 2 * (int64_t)h[1];
             if ((int64_t)h[2] > cap_near) cap_near = 2 * (int64_t)h[2];
+            if ((int64_t)h[5] > cap_corr) cap_corr = 2 * (int64_t)h[5];
             cap_front *= 2;
             continue;
         }
         t.nfar = (int64_t)h[1];
         t.nnear = (int64_t)h[2];
+        t.ncorr = corr ? (int64_t)h[5] : 0;
         ws.list_candidates = candidates;
         ws.list_evals = (int64_t)h[4];
         // sort both lists by (target, source) and build CSR offsets; the keys
@@ -852,6 +881,29 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
         k_csr_offsets<<<grid_for(M + 1, 256), 256, 0, st>>>(M, t.nfar, ws.far_sorted.as<uint64_t>(), t.far_off, 36);
         count_launches(1);
         k_csr_offsets<<<grid_for(M + 1, 256), 256, 0, st>>>(M, t.nnear, ws.near_sorted.as<uint64_t>(), t.near_off, 32);
+        t.corr_off = t.corr_src = nullptr;
+        if (corr) {
+            // damping-correction list: sorted by (target, source), CSR by target
+            FMM_TRY(ws.corr_sorted.ensure(sizeof(uint64_t) * std::max<int64_t>(1, t.ncorr)));
+            FMM_TRY(ws.corr_src.ensure(sizeof(int32_t) * (std::max<int64_t>(1, t.ncorr) + (M + 1))));
+            t.corr_src = ws.corr_src.as<int32_t>();
+            t.corr_off = t.corr_src + std::max<int64_t>(1, t.ncorr);
+            if (t.ncorr > 0) {
+                size_t tb3 = 0;
+                cub::DeviceRadixSort::SortKeys(nullptr, tb3, ws.corr_pairs.as<uint64_t>(),
+                                               ws.corr_sorted.as<uint64_t>(), (int)t.ncorr, 0, near_bits, st);
+                FMM_TRY(ensure_cub_tmp(ws, tb3));
+                FMM_CUDA_TRY(cub::DeviceRadixSort::SortKeys(ws.cub_tmp.p, tb3, ws.corr_pairs.as<uint64_t>(),
+                                                            ws.corr_sorted.as<uint64_t>(), (int)t.ncorr, 0,
+                                                            near_bits, st));
+                count_launches(1);
+                k_split_pairs<<<grid_for(t.ncorr, 256), 256, 0, st>>>(t.ncorr, ws.corr_sorted.as<uint64_t>(),
+                                                                       t.corr_src, nullptr);
+            }
+            count_launches(1);
+            k_csr_offsets<<<grid_for(M + 1, 256), 256, 0, st>>>(M, t.ncorr, ws.corr_sorted.as<uint64_t>(),
+                                                                t.corr_off, 32);
+        }
         unsigned long long* pc = ctr + 4;
         FMM_CUDA_TRY(cudaMemsetAsync(pc, 0, sizeof(unsigned long long), st));
         if (t.nnear > 0) {

@@ -230,8 +230,10 @@ int fmm_release_workspace(void);
  * learned selector's network evaluated, and the number of lattice levels the
  * periodic sum used (0 without a periodic box); then the ncrit the call used,
  * the FP32 near field's launch shape (threads per block, staging float4s,
- * work queue 0/1) and 1 if this call ran the autotuner.  Returns the number
- * written (at most 40). */
+ * work queue 0/1) and 1 if this call ran the autotuner; then the number of
+ * far leaf pairs inside the damping range whose particle pairs the near
+ * field corrected (learned lists with the packed FP32 near field, AMOEBA;
+ * else 0).  Returns the number written (at most 41). */
 int fmm_last_stats(double *out, int len);
 
 /* Diagnostics (no counterpart in the reference): builds the octree and

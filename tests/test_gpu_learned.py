@@ -101,3 +101,56 @@ def test_learned_on_clustered_particles_meets_target():
         rows = np.sort(rng.choice(F.shape[0], 256, replace=False))
         ref = bench.sampled_reference(s, rows, "AMOEBA")
         assert bench.rel_errors(F[rows], ref)["rms_rel_err"] <= 1e-6
+
+
+def test_damping_correction_meets_target_with_fewer_near_pairs(water, monkeypatch):
+    """Learned lists with the damping correction (leaf pairs inside the
+    damping range accepted as far pairs, the damped-minus-undamped kernel of
+    their close particle pairs added in the near field) meet the target like
+    the demoting rule (FMM_GB300_DAMP_CORR=0) with fewer near pairs."""
+    s, D = water
+    F, st = _run(s, "learned")
+    monkeypatch.setenv("FMM_GB300_DAMP_CORR", "0")
+    F0, st0 = _run(s, "learned")
+    assert st["selector_fallback"] == 0 and st0["selector_fallback"] == 0
+    assert _rms(F, D) <= 1e-6
+    assert _rms(F0, D) <= 1e-6
+    assert st["p2p_particle_pairs"] < st0["p2p_particle_pairs"]
+
+
+def test_damping_correction_with_distant_exclusions(water):
+    """Exclusions between particles of distant leaves: an excluded pair in a
+    corrected far leaf pair gets neither the correction nor the field (the
+    M2L's undamped share is removed by the exclusion pass), as in the direct
+    sum; the result meets the target (with the learned lists or, when the
+    sampled check rejects them, with the fixed rule)."""
+    s, _ = water
+    n = s["coordinates"].shape[0]
+    E = np.hstack([np.array(s["exclusions"]), np.zeros((n, 1), dtype=np.array(s["exclusions"]).dtype)])
+    rng = np.random.default_rng(13)
+    # 600 pairs of particles 10-14 bohr apart also exclude each other (both lists)
+    X = s["coordinates"]
+    picked = 0
+    for i in rng.permutation(n):
+        if picked >= 600:
+            break
+        if E[i, -1] != 0:
+            continue
+        d = np.linalg.norm(X - X[i], axis=1)
+        cand = [j for j in np.nonzero((d > 10.0) & (d < 14.0))[0] if E[j, -1] == 0]
+        if not cand:
+            continue
+        j = int(cand[0])
+        E[i, -1] = j + 1
+        E[j, -1] = i + 1
+        picked += 1
+    assert picked == 600
+    E2 = np.asfortranarray(E)
+    D = fmm_gb300.field_direct(0, X, s["multipoles"], E2, 1, "AMOEBA", s["damping_factors"],
+                               options=Options(excl_mode="mask"))
+    opt = Options.exact(precision="mixed", mac_mode="damping", selector="learned")
+    F = fmm_gb300.field_fmm(0, X, s["multipoles"], E2, 0.3, 64, 10, 1, "AMOEBA", s["damping_factors"], options=opt)
+    st = fmm_gb300.last_stats()
+    if st["selector_fallback"] == 0:
+        assert st["corr_leaf_pairs"] > 0
+    assert _rms(F, D) <= 1e-6
