@@ -582,7 +582,10 @@ def main():
     prec = 1 if args.arm != "fp64" else 0
     peak = ctypes.c_double(0)
     _lib.check(L.fmm_measure_fma_peak(prec, ctypes.byref(peak)), "fma peak")
-    p2p_pairs = stats["p2p_particle_pairs"] - n
+    # near-field pairs (the self pairs excluded) plus the particle pairs of far
+    # leaf pairs inside the damping range whose damping correction the
+    # near-field kernel evaluated (the same pair arithmetic)
+    p2p_pairs = stats["p2p_particle_pairs"] - n + stats.get("corr_particle_pairs", 0.0)
     m2l_product_flops = sum(stats["m2l_pairs_q%d" % q] * m2l_product_flops_per_pair(q) for q in range(13))
     # the FP32 M2L product runs on the tensor cores (tcgen05 kind::tf32)
     # unless FMM_GB300_M2L_PRODUCT=cuda moves it to the CUDA cores
@@ -747,7 +750,7 @@ def main():
         "other_workloads": extras or None,
         "tree": {k: stats[k] for k in ("num_nodes", "num_leaves", "max_depth", "m2l_pairs", "m2l_groups",
                                        "m2l_order_mean", "p2p_leaf_pairs", "p2p_particle_pairs", "list_candidates",
-                                       "list_evals", "corr_leaf_pairs")},
+                                       "list_evals", "corr_leaf_pairs", "corr_particle_pairs")},
     }
     print(json.dumps(line), flush=True)
     if dist:

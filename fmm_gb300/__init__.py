@@ -343,7 +343,7 @@ STAT_NAMES = ["num_nodes", "num_leaves", "max_depth", "m2l_pairs", "p2p_leaf_pai
               "t_p2m_m2m", "t_lists", "t_p2p", "t_m2l", "t_l2l_l2p", "t_total", "selector_fallback",
               "sampled_rms_err", "m2l_order_mean"] + ["m2l_pairs_q%d" % q for q in range(13)] + \
              ["t_p2p_kernel", "t_m2l_product", "m2l_groups", "list_candidates", "list_evals", "lattice_levels",
-              "ncrit_used", "p2p_threads", "p2p_stage", "p2p_queue", "tuned", "corr_leaf_pairs"]
+              "ncrit_used", "p2p_threads", "p2p_stage", "p2p_queue", "tuned", "corr_leaf_pairs", "corr_particle_pairs"]
 
 
 def last_stats():

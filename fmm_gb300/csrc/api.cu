@@ -47,7 +47,7 @@ void Workspace::release_buffers(bool keep_selector) {
                      &sz,        &smc,       &sd,          &fsorted,    &mom,        &loc,        &partial,
                      &term_off,  &term_abc,  &term_c, &f32buf, &wred, &far_ord, &sel_norms, &sel_params, &sel_scratch, &sysbuf,
                      &m2l_tgt, &m2l_keys, &m2l_keys2, &m2l_vals, &m2l_vals2, &m2l_ukeys, &m2l_cnt, &m2l_gstart,
-                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &m2l_wsplit, &m2l_gop, &m2l_gopoff, &m2l_rowbase, &xlate, &l2pt, &dsmc, &f32node, &lattice, &p2p_order, &p2p_pad, &f32x2, &sel_budget, &corr_pairs, &corr_sorted, &corr_src};
+                     &m2l_tcnt, &m2l_toff, &m2l_tasks, &m2l_T, &m2l_gq, &m2l_gab, &m2l_wsc, &m2l_out, &m2l_wsplit, &m2l_gop, &m2l_gopoff, &m2l_rowbase, &xlate, &l2pt, &dsmc, &f32node, &lattice, &p2p_order, &p2p_pad, &f32x2, &sel_budget, &corr_pairs, &corr_sorted, &corr_src, &leaf_ext};
     for (DevBuf* b : all)
         if (!(keep_selector && b == &sel_params)) b->release();
     if (!keep_selector) sel_ready = false;
@@ -79,7 +79,7 @@ Workspace& thread_workspace() {
 
 namespace {
 
-constexpr int kNumStats = 16 + kMaxP + 1 + 6 + 5 + 1;
+constexpr int kNumStats = 16 + kMaxP + 1 + 6 + 5 + 2;
 constexpr int kTuneStats = 16 + kMaxP + 1 + 6;  // ncrit used, near-field shape (3), tuned by this call
 struct Stats {
     double v[kNumStats] = {0};
@@ -566,6 +566,11 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
                                                                                                     d_hist);
     }
     FMM_CUDA_TRY(cudaMemcpyAsync(hist, d_hist, sizeof(hist), cudaMemcpyDeviceToHost, st));
+    // particle pairs the near field's damping correction evaluated (counter 9)
+    unsigned long long corr_evals = 0;
+    if (t.ncorr > 0)
+        FMM_CUDA_TRY(cudaMemcpyAsync(&corr_evals, ws.counters.as<unsigned long long>() + 9, sizeof(corr_evals),
+                                     cudaMemcpyDeviceToHost, st));
     int product_err = 0;
     if (ws.product_err)
         FMM_CUDA_TRY(cudaMemcpyAsync(&product_err, ws.product_err, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -609,6 +614,7 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
     s.v[kTuneStats + 3] = ws.p2p_shape.queue;
     s.v[kTuneStats + 4] = 0.0;
     s.v[kTuneStats + 5] = (double)t.ncorr;
+    s.v[kTuneStats + 6] = (double)corr_evals;
     g_stats = s;
     return FMM_OK;
 }

@@ -185,6 +185,7 @@ struct Workspace {
     P2pShape p2p_shape;  // FP32 near-field launch shape
     DevBuf p2p_order;    // target leaves by decreasing pair work (queue mode), and scratch
     float corr_xcut2 = 0.0f;  // damping correction: (a r)^2 beyond which a pair needs none
+    DevBuf leaf_ext;          // damping correction: per leaf (particle extent, smallest damping factor)
     DevBuf p2p_pad;      // packed near field: padded leaf starts (node-indexed), odd-leaf flags and their scan
     DevBuf f32x2;        // packed near field: interleaved source records of padded leaves
     int m2l_ng = 0, m2l_ntasks = 0;  // grouped M2L structure of the last evaluation

@@ -104,6 +104,27 @@ __global__ void k_gather_x2(int64_t n, int nv, bool q1, const TreeDev t, const i
     }
 }
 
+// Per leaf: the largest distance of its particles from its centre (from the
+// FP32 records, plus a rounding margin) and its smallest damping factor;
+// bounds for skipping whole damping-correction pieces.
+__global__ void k_leaf_extent(int nv, const TreeDev t, const float4* __restrict__ rec, float2* __restrict__ ext) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= t.num_leaves) return;
+    const int leaf = t.leaves[w];
+    const int s0 = t.start[leaf], cnt = t.count[leaf];
+    float r2 = 0.0f, dmin = 3.0e38f;
+    for (int k = lane; k < cnt; k += 32) {
+        const float4 a = rec[(size_t)(s0 + k) * nv];
+        r2 = fmaxf(r2, a.x * a.x + a.y * a.y + a.z * a.z);
+        dmin = fminf(dmin, a.w);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        r2 = fmaxf(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+        dmin = fminf(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
+    }
+    if (lane == 0) ext[leaf] = make_float2(sqrtf(r2) * 1.0001f + 1e-3f, dmin);
+}
+
 __global__ void k_leaf_odd(const TreeDev t, int32_t* __restrict__ odd) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w < t.num_leaves) odd[w] = t.count[t.leaves[w]] & 1;
@@ -270,7 +291,7 @@ template <int M, int F, int DAMP, bool CHECK, bool CORR = false>
 __device__ __forceinline__ void p2p_leaf_x2(const float4* src, int nblk, int k0, int grp, int ngr, int tgt, f2 xo,
                                             f2 yo, f2 zo, f2 dt, f2 oxl, f2 oyl, f2 ozl,
                                             const int32_t* __restrict__ excl, int exw, int64_t n, int ot, f2* H,
-                                            f2* L, float xcut2 = 0.0f) {
+                                            f2* L, float xcut2 = 0.0f, int* ncorr = nullptr) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM), NE = 4 * (NV - 2);
     f2 B[NF];
 #pragma unroll
@@ -287,6 +308,7 @@ __device__ __forceinline__ void p2p_leaf_x2(const float4* src, int nblk, int k0,
             float t0, t1;
             sp2(tt, t0, t1);
             if (!__any_sync(__activemask(), t0 < xcut2 || t1 < xcut2)) continue;
+            *ncorr += (t0 < xcut2 ? 1 : 0) + (t1 < xcut2 ? 1 : 0);  // pairs whose correction is needed
         }
         const ulonglong2 v2 = r[2], v3 = r[3];
         f2 mc[NE];
@@ -376,7 +398,8 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
                                                     const int32_t* __restrict__ excl, int exw, int64_t n,
                                                     double* __restrict__ fs, int stage,
                                                     const int32_t* __restrict__ order, unsigned* __restrict__ next,
-                                                    float xcut2) {
+                                                    float xcut2, unsigned long long* __restrict__ corr_count,
+                                                    const float2* __restrict__ lext) {
     constexpr int NF = nT(F), NM = nT(M), NV = rec_vec(NM);
     // the damping-correction list is walked after the near list (packed
     // kernel, AMOEBA)
@@ -386,6 +409,7 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
     const int lane = threadIdx.x & 31;
     float4* const bufs = sbuf_p2p + (size_t)(threadIdx.x >> 5) * 2 * stage;
     const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int ncorr = 0;  // corrected pairs evaluated by this lane
     for (int round = 0;; ++round) {
     int item;
     if (next) {
@@ -438,7 +462,31 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
         }
         // current piece (q, off) of source leaf j = [js, js + jc); the first
         // one is staged before the loop
-        int q = 0, off = 0, j = 0, js = 0, jc = 0;
+        // correction entries whose leaf cannot hold a pair that needs a
+        // correction for any of this chunk's targets are passed over without
+        // staging: for target t and leaf B, a r >= d_t dmin_B (|x_t - c_B| -
+        // extent_B) (all lanes take part)
+        auto next_entry = [&](int q) {
+            if constexpr (kCorr) {
+                const float txa = ta.x + ca.x, tya = ta.y + ca.y, tza = ta.z + ca.z;
+                while (q < q1 && q >= nn) {
+                    const int B = t.corr_src[c0 + q - nn];
+                    bool need = false;
+                    if (valid) {
+                        const float4 cb = chi[B];
+                        const float2 eb = lext[B];
+                        const float dx = txa - cb.x, dy = tya - cb.y, dz = tza - cb.z;
+                        const float rmin = fmaxf(sqrtf(dx * dx + dy * dy + dz * dz) - eb.x - 1e-2f, 0.0f);
+                        const float xm = ta.w * eb.y * rmin;
+                        need = xm * xm < xcut2;
+                    }
+                    if (__any_sync(0xffffffffu, need)) break;
+                    ++q;
+                }
+            }
+            return q;
+        };
+        int q = next_entry(0), off = 0, j = 0, js = 0, jc = 0;
         if (q < q1) {
             j = src_of(q);
             js = sstart[j];
@@ -453,7 +501,7 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
             // stage the next piece
             int nq = q, noff = off + cap, nj = j, njs = js, njc = jc;
             if (noff >= jc) {
-                nq = q + 1;
+                nq = next_entry(q + 1);
                 noff = 0;
                 if (nq < q1) {
                     nj = src_of(nq);
@@ -493,11 +541,12 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
                         if constexpr (kCorr) {
                             if (anyneed)
                                 p2p_leaf_x2<M, F, DAMP, true, true>(cur, pc >> 1, k0, grp, ngr, tgt, xo, yo, zo, dt,
-                                                                    oxl2, oyl2, ozl2, excl, exw, n, ot, XH, XL, xcut2);
+                                                                    oxl2, oyl2, ozl2, excl, exw, n, ot, XH, XL, xcut2,
+                                                                    &ncorr);
                             else
                                 p2p_leaf_x2<M, F, DAMP, false, true>(cur, pc >> 1, k0, grp, ngr, tgt, xo, yo, zo, dt,
                                                                      oxl2, oyl2, ozl2, excl, exw, n, ot, XH, XL,
-                                                                     xcut2);
+                                                                     xcut2, &ncorr);
                         }
                     } else if (anyneed)
                         p2p_leaf_x2<M, F, DAMP, true>(cur, pc >> 1, k0, grp, ngr, tgt, xo, yo, zo, dt, oxl2, oyl2,
@@ -568,6 +617,11 @@ __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float
             for (int f = 0; f < NF; ++f) fs[(size_t)f * n + tgt] = acc[f];
         }
     }
+    }
+    if (kCorr && corr_count) {
+        // every lane of the warp is here (leaves are taken per warp)
+        const int sc = __reduce_add_sync(0xffffffffu, ncorr);
+        if ((threadIdx.x & 31) == 0 && sc) atomicAdd(corr_count, (unsigned long long)sc);
     }
 }
 
@@ -676,26 +730,26 @@ template <int M, int F, bool X2>
 void launch_p2p_kind(unsigned blocks, int threads, size_t smem, int stage, const int32_t* order, unsigned* next,
                      cudaStream_t st, const TreeDev& t, const float4* rec, const float4* srec, const int32_t* sstart,
                      const float4* chi, const float4* clo, const int32_t* excl, int exw, int64_t n, int damp,
-                     double* fs, float xcut2) {
+                     double* fs, float xcut2, unsigned long long* corr_count, const float2* lext) {
     if constexpr (X2 && F > 1) {
         return;  // not instantiated: the packed kernel is used for field orders 0 and 1
     } else {
     switch (damp) {
         case DAMP_AMOEBA:
             k_p2p_f32<M, F, DAMP_AMOEBA, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw,
-                                                                              n, fs, stage, order, next, xcut2);
+                                                                              n, fs, stage, order, next, xcut2, corr_count, lext);
             break;
         case DAMP_THOLE:
             k_p2p_f32<M, F, DAMP_THOLE, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw,
-                                                                             n, fs, stage, order, next, xcut2);
+                                                                             n, fs, stage, order, next, xcut2, corr_count, lext);
             break;
         case DAMP_ERF:
             k_p2p_f32<M, F, DAMP_ERF, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw, n,
-                                                                           fs, stage, order, next, xcut2);
+                                                                           fs, stage, order, next, xcut2, corr_count, lext);
             break;
         default:
             k_p2p_f32<M, F, DAMP_NONE, X2><<<blocks, threads, smem, st>>>(t, rec, srec, sstart, chi, clo, excl, exw,
-                                                                            n, fs, stage, order, next, xcut2);
+                                                                            n, fs, stage, order, next, xcut2, corr_count, lext);
             break;
     }
     }
@@ -831,8 +885,20 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
     // one-source kernel); FMM_GB300_P2P_PACKED=0 selects the one-source kernel
     const bool x2 = p2p_packed_enabled(sh, field_order, P.damp_type) && t.num_leaves > 0 &&
                     n + (int64_t)t.num_leaves < (int64_t)INT32_MAX;
-    // a damping-correction list is walked by the packed kernel only
+    // a damping-correction list is walked by the packed kernel only; the
+    // pairs it corrects are counted in counter 9
     if (t.ncorr > 0 && !(x2 && P.damp_type == DAMP_AMOEBA)) return FMM_ENOTSUP;
+    FMM_TRY(ws.counters.ensure(sizeof(unsigned long long) * 32));
+    unsigned long long* corr_count = ws.counters.as<unsigned long long>() + 9;
+    FMM_CUDA_TRY(cudaMemsetAsync(corr_count, 0, sizeof(unsigned long long), st));
+    const float2* lext = nullptr;
+    if (t.ncorr > 0) {
+        FMM_TRY(ws.leaf_ext.ensure(sizeof(float2) * (size_t)t.num_nodes));
+        count_launches(1);
+        k_leaf_extent<<<grid_for((int64_t)t.num_leaves * 32, 128), 128, 0, st>>>(rec_vec(P.dim), t, rec,
+                                                                                 ws.leaf_ext.as<float2>());
+        lext = ws.leaf_ext.as<float2>();
+    }
     if (x2) {
         const int nv = rec_vec(P.dim);
         const int L = t.num_leaves;
@@ -893,12 +959,12 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
                       (launch_p2p_kind<MM, FF, true>(blocks, sh.threads, smem, sh.stage, order, next, st, t, rec,
                                                      ws.f32x2.as<float4>(), ws.p2p_pad.as<int32_t>(), chi, clo,
                                                      P.excl, P.exw, n, P.damp_type, ws.fsorted.as<double>(),
-                                                     ws.corr_xcut2)));
+                                                     ws.corr_xcut2, corr_count, lext)));
     } else {
         FMM_MF_SWITCH(m, field_order,
                       (launch_p2p_kind<MM, FF, false>(blocks, sh.threads, smem, sh.stage, order, next, st, t, rec, rec,
                                                       t.start, chi, clo, P.excl, P.exw, n, P.damp_type,
-                                                      ws.fsorted.as<double>(), 0.0f)));
+                                                      ws.fsorted.as<double>(), 0.0f, nullptr, nullptr)));
     }
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;

@@ -233,7 +233,8 @@ int fmm_release_workspace(void);
  * work queue 0/1) and 1 if this call ran the autotuner; then the number of
  * far leaf pairs inside the damping range whose particle pairs the near
  * field corrected (learned lists with the packed FP32 near field, AMOEBA;
- * else 0).  Returns the number written (at most 41). */
+ * else 0) and the number of particle pairs of those leaf pairs whose
+ * correction it evaluated.  Returns the number written (at most 42). */
 int fmm_last_stats(double *out, int len);
 
 /* Diagnostics (no counterpart in the reference): builds the octree and

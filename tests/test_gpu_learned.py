@@ -116,6 +116,8 @@ def test_damping_correction_meets_target_with_fewer_near_pairs(water, monkeypatc
     assert _rms(F, D) <= 1e-6
     assert _rms(F0, D) <= 1e-6
     assert st["p2p_particle_pairs"] < st0["p2p_particle_pairs"]
+    assert st["corr_leaf_pairs"] > 0
+    assert st0["corr_leaf_pairs"] == 0 and st0["corr_particle_pairs"] == 0
 
 
 def test_damping_correction_with_distant_exclusions(water):
