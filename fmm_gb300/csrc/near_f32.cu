@@ -10,6 +10,14 @@
 // 1/r Newton-refined.  Contributions are summed over one source leaf in
 // compensated FP32 (TwoSum hi + lo) and the per-leaf sums are added into FP64
 // accumulators.  Excluded partners and the self pair are masked in the loop.
+//
+// The packed kernel (field orders 0 and 1, all kernels but erf) evaluates
+// each target against two sources at once in f32x2 arithmetic from a second
+// record array with even leaf starts and interleaved slot pairs, and, with
+// learned lists on AMOEBA, walks a damping-correction list after the near
+// list: far leaf pairs inside the damping range, of which only the pairs
+// with a r below the range's cutoff are evaluated, as the difference of the
+// damped and undamped kernels (the M2L carries the undamped one).
 #include <algorithm>
 #include <cstdlib>
 
@@ -687,8 +695,16 @@ __global__ void __launch_bounds__(128) k_leaf_field_scale(const TreeDev t, const
                 mc[4 * v + 2] = wv.z;
                 mc[4 * v + 3] = wv.w;
             }
-            pair_field<M, 1, float>(tx - (sa.x + cb.x), ty - (sa.y + cb.y), tz - (sa.z + cb.z), ta.w * sa.w, damp,
-                                    mc, acc);
+            const float dx = tx - (sa.x + cb.x), dy = ty - (sa.y + cb.y), dz = tz - (sa.z + cb.z);
+            if constexpr (M == 2) {
+                // quadrupole sources: the dot-product contraction (the record's
+                // pad slot holds the trace of the second moments)
+                float g[4];
+                radial_g<3, float>(damp, dx * dx + dy * dy + dz * dz, ta.w * sa.w, g);
+                contract_q1<float>(dx, dy, dz, g, mc, mc[10], damp, acc);
+            } else {
+                pair_field<M, 1, float>(dx, dy, dz, ta.w * sa.w, damp, mc, acc);
+            }
         }
 #pragma unroll
         for (int c = 1; c < 4; ++c)

@@ -156,3 +156,23 @@ def test_damping_correction_with_distant_exclusions(water):
     if st["selector_fallback"] == 0:
         assert st["corr_leaf_pairs"] > 0
     assert _rms(F, D) <= 1e-6
+
+
+def test_damping_correction_applied_with_longer_damping_range(water):
+    """Damping factors scaled by 0.7 (a longer damping range): the learned
+    lists' far leaf pairs inside the range hold millions of particle pairs
+    whose damping correction is evaluated; the result stays at the FP32
+    floor of such a strongly damped system (about 1.2e-6 for the fixed rule
+    on the same mixed path, measured), where a wrong correction would be
+    orders of magnitude off."""
+    s, _ = water
+    d = s["damping_factors"] * 0.7
+    D = fmm_gb300.field_direct(0, s["coordinates"], s["multipoles"], s["exclusions"], 1, "AMOEBA", d,
+                               options=Options(excl_mode="mask"))
+    opt = Options.exact(precision="mixed", mac_mode="damping", selector="learned")
+    F = fmm_gb300.field_fmm(0, s["coordinates"], s["multipoles"], s["exclusions"], 0.3, 64, 10, 1, "AMOEBA", d,
+                            options=opt)
+    st = fmm_gb300.last_stats()
+    if st["selector_fallback"] == 0:
+        assert st["corr_particle_pairs"] > 1e6
+    assert _rms(F, D) <= 2e-6
