@@ -490,6 +490,11 @@ int run_fmm(Workspace& ws, const Particles& P, double theta, int ncrit, int p, i
         FMM_TRY(selector_node_budgets(ws, P, t, base, st));
         tpl.sel_budget = ws.sel_budget.as<float>();
         tpl.sel_theta = sel_theta_loose();
+        if (tpl.corr_mode) {
+            FMM_TRY(launch_leaf_extent(ws, P, t, st));
+            tpl.corr_ext = ws.leaf_ext.as<float2>();
+            tpl.corr_xcut2 = ws.corr_xcut2;
+        }
     }
     cudaEventRecord(ws.ev[2], st);
     bool fallback = false;

@@ -93,6 +93,8 @@ struct TreeParams {
     double root_r = 0.0;                // > 0: root half-width given (batched packing box)
     int corr_mode = 0;                  // learned lists: leaf pairs inside the damping range may be far
                                         // (listed in the damping-correction list)
+    const float2* corr_ext = nullptr;   // per leaf (particle extent, smallest damping factor)
+    float corr_xcut2 = 0.0f;            // (a r)^2 beyond which a pair needs no damping correction
     const int32_t* d_sys = nullptr;     // batched systems: system id of each particle (input order)
 };
 
@@ -231,6 +233,9 @@ int launch_direct_f64(Workspace& ws, const Particles& P, int field_order, const 
 // FP32 particle records and node centres of the mixed-precision near field
 // (near_f32.cu; after gather_sorted).
 int prepare_f32_records(Workspace& ws, const Particles& P, const TreeDev& t, cudaStream_t st);
+// Per leaf: particle extent from the leaf centre and smallest damping factor
+// (ws.leaf_ext, from the FP32 records), for the damping correction.
+int launch_leaf_extent(Workspace& ws, const Particles& P, const TreeDev& t, cudaStream_t st);
 // FP32 field estimate at a few targets (exclusions masked) from those
 // records, into d_out (ntgt x nT(field_order), FP64, column-major).
 int launch_direct_scale_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, double* d_out,

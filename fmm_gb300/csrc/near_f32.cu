@@ -833,6 +833,15 @@ int prepare_f32_records(Workspace& ws, const Particles& P, const TreeDev& t, cud
     return FMM_OK;
 }
 
+int launch_leaf_extent(Workspace& ws, const Particles& P, const TreeDev& t, cudaStream_t st) {
+    FMM_TRY(ws.leaf_ext.ensure(sizeof(float2) * (size_t)t.num_nodes));
+    count_launches(1);
+    k_leaf_extent<<<grid_for((int64_t)t.num_leaves * 32, 128), 128, 0, st>>>(rec_vec(P.dim), t, ws.f32buf.as<float4>(),
+                                                                             ws.leaf_ext.as<float2>());
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
 int launch_direct_scale_f32(Workspace& ws, const Particles& P, const TreeDev& t, int field_order, double* d_out,
                             cudaStream_t st, int64_t ntgt, const int64_t* d_targets) {
     const int m = dim_to_order(P.dim);
@@ -907,14 +916,8 @@ int launch_p2p_f32(Workspace& ws, const Particles& P, const TreeDev& t, int fiel
     FMM_TRY(ws.counters.ensure(sizeof(unsigned long long) * 32));
     unsigned long long* corr_count = ws.counters.as<unsigned long long>() + 9;
     FMM_CUDA_TRY(cudaMemsetAsync(corr_count, 0, sizeof(unsigned long long), st));
-    const float2* lext = nullptr;
-    if (t.ncorr > 0) {
-        FMM_TRY(ws.leaf_ext.ensure(sizeof(float2) * (size_t)t.num_nodes));
-        count_launches(1);
-        k_leaf_extent<<<grid_for((int64_t)t.num_leaves * 32, 128), 128, 0, st>>>(rec_vec(P.dim), t, rec,
-                                                                                 ws.leaf_ext.as<float2>());
-        lext = ws.leaf_ext.as<float2>();
-    }
+    // leaf extents: computed with the lists (launch_leaf_extent)
+    const float2* lext = t.ncorr > 0 ? ws.leaf_ext.as<float2>() : nullptr;
     if (x2) {
         const int nv = rec_vec(P.dim);
         const int L = t.num_leaves;

@@ -417,7 +417,8 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
     int64_t cap_far, uint64_t* __restrict__ nearp, int64_t cap_near, const TreeDev t, float theta_loose, float rdamp,
     int qmax, const float* __restrict__ params, const float* __restrict__ lnorm, const float* __restrict__ dmin,
     int P, const float* __restrict__ log_budget, const float4* __restrict__ chi, const float4* __restrict__ clo,
-    unsigned long long* counters, int corr_mode, uint64_t* __restrict__ corrp, int64_t cap_corr) {
+    unsigned long long* counters, int corr_mode, uint64_t* __restrict__ corrp, int64_t cap_corr,
+    const float2* __restrict__ lext, float xcut2) {
     extern __shared__ __align__(16) float sm_sel[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float* X = sm_sel + wib * kWarpTcFloats;  // this warp's network scratch
@@ -427,7 +428,7 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
     bool skip = q >= nin;
     int i = 0, j = 0;
     float ri = 0.0f, rj = 0.0f;  // FP32 node data throughout: the FP64 pipe is the scarce one
-    bool li = false, lj = false, mixed = false, accept = false, corr = false;
+    bool li = false, lj = false, mixed = false, accept = false, corr = false, ingap = false;
     float4 ci = make_float4(0.f, 0.f, 0.f, 0.f), cj = ci, oi = ci, oj = ci;
     if (!skip) {
         i = in[q].x;
@@ -456,10 +457,17 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
         if (accept && rdamp > 0.0f) {
             const float gap = r - 1.7320508f * (oi.w + oj.w);
             if (gap < rdamp) {
-                if (corr_mode && li && lj)
-                    corr = true;
-                else
+                if (corr_mode && li && lj) {
+                    // listed for the correction unless no particle pair of the
+                    // two leaves can have a r below the cutoff: a r >= dmin_i
+                    // dmin_j (r - extent_i - extent_j)
+                    ingap = true;
+                    const float2 ea = lext[i], eb = lext[j];
+                    const float xm = ea.y * eb.y * fmaxf(r - ea.x - eb.x - 1e-2f, 0.0f);
+                    corr = xm * xm < xcut2;
+                } else {
                     accept = false;
+                }
             }
         }
     }
@@ -472,7 +480,7 @@ __global__ void __launch_bounds__(128) k_list_iter_learned(
         if (accept) {
             float x[kMlpIn];
             selector_features_f32(chi, clo, t.count, lnorm, dmin, P, i, j, x);
-            if (corr) x[16] = 1.0f;  // the M2L carries the undamped kernel; the damping is corrected pairwise
+            if (ingap) x[16] = 1.0f;  // the M2L carries the undamped kernel; the damping is corrected pairwise
             mlp_input(S, x, X + slot * kMlpInP);
         }
         __syncwarp();
@@ -779,7 +787,7 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
     int64_t cap_near = std::max<int64_t>(
         {4096, (int64_t)(0.4 * per * t.num_leaves), (int64_t)(ws.near_pairs.cap / sizeof(uint64_t))});
     int64_t cap_front = std::max<int64_t>({4096, cap_far, (int64_t)(ws.front_a.cap / sizeof(int2))});
-    const bool corr = tp.sel_params && tp.corr_mode && tp.mac_mode == 1 && tp.rdamp > 0.0;
+    const bool corr = tp.sel_params && tp.corr_mode && tp.mac_mode == 1 && tp.rdamp > 0.0 && tp.corr_ext;
     int64_t cap_corr = corr ? std::max<int64_t>({4096, cap_near, (int64_t)(ws.corr_pairs.cap / sizeof(uint64_t))}) : 0;
     unsigned long long* ctr = ws.counters.as<unsigned long long>();
     for (int attempt = 0; attempt < 8; ++attempt) {
@@ -810,7 +818,8 @@ int build_lists(Workspace& ws, TreeDev& t, const TreeParams& tp, cudaStream_t st
                     fin, (int)nin, fout, cap_front, ws.far_pairs.as<uint64_t>(), cap_far, ws.near_pairs.as<uint64_t>(),
                     cap_near, t, (float)tp.sel_theta, tp.mac_mode == 1 ? (float)tp.rdamp : 0.0f, tp.order,
                     tp.sel_params, tp.sel_lnorm, tp.sel_dmin, tp.sel_P, tp.sel_budget, tp.sel_chi, tp.sel_clo,
-                    ctr, corr ? 1 : 0, corr ? ws.corr_pairs.as<uint64_t>() : nullptr, cap_corr);
+                    ctr, corr ? 1 : 0, corr ? ws.corr_pairs.as<uint64_t>() : nullptr, cap_corr, tp.corr_ext,
+                    tp.corr_xcut2);
             } else
             k_list_iter<<<grid_for(nin, 256), 256, 0, st>>>(fin, (int)nin, fout, cap_front,
                                                              ws.far_pairs.as<uint64_t>(), cap_far,
