@@ -320,8 +320,11 @@ int launch_m2l_reduced(Workspace& ws, const TreeDev& t, int p, bool fp32, cudaSt
     // kernel made when the structure was built)
     const int gst = (ws.reuse_structure && ws.m2l_pairwise) ? FMM_ENOTSUP : launch_m2l_grouped(ws, t, p, fp32, st);
     if (gst == FMM_ENOTSUP) {
-        // FP64 operator too large for shared memory: per-pair kernel
-        if (fp32)
+        // per-pair kernel (FP64 operator too large for shared memory, or
+        // displacement groups of a few pairs); in FP32 only up to order 8:
+        // its tensors come from an FP32 recursion, which at higher orders
+        // falls short of the mixed path's accuracy
+        if (fp32 && p <= 8)
             FMM_TRY(launch_red<float>(ws, t, p, st));
         else
             FMM_TRY(launch_red<double>(ws, t, p, st));
