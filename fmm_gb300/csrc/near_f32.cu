@@ -398,6 +398,10 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // start first and the last wave is made of the smallest.
 // X2: sources from the packed records `srec` (k_gather_x2, padded leaf starts
 // sstart) evaluated two at a time; otherwise srec = rec, sstart = t.start.
+// With a damping-correction list (packed kernel, AMOEBA: t.corr_off) each
+// target chunk walks it after its near list, passing over the entries whose
+// leaf bound (lext) rules out a pair inside xcut2 for every lane, and counts
+// the corrected pairs into corr_count.
 template <int M, int F, int DAMP, bool X2>
 __global__ void __launch_bounds__(256, 2) k_p2p_f32(const TreeDev t, const float4* __restrict__ rec,
                                                     const float4* __restrict__ srec,
