@@ -93,7 +93,7 @@ def workload_config(arm, system="water", n=3 * N_MOL):
 # DRAM bytes (read + write) per unit of the two dominant kernels, from one ncu
 # capture of each on the 100k water case
 P2P_DRAM_PER_PAIR = (21.25e6 + 0.13e6) / 413.08e6
-TC_DRAM_PER_PAIR = (571.38e6 + 479.74e6) / 1.084818e6
+TC_DRAM_PER_PAIR = (517.86e6 + 641.59e6) / 1.424928e6
 
 
 def measured_peaks():
