@@ -318,7 +318,8 @@ def test_packed_near_field_matches_one_source_kernel(damp, mf, one_sided, monkey
     """The packed near field (two sources per thread in f32x2 arithmetic, odd
     leaves padded with an empty particle, skipped halves zeroed) agrees with
     the one-source FP32 kernel to FP32 rounding, and both with the FP64 path;
-    exclusions listed by one partner only included."""
+    exclusions listed by one partner only included.  (erf damping runs the
+    one-source kernel either way; its case checks that selection.)"""
     from fmm_gb300 import systems
     m, f = mf
     s = systems.water(3001, 70.0, order=m, seed=41)
