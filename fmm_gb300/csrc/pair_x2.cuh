@@ -2,9 +2,10 @@
 // thread in one 64-bit register pair.
 //
 // Blackwell executes add, sub, mul and fma on two FP32 values with one
-// instruction (`add/sub/mul/fma.rn.f32x2`); the near field is bound by
-// instruction issue, not by the FMA pipe, so evaluating a target against two
-// sources at once in packed form halves the issued arithmetic.  Each half
+// instruction (`add/sub/mul/fma.rn.f32x2`) at the FMA pipe's element rate of
+// the scalar forms, so packing halves the issue slots the arithmetic takes;
+// the one-source near field was bound by instruction issue, not by the FMA
+// pipe, so a target is evaluated against two sources at once.  Each half
 // rounds exactly as the scalar FP32 instruction would (round to nearest,
 // IEEE denormals), so a packed pair equals the scalar evaluation written with
 // the same operation order.  The transcendental pieces (rsqrt, exp) and the
