@@ -75,3 +75,15 @@ def test_product_path_has_no_oracle_dependency():
                 txt = open(os.path.join(d, f)).read()
                 assert "import oracle" not in txt and "from oracle" not in txt, f
                 assert "liboracle" not in txt, f
+
+
+def test_stats_vector_matches_the_python_names(L):
+    """fmm_last_stats (host-side, no GPU needed) writes exactly the entries
+    the Python binding names, in the documented count."""
+    import fmm_gb300
+    buf = (ctypes.c_double * 64)()
+    k = L.fmm_last_stats(buf, 64)
+    assert k == len(fmm_gb300.STAT_NAMES) == 42
+    assert fmm_gb300.STAT_NAMES[-2:] == ["corr_leaf_pairs", "corr_particle_pairs"]
+    txt = open(os.path.join(ROOT, "include", "fmm_gpu.h")).read()
+    assert "at most 42" in txt
