@@ -58,3 +58,27 @@ def test_q1_contraction_with_halved_moments(damp):
         got = q1_halved(Mc, R, g, damp == "AMOEBA")
         scale = np.max(np.abs(ref)) + 1e-300
         assert np.max(np.abs(got - ref)) <= 1e-12 * scale, (damp, R, a)
+
+
+def test_amoeba_damping_correction_numerators():
+    """The near field's damping correction (pair_x2.cuh radial_g_x2<N, true>)
+    evaluates g_damped - g_undamped of AMOEBA as e^{-u} Q_j(u) / r^(2j+1) with
+    the Q_j of the closed form (csrc/gen_tables.py), and -1/r for the
+    potential; checked against the oracle's two kernels."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "fmm_gb300", "csrc"))
+    import gen_tables
+    Q = gen_tables.amoeba_q()
+    rng = np.random.default_rng(9)
+    for _ in range(40):
+        a = rng.uniform(0.15, 0.6)
+        r = rng.uniform(2.0, 20.0)
+        u = (a * r) ** 3
+        gd = oracle.radial_g("AMOEBA", r, a, 4)
+        gu = oracle.radial_g("", r, a, 4)
+        assert abs((gd[0] - gu[0]) - (-1.0 / r)) <= 1e-14 / r
+        for j in range(1, 5):
+            corr = np.exp(-u) * sum(float(c) * u ** d for d, c in enumerate(Q[j])) / r ** (2 * j + 1)
+            scale = abs(gu[j])
+            assert abs((gd[j] - gu[j]) - corr) <= 1e-12 * scale, (a, r, j)
